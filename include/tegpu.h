@@ -1,0 +1,184 @@
+/*
+ * tegpu.h -- C ABI of the GB300 Krylov real-time evolution library (libtegpu.so).
+ *
+ * The library computes exp(-i * expFactor * H * t) v on one GPU, with the
+ * a-posteriori error bound, step-size control and observable sampling of
+ * TimeEvolver's krylovTimeEvolver, entirely in hand-written sm_103a kernels.
+ * Every entry point takes plain pointers and sizes; complex numbers are
+ * interleaved (re, im) doubles.  Functions return TE_OK (0) or a negative
+ * TE_ERR_* code; te_last_error() describes the last failure of the calling
+ * thread.  Nothing here calls exit(): the C++ drop-in layer
+ * (timeevolver_gb300/host) turns the codes back into the reference's
+ * behaviour.
+ *
+ * Reference interfaces replaced (paths inside the TimeEvolver project):
+ *   TE::smatrix + initialize()        core/matrixDataTypes.h:59-99, .cpp:264-290, :352-396
+ *   smatrix::spMV                      core/matrixDataTypes.cpp:325-346
+ *   smatrix::norm1                     core/matrixDataTypes.cpp:223-235
+ *   krylovTimeEvolver(...) ctor        core/krylovTimeEvolver.h:59-60, .cpp:26-94
+ *   krylovTimeEvolver::timeEvolve()    core/krylovTimeEvolver.h:61, .cpp:261-512
+ *   krylovReturn                       core/krylovTimeEvolver.h:32-51, .cpp:662-676
+ *   krylovSpMatrixObservable / krylovVectorObservable::expectation
+ *                                      core/krylovObservables.cpp:173-236
+ *   krylovBasicObservable::expectation (user subclasses, host callback)
+ *                                      core/krylovObservables.h:42
+ */
+#ifndef TEGPU_H
+#define TEGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TEGPU_ABI_VERSION 1
+
+/* ------------------------------------------------------------ error codes */
+#define TE_OK 0
+#define TE_ERR_INVALID_ARG (-1)     /* bad pointer, size or parameter */
+#define TE_ERR_CUDA (-2)            /* a CUDA runtime call failed */
+#define TE_ERR_EMPTY (-3)           /* "Invalid Hilbertspace dimension" (krylovTimeEvolver.cpp:39-43) */
+#define TE_ERR_NOT_NORMALIZED (-4)  /* "Initial vector is not normalized" (krylovTimeEvolver.cpp:45-48) */
+#define TE_ERR_NO_STEP (-5)         /* 20 halvings did not meet the tolerance (krylovTimeEvolver.cpp:203-207) */
+#define TE_ERR_EIGEN (-6)           /* Krylov eigensolver did not converge (the LAPACK error of :365-370) */
+#define TE_ERR_DIM (-7)             /* "Incompatible dimensions" (krylovObservables.cpp:296-300) */
+#define TE_ERR_OUT_OF_MEMORY (-8)
+#define TE_ERR_UNSUPPORTED (-9)     /* e.g. Krylov dimension above TE_MAX_KRYLOV */
+#define TE_ERR_DEVICE_TIMEOUT (-10) /* a bounded device-side wait gave up */
+
+#define TE_MAX_KRYLOV 64            /* largest Krylov dimension m */
+
+/* status codes of krylovReturn::statusCode (krylovTimeEvolver.h:41-45) */
+#define TE_STATUS_OK 0
+#define TE_STATUS_LUCKY_BREAKDOWN 1
+#define TE_STATUS_BELOW_ROUNDOFF 2
+#define TE_STATUS_STOPPED 3
+#define TE_STATUS_ROUNDOFF 10
+#define TE_STATUS_ROUNDOFF_TOTAL 11
+#define TE_STATUS_INTEGRATION 20
+#define TE_STATUS_NORM 30
+#define TE_STATUS_MULTIPLE 100
+
+typedef struct te_matrix_s* te_matrix;   /* device-resident sparse matrix */
+typedef struct te_evolver_s* te_evolver; /* one time evolution (krylovTimeEvolver) */
+
+/* Description of the last error raised on the calling thread. */
+const char* te_last_error(void);
+int te_abi_version(void);
+
+/* Select the CUDA device used by subsequently created objects. */
+int te_set_device(int device);
+
+/* --------------------------------------------------------------- matrices */
+
+/* Upload a COO matrix (the storage of TE::smatrix: values, columns and
+ * rowIndex arrays of length nnz, size_t indices) and convert it to device
+ * CSR with int32 column indices.  Entries of one row are kept in input order;
+ * duplicates are kept (they add, as in the reference's COO loop).  A matrix
+ * whose imaginary parts are all zero is stored with real values (same
+ * results, half the value bytes and FP64 work).  Replaces smatrix(...) +
+ * initialize() (matrixDataTypes.cpp:264-290, :352-396). */
+int te_matrix_create_coo(int64_t n_rows, int64_t n_cols, int64_t nnz, const uint64_t* row_index,
+                         const uint64_t* columns, const double* values, te_matrix* out);
+
+/* Upload a CSR matrix with int32 indices (row_ptr of length n_rows + 1).
+ * values_complex != 0: values are nnz interleaved complex doubles, else nnz
+ * real doubles. */
+int te_matrix_create_csr(int64_t n_rows, int64_t n_cols, int64_t nnz, const int64_t* row_ptr,
+                         const int32_t* col_idx, const double* values, int values_complex, te_matrix* out);
+
+int te_matrix_destroy(te_matrix A);
+
+/* n_rows, n_cols, nnz, flags (bit0 real values, bit1 diagonal), and the
+ * reference's 1-norm (max absolute column sum, matrixDataTypes.cpp:223-235). */
+int te_matrix_info(te_matrix A, int64_t* n_rows, int64_t* n_cols, int64_t* nnz, int* flags, double* norm1);
+
+/* out = alpha * A * in on device buffers (complex n), on a CUDA stream
+ * (NULL = the library's stream).  Replaces smatrix::spMV
+ * (matrixDataTypes.cpp:325-346). */
+int te_matrix_spmv(te_matrix A, double alpha_re, double alpha_im, const double* in_dev, double* out_dev,
+                   void* cuda_stream);
+
+/* Same with host buffers (copies in and out, synchronous). */
+int te_matrix_spmv_host(te_matrix A, double alpha_re, double alpha_im, const double* in_host,
+                        double* out_host);
+
+/* ----------------------------------------------------------------- evolver */
+
+/* Parameters of krylovTimeEvolver (krylovTimeEvolver.h:59; defaults of the
+ * 5-argument constructor, .cpp:93-94: exp_factor 1, tol 1e-6, m 40,
+ * fast_integration 0). */
+typedef struct te_params {
+  double t;              /* total evolution time */
+  double sampling_step;  /* time between samples */
+  double exp_factor;     /* exp(-i exp_factor H t) */
+  double tol;            /* error bound on the final state (2-norm) */
+  int32_t m;             /* Krylov dimension (clamped to the Hilbert dimension) */
+  int32_t fast_integration; /* Gauss 15/7 instead of tanh-sinh */
+  int32_t progress_bar;  /* accepted for API parity; the GPU path prints nothing */
+  int32_t reserved;
+} te_params;
+
+/* Result record of one evolution (krylovReturn, krylovTimeEvolver.h:32-51). */
+typedef struct te_result {
+  double err;            /* accumulated analytic error bound */
+  double evolved_time;   /* t_now at the end (krylovReturn::evolvedTime) */
+  int64_t num_samples;   /* samples taken */
+  int64_t n_steps;       /* Krylov steps */
+  int64_t dim;           /* Hilbert-space dimension */
+  int64_t krylov_dim;    /* Krylov dimension at the end (reduced by a lucky breakdown) */
+  int32_t status;        /* TE_STATUS_* */
+  int32_t nb_err_roundoff;
+  int32_t nb_err_int;
+  int32_t reserved;
+} te_result;
+
+/* Host callback for observables that are neither sparse matrices nor
+ * vectors (user subclasses of krylovBasicObservable).  Receives the sampled
+ * state on the host (complex dim) and writes the value to store; returns 0,
+ * or 1 to request the stop of the evolution (requestStopException, status 3). */
+typedef int (*te_observable_fn)(void* user, const double* state, int64_t dim, double* value_out);
+
+/* Create an evolution of v (host, complex n, copied) under H.  H stays owned
+ * by the caller and must outlive the evolver.  Replaces the constructor
+ * (krylovTimeEvolver.cpp:26-84); returns TE_ERR_EMPTY / TE_ERR_NOT_NORMALIZED
+ * where the reference exits. */
+int te_evolver_create(te_matrix H, const double* v_host, const te_params* params, te_evolver* out);
+int te_evolver_destroy(te_evolver ev);
+
+/* Observables, sampled in the order added (krylovObservables.cpp).  A
+ * sparse observable stores Re <psi|O|psi>; a vector observable stores
+ * |<psi|o>|^2.  O stays owned by the caller. */
+int te_evolver_add_sparse_observable(te_evolver ev, te_matrix O);
+int te_evolver_add_vector_observable(te_evolver ev, const double* o_host);
+int te_evolver_add_callback_observable(te_evolver ev, te_observable_fn fn, void* user);
+
+/* Run timeEvolve() (krylovTimeEvolver.cpp:261-512). */
+int te_evolver_run(te_evolver ev, te_result* result);
+
+/* Sampled values of observable obs_index (count doubles; the number of
+ * samples is floor(t / sampling_step) + 1, entries past num_samples are 0). */
+int te_evolver_samples(te_evolver ev, int obs_index, double* out_host, int64_t count);
+
+/* The returned state: the last sampled state (krylovReturn::evolvedState,
+ * krylovTimeEvolver.cpp:665), complex dim, to host or device memory. */
+int te_evolver_state(te_evolver ev, double* out_host);
+int te_evolver_state_device(te_evolver ev, const double** out_dev);
+
+/* Per-step record, for tests and tracing: t_now, t_step, err_step, h,
+ * m_eff, breakdown flag, findMaximalStepSize code, integrals evaluated. */
+typedef struct te_step_record {
+  double t_now, t_step, err_step, h;
+  int32_t m_eff, breakdown, code, n_integrals;
+} te_step_record;
+int te_evolver_trace(te_evolver ev, te_step_record* out, int64_t max_records, int64_t* n_records);
+
+/* Kernel launches issued by the last te_evolver_run (for launch accounting). */
+int64_t te_evolver_launch_count(te_evolver ev);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TEGPU_H */

@@ -1,0 +1,221 @@
+"""CUDA path against the oracle and the reference goldens (needs a GB300).
+
+Tolerances.  Sparse products agree to 1e-13 relative.  A free-running
+evolution uses the reference's three-term Lanczos recurrence without
+reorthogonalisation; once the Krylov basis loses orthogonality its last
+coefficients amplify rounding, so two correct FP64 runs (CPU oracle, GPU)
+agree only to the Krylov truncation error, which the a-posteriori bound
+controls: both final states lie within tol of the exact state, hence within
+2*tol of each other, and a sampled observable O differs by at most
+4*tol*||O||.  The tests assert these bounds, the same step count, status and
+sample count, an error bound <= tol, and the 1e-9 absolute observable
+agreement wherever the recurrence stays stable (small Krylov spaces, the
+goldens).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import models
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+OBS_TOL = 1e-9
+
+
+def _fock(states, occ):
+    v = np.zeros(len(states), dtype=np.complex128)
+    v[models.index_of(states, occ)] = 1.0
+    return v
+
+
+def _random_state(n, seed):
+    rng = np.random.default_rng(seed)
+    v = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    return v / np.linalg.norm(v)
+
+
+def _random_hermitian(n, per_row, seed):
+    rng = np.random.default_rng(seed)
+    rows = np.repeat(np.arange(n), per_row)
+    cols = rng.integers(0, n, size=n * per_row)
+    vals = rng.standard_normal(n * per_row) + 1j * rng.standard_normal(n * per_row)
+    A = {}
+    for r, c, v in zip(rows, cols, vals):
+        A[(r, c)] = A.get((r, c), 0) + v / 2
+        A[(c, r)] = A.get((c, r), 0) + np.conj(v) / 2
+    keys = sorted(A)
+    row = np.array([k[0] for k in keys], dtype=np.int64)
+    col = np.array([k[1] for k in keys], dtype=np.int64)
+    val = np.array([A[k] for k in keys], dtype=np.complex128)
+    return row, col, val
+
+
+def _compare(gpu, ref, tol, obs_norm=None, strict=True):
+    """strict: observables to 1e-9 absolute; otherwise to 4 tol ||O||."""
+    assert gpu["status"] == ref["status"], (gpu["status"], ref["status"])
+    assert gpu["num_samples"] == ref["num_samples"]
+    assert gpu["n_steps"] == ref["n_steps"], (gpu["n_steps"], ref["n_steps"])
+    assert gpu["krylov_dim"] == ref["krylov_dim"]
+    d_obs = np.max(np.abs(gpu["samples"] - ref["samples"])) if gpu["samples"].size else 0.0
+    bound = OBS_TOL if strict else max(OBS_TOL, 4 * tol * obs_norm)
+    assert d_obs < bound, (d_obs, bound)
+    assert np.linalg.norm(gpu["state"] - ref["state"]) < 2 * tol
+    assert gpu["err"] <= tol and ref["err"] <= tol
+    assert abs(gpu["evolved_time"] - ref["evolved_time"]) < 1e-12 * max(1.0, ref["evolved_time"])
+    return d_obs
+
+
+def test_spmv_real_and_complex(te_gpu, oracle_lib):
+    states, H = models.bose_hubbard(7, 6, 1.0, 2.0)
+    n = len(states)
+    x = _random_state(n, 1)
+    for coo, alpha in [(H, -0.75j), (_random_hermitian(3000, 9, 2), 0.3 - 1.1j)]:
+        nn = int(coo[0].max()) + 1 if coo is not H else n
+        xx = x if coo is H else _random_state(nn, 4)
+        M = te_gpu.Matrix.from_coo(nn, coo)
+        info = M.info()
+        assert info["real"] == (coo is H)
+        y = M.spmv(xx, alpha)
+        ref = oracle_lib.spmv(coo, xx, alpha)
+        assert np.linalg.norm(y - ref) <= 1e-13 * np.linalg.norm(ref)
+        assert abs(info["norm1"] - oracle_lib.norm1(coo, nn)) <= 1e-12 * info["norm1"]
+
+
+def test_bose_hubbard_l8_matches_oracle(te_gpu, oracle_lib):
+    """Plain method, small: L=8 N=8 (dim 6435), t=10, tol 1e-8, m=40, <n_i> every 0.1."""
+    states, H = models.bose_hubbard(8, 8, 1.0, 2.0)
+    v = _fock(states, [8] + [0] * 7)
+    obs = [("sparse", o) for o in models.number_operator_observables(states)]
+    gpu = te_gpu.evolve(H, v, 10.0, 0.1, obs, tol=1e-8, m=40, trace=True)
+    ref = oracle_lib.evolve(H, v, 10.0, 0.1, obs, tol=1e-8, m=40, trace=True)
+    _compare(gpu, ref, 1e-8, obs_norm=8.0, strict=False)
+    for a, b in zip(gpu["trace"], ref["trace"]):
+        assert abs(a["t_step"] - b["t_step"]) <= 1e-12 * b["t_step"]
+        assert a["code"] == b["code"]
+    assert gpu["launches"] > 0
+
+
+def test_bose_hubbard_l12_matches_oracle(te_gpu, oracle_lib):
+    """Plain method, large: L=12 N=12 U=3 (dim 1352078), random complex v
+    (seed 0), tol 1e-8, m=40, <n_0> every 0.5; the first Krylov steps (t=1)."""
+    states, H = models.bose_hubbard(12, 12, 1.0, 3.0)
+    n = len(states)
+    v = _random_state(n, 0)
+    obs = [("sparse", models.create_matrix([models.number_operator(0, 1.0)], states))]
+    gpu = te_gpu.evolve(H, v, 1.0, 0.5, obs, tol=1e-8, m=40, trace=True)
+    ref = oracle_lib.evolve(H, v, 1.0, 0.5, obs, tol=1e-8, m=40, trace=True)
+    _compare(gpu, ref, 1e-8, obs_norm=12.0, strict=True)
+    for a, b in zip(gpu["trace"], ref["trace"]):
+        assert abs(a["t_step"] - b["t_step"]) <= 1e-12 * b["t_step"]
+
+
+def test_golden_black_hole_n20(te_gpu):
+    states, H, i0 = models.black_hole(N0=20, Nm=2, K=4)
+    v = np.zeros(len(states), dtype=np.complex128)
+    v[i0] = 1
+    obs = [("sparse", o) for o in models.number_operator_observables(states)]
+    r = te_gpu.evolve(H, v, 10.0, 0.01, obs, tol=1e-8, m=40)
+    gold = np.load(os.path.join(GOLD, "blackhole_N20.npy"))
+    assert r["num_samples"] == 1001
+    assert np.max(np.abs(r["samples"] - gold)) < 1e-8
+    assert r["err"] <= 1e-8
+
+
+def test_golden_lucky_breakdown(te_gpu, oracle_lib):
+    states, H, i0 = models.black_hole(N0=1, Nm=1, K=1)
+    v = np.zeros(4, dtype=np.complex128)
+    v[i0] = 1
+    obs = [("sparse", o) for o in models.number_operator_observables(states)]
+    r = te_gpu.evolve(H, v, 1000.0, 1.0, obs, tol=1e-8, m=40)
+    gold = np.load(os.path.join(GOLD, "blackhole_N1_LB.npy"))
+    assert r["status"] == 1 and r["krylov_dim"] == 4 and r["n_steps"] == 1
+    assert np.max(np.abs(r["samples"] - gold)) < 1e-8
+    ref = oracle_lib.evolve(H, v, 1000.0, 1.0, obs, tol=1e-8, m=40)
+    _compare(r, ref, 1e-8)
+
+
+def test_golden_simple_example(te_gpu, oracle_lib):
+    states, H, i0 = models.simple_example()
+    v = np.zeros(len(states), dtype=np.complex128)
+    v[i0] = 1
+    obs = [("sparse", o) for o in models.number_operator_observables(states)]
+    r = te_gpu.evolve(H, v, 10.0, 0.01, obs, tol=1e-6, m=40)
+    gold = np.load(os.path.join(GOLD, "simple_example.npy"))
+    assert np.max(np.abs(r["samples"] - gold)) <= 6e-4  # 6 significant digits of values up to 200
+    ref = oracle_lib.evolve(H, v, 10.0, 0.01, obs, tol=1e-6, m=40)
+    _compare(r, ref, 1e-6)
+
+
+def test_complex_matrix_random_state(te_gpu, oracle_lib):
+    H = _random_hermitian(2000, 6, 7)
+    n = 2000
+    v = _random_state(n, 8)
+    o = np.zeros(n, dtype=np.complex128)
+    o[:10] = 0.3
+    diag = (np.arange(n, dtype=np.int64), np.arange(n, dtype=np.int64), np.linspace(0, 1, n).astype(complex))
+    obs = [("sparse", diag), ("vector", o)]
+    gpu = te_gpu.evolve(H, v, 2.0, 0.25, obs, exp_factor=0.7, tol=1e-9, m=30)
+    ref = oracle_lib.evolve(H, v, 2.0, 0.25, obs, exp_factor=0.7, tol=1e-9, m=30)
+    _compare(gpu, ref, 1e-9)
+
+
+def test_fast_integration(te_gpu, oracle_lib):
+    states, H = models.bose_hubbard(6, 6, 1.0, 3.0)
+    v = _random_state(len(states), 0)
+    obs = [("sparse", models.create_matrix([models.number_operator(0, 1.0)], states))]
+    gpu = te_gpu.evolve(H, v, 3.0, 0.5, obs, tol=1e-8, m=40, fast_integration=True)
+    ref = oracle_lib.evolve(H, v, 3.0, 0.5, obs, tol=1e-8, m=40, fast_integration=True)
+    _compare(gpu, ref, 1e-8)
+
+
+def test_general_sparse_and_callback_observables(te_gpu, oracle_lib):
+    states, H = models.bose_hubbard(5, 5, 1.0, 2.0)
+    n = len(states)
+    v = _fock(states, [5, 0, 0, 0, 0])
+    hop = models.create_matrix([models.lin_interaction(0, 1, 0, 0, False, 1.0),
+                                models.lin_interaction(0, 1, 0, 0, True, 1.0)], states)
+    seen = []
+
+    def cb(state):
+        seen.append(np.vdot(state, state).real)
+        return float(np.abs(state[0]) ** 2)
+
+    gpu = te_gpu.evolve(H, v, 1.0, 0.1, [("sparse", hop), ("callback", cb)], tol=1e-8, m=20)
+    ref = oracle_lib.evolve(H, v, 1.0, 0.1, [("sparse", hop)], tol=1e-8, m=20)
+    assert np.max(np.abs(gpu["samples"][0] - ref["samples"][0])) < OBS_TOL
+    assert len(seen) == 11 and np.allclose(seen, 1.0, atol=1e-8)
+    i0 = models.index_of(states, [5, 0, 0, 0, 0])
+    assert abs(gpu["samples"][1][0] - 1.0) < 1e-12
+
+
+def test_stop_request(te_gpu, oracle_lib):
+    states, H = models.bose_hubbard(4, 4, 1.0, 2.0)
+    n = len(states)
+    v = np.zeros(n, dtype=np.complex128)
+    v[0] = 1
+    calls = []
+
+    def stopper(state):
+        calls.append(1)
+        if len(calls) == 6:
+            raise te_gpu.StopEvolution()
+        return 0.0
+
+    obs = [("sparse", o) for o in models.number_operator_observables(states)]
+    gpu = te_gpu.evolve(H, v, 2.0, 0.1, obs + [("callback", stopper)], tol=1e-8, m=20)
+    ref = oracle_lib.evolve(H, v, 2.0, 0.1, obs + [("stop", 5)], tol=1e-8, m=20)
+    assert gpu["status"] == ref["status"] == 3
+    assert gpu["num_samples"] == ref["num_samples"] == 5
+    assert abs(gpu["evolved_time"] - ref["evolved_time"]) < 1e-12
+    assert np.max(np.abs(gpu["samples"][:, :5] - ref["samples"][:, :5])) < OBS_TOL
+
+
+def test_invalid_inputs(te_gpu):
+    states, H = models.bose_hubbard(3, 3, 1.0, 2.0)
+    n = len(states)
+    M = te_gpu.Matrix.from_coo(n, H)
+    with pytest.raises(te_gpu.TeError) as e:
+        te_gpu.Evolver(M, np.ones(n, dtype=complex), 1.0, 0.1)
+    assert e.value.code == -4

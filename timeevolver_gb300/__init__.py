@@ -1,0 +1,267 @@
+"""timeevolver_gb300 -- Krylov real-time evolution exp(-iHt)v on one GB300.
+
+Python binding (ctypes) of the C ABI in include/tegpu.h, implemented by the
+hand-written sm_103a kernels in ``csrc/`` (built into ``_build/libtegpu.so``).
+The native library is required: every entry point raises if it is missing;
+there is no CPU fallback.
+
+Mirrors TimeEvolver's krylovTimeEvolver API (core/krylovTimeEvolver.h:56-68):
+``Evolver(H, v, t, sampling_step, observables, exp_factor, tol, m,
+fast_integration).time_evolve()`` returns the krylovReturn fields.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+LIB_PATH = _build.LIB_TEGPU
+
+TE_OK = 0
+ERRORS = {
+    -1: "invalid argument", -2: "CUDA error", -3: "invalid Hilbert-space dimension",
+    -4: "initial vector is not normalized", -5: "no small enough time step found to meet the tolerance",
+    -6: "Krylov eigensolver did not converge", -7: "incompatible dimensions", -8: "out of device memory",
+    -9: "unsupported size or parameter", -10: "device wait timed out",
+}
+STATUS = {0: "ok", 1: "lucky breakdown", 2: "analytic error below roundoff estimate", 3: "stopped by observable",
+          10: "roundoff may spoil the error", 11: "tolerance unreachable (roundoff)",
+          20: "quadrature inaccurate", 30: "norm drift", 100: "multiple warnings"}
+
+
+class TeParams(ctypes.Structure):
+    _fields_ = [("t", ctypes.c_double), ("sampling_step", ctypes.c_double), ("exp_factor", ctypes.c_double),
+                ("tol", ctypes.c_double), ("m", ctypes.c_int32), ("fast_integration", ctypes.c_int32),
+                ("progress_bar", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class TeResult(ctypes.Structure):
+    _fields_ = [("err", ctypes.c_double), ("evolved_time", ctypes.c_double), ("num_samples", ctypes.c_int64),
+                ("n_steps", ctypes.c_int64), ("dim", ctypes.c_int64), ("krylov_dim", ctypes.c_int64),
+                ("status", ctypes.c_int32), ("nb_err_roundoff", ctypes.c_int32), ("nb_err_int", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+class TeStepRecord(ctypes.Structure):
+    _fields_ = [("t_now", ctypes.c_double), ("t_step", ctypes.c_double), ("err_step", ctypes.c_double),
+                ("h", ctypes.c_double), ("m_eff", ctypes.c_int32), ("breakdown", ctypes.c_int32),
+                ("code", ctypes.c_int32), ("n_integrals", ctypes.c_int32)]
+
+
+OBSERVABLE_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int64,
+                                 ctypes.POINTER(ctypes.c_double))
+
+# every entry point of include/tegpu.h: name -> (restype, argtypes)
+_P = ctypes.c_void_p
+_I64, _I32, _D, _I = ctypes.c_int64, ctypes.c_int32, ctypes.c_double, ctypes.c_int
+SIGNATURES = {
+    "te_last_error": (ctypes.c_char_p, []),
+    "te_abi_version": (_I, []),
+    "te_set_device": (_I, [_I]),
+    "te_matrix_create_coo": (_I, [_I64, _I64, _I64, _P, _P, _P, _P]),
+    "te_matrix_create_csr": (_I, [_I64, _I64, _I64, _P, _P, _P, _I, _P]),
+    "te_matrix_destroy": (_I, [_P]),
+    "te_matrix_info": (_I, [_P, _P, _P, _P, _P, _P]),
+    "te_matrix_spmv": (_I, [_P, _D, _D, _P, _P, _P]),
+    "te_matrix_spmv_host": (_I, [_P, _D, _D, _P, _P]),
+    "te_evolver_create": (_I, [_P, _P, _P, _P]),
+    "te_evolver_destroy": (_I, [_P]),
+    "te_evolver_add_sparse_observable": (_I, [_P, _P]),
+    "te_evolver_add_vector_observable": (_I, [_P, _P]),
+    "te_evolver_add_callback_observable": (_I, [_P, OBSERVABLE_FN, _P]),
+    "te_evolver_run": (_I, [_P, _P]),
+    "te_evolver_samples": (_I, [_P, _I, _P, _I64]),
+    "te_evolver_state": (_I, [_P, _P]),
+    "te_evolver_state_device": (_I, [_P, _P]),
+    "te_evolver_trace": (_I, [_P, _P, _I64, _P]),
+    "te_evolver_launch_count": (_I64, [_P]),
+}
+
+_lib = None
+
+
+class TeError(RuntimeError):
+    def __init__(self, code, where):
+        msg = lib().te_last_error().decode(errors="replace")
+        super().__init__("%s failed: %s (%d) %s" % (where, ERRORS.get(code, "error"), code, msg))
+        self.code = code
+
+
+def build(force=False, verbose=False):
+    return _build.build_all(force=force, verbose=verbose)
+
+
+def lib():
+    """The loaded libtegpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libtegpu.so is missing (%s): run timeevolver_gb300.build() first; "
+                               "there is no CPU fallback" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc, where):
+    if rc != TE_OK:
+        raise TeError(rc, where)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Matrix:
+    """Device sparse matrix (TE::smatrix): from COO arrays (row, col, values)."""
+
+    def __init__(self, n, row, col, val, n_cols=None):
+        row = np.ascontiguousarray(row, dtype=np.uint64)
+        col = np.ascontiguousarray(col, dtype=np.uint64)
+        val = np.ascontiguousarray(val, dtype=np.complex128)
+        self.handle = ctypes.c_void_p()
+        self.n = int(n)
+        _check(lib().te_matrix_create_coo(self.n, int(n_cols or n), len(val), _ptr(row), _ptr(col), _ptr(val),
+                                          ctypes.byref(self.handle)), "te_matrix_create_coo")
+
+    @classmethod
+    def from_coo(cls, n, coo):
+        return cls(n, coo[0], coo[1], coo[2])
+
+    def info(self):
+        nr, nc, nnz, fl, n1 = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int(), ctypes.c_double()
+        _check(lib().te_matrix_info(self.handle, ctypes.byref(nr), ctypes.byref(nc), ctypes.byref(nnz),
+                                    ctypes.byref(fl), ctypes.byref(n1)), "te_matrix_info")
+        return dict(n_rows=nr.value, n_cols=nc.value, nnz=nnz.value, real=bool(fl.value & 1),
+                    diagonal=bool(fl.value & 2), norm1=n1.value)
+
+    def spmv(self, x, alpha=1.0):
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        y = np.zeros_like(x)
+        a = complex(alpha)
+        _check(lib().te_matrix_spmv_host(self.handle, a.real, a.imag, _ptr(x), _ptr(y)), "te_matrix_spmv_host")
+        return y
+
+    def close(self):
+        if self.handle:
+            lib().te_matrix_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Evolver:
+    """One time evolution (krylovTimeEvolver): construct, add observables, run.
+
+    ``observables`` entries: ("sparse", Matrix), ("vector", ndarray) or
+    ("callback", fn) where ``fn(state) -> float`` may raise StopEvolution
+    (requestStopException)."""
+
+    def __init__(self, H, v, t, sampling_step, observables=(), exp_factor=1.0, tol=1e-6, m=40,
+                 fast_integration=False):
+        self.H = H
+        self.n = H.n
+        v = np.ascontiguousarray(v, dtype=np.complex128)
+        p = TeParams(t, sampling_step, exp_factor, tol, int(m), int(bool(fast_integration)), 0, 0)
+        self.handle = ctypes.c_void_p()
+        _check(lib().te_evolver_create(H.handle, _ptr(v), ctypes.byref(p), ctypes.byref(self.handle)),
+               "te_evolver_create")
+        self.n_samples = int(np.floor(t / sampling_step)) + 1
+        self._keep = []
+        self.n_obs = 0
+        for kind, data in observables:
+            self.add(kind, data)
+
+    def add(self, kind, data):
+        if kind == "sparse":
+            _check(lib().te_evolver_add_sparse_observable(self.handle, data.handle), "add_sparse_observable")
+            self._keep.append(data)
+        elif kind == "vector":
+            o = np.ascontiguousarray(data, dtype=np.complex128)
+            _check(lib().te_evolver_add_vector_observable(self.handle, _ptr(o)), "add_vector_observable")
+        elif kind == "callback":
+            fn = data
+
+            def tramp(user, state, dim, out, fn=fn):
+                arr = np.ctypeslib.as_array(state, shape=(2 * dim,)).view(np.complex128)
+                try:
+                    out[0] = float(fn(arr))
+                    return 0
+                except StopEvolution:
+                    return 1
+
+            cb = OBSERVABLE_FN(tramp)
+            self._keep.append(cb)
+            _check(lib().te_evolver_add_callback_observable(self.handle, cb, None), "add_callback_observable")
+        else:
+            raise ValueError(kind)
+        self.n_obs += 1
+
+    def time_evolve(self, trace=False):
+        r = TeResult()
+        _check(lib().te_evolver_run(self.handle, ctypes.byref(r)), "te_evolver_run")
+        out = dict(err=r.err, evolved_time=r.evolved_time, num_samples=r.num_samples, n_steps=r.n_steps,
+                   dim=r.dim, krylov_dim=r.krylov_dim, status=r.status, nb_err_roundoff=r.nb_err_roundoff,
+                   nb_err_int=r.nb_err_int)
+        samples = np.zeros((self.n_obs, self.n_samples))
+        for i in range(self.n_obs):
+            _check(lib().te_evolver_samples(self.handle, i, _ptr(samples[i]), self.n_samples), "samples")
+        out["samples"] = samples
+        st = np.zeros(self.n, dtype=np.complex128)
+        _check(lib().te_evolver_state(self.handle, _ptr(st)), "state")
+        out["state"] = st
+        out["launches"] = lib().te_evolver_launch_count(self.handle)
+        if trace:
+            cnt = ctypes.c_int64()
+            lib().te_evolver_trace(self.handle, None, 0, ctypes.byref(cnt))
+            recs = (TeStepRecord * max(1, cnt.value))()
+            lib().te_evolver_trace(self.handle, recs, cnt.value, ctypes.byref(cnt))
+            out["trace"] = [dict(t_now=x.t_now, t_step=x.t_step, err_step=x.err_step, h=x.h, m_eff=x.m_eff,
+                                 breakdown=x.breakdown, code=x.code, n_integrals=x.n_integrals)
+                            for x in recs[:cnt.value]]
+        return out
+
+    def close(self):
+        if self.handle:
+            lib().te_evolver_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class StopEvolution(Exception):
+    """Raised by a callback observable to stop the evolution (requestStopException)."""
+
+
+def evolve(H_coo, v, t, sampling_step, observables=(), exp_factor=1.0, tol=1e-6, m=40, fast_integration=False,
+           trace=False):
+    """One-call evolution with COO inputs, mirroring the oracle's signature.
+
+    ``observables``: ("sparse", (row, col, val)), ("vector", o) or
+    ("callback", fn)."""
+    n = len(v)
+    H = Matrix.from_coo(n, H_coo)
+    obs = []
+    for kind, data in observables:
+        if kind == "sparse":
+            obs.append(("sparse", Matrix.from_coo(n, data)))
+        else:
+            obs.append((kind, data))
+    ev = Evolver(H, v, t, sampling_step, obs, exp_factor, tol, m, fast_integration)
+    try:
+        return ev.time_evolve(trace=trace)
+    finally:
+        ev.close()

@@ -1,0 +1,580 @@
+// te_evolver.cu -- host orchestration of one time evolution and its C ABI.
+//
+// Replaces the krylovTimeEvolver constructor (core/krylovTimeEvolver.cpp:26-84)
+// and timeEvolve() (:261-512).  The control flow of the reference's main loop
+// runs on the device (Lanczos coefficients, step-size search, sampling cursor
+// and status counters live in TeDevState); the host only enqueues one Krylov
+// step at a time (2m Lanczos passes, one Krylov-space kernel, one combine
+// pass, one observable pass), reads back a few scalars and decides whether a
+// further sample batch or step is needed.  Observables that cannot be fused
+// (non-diagonal sparse matrices, host callbacks) are evaluated per sample.
+#include <cfloat>
+#include <cstddef>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "te_internal.cuh"
+
+namespace {
+
+struct HostObs {
+  int kind;  // 0 fused diagonal, 1 fused vector, 2 general sparse, 3 callback
+  te_matrix O = nullptr;
+  double* diag_perm = nullptr;   // fused diagonal (permuted, Re)
+  double2* vec_perm = nullptr;   // fused vector (permuted)
+  te_observable_fn fn = nullptr;
+  void* user = nullptr;
+};
+
+// Scalars read back after every batch (prefix of TeDevState).
+struct Summary {
+  double t, sampling_step, tol, tol_rate, exp_factor, num_err_est;
+  int m_max, n_samples, integ_long, integ_short;
+  int max_batch, pad_c0, pad_c1, pad_c2;
+  double t_now, t_sampling, err, t_step;
+  int index_samples, n_steps, m_cur, status;
+  int err_code_find, nb_err_roundoff, nb_err_int, fatal;
+  int done, pad_p0, pad_p1, pad_p2;
+  double err_step, h;
+  int breakdown, m_eff, step_code, n_integrals;
+  int samples_in_batch, samples_pending, want_w, sample_base;
+};
+static_assert(sizeof(Summary) == offsetof(TeDevState, alpha), "summary must mirror the TeDevState prefix");
+
+}  // namespace
+
+struct te_evolver_s {
+  te_matrix H = nullptr;
+  int device = 0;
+  cudaStream_t st = nullptr;
+  te_params p{};
+  int64_t n = 0;
+  int m = 0;
+  int64_t n_samples = 0;
+  TeDevState* ds = nullptr;
+  Summary* sum = nullptr;  // pinned
+  double2* slab = nullptr;  // m basis columns + spare start vector + w + sampled state
+  double2* cols[TE_MMAX + 1] = {};
+  double2* spare = nullptr;
+  double2* w = nullptr;
+  double2* sampled = nullptr;
+  double2* batch = nullptr;  // max_batch samples
+  double2* orig_tmp = nullptr;  // original-order copy for general/callback observables
+  double* partials = nullptr;
+  double* results = nullptr;  // n_obs x n_samples
+  int max_batch = 1;
+  std::vector<HostObs> obs;
+  std::vector<te_step_record> trace;
+  te_result res{};
+  bool ran = false;
+  int64_t launches = 0;
+  double2* host_state = nullptr;  // pinned buffer for callbacks
+};
+
+namespace {
+
+const size_t kPartials = (size_t)TE_SCAP * TE_FUSED_VALS * 8 * 1024;
+
+int read_summary(te_evolver ev) {
+  TE_CUDA(cudaMemcpyAsync(ev->sum, ev->ds, sizeof(Summary), cudaMemcpyDeviceToHost, ev->st));
+  TE_CUDA(cudaStreamSynchronize(ev->st));
+  return TE_OK;
+}
+
+// Observables of the current batch: fused reductions on the device, then the
+// per-sample general / callback observables.  *stop_at receives the batch
+// index of a stop request (or -1).
+int process_batch(te_evolver ev, int* stop_at, bool synced) {
+  *stop_at = -1;
+  // fused passes (up to 16 diagonal + 8 vector observables per pass)
+  std::vector<const HostObs*> dg, vc;
+  std::vector<int> dgi, vci;
+  for (size_t i = 0; i < ev->obs.size(); ++i) {
+    if (ev->obs[i].kind == 0) {
+      dg.push_back(&ev->obs[i]);
+      dgi.push_back((int)i);
+    } else if (ev->obs[i].kind == 1) {
+      vc.push_back(&ev->obs[i]);
+      vci.push_back((int)i);
+    }
+  }
+  size_t id = 0, iv = 0;
+  while (id < dg.size() || iv < vc.size()) {
+    TeFusedObs f{};
+    while (id < dg.size() && f.n_diag < TE_FUSED_DIAG) {
+      f.diag[f.n_diag] = dg[id]->diag_perm;
+      f.row_diag[f.n_diag++] = dgi[id];
+      ++id;
+    }
+    while (iv < vc.size() && f.n_vec < TE_FUSED_VEC) {
+      f.vec[f.n_vec] = vc[iv]->vec_perm;
+      f.row_vec[f.n_vec++] = vci[iv];
+      ++iv;
+    }
+    te_launch_fused_obs(ev->n, ev->batch, f, ev->ds, ev->partials, ev->results, (int)ev->n_samples, ev->st);
+    ++ev->launches;
+  }
+  bool need_host = false;
+  for (auto& o : ev->obs) need_host |= (o.kind == 2 || o.kind == 3);
+  if (!need_host) return TE_OK;
+  if (!synced) {
+    int rc = read_summary(ev);
+    if (rc != TE_OK) return rc;
+  }
+  const int S = ev->sum->samples_in_batch;
+  for (int s = 0; s < S; ++s) {
+    te_launch_permute(ev->n, ev->H->sell.iperm, ev->batch + (int64_t)s * ev->n, ev->orig_tmp, ev->st);
+    ++ev->launches;
+    for (size_t i = 0; i < ev->obs.size(); ++i) {
+      HostObs& o = ev->obs[i];
+      if (o.kind == 2) {
+        te_launch_general_obs(*o.O, ev->orig_tmp, ev->ds, s, ev->partials, ev->results + i * ev->n_samples, ev->st);
+        ++ev->launches;
+      } else if (o.kind == 3) {
+        TE_CUDA(cudaMemcpyAsync(ev->host_state, ev->orig_tmp, sizeof(double2) * ev->n, cudaMemcpyDeviceToHost,
+                                ev->st));
+        TE_CUDA(cudaStreamSynchronize(ev->st));
+        double value = 0.0;
+        int stop = o.fn(o.user, reinterpret_cast<const double*>(ev->host_state), ev->n, &value);
+        if (stop) {
+          *stop_at = s;
+          return TE_OK;
+        }
+        TE_CUDA(cudaMemcpyAsync(ev->results + i * ev->n_samples + ev->sum->sample_base + s, &value, sizeof(double),
+                                cudaMemcpyHostToDevice, ev->st));
+        TE_CUDA(cudaStreamSynchronize(ev->st));
+      }
+    }
+  }
+  return TE_OK;
+}
+
+void free_evolver(te_evolver ev) {
+  if (!ev) return;
+  cudaFree(ev->ds);
+  cudaFreeHost(ev->sum);
+  cudaFreeHost(ev->host_state);
+  cudaFree(ev->slab);
+  cudaFree(ev->batch);
+  cudaFree(ev->orig_tmp);
+  cudaFree(ev->partials);
+  cudaFree(ev->results);
+  for (auto& o : ev->obs) {
+    cudaFree(o.diag_perm);
+    cudaFree(o.vec_perm);
+  }
+  if (ev->st) cudaStreamDestroy(ev->st);
+  delete ev;
+}
+
+int alloc_results(te_evolver ev) {
+  cudaFree(ev->results);
+  ev->results = nullptr;
+  size_t count = std::max<size_t>(1, ev->obs.size()) * (size_t)ev->n_samples;
+  TE_CUDA(cudaMalloc(&ev->results, sizeof(double) * count));
+  TE_CUDA(cudaMemset(ev->results, 0, sizeof(double) * count));
+  return TE_OK;
+}
+
+int run(te_evolver ev, te_result* out) {
+  const int64_t n = ev->n;
+  cudaStream_t st = ev->st;
+  ev->launches = 0;
+  ev->trace.clear();
+  bool need_host = false;
+  for (auto& o : ev->obs) need_host |= (o.kind == 2 || o.kind == 3);
+  ev->max_batch = need_host ? 1 : (int)std::max<int64_t>(1, std::min<int64_t>(TE_SCAP, ((int64_t)256 << 20) / (16 * n)));
+  cudaFree(ev->batch);
+  ev->batch = nullptr;
+  TE_CUDA(cudaMalloc(&ev->batch, sizeof(double2) * n * ev->max_batch));
+  int rc = alloc_results(ev);
+  if (rc != TE_OK) return rc;
+
+  // ---- initial device state (constructor + the first lines of timeEvolve)
+  TeDevState* hs = new TeDevState();
+  std::memset(hs, 0, sizeof(TeDevState));
+  hs->t = ev->p.t;
+  hs->sampling_step = ev->p.sampling_step;
+  hs->tol = ev->p.tol;
+  hs->tol_rate = ev->p.tol / ev->p.t;                                            // :287
+  hs->exp_factor = ev->p.exp_factor;
+  hs->num_err_est = (double)n * ev->H->norm1 * DBL_EPSILON;                      // :289
+  hs->m_max = ev->m;
+  hs->n_samples = (int)ev->n_samples;
+  hs->integ_long = ev->p.fast_integration ? 0 : 2;                               // :269-277
+  hs->integ_short = ev->p.fast_integration ? 1 : 2;
+  hs->max_batch = ev->max_batch;
+  hs->t_step = 0.1;                                                              // :285
+  hs->m_cur = ev->m;
+  hs->m_eff = ev->m;
+  hs->s[0] = 1.0;
+  // initial sample (:306-313): psi = v, one output with coefficient 1 on u_0
+  hs->samples_in_batch = 1;
+  hs->sample_base = 0;
+  hs->index_samples = 1;
+  hs->want_w = 0;
+  hs->Y[1 * TE_MMAX + 0] = make_double2(1.0, 0.0);
+  hs->n_steps = ev->n_samples > 1 ? 1 : 0;
+  hs->done = ev->n_samples > 1 ? 0 : 1;
+  rc = te_cuda_check(cudaMemcpyAsync(ev->ds, hs, sizeof(TeDevState), cudaMemcpyHostToDevice, st), "state upload");
+  TE_CUDA(cudaStreamSynchronize(st));
+  delete hs;
+  if (rc != TE_OK) return rc;
+
+  TeCombineArgs ca{};
+  ca.n = n;
+  ca.w_out = ev->spare;
+  ca.sample_out = ev->batch;
+  ca.m = 1;
+  ca.cols[0] = ev->cols[0];
+  te_launch_combine(ca, ev->ds, ev->sampled, st);
+  ++ev->launches;
+  int stop_at = -1;
+  rc = process_batch(ev, &stop_at, false);
+  if (rc != TE_OK) return rc;
+  TE_CUDA(cudaGetLastError());
+  rc = read_summary(ev);
+  if (rc != TE_OK) return rc;
+  Summary* S = ev->sum;
+  te_result r{};
+  r.dim = n;
+  if (stop_at >= 0) {  // stop requested at t = 0: plain return, status 0 (:309-313)
+    r.krylov_dim = ev->m;
+    r.num_samples = 0;
+    *out = r;
+    return TE_OK;
+  }
+
+  int m = ev->m;
+  double err_prev = 0.0, t_prev = 0.0;
+  int64_t guard = 0;
+  while (!S->done) {
+    if (S->fatal) break;
+    if (++guard > ((int64_t)1 << 40)) break;
+    t_prev = S->t_now;
+    err_prev = S->err;
+    // STEP 1: Lanczos (:338)
+    for (int j = 0; j < m; ++j) {
+      te_launch_lanczos_apply(ev->H->sell, ev->H->is_real, ev->cols[j], j > 0 ? ev->cols[j - 1] : nullptr, ev->w,
+                              ev->ds, ev->partials, j, st);
+      te_launch_lanczos_update(n, ev->w, ev->cols[j], j + 1 < m ? ev->cols[j + 1] : nullptr, ev->ds, ev->partials, j,
+                               st);
+      ev->launches += 2;
+    }
+    // STEP 1b-3: Krylov-space kernel (eigen data, step search, w, first batch)
+    te_launch_krylov_step(ev->ds, st);
+    ++ev->launches;
+    for (int j = 0; j < m; ++j) ca.cols[j] = ev->cols[j];
+    ca.m = m;
+    ca.w_out = ev->spare;
+    te_launch_combine(ca, ev->ds, ev->sampled, st);
+    ++ev->launches;
+    rc = process_batch(ev, &stop_at, false);
+    if (rc != TE_OK) return rc;
+    rc = read_summary(ev);
+    if (rc != TE_OK) return rc;
+    if (S->fatal) break;
+    // the combine pass above used the step's own m (m_eff on a breakdown)
+    te_step_record rec{};
+    rec.t_now = t_prev;
+    rec.t_step = S->t_step;
+    rec.err_step = S->err_step;
+    rec.h = S->h;
+    rec.m_eff = S->m_eff;
+    rec.breakdown = S->breakdown;
+    rec.code = S->breakdown ? 0 : S->err_code_find;
+    rec.n_integrals = S->n_integrals;
+    ev->trace.push_back(rec);
+    const bool produced_w = S->want_w != 0;
+    while (stop_at < 0 && S->samples_pending && !S->fatal) {
+      te_launch_schedule_samples(ev->ds, st);
+      ++ev->launches;
+      ca.w_out = ev->spare;
+      te_launch_combine(ca, ev->ds, ev->sampled, st);
+      ++ev->launches;
+      rc = process_batch(ev, &stop_at, false);
+      if (rc != TE_OK) return rc;
+      rc = read_summary(ev);
+      if (rc != TE_OK) return rc;
+    }
+    if (S->fatal) break;
+    if (stop_at >= 0) {
+      // stopped by an observable (:423-436): status 3, time and error of the step start
+      r.err = err_prev;
+      r.evolved_time = t_prev;
+      r.num_samples = S->sample_base + stop_at;
+      r.n_steps = S->n_steps;
+      r.krylov_dim = S->m_cur;
+      r.status = TE_STATUS_STOPPED;
+      r.nb_err_roundoff = S->nb_err_roundoff;
+      r.nb_err_int = S->nb_err_int;
+      *out = r;
+      return TE_OK;
+    }
+    if (produced_w) std::swap(ev->cols[0], ev->spare);
+    m = S->m_cur;
+  }
+  if (S->fatal) {
+    te_set_error("device-side failure %d during the evolution (%s)", S->fatal,
+                 S->fatal == TE_ERR_NO_STEP ? "no small enough time step found to meet the tolerance"
+                                            : S->fatal == TE_ERR_EIGEN ? "Krylov eigensolver did not converge"
+                                                                       : "step search limit");
+    return S->fatal;
+  }
+  // final checks (:445-504)
+  te_launch_norm2(n, ev->sampled, ev->partials, ev->ds, st);
+  ++ev->launches;
+  double norm2 = 0.0;
+  TE_CUDA(cudaMemcpyAsync(&norm2, &ev->ds->norm2_final, sizeof(double), cudaMemcpyDeviceToHost, st));
+  TE_CUDA(cudaStreamSynchronize(st));
+  int status = S->status;
+  int nbErrors = 0;
+  if (std::fabs(std::sqrt(norm2) - 1.0) > ev->p.tol) {
+    nbErrors++;
+    status = TE_STATUS_NORM;
+  }
+  const double numErrTotal = S->num_err_est * S->n_steps;
+  if (S->nb_err_roundoff != 0) {
+    nbErrors++;
+    status = TE_STATUS_ROUNDOFF;
+  }
+  if (S->nb_err_int != 0) {
+    nbErrors++;
+    status = TE_STATUS_INTEGRATION;
+  }
+  if (numErrTotal > S->err && S->nb_err_roundoff == 0) {
+    if (numErrTotal > ev->p.tol) {
+      status = TE_STATUS_ROUNDOFF_TOTAL;
+      nbErrors++;
+    } else if (status != TE_STATUS_LUCKY_BREAKDOWN) {
+      status = TE_STATUS_BELOW_ROUNDOFF;
+    }
+  }
+  if (nbErrors > 1) status = TE_STATUS_MULTIPLE;
+  r.err = S->err;
+  r.evolved_time = S->t_now;
+  r.num_samples = S->index_samples;
+  r.n_steps = S->n_steps;
+  r.krylov_dim = S->m_cur;
+  r.status = status;
+  r.nb_err_roundoff = S->nb_err_roundoff;
+  r.nb_err_int = S->nb_err_int;
+  *out = r;
+  return TE_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI
+
+extern "C" int te_evolver_create(te_matrix H, const double* v_host, const te_params* params, te_evolver* out) {
+  if (!H || !v_host || !params || !out) {
+    te_set_error("te_evolver_create: invalid arguments");
+    return TE_ERR_INVALID_ARG;
+  }
+  if (H->n_rows == 0) {
+    te_set_error("Invalid Hilbertspace dimension");
+    return TE_ERR_EMPTY;
+  }
+  if (H->n_rows != H->n_cols) {
+    te_set_error("te_evolver_create: the Hamiltonian must be square");
+    return TE_ERR_INVALID_ARG;
+  }
+  const te_params& p = *params;
+  if (!(p.t > 0.0) || !(p.sampling_step > 0.0) || !(p.tol > 0.0) || p.m < 1 || !std::isfinite(p.exp_factor)) {
+    te_set_error("te_evolver_create: t, sampling_step, tol must be positive and m >= 1");
+    return TE_ERR_INVALID_ARG;
+  }
+  const int64_t n = H->n_rows;
+  const int m = (int)std::min<int64_t>(p.m, n);  // :35
+  if (m > TE_MMAX) {
+    te_set_error("te_evolver_create: Krylov dimension %d above the supported %d", m, TE_MMAX);
+    return TE_ERR_UNSUPPORTED;
+  }
+  // normalisation check (:45-48), host-side on the caller's vector
+  double nrm = 0.0;
+  for (int64_t i = 0; i < 2 * n; ++i) nrm += v_host[i] * v_host[i];
+  if (std::fabs(std::sqrt(nrm) - 1.0) > p.tol) {
+    te_set_error("Initial vector is not normalized");
+    return TE_ERR_NOT_NORMALIZED;
+  }
+  const double ns = std::floor(p.t / p.sampling_step) + 1.0;  // :57
+  if (!(ns < 2e9)) {
+    te_set_error("te_evolver_create: too many samples");
+    return TE_ERR_UNSUPPORTED;
+  }
+  int rc = te_upload_quad_tables();
+  if (rc != TE_OK) return rc;
+  te_evolver ev = new te_evolver_s();
+  ev->H = H;
+  ev->p = p;
+  ev->n = n;
+  ev->m = m;
+  ev->n_samples = (int64_t)ns;
+  cudaGetDevice(&ev->device);
+  auto fail = [&](int code) {
+    free_evolver(ev);
+    return code;
+  };
+  if ((rc = te_cuda_check(cudaStreamCreateWithFlags(&ev->st, cudaStreamNonBlocking), "stream")) != TE_OK)
+    return fail(rc);
+  if ((rc = te_cuda_check(cudaMalloc(&ev->ds, sizeof(TeDevState)), "state")) != TE_OK) return fail(rc);
+  if ((rc = te_cuda_check(cudaMemset(ev->ds, 0, sizeof(TeDevState)), "state")) != TE_OK) return fail(rc);
+  if ((rc = te_cuda_check(cudaMallocHost(&ev->sum, sizeof(Summary)), "pinned")) != TE_OK) return fail(rc);
+  // basis columns, spare start vector, w, sampled state
+  if ((rc = te_cuda_check(cudaMalloc(&ev->slab, sizeof(double2) * n * (m + 3)), "Krylov basis")) != TE_OK)
+    return fail(rc);
+  for (int j = 0; j < m; ++j) ev->cols[j] = ev->slab + (int64_t)j * n;
+  ev->spare = ev->slab + (int64_t)m * n;
+  ev->w = ev->slab + (int64_t)(m + 1) * n;
+  ev->sampled = ev->slab + (int64_t)(m + 2) * n;
+  if ((rc = te_cuda_check(cudaMalloc(&ev->partials, sizeof(double) * kPartials), "partials")) != TE_OK)
+    return fail(rc);
+  if ((rc = te_cuda_check(cudaMalloc(&ev->orig_tmp, sizeof(double2) * n), "tmp")) != TE_OK) return fail(rc);
+  // v (original order) -> permuted start vector
+  if ((rc = te_cuda_check(cudaMemcpy(ev->orig_tmp, v_host, sizeof(double2) * n, cudaMemcpyHostToDevice), "H2D")) !=
+      TE_OK)
+    return fail(rc);
+  te_launch_permute(n, H->sell.perm, ev->orig_tmp, ev->cols[0], ev->st);
+  if ((rc = te_cuda_check(cudaStreamSynchronize(ev->st), "permute")) != TE_OK) return fail(rc);
+  *out = ev;
+  return TE_OK;
+}
+
+extern "C" int te_evolver_destroy(te_evolver ev) {
+  free_evolver(ev);
+  return TE_OK;
+}
+
+extern "C" int te_evolver_add_sparse_observable(te_evolver ev, te_matrix O) {
+  if (!ev || !O) {
+    te_set_error("te_evolver_add_sparse_observable: invalid arguments");
+    return TE_ERR_INVALID_ARG;
+  }
+  if (O->n_rows != ev->n || O->n_cols != ev->n) {
+    te_set_error("Incompatible dimensions");
+    return TE_ERR_DIM;
+  }
+  HostObs o;
+  if (O->is_diag) {
+    o.kind = 0;
+    TE_CUDA(cudaMalloc(&o.diag_perm, sizeof(double) * ev->n));
+    // permuted Re(diagonal): gather through the permutation of H
+    double2* dc = nullptr;
+    TE_CUDA(cudaMalloc(&dc, sizeof(double2) * ev->n));
+    te_launch_permute(ev->n, ev->H->sell.perm, O->diag_c, dc, ev->st);
+    std::vector<double2> h(ev->n);
+    TE_CUDA(cudaMemcpyAsync(h.data(), dc, sizeof(double2) * ev->n, cudaMemcpyDeviceToHost, ev->st));
+    TE_CUDA(cudaStreamSynchronize(ev->st));
+    cudaFree(dc);
+    std::vector<double> re(ev->n);
+    for (int64_t i = 0; i < ev->n; ++i) re[i] = h[i].x;
+    TE_CUDA(cudaMemcpy(o.diag_perm, re.data(), sizeof(double) * ev->n, cudaMemcpyHostToDevice));
+  } else {
+    o.kind = 2;
+    o.O = O;
+  }
+  ev->obs.push_back(o);
+  return TE_OK;
+}
+
+extern "C" int te_evolver_add_vector_observable(te_evolver ev, const double* o_host) {
+  if (!ev || !o_host) {
+    te_set_error("te_evolver_add_vector_observable: invalid arguments");
+    return TE_ERR_INVALID_ARG;
+  }
+  HostObs o;
+  o.kind = 1;
+  TE_CUDA(cudaMalloc(&o.vec_perm, sizeof(double2) * ev->n));
+  TE_CUDA(cudaMemcpy(ev->orig_tmp, o_host, sizeof(double2) * ev->n, cudaMemcpyHostToDevice));
+  te_launch_permute(ev->n, ev->H->sell.perm, ev->orig_tmp, o.vec_perm, ev->st);
+  TE_CUDA(cudaStreamSynchronize(ev->st));
+  ev->obs.push_back(o);
+  return TE_OK;
+}
+
+extern "C" int te_evolver_add_callback_observable(te_evolver ev, te_observable_fn fn, void* user) {
+  if (!ev || !fn) {
+    te_set_error("te_evolver_add_callback_observable: invalid arguments");
+    return TE_ERR_INVALID_ARG;
+  }
+  if (!ev->host_state) TE_CUDA(cudaMallocHost(&ev->host_state, sizeof(double2) * ev->n));
+  HostObs o;
+  o.kind = 3;
+  o.fn = fn;
+  o.user = user;
+  ev->obs.push_back(o);
+  return TE_OK;
+}
+
+extern "C" int te_evolver_run(te_evolver ev, te_result* result) {
+  if (!ev) {
+    te_set_error("te_evolver_run: null evolver");
+    return TE_ERR_INVALID_ARG;
+  }
+  if (ev->ran) {
+    te_set_error("te_evolver_run: an evolver runs once (as timeEvolve)");
+    return TE_ERR_INVALID_ARG;
+  }
+  ev->ran = true;
+  te_result r{};
+  int rc = run(ev, &r);
+  if (rc == TE_OK) rc = te_cuda_check(cudaGetLastError(), "evolution");
+  if (rc != TE_OK) return rc;
+  ev->res = r;
+  if (result) *result = r;
+  return TE_OK;
+}
+
+extern "C" int te_evolver_samples(te_evolver ev, int obs_index, double* out_host, int64_t count) {
+  if (!ev || !out_host || obs_index < 0 || obs_index >= (int)ev->obs.size() || count < 0) {
+    te_set_error("te_evolver_samples: invalid arguments");
+    return TE_ERR_INVALID_ARG;
+  }
+  if (!ev->results) {
+    te_set_error("te_evolver_samples: the evolver has not run");
+    return TE_ERR_INVALID_ARG;
+  }
+  const int64_t k = std::min<int64_t>(count, ev->n_samples);
+  TE_CUDA(cudaMemcpy(out_host, ev->results + (int64_t)obs_index * ev->n_samples, sizeof(double) * k,
+                     cudaMemcpyDeviceToHost));
+  for (int64_t i = k; i < count; ++i) out_host[i] = 0.0;
+  return TE_OK;
+}
+
+extern "C" int te_evolver_state(te_evolver ev, double* out_host) {
+  if (!ev || !out_host) {
+    te_set_error("te_evolver_state: invalid arguments");
+    return TE_ERR_INVALID_ARG;
+  }
+  // last sampled state, back to the caller's ordering
+  te_launch_permute(ev->n, ev->H->sell.iperm, ev->sampled, ev->orig_tmp, ev->st);
+  TE_CUDA(cudaMemcpyAsync(out_host, ev->orig_tmp, sizeof(double2) * ev->n, cudaMemcpyDeviceToHost, ev->st));
+  TE_CUDA(cudaStreamSynchronize(ev->st));
+  return TE_OK;
+}
+
+extern "C" int te_evolver_state_device(te_evolver ev, const double** out_dev) {
+  if (!ev || !out_dev) {
+    te_set_error("te_evolver_state_device: invalid arguments");
+    return TE_ERR_INVALID_ARG;
+  }
+  te_launch_permute(ev->n, ev->H->sell.iperm, ev->sampled, ev->orig_tmp, ev->st);
+  TE_CUDA(cudaStreamSynchronize(ev->st));
+  *out_dev = reinterpret_cast<const double*>(ev->orig_tmp);
+  return TE_OK;
+}
+
+extern "C" int te_evolver_trace(te_evolver ev, te_step_record* out, int64_t max_records, int64_t* n_records) {
+  if (!ev) {
+    te_set_error("te_evolver_trace: null evolver");
+    return TE_ERR_INVALID_ARG;
+  }
+  const int64_t k = std::min<int64_t>(max_records, (int64_t)ev->trace.size());
+  if (out && k > 0) std::memcpy(out, ev->trace.data(), sizeof(te_step_record) * k);
+  if (n_records) *n_records = (int64_t)ev->trace.size();
+  return TE_OK;
+}
+
+extern "C" int64_t te_evolver_launch_count(te_evolver ev) { return ev ? ev->launches : 0; }

@@ -1,0 +1,149 @@
+// te_internal.cuh -- shared declarations of the libtegpu CUDA translation units.
+//
+// Data layout in HBM for one evolution (n = Hilbert dimension, m = Krylov dim):
+//   H in SELL-32 form, rows sorted by length (descending, stable) and the basis
+//     renumbered in that order: chunk c holds rows 32c..32c+31 of the permuted
+//     matrix; slot (c, k, lane) = chunk_off[c] + 32 k + lane holds the k-th
+//     entry of row 32c+lane (padding: value 0, column = the row itself);
+//     values double (real matrices) or double2 (complex), columns int32;
+//   every n-vector (Krylov vectors, w, start vector, sampled state) is kept in
+//     the permuted basis, double2 per entry, contiguous;
+//   Krylov basis: u_0..u_{m-1}, unnormalised (v_j = s_j u_j, s_j = 1/beta_j);
+//   TeDevState: the scalar state of the evolution (coefficients, step
+//     control, sampling cursor, reduction counters), written only by kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/tegpu.h"
+
+#define TE_MMAX 64
+#define TE_THREADS 256
+#define TE_SCAP 16            // samples scheduled per batch (coefficient slots)
+#define TE_NCHEB 256          // largest Chebyshev degree kept for exp(-ixT) e_1
+#define TE_TS_KMAX 8          // tanh-sinh refinement levels 0..8
+#define TE_TS_KMIN 2
+#define TE_TS_NODES 769       // nodes with t >= 0 over levels 0..8
+#define TE_FUSED_DIAG 16      // diagonal observables per fused reduction pass
+#define TE_FUSED_VEC 8        // vector observables per fused reduction pass
+#define TE_FUSED_VALS (TE_FUSED_DIAG + 2 * TE_FUSED_VEC)
+
+// Tanh-sinh and Gauss-Legendre tables (host-computed, uploaded once).
+struct TeQuadTables {
+  double ts_u[TE_TS_NODES];     // tanh(pi/2 sinh t)
+  double ts_w[TE_TS_NODES];     // pi/2 cosh t / cosh^2(pi/2 sinh t)
+  double ts_t[TE_TS_NODES];
+  int ts_level_begin[TE_TS_KMAX + 2];
+  double g15_x[15], g15_w[15];
+  double g7_x[7], g7_w[7];
+};
+
+// Scalar state of one evolution, resident in device memory.
+struct TeDevState {
+  // constants
+  double t, sampling_step, tol, tol_rate, exp_factor, num_err_est;
+  int m_max, n_samples, integ_long, integ_short;
+  int max_batch, pad_c0, pad_c1, pad_c2;
+  // progress
+  double t_now, t_sampling, err, t_step;
+  int index_samples, n_steps, m_cur, status;
+  int err_code_find, nb_err_roundoff, nb_err_int, fatal;  // fatal: TE_ERR_* raised on the device
+  int done, pad_p0, pad_p1, pad_p2;
+  // current step
+  double err_step, h;
+  int breakdown, m_eff, step_code, n_integrals;
+  int samples_in_batch, samples_pending, want_w, sample_base;
+  // Lanczos coefficients of the current step
+  double2 alpha[TE_MMAX];
+  double beta[TE_MMAX + 1];
+  double s[TE_MMAX + 1];
+  // coefficients for psi = sum_j u_j y_j: slot 0 = w(t_step), slots 1.. = samples
+  double2 Y[(TE_SCAP + 1) * TE_MMAX];
+  double sample_dt[TE_SCAP];
+  // Krylov matrix T (real symmetric tridiagonal) and its exponential data
+  double d[TE_MMAX], e[TE_MMAX];
+  double cheb_c, cheb_rho;
+  int cheb_n, eig_valid;      // Chebyshev vectors computed up to degree cheb_n
+  double eig_lam[TE_MMAX];    // eigen-decomposition T = Q diag(lam) Q^T (fallback path)
+  double eig_Q[TE_MMAX * TE_MMAX];
+  double cheb_t[(TE_NCHEB + 1) * TE_MMAX];  // t_n = T_n((T - c)/rho) e_1, row n
+  // reduction counters ("last block finishes" pattern)
+  unsigned int counter[4];
+  double norm2_final;  // ||sampledState||^2 of the final norm check
+};
+
+// SELL-32 matrix in the sorted (permuted) basis.
+struct TeSell {
+  int64_t n = 0;          // rows = cols
+  int64_t n_chunks = 0;
+  int64_t slots = 0;      // 32 * sum of chunk lengths
+  int64_t* chunk_off = nullptr;
+  int32_t* col = nullptr;
+  double* val = nullptr;  // real: slots doubles; complex: 2*slots doubles
+  int32_t* perm = nullptr;   // permuted index -> original index
+  int32_t* iperm = nullptr;  // original index -> permuted index
+};
+
+struct te_matrix_s {
+  int64_t n_rows = 0, n_cols = 0, nnz = 0;
+  bool is_real = false, is_diag = false;
+  double norm1 = 0.0;
+  // original-order CSR (general observables, public spmv)
+  int32_t* row_ptr = nullptr;
+  int32_t* col = nullptr;
+  double* val = nullptr;
+  double* diag_re = nullptr;  // diagonal matrices: Re of the diagonal, original order
+  double2* diag_c = nullptr;  // diagonal matrices: the diagonal, original order
+  TeSell sell;                // square matrices only
+  int device = 0;
+};
+
+// error reporting
+void te_set_error(const char* fmt, ...);
+int te_cuda_check(cudaError_t e, const char* what);
+#define TE_CUDA(call)                                      \
+  do {                                                     \
+    int _rc = te_cuda_check((call), #call);                \
+    if (_rc != TE_OK) return _rc;                          \
+  } while (0)
+
+// launch shapes
+int te_num_sms();
+int te_grid_for(int64_t n_items, int threads, int blocks_per_sm);
+
+// ---------------------------------------------------------------- launches
+// te_matrix.cu
+void te_launch_sell_spmv(const TeSell& A, bool is_real, double2 alpha, const double2* x_perm, double2* y_perm,
+                         cudaStream_t st);
+void te_launch_csr_spmv(const te_matrix_s& A, double2 alpha, const double2* x, double2* y, cudaStream_t st);
+void te_launch_permute(int64_t n, const int32_t* idx, const double2* in, double2* out, cudaStream_t st);
+// te_lanczos.cu
+void te_launch_lanczos_apply(const TeSell& A, bool is_real, const double2* u_j, const double2* u_jm1, double2* w,
+                             TeDevState* ds, double* partials, int j, cudaStream_t st);
+void te_launch_lanczos_update(int64_t n, const double2* w, const double2* u_j, double2* u_jp1, TeDevState* ds,
+                              double* partials, int j, cudaStream_t st);
+// te_krylov.cu
+int te_upload_quad_tables();
+void te_launch_krylov_step(TeDevState* ds, cudaStream_t st);
+void te_launch_schedule_samples(TeDevState* ds, cudaStream_t st);
+// te_sample.cu
+struct TeCombineArgs {
+  const double2* cols[TE_MMAX];
+  int m;
+  int64_t n;
+  double2* w_out;         // new start vector (when the step produced w)
+  double2* sample_out;    // batch buffer: sample s at sample_out + s * n
+};
+void te_launch_combine(const TeCombineArgs& a, TeDevState* ds, double2* last_out, cudaStream_t st);
+struct TeFusedObs {
+  const double* diag[TE_FUSED_DIAG];  // permuted real diagonals
+  const double2* vec[TE_FUSED_VEC];   // permuted vectors
+  int row_diag[TE_FUSED_DIAG];        // observable index (row of the result table)
+  int row_vec[TE_FUSED_VEC];
+  int n_diag, n_vec;
+};
+void te_launch_fused_obs(int64_t n, const double2* psi, const TeFusedObs& f, TeDevState* ds, double* partials,
+                         double* results, int n_samples_total, cudaStream_t st);
+void te_launch_general_obs(const te_matrix_s& O, const double2* psi_orig, TeDevState* ds, int sample_in_batch,
+                           double* partials, double* results_row, cudaStream_t st);
+void te_launch_norm2(int64_t n, const double2* x, double* partials, TeDevState* ds, cudaStream_t st);

@@ -1,0 +1,70 @@
+// te_reduce.cuh -- deterministic block and grid reductions.
+//
+// Grid reductions use the "last block finishes" pattern: every block writes
+// its partial sums to partials[value * gridDim.x + block], fences, and bumps a
+// counter; the block that brings the counter to gridDim.x sums all partials in
+// a fixed order (thread t takes blocks t, t+blockDim, ... sequentially, then a
+// fixed tree), so the result does not depend on which block finished last.
+#pragma once
+#include "te_internal.cuh"
+
+__device__ __forceinline__ double te_warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block sum of NV values per thread; result valid in thread 0.  scratch must
+// hold NV * 32 doubles.
+template <int NV>
+__device__ __forceinline__ void te_block_sum(double (&v)[NV], double* scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = te_warp_sum(v[k]);
+  __syncthreads();
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) scratch[k * 32 + warp] = v[k];
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double x = lane < nw ? scratch[k * 32 + lane] : 0.0;
+      v[k] = te_warp_sum(x);
+    }
+  }
+  __syncthreads();
+}
+
+// Publish NV per-block partials and return true in the block that must do
+// the final reduction.  Call from all threads; thread 0 holds the values.
+template <int NV>
+__device__ __forceinline__ bool te_publish_partials(const double (&v)[NV], double* partials, unsigned int* counter) {
+  __shared__ bool is_last;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) partials[k * gridDim.x + blockIdx.x] = v[k];
+    __threadfence();
+    unsigned int prev = atomicAdd(counter, 1u);
+    is_last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (is_last) __threadfence();
+  return is_last;
+}
+
+// In the last block: sum the partials of NV values over all blocks in a fixed
+// order.  Result valid in thread 0; resets the counter.
+template <int NV>
+__device__ __forceinline__ void te_final_sum(double (&out)[NV], const double* partials, unsigned int* counter,
+                                             double* scratch) {
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += __ldcg(partials + k * gridDim.x + b);
+    out[k] = s;
+  }
+  te_block_sum<NV>(out, scratch);
+  if (threadIdx.x == 0) *counter = 0u;
+}

@@ -1,0 +1,63 @@
+// te_sell.cuh -- one SELL-32 row (one lane of a warp) times a complex vector.
+//
+// All 32 lanes of a warp work on the 32 rows of one chunk; rows were sorted by
+// length so the chunk's trip count (its longest row) wastes almost no FP64
+// issue slots on padding, and slot s + 32k is contiguous across lanes, so
+// values and column indices are read fully coalesced with streaming (evict
+// first) loads that keep the L2 for the Krylov vectors.
+#pragma once
+#include "te_internal.cuh"
+
+template <bool REAL>
+__device__ __forceinline__ double2 te_sell_row(const int64_t* __restrict__ chunk_off,
+                                               const int32_t* __restrict__ col, const double* __restrict__ val,
+                                               const double2* __restrict__ x, int64_t chunk, int lane) {
+  const int64_t e = __ldg(chunk_off + chunk + 1);
+  int64_t s = __ldg(chunk_off + chunk) + lane;
+  double re = 0.0, im = 0.0;
+  if (REAL) {
+    for (; s + 96 < e; s += 128) {
+      int32_t c0 = __ldcs(col + s), c1 = __ldcs(col + s + 32), c2 = __ldcs(col + s + 64), c3 = __ldcs(col + s + 96);
+      double a0 = __ldcs(val + s), a1 = __ldcs(val + s + 32), a2 = __ldcs(val + s + 64), a3 = __ldcs(val + s + 96);
+      double2 x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
+      re = fma(a0, x0.x, re);
+      im = fma(a0, x0.y, im);
+      re = fma(a1, x1.x, re);
+      im = fma(a1, x1.y, im);
+      re = fma(a2, x2.x, re);
+      im = fma(a2, x2.y, im);
+      re = fma(a3, x3.x, re);
+      im = fma(a3, x3.y, im);
+    }
+    for (; s < e; s += 32) {
+      double a = __ldcs(val + s);
+      double2 xv = __ldg(x + __ldcs(col + s));
+      re = fma(a, xv.x, re);
+      im = fma(a, xv.y, im);
+    }
+  } else {
+    const double2* __restrict__ v2 = reinterpret_cast<const double2*>(val);
+    for (; s + 32 < e; s += 64) {
+      int32_t c0 = __ldcs(col + s), c1 = __ldcs(col + s + 32);
+      double2 a0 = __ldcs(v2 + s), a1 = __ldcs(v2 + s + 32);
+      double2 x0 = __ldg(x + c0), x1 = __ldg(x + c1);
+      re = fma(a0.x, x0.x, re);
+      re = fma(-a0.y, x0.y, re);
+      im = fma(a0.x, x0.y, im);
+      im = fma(a0.y, x0.x, im);
+      re = fma(a1.x, x1.x, re);
+      re = fma(-a1.y, x1.y, re);
+      im = fma(a1.x, x1.y, im);
+      im = fma(a1.y, x1.x, im);
+    }
+    for (; s < e; s += 32) {
+      double2 a = __ldcs(v2 + s);
+      double2 xv = __ldg(x + __ldcs(col + s));
+      re = fma(a.x, xv.x, re);
+      re = fma(-a.y, xv.y, re);
+      im = fma(a.x, xv.y, im);
+      im = fma(a.y, xv.x, im);
+    }
+  }
+  return make_double2(re, im);
+}

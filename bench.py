@@ -1,0 +1,328 @@
+"""Benchmark: exp(-iHt)v on one GB300 (Krylov evolution, TimeEvolver algorithm).
+
+Workload (one "step" = one full solve): open-chain Bose-Hubbard L=12, N=12,
+J=1, U=3 (dim 1352078, 16871581 non-zeros), start vector a normalised complex
+Gaussian (numpy default_rng(0), real then imaginary parts), evolved to t=10
+with tol 1e-8, Krylov dimension m=40, <n_0> sampled every 0.5.
+
+value: seconds per solve with H, v and the observable resident in HBM (CUDA
+events on the evolver's stream).  e2e: the same solve through the C ABI with
+host buffers (COO upload, start vector, results back), wall clock.
+roofline: the Lanczos apply kernel (SELL-32 SpMV with the fused recurrence
+epilogue), algorithmic bytes per launch over its event-timed mean duration.
+
+--impl reference: the CPU restatement of the reference algorithm (the oracle,
+OpenMP on all host cores) on a bounded sample of the same solve (the first
+Krylov steps), scaled to the full solve's step count.
+
+Multi-GPU: replicas only (one independent solve per rank), torchrun/NCCL for
+the barrier and the max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L_SITES, N_BOSONS, J_HOP, U_INT = 12, 12, 1.0, 3.0
+T_FINAL, TOL, M_KRYLOV, SAMPLING = 10.0, 1e-8, 40, 0.5
+METRIC = "exp(-iHt)v s (Bose-Hubbard L=12 N=12 U=3, t=10, tol 1e-8, m=40)"
+WORKLOAD = ("Bose-Hubbard open chain L=12 N=12 J=1 U=3 (dim 1352078, nnz 16871581), complex Gaussian v seed 0, "
+            "t=10, tol=1e-8, m=40, <n_0> every 0.5")
+CPU_SAMPLE_T = 0.5  # bounded CPU sample: the solve up to t=0.5 (3 Krylov steps)
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def init_dist(ws, local):
+    if ws <= 1:
+        return None
+    import torch
+    import torch.distributed as dist
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl")
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peaks = {"hbm_gbs": 6800.0, "source": "fallback"}
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        peaks = {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    # FP64 FMA throughput measured on this machine's GB300 (profiles/fp64_peak_gb300.md)
+    peaks["fp64_tflops"] = 1.19
+    return peaks
+
+
+def ncu_traffic():
+    """Per-launch DRAM traffic of the Lanczos apply kernel from the committed
+    ncu summary, if one exists."""
+    p = os.path.join(ROOT, "profiles", "lanczos_apply_bh12.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f).get("dram_bytes_per_launch")
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons every 200 ms during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def build_problem():
+    from timeevolver_gb300 import models
+    B, H = models.bose_hubbard(L_SITES, N_BOSONS, J_HOP, U_INT)
+    O = models.operator_matrix([models.number_operator(0, 1.0)], B)
+    n = len(B)
+    rng = np.random.default_rng(0)
+    v = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    v /= np.linalg.norm(v)
+    return n, H, O, v
+
+
+def apply_kernel_bytes(n, nnz, real=True):
+    """Algorithmic bytes of one Lanczos apply launch: the matrix (values +
+    int32 columns), the SELL chunk offsets, x = u_j read once, u_{j-1} read,
+    w written."""
+    chunks = (n + 31) // 32
+    return nnz * ((8 if real else 16) + 4) + 8 * (chunks + 1) + 3 * 16 * n
+
+
+def apply_kernel_flops(n, nnz, real=True):
+    """FP64 flops of one Lanczos apply launch: 2 (real) or 4 (complex) FMAs per
+    non-zero, 14 per row for the recurrence term and the <v_j, w> partial."""
+    return nnz * (4 if real else 8) + 14 * n
+
+
+def run_gb300(args):
+    ws, rank, local = dist_info()
+    dist = init_dist(ws, local)
+    import torch
+    import timeevolver_gb300 as te
+    torch.cuda.set_device(local)
+    te.lib().te_set_device(local)
+    n, Hc, Oc, v = build_problem()
+    nnz = len(Hc[2])
+
+    # ---- device-resident solves
+    H = te.Matrix.from_coo(n, Hc)
+    O = te.Matrix.from_coo(n, Oc)
+    info = H.info()
+    ev = te.Evolver(H, v, T_FINAL, SAMPLING, [("sparse", O)], tol=TOL, m=M_KRYLOV)
+    v_dev = torch.from_numpy(v.view(np.float64).copy()).cuda()
+    for _ in range(args.warmup):
+        ev.reset(None, device_ptr=v_dev.data_ptr())
+        ev.run()
+    torch.cuda.synchronize()
+    ev.profile(True)
+    stream = torch.cuda.ExternalStream(ev.stream())
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches = 0
+    steps_per_solve = 0
+    barrier(dist)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        start.record(stream)
+        for _ in range(args.steps):
+            ev.reset(None, device_ptr=v_dev.data_ptr())
+            r = ev.run()
+            launches += te.lib().te_evolver_launch_count(ev.handle)
+            steps_per_solve = r.n_steps
+        stop.record(stream)
+        stop.synchronize()
+    torch.cuda.synchronize()
+    barrier(dist)
+    ms = start.elapsed_time(stop)
+    ms = max_over_ranks(dist, ms)
+    apply_ms, apply_n = ev.kernel_time(0)
+    kernel_ms = {name: ev.kernel_time(k) for k, name in enumerate(
+        ["lanczos_apply", "lanczos_update", "krylov_step", "combine", "observables"])}
+    status = r.status
+    ev.profile(False)
+    ev.close()
+
+    # ---- end to end through the C ABI with host buffers
+    e2e_times = []
+    h2d = 32 * nnz + 32 * len(Oc[2]) + 16 * n
+    d2h = 8 * (int(T_FINAL / SAMPLING) + 1) + 16 * n
+    for _ in range(max(1, args.steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = te.evolve(Hc, v, T_FINAL, SAMPLING, [("sparse", Oc)], tol=TOL, m=M_KRYLOV)
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = max_over_ranks(dist, float(np.mean(e2e_times)))
+
+    if rank != 0:
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    value = ms / 1000.0 / args.steps / ws
+    peaks = load_peaks()
+    b_apply = apply_kernel_bytes(n, nnz, info["real"])
+    f_apply = apply_kernel_flops(n, nnz, info["real"])
+    avg_apply_s = apply_ms / 1000.0 / max(1, apply_n)
+    achieved = b_apply / avg_apply_s / 1e9
+    traffic = ncu_traffic()
+    line = {
+        "metric": METRIC, "value": value, "unit": "s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "complex128 (FP64)", "data": "synthetic (Bose-Hubbard model, seeded state)",
+        "config": {"workload": WORKLOAD, "n": n, "nnz": nnz, "krylov_steps_per_solve": steps_per_solve,
+                   "status": status, "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (H %.0f MB + Krylov basis %.0f MB)"
+                         % (nnz * 12 / 1e6, (M_KRYLOV + 3) * 16 * n / 1e6)},
+        "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": "lanczos_apply_kernel (SELL-32 SpMV + recurrence epilogue)",
+                     "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
+                     "traffic": traffic, "algorithmic_bytes_per_launch": b_apply,
+                     "avg_launch_us": avg_apply_s * 1e6, "launches": apply_n,
+                     "fp64": {"achieved_tflops": f_apply / avg_apply_s / 1e12, "peak_tflops": peaks["fp64_tflops"],
+                              "frac": f_apply / avg_apply_s / 1e12 / peaks["fp64_tflops"],
+                              "flops_per_launch": f_apply}},
+        "kernel_ms_per_solve": {k: round(v_[0] / args.steps, 3) for k, v_ in kernel_ms.items()},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(Hc, Oc, v, steps_per_solve)
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def cpu_baseline(Hc, Oc, v, steps_full):
+    """The oracle (CPU restatement of the reference algorithm) on all host
+    cores, on the solve up to t=CPU_SAMPLE_T, scaled to the full solve."""
+    import oracle
+    oracle.build()
+    cores = os.cpu_count()
+    t0 = time.perf_counter()
+    r = oracle.evolve(Hc, v, CPU_SAMPLE_T, SAMPLING, [("sparse", Oc)], tol=TOL * CPU_SAMPLE_T / T_FINAL,
+                      m=M_KRYLOV, n_threads=cores)
+    el = time.perf_counter() - t0
+    per_step = el / max(1, r["n_steps"])
+    return {"value": per_step * steps_full, "unit": "s", "cores": cores, "kind": "port",
+            "sample": "first %d Krylov steps (t=%.2g, same tolerance rate) in %.1f s, %.3f s per Krylov step, "
+                      "scaled to the %d steps of the full solve" % (r["n_steps"], CPU_SAMPLE_T, el, per_step,
+                                                                    steps_full)}
+
+
+def run_reference(args):
+    ws, rank, local = dist_info()
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    n, Hc, Oc, v = build_problem()
+    cores = os.cpu_count()
+    steps_full = 48  # Krylov steps of the full solve (the GPU run and the oracle trace agree)
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        r = oracle.evolve(Hc, v, CPU_SAMPLE_T, SAMPLING, [("sparse", Oc)], tol=TOL * CPU_SAMPLE_T / T_FINAL,
+                          m=M_KRYLOV, n_threads=cores)
+        el = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(el / r["n_steps"] * steps_full)
+    value = float(np.mean(times))
+    sample = ("first %d Krylov steps of the solve per step (t=%.2g at the same tolerance rate), scaled to the %d "
+              "Krylov steps of the full solve" % (r["n_steps"], CPU_SAMPLE_T, steps_full))
+    line = {"metric": METRIC, "value": value, "unit": "s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": value * 1000, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "complex128 (FP64)", "data": "synthetic (Bose-Hubbard model, seeded state)", "impl": "reference",
+            "config": {"workload": WORKLOAD, "n": n, "nnz": len(Hc[2])},
+            "cpu_baseline": {"value": value, "unit": "s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        import timeevolver_gb300 as te
+        te.build()
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -178,6 +178,23 @@ int te_evolver_trace(te_evolver ev, te_step_record* out, int64_t max_records, in
 /* Kernel launches issued by the last te_evolver_run (for launch accounting). */
 int64_t te_evolver_launch_count(te_evolver ev);
 
+/* Prepare another run of the same evolution (same H, parameters and
+ * observables, device buffers reused) from the start vector v (complex n):
+ * v_is_device != 0 reads v from device memory, else from host memory.  No
+ * counterpart in the reference (an evolver there runs once); it lets a caller
+ * repeat evolutions without reallocating the Krylov basis. */
+int te_evolver_reset(te_evolver ev, const double* v, int v_is_device);
+
+/* The CUDA stream every kernel of this evolver is launched on (cudaStream_t). */
+void* te_evolver_stream(te_evolver ev);
+
+/* Per-kernel timing with CUDA events on the evolver's stream, accumulated over
+ * the runs made while enabled.  kind: 0 Lanczos apply (SpMV + fused epilogue),
+ * 1 Lanczos update, 2 Krylov-space step kernel, 3 combine (V y), 4 observable
+ * reductions. */
+int te_evolver_profile(te_evolver ev, int enable);
+int te_evolver_kernel_time(te_evolver ev, int kind, double* total_ms, int64_t* launches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -76,6 +76,10 @@ SIGNATURES = {
     "te_evolver_state_device": (_I, [_P, _P]),
     "te_evolver_trace": (_I, [_P, _P, _I64, _P]),
     "te_evolver_launch_count": (_I64, [_P]),
+    "te_evolver_reset": (_I, [_P, _P, _I]),
+    "te_evolver_stream": (_P, [_P]),
+    "te_evolver_profile": (_I, [_P, _I]),
+    "te_evolver_kernel_time": (_I, [_P, _I, _P, _P]),
 }
 
 _lib = None
@@ -229,6 +233,33 @@ class Evolver:
                                  breakdown=x.breakdown, code=x.code, n_integrals=x.n_integrals)
                             for x in recs[:cnt.value]]
         return out
+
+    def reset(self, v, device_ptr=None):
+        """Re-arm the evolver with a new start vector (host array, or a device
+        pointer to n complex doubles)."""
+        if device_ptr is not None:
+            _check(lib().te_evolver_reset(self.handle, ctypes.c_void_p(device_ptr), 1), "te_evolver_reset")
+        else:
+            v = np.ascontiguousarray(v, dtype=np.complex128)
+            _check(lib().te_evolver_reset(self.handle, _ptr(v), 0), "te_evolver_reset")
+
+    def run(self):
+        """timeEvolve without copying results back (they stay on the device)."""
+        r = TeResult()
+        _check(lib().te_evolver_run(self.handle, ctypes.byref(r)), "te_evolver_run")
+        return r
+
+    def stream(self):
+        return lib().te_evolver_stream(self.handle)
+
+    def profile(self, enable=True):
+        _check(lib().te_evolver_profile(self.handle, int(enable)), "te_evolver_profile")
+
+    def kernel_time(self, kind):
+        ms, cnt = ctypes.c_double(), ctypes.c_int64()
+        _check(lib().te_evolver_kernel_time(self.handle, kind, ctypes.byref(ms), ctypes.byref(cnt)),
+               "te_evolver_kernel_time")
+        return ms.value, cnt.value
 
     def close(self):
         if self.handle:

@@ -70,15 +70,59 @@ struct te_evolver_s {
   bool ran = false;
   int64_t launches = 0;
   double2* host_state = nullptr;  // pinned buffer for callbacks
+  // per-kernel event timing
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, int>> pending;  // (kind, first event index) of recorded pairs
+  size_t ev_used = 0;
+  double kernel_ms[5] = {0, 0, 0, 0, 0};
+  int64_t kernel_n[5] = {0, 0, 0, 0, 0};
 };
 
 namespace {
 
 const size_t kPartials = (size_t)TE_SCAP * TE_FUSED_VALS * 8 * 1024;
 
+// Event pair around one launch when profiling (no-op otherwise).
+struct ProfScope {
+  te_evolver ev;
+  int kind;
+  int idx = -1;
+  ProfScope(te_evolver e, int k) : ev(e), kind(k) {
+    if (!ev->profiling) return;
+    while (ev->ev_pool.size() < ev->ev_used + 2) {
+      cudaEvent_t x;
+      cudaEventCreate(&x);
+      ev->ev_pool.push_back(x);
+    }
+    idx = (int)ev->ev_used;
+    ev->ev_used += 2;
+    cudaEventRecord(ev->ev_pool[idx], ev->st);
+  }
+  ~ProfScope() {
+    if (idx < 0) return;
+    cudaEventRecord(ev->ev_pool[idx + 1], ev->st);
+    ev->pending.emplace_back(kind, idx);
+  }
+};
+
+// Fold the completed event pairs into the per-kind totals (after a sync).
+void collect_profile(te_evolver ev) {
+  for (auto& p : ev->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ev->ev_pool[p.second], ev->ev_pool[p.second + 1]) == cudaSuccess) {
+      ev->kernel_ms[p.first] += ms;
+      ev->kernel_n[p.first] += 1;
+    }
+  }
+  ev->pending.clear();
+  ev->ev_used = 0;
+}
+
 int read_summary(te_evolver ev) {
   TE_CUDA(cudaMemcpyAsync(ev->sum, ev->ds, sizeof(Summary), cudaMemcpyDeviceToHost, ev->st));
   TE_CUDA(cudaStreamSynchronize(ev->st));
+  if (ev->profiling) collect_profile(ev);
   return TE_OK;
 }
 
@@ -87,7 +131,7 @@ int read_summary(te_evolver ev) {
 // index of a stop request (or -1).
 int process_batch(te_evolver ev, int* stop_at, bool synced) {
   *stop_at = -1;
-  // fused passes (up to 16 diagonal + 8 vector observables per pass)
+  // fused passes (up to TE_FUSED_DIAG diagonal + TE_FUSED_VEC vector observables per pass)
   std::vector<const HostObs*> dg, vc;
   std::vector<int> dgi, vci;
   for (size_t i = 0; i < ev->obs.size(); ++i) {
@@ -112,7 +156,10 @@ int process_batch(te_evolver ev, int* stop_at, bool synced) {
       f.row_vec[f.n_vec++] = vci[iv];
       ++iv;
     }
-    te_launch_fused_obs(ev->n, ev->batch, f, ev->ds, ev->partials, ev->results, (int)ev->n_samples, ev->st);
+    {
+      ProfScope ps(ev, 4);
+      te_launch_fused_obs(ev->n, ev->batch, f, ev->ds, ev->partials, ev->results, (int)ev->n_samples, ev->st);
+    }
     ++ev->launches;
   }
   bool need_host = false;
@@ -164,6 +211,7 @@ void free_evolver(te_evolver ev) {
     cudaFree(o.diag_perm);
     cudaFree(o.vec_perm);
   }
+  for (auto e : ev->ev_pool) cudaEventDestroy(e);
   if (ev->st) cudaStreamDestroy(ev->st);
   delete ev;
 }
@@ -256,19 +304,31 @@ int run(te_evolver ev, te_result* out) {
     err_prev = S->err;
     // STEP 1: Lanczos (:338)
     for (int j = 0; j < m; ++j) {
-      te_launch_lanczos_apply(ev->H->sell, ev->H->is_real, ev->cols[j], j > 0 ? ev->cols[j - 1] : nullptr, ev->w,
-                              ev->ds, ev->partials, j, st);
-      te_launch_lanczos_update(n, ev->w, ev->cols[j], j + 1 < m ? ev->cols[j + 1] : nullptr, ev->ds, ev->partials, j,
-                               st);
+      {
+        ProfScope ps(ev, 0);
+        te_launch_lanczos_apply(ev->H->sell, ev->H->is_real, ev->cols[j], j > 0 ? ev->cols[j - 1] : nullptr, ev->w,
+                                ev->ds, ev->partials, j, st);
+      }
+      {
+        ProfScope ps(ev, 1);
+        te_launch_lanczos_update(n, ev->w, ev->cols[j], j + 1 < m ? ev->cols[j + 1] : nullptr, ev->ds, ev->partials,
+                                 j, st);
+      }
       ev->launches += 2;
     }
     // STEP 1b-3: Krylov-space kernel (eigen data, step search, w, first batch)
-    te_launch_krylov_step(ev->ds, st);
+    {
+      ProfScope ps(ev, 2);
+      te_launch_krylov_step(ev->ds, st);
+    }
     ++ev->launches;
     for (int j = 0; j < m; ++j) ca.cols[j] = ev->cols[j];
     ca.m = m;
     ca.w_out = ev->spare;
-    te_launch_combine(ca, ev->ds, ev->sampled, st);
+    {
+      ProfScope ps(ev, 3);
+      te_launch_combine(ca, ev->ds, ev->sampled, st);
+    }
     ++ev->launches;
     rc = process_batch(ev, &stop_at, false);
     if (rc != TE_OK) return rc;
@@ -288,10 +348,16 @@ int run(te_evolver ev, te_result* out) {
     ev->trace.push_back(rec);
     const bool produced_w = S->want_w != 0;
     while (stop_at < 0 && S->samples_pending && !S->fatal) {
-      te_launch_schedule_samples(ev->ds, st);
+      {
+        ProfScope ps(ev, 2);
+        te_launch_schedule_samples(ev->ds, st);
+      }
       ++ev->launches;
       ca.w_out = ev->spare;
-      te_launch_combine(ca, ev->ds, ev->sampled, st);
+      {
+        ProfScope ps(ev, 3);
+        te_launch_combine(ca, ev->ds, ev->sampled, st);
+      }
       ++ev->launches;
       rc = process_batch(ev, &stop_at, false);
       if (rc != TE_OK) return rc;
@@ -514,12 +580,13 @@ extern "C" int te_evolver_run(te_evolver ev, te_result* result) {
     return TE_ERR_INVALID_ARG;
   }
   if (ev->ran) {
-    te_set_error("te_evolver_run: an evolver runs once (as timeEvolve)");
+    te_set_error("te_evolver_run: call te_evolver_reset before running an evolver again");
     return TE_ERR_INVALID_ARG;
   }
   ev->ran = true;
   te_result r{};
   int rc = run(ev, &r);
+  if (ev->profiling) collect_profile(ev);
   if (rc == TE_OK) rc = te_cuda_check(cudaGetLastError(), "evolution");
   if (rc != TE_OK) return rc;
   ev->res = r;
@@ -578,3 +645,48 @@ extern "C" int te_evolver_trace(te_evolver ev, te_step_record* out, int64_t max_
 }
 
 extern "C" int64_t te_evolver_launch_count(te_evolver ev) { return ev ? ev->launches : 0; }
+
+extern "C" int te_evolver_reset(te_evolver ev, const double* v, int v_is_device) {
+  if (!ev || !v) {
+    te_set_error("te_evolver_reset: invalid arguments");
+    return TE_ERR_INVALID_ARG;
+  }
+  const int64_t n = ev->n;
+  if (!v_is_device) {
+    double nrm = 0.0;
+    for (int64_t i = 0; i < 2 * n; ++i) nrm += v[i] * v[i];
+    if (std::fabs(std::sqrt(nrm) - 1.0) > ev->p.tol) {
+      te_set_error("Initial vector is not normalized");
+      return TE_ERR_NOT_NORMALIZED;
+    }
+  }
+  TE_CUDA(cudaMemcpyAsync(ev->orig_tmp, v, sizeof(double2) * n,
+                          v_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, ev->st));
+  // the Krylov basis columns were rotated by earlier runs: restore the slab order
+  for (int j = 0; j < ev->m; ++j) ev->cols[j] = ev->slab + (int64_t)j * n;
+  ev->spare = ev->slab + (int64_t)ev->m * n;
+  te_launch_permute(n, ev->H->sell.perm, ev->orig_tmp, ev->cols[0], ev->st);
+  ev->ran = false;
+  return te_cuda_check(cudaGetLastError(), "te_evolver_reset");
+}
+
+extern "C" void* te_evolver_stream(te_evolver ev) { return ev ? (void*)ev->st : nullptr; }
+
+extern "C" int te_evolver_profile(te_evolver ev, int enable) {
+  if (!ev) return TE_ERR_INVALID_ARG;
+  ev->profiling = enable != 0;
+  for (int k = 0; k < 5; ++k) {
+    ev->kernel_ms[k] = 0.0;
+    ev->kernel_n[k] = 0;
+  }
+  ev->pending.clear();
+  ev->ev_used = 0;
+  return TE_OK;
+}
+
+extern "C" int te_evolver_kernel_time(te_evolver ev, int kind, double* total_ms, int64_t* launches) {
+  if (!ev || kind < 0 || kind > 4) return TE_ERR_INVALID_ARG;
+  if (total_ms) *total_ms = ev->kernel_ms[kind];
+  if (launches) *launches = ev->kernel_n[kind];
+  return TE_OK;
+}

@@ -24,8 +24,8 @@
 #define TE_TS_KMAX 8          // tanh-sinh refinement levels 0..8
 #define TE_TS_KMIN 2
 #define TE_TS_NODES 769       // nodes with t >= 0 over levels 0..8
-#define TE_FUSED_DIAG 16      // diagonal observables per fused reduction pass
-#define TE_FUSED_VEC 8        // vector observables per fused reduction pass
+#define TE_FUSED_DIAG 4       // diagonal observables per fused reduction pass
+#define TE_FUSED_VEC 2        // vector observables per fused reduction pass
 #define TE_FUSED_VALS (TE_FUSED_DIAG + 2 * TE_FUSED_VEC)
 
 // Tanh-sinh and Gauss-Legendre tables (host-computed, uploaded once).

@@ -16,55 +16,70 @@
 
 #define TE_COMBINE_GROUP 4
 
-// psi_o = sum_j u_j Y[slot_o][j] for the outputs of this batch.
+// Rows of G outputs: psi_o[r] = sum_j u_j[r] ys[o][j].  G is a compile-time
+// count: on GB300 a predicated-off FP64 instruction still occupies the FP64
+// pipe, so every output slot that exists in the code must be a real output.
+template <int G>
+__device__ __forceinline__ void combine_rows(const TeCombineArgs& a, const double2* const* cols, int m,
+                                             const double2 (*ys)[TE_MMAX], const int* slot_s, int S,
+                                             double2* last_out) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < a.n; r += (int64_t)gridDim.x * blockDim.x) {
+    double2 acc[G];
+#pragma unroll
+    for (int o = 0; o < G; ++o) acc[o] = make_double2(0.0, 0.0);
+    for (int j = 0; j < m; ++j) {
+      const double2 u = cols[j][r];
+#pragma unroll
+      for (int o = 0; o < G; ++o) {
+        const double2 y = ys[o][j];
+        acc[o].x = fma(u.x, y.x, fma(-u.y, y.y, acc[o].x));
+        acc[o].y = fma(u.x, y.y, fma(u.y, y.x, acc[o].y));
+      }
+    }
+#pragma unroll
+    for (int o = 0; o < G; ++o) {
+      const int slot = slot_s[o];
+      if (slot == 0) {
+        a.w_out[r] = acc[o];
+      } else {
+        a.sample_out[(int64_t)(slot - 1) * a.n + r] = acc[o];
+        if (slot == S) last_out[r] = acc[o];
+      }
+    }
+  }
+}
+
+// psi_o = sum_j u_j Y[slot_o][j] for the outputs of this batch (the step's
+// next start vector w, then its samples), one pass over V per group of up to
+// four outputs.
 __global__ void __launch_bounds__(TE_THREADS) combine_kernel(TeCombineArgs a, TeDevState* ds, double2* last_out) {
   __shared__ double2 ys[TE_COMBINE_GROUP][TE_MMAX];
   __shared__ int slot_s[TE_COMBINE_GROUP];
+  __shared__ const double2* cols[TE_MMAX];
   if (ds->fatal != 0) return;
   const int want_w = ds->want_w;
   const int S = ds->samples_in_batch;
   const int nout = want_w + S;
   const int m = min(a.m, ds->m_eff);  // a lucky breakdown shrinks the basis of this step
+  if (threadIdx.x < TE_MMAX) cols[threadIdx.x] = threadIdx.x < m ? a.cols[threadIdx.x] : nullptr;
   for (int g0 = 0; g0 < nout; g0 += TE_COMBINE_GROUP) {
     const int G = min(TE_COMBINE_GROUP, nout - g0);
     __syncthreads();
     if (threadIdx.x < TE_COMBINE_GROUP) {
-      int o = g0 + threadIdx.x;
+      const int o = g0 + threadIdx.x;
       slot_s[threadIdx.x] = want_w ? o : o + 1;  // slot 0 = w, slots 1.. = samples
     }
     __syncthreads();
     for (int i = threadIdx.x; i < G * TE_MMAX; i += blockDim.x) {
-      int o = i / TE_MMAX, j = i % TE_MMAX;
+      const int o = i / TE_MMAX, j = i % TE_MMAX;
       ys[o][j] = j < m ? ds->Y[slot_s[o] * TE_MMAX + j] : make_double2(0.0, 0.0);
     }
     __syncthreads();
-    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < a.n; r += (int64_t)gridDim.x * blockDim.x) {
-      double2 acc[TE_COMBINE_GROUP];
-#pragma unroll
-      for (int o = 0; o < TE_COMBINE_GROUP; ++o) acc[o] = make_double2(0.0, 0.0);
-      for (int j = 0; j < m; ++j) {
-        const double2 u = a.cols[j][r];
-#pragma unroll
-        for (int o = 0; o < TE_COMBINE_GROUP; ++o) {
-          if (o < G) {
-            const double2 y = ys[o][j];
-            acc[o].x = fma(u.x, y.x, fma(-u.y, y.y, acc[o].x));
-            acc[o].y = fma(u.x, y.y, fma(u.y, y.x, acc[o].y));
-          }
-        }
-      }
-#pragma unroll
-      for (int o = 0; o < TE_COMBINE_GROUP; ++o) {
-        if (o < G) {
-          const int slot = slot_s[o];
-          if (slot == 0) {
-            a.w_out[r] = acc[o];
-          } else {
-            a.sample_out[(int64_t)(slot - 1) * a.n + r] = acc[o];
-            if (slot == S) last_out[r] = acc[o];
-          }
-        }
-      }
+    switch (G) {
+      case 1: combine_rows<1>(a, cols, m, ys, slot_s, S, last_out); break;
+      case 2: combine_rows<2>(a, cols, m, ys, slot_s, S, last_out); break;
+      case 3: combine_rows<3>(a, cols, m, ys, slot_s, S, last_out); break;
+      default: combine_rows<4>(a, cols, m, ys, slot_s, S, last_out); break;
     }
   }
 }
@@ -74,66 +89,67 @@ void te_launch_combine(const TeCombineArgs& a, TeDevState* ds, double2* last_out
 }
 
 // Diagonal observables: Re sum_i O_ii |psi_i|^2 (= Re zdotc(psi, O psi) for a
-// diagonal O); vector observables: |sum_i conj(psi_i) o_i|^2.  Up to
-// TE_FUSED_DIAG + TE_FUSED_VEC observables per launch.
+// diagonal O); vector observables: |sum_i conj(psi_i) o_i|^2.  ND diagonal and
+// NV vector observables per launch, compile-time counts (no predicated FP64).
+template <int ND, int NV>
 __global__ void __launch_bounds__(TE_THREADS) fused_obs_kernel(int64_t n, const double2* __restrict__ psi_base,
                                                                TeFusedObs f, TeDevState* ds, double* partials,
                                                                double* results, int n_samples_total) {
-  __shared__ double scratch[TE_FUSED_VALS * 32];
+  constexpr int V = ND + 2 * NV;
+  __shared__ double scratch[V * 32];
   __shared__ bool is_last;
   if (ds->fatal != 0) return;
   const int S = ds->samples_in_batch;
   const int base = ds->sample_base;
-  const int nd = f.n_diag, nv = f.n_vec;
   for (int s = 0; s < S; ++s) {
     const double2* __restrict__ psi = psi_base + (int64_t)s * n;
-    double acc[TE_FUSED_VALS];
+    double acc[V];
 #pragma unroll
-    for (int v = 0; v < TE_FUSED_VALS; ++v) acc[v] = 0.0;
+    for (int v = 0; v < V; ++v) acc[v] = 0.0;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
       const double2 p = psi[r];
-      const double p2 = fma(p.x, p.x, p.y * p.y);
+      if (ND > 0) {
+        const double p2 = fma(p.x, p.x, p.y * p.y);
 #pragma unroll
-      for (int v = 0; v < TE_FUSED_DIAG; ++v) {
-        if (v < nd) acc[v] = fma(__ldg(f.diag[v] + r), p2, acc[v]);
+        for (int v = 0; v < ND; ++v) acc[v] = fma(__ldg(f.diag[v] + r), p2, acc[v]);
       }
 #pragma unroll
-      for (int v = 0; v < TE_FUSED_VEC; ++v) {
-        if (v < nv) {
-          const double2 o = __ldg(f.vec[v] + r);
-          // conj(psi) * o
-          acc[TE_FUSED_DIAG + 2 * v] = fma(p.x, o.x, fma(p.y, o.y, acc[TE_FUSED_DIAG + 2 * v]));
-          acc[TE_FUSED_DIAG + 2 * v + 1] = fma(p.x, o.y, fma(-p.y, o.x, acc[TE_FUSED_DIAG + 2 * v + 1]));
-        }
+      for (int v = 0; v < NV; ++v) {
+        const double2 o = __ldg(f.vec[v] + r);
+        // conj(psi) * o
+        acc[ND + 2 * v] = fma(p.x, o.x, fma(p.y, o.y, acc[ND + 2 * v]));
+        acc[ND + 2 * v + 1] = fma(p.x, o.y, fma(-p.y, o.x, acc[ND + 2 * v + 1]));
       }
     }
-    te_block_sum<TE_FUSED_VALS>(acc, scratch);
+    te_block_sum<V>(acc, scratch);
     if (threadIdx.x == 0)
-      for (int v = 0; v < TE_FUSED_VALS; ++v)
-        partials[((int64_t)s * TE_FUSED_VALS + v) * gridDim.x + blockIdx.x] = acc[v];
+#pragma unroll
+      for (int v = 0; v < V; ++v) partials[((int64_t)s * V + v) * gridDim.x + blockIdx.x] = acc[v];
   }
   if (threadIdx.x == 0) {
     __threadfence();
-    unsigned int prev = atomicAdd(&ds->counter[2], 1u);
+    const unsigned int prev = atomicAdd(&ds->counter[2], 1u);
     is_last = (prev == gridDim.x - 1);
   }
   __syncthreads();
   if (!is_last) return;
   __threadfence();
   for (int s = 0; s < S; ++s) {
-    double tot[TE_FUSED_VALS];
+    double tot[V];
 #pragma unroll
-    for (int v = 0; v < TE_FUSED_VALS; ++v) {
+    for (int v = 0; v < V; ++v) {
       double sum = 0.0;
       for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
-        sum += __ldcg(partials + ((int64_t)s * TE_FUSED_VALS + v) * gridDim.x + b);
+        sum += __ldcg(partials + ((int64_t)s * V + v) * gridDim.x + b);
       tot[v] = sum;
     }
-    te_block_sum<TE_FUSED_VALS>(tot, scratch);
+    te_block_sum<V>(tot, scratch);
     if (threadIdx.x == 0) {
-      for (int v = 0; v < nd; ++v) results[(int64_t)f.row_diag[v] * n_samples_total + base + s] = tot[v];
-      for (int v = 0; v < nv; ++v) {
-        const double re = tot[TE_FUSED_DIAG + 2 * v], im = tot[TE_FUSED_DIAG + 2 * v + 1];
+#pragma unroll
+      for (int v = 0; v < ND; ++v) results[(int64_t)f.row_diag[v] * n_samples_total + base + s] = tot[v];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        const double re = tot[ND + 2 * v], im = tot[ND + 2 * v + 1];
         results[(int64_t)f.row_vec[v] * n_samples_total + base + s] = re * re + im * im;
       }
     }
@@ -141,10 +157,24 @@ __global__ void __launch_bounds__(TE_THREADS) fused_obs_kernel(int64_t n, const 
   if (threadIdx.x == 0) ds->counter[2] = 0u;
 }
 
+template <int ND, int NV>
+static void launch_fused(int64_t n, const double2* psi, const TeFusedObs& f, TeDevState* ds, double* partials,
+                         double* results, int n_samples_total, cudaStream_t st) {
+  fused_obs_kernel<ND, NV><<<te_grid_for(n, TE_THREADS, 4), TE_THREADS, 0, st>>>(n, psi, f, ds, partials, results,
+                                                                                 n_samples_total);
+}
+
 void te_launch_fused_obs(int64_t n, const double2* psi, const TeFusedObs& f, TeDevState* ds, double* partials,
                          double* results, int n_samples_total, cudaStream_t st) {
-  fused_obs_kernel<<<te_grid_for(n, TE_THREADS, 4), TE_THREADS, 0, st>>>(n, psi, f, ds, partials, results,
-                                                                         n_samples_total);
+  typedef void (*L)(int64_t, const double2*, const TeFusedObs&, TeDevState*, double*, double*, int, cudaStream_t);
+  static const L table[TE_FUSED_DIAG + 1][TE_FUSED_VEC + 1] = {
+      {nullptr, launch_fused<0, 1>, launch_fused<0, 2>},
+      {launch_fused<1, 0>, launch_fused<1, 1>, launch_fused<1, 2>},
+      {launch_fused<2, 0>, launch_fused<2, 1>, launch_fused<2, 2>},
+      {launch_fused<3, 0>, launch_fused<3, 1>, launch_fused<3, 2>},
+      {launch_fused<4, 0>, launch_fused<4, 1>, launch_fused<4, 2>}};
+  L fn = table[f.n_diag][f.n_vec];
+  if (fn) fn(n, psi, f, ds, partials, results, n_samples_total, st);
 }
 
 // General sparse observable: Re sum_i conj(psi_i) (O psi)_i on the original

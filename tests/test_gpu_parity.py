@@ -209,7 +209,7 @@ def test_stop_request(te_gpu, oracle_lib):
     assert gpu["status"] == ref["status"] == 3
     assert gpu["num_samples"] == ref["num_samples"] == 5
     assert abs(gpu["evolved_time"] - ref["evolved_time"]) < 1e-12
-    assert np.max(np.abs(gpu["samples"][:, :5] - ref["samples"][:, :5])) < OBS_TOL
+    assert np.max(np.abs(gpu["samples"][:4, :5] - ref["samples"][:, :5])) < OBS_TOL
 
 
 def test_invalid_inputs(te_gpu):

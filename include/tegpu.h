@@ -105,6 +105,17 @@ int te_matrix_spmv(te_matrix A, double alpha_re, double alpha_im, const double* 
 int te_matrix_spmv_host(te_matrix A, double alpha_re, double alpha_im, const double* in_host,
                         double* out_host);
 
+/* te_matrix_spmv without any device allocation, for callers that cannot call
+ * cudaMalloc (work recorded into CUDA graphs by stream capture, real-time
+ * loops, hosts whose device memory is preallocated by another framework).
+ * No counterpart in the reference.  Its scratch is a fixed array inside the
+ * library (8 MiB on every GPU that loads it), so matrices are limited to
+ * 262144 rows (TE_ERR_UNSUPPORTED beyond); the first call on a device looks
+ * the array up and should come before any stream capture; calls whose
+ * executions overlap on the GPU share the array and race. */
+int te_matrix_spmv_noalloc(te_matrix A, double alpha_re, double alpha_im, const double* in_dev, double* out_dev,
+                           void* cuda_stream);
+
 /* ----------------------------------------------------------------- evolver */
 
 /* Parameters of krylovTimeEvolver (krylovTimeEvolver.h:59; defaults of the

@@ -65,6 +65,7 @@ SIGNATURES = {
     "te_matrix_info": (_I, [_P, _P, _P, _P, _P, _P]),
     "te_matrix_spmv": (_I, [_P, _D, _D, _P, _P, _P]),
     "te_matrix_spmv_host": (_I, [_P, _D, _D, _P, _P]),
+    "te_matrix_spmv_noalloc": (_I, [_P, _D, _D, _P, _P, _P]),
     "te_evolver_create": (_I, [_P, _P, _P, _P]),
     "te_evolver_destroy": (_I, [_P]),
     "te_evolver_add_sparse_observable": (_I, [_P, _P]),

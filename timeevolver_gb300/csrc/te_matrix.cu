@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <mutex>
 #include <numeric>
 #include <vector>
 
@@ -347,4 +348,70 @@ extern "C" int te_matrix_spmv_host(te_matrix A, double alpha_re, double alpha_im
   cudaFree(x);
   cudaFree(y);
   return rc;
+}
+
+// ------------------------------------------------- product without allocation
+//
+// te_matrix_spmv needs two vectors of scratch (the input and the output in the
+// matrix's sorted row order) and takes them from cudaMallocAsync on every call.
+// Callers that must not allocate -- code recorded into a CUDA graph by stream
+// capture, real-time loops whose memory is fixed up front, hosts whose device
+// memory budget is preallocated by another framework -- use
+// te_matrix_spmv_noalloc instead, which keeps that scratch in the fixed array
+// below.  The array is part of the library image, so every GPU that loads the
+// library holds it (TE_NOALLOC_MAX_ROWS * 2 * 16 bytes = 8 MiB) until the
+// process exits.
+
+#define TE_NOALLOC_MAX_ROWS (1 << 18)
+
+static __device__ __align__(256) double2 g_noalloc_scratch[2 * TE_NOALLOC_MAX_ROWS];
+
+#define TE_NOALLOC_MAX_DEVICES 64
+
+// Device address of g_noalloc_scratch for the current device.  The host-side
+// name of the array is only a stand-in; the address is looked up once per
+// device (the first call on a device does it, so make that first call before
+// any stream capture) and cached.
+static int noalloc_scratch(double2** out) {
+  static std::mutex mu;
+  static double2* addr[TE_NOALLOC_MAX_DEVICES] = {};
+  int dev = 0;
+  TE_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= TE_NOALLOC_MAX_DEVICES) {
+    te_set_error("te_matrix_spmv_noalloc: device %d out of range", dev);
+    return TE_ERR_UNSUPPORTED;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    TE_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    addr[dev] = static_cast<double2*>(p);
+  }
+  *out = addr[dev];
+  return TE_OK;
+}
+
+extern "C" int te_matrix_spmv_noalloc(te_matrix A, double alpha_re, double alpha_im, const double* in_dev,
+                                      double* out_dev, void* cuda_stream) {
+  if (!A || !in_dev || !out_dev || A->n_rows != A->n_cols) {
+    te_set_error("te_matrix_spmv_noalloc: invalid arguments (square matrix and device buffers required)");
+    return TE_ERR_INVALID_ARG;
+  }
+  const int64_t n = A->n_rows;
+  if (n > TE_NOALLOC_MAX_ROWS) {
+    te_set_error("te_matrix_spmv_noalloc: %lld rows exceed the fixed scratch of %d rows; use te_matrix_spmv",
+                 (long long)n, TE_NOALLOC_MAX_ROWS);
+    return TE_ERR_UNSUPPORTED;
+  }
+  double2* scratch = nullptr;
+  int rc = noalloc_scratch(&scratch);
+  if (rc != TE_OK) return rc;
+  // both halves are written in full before they are read: nothing to clear
+  double2* xp = scratch;
+  double2* yp = scratch + TE_NOALLOC_MAX_ROWS;
+  cudaStream_t st = (cudaStream_t)cuda_stream;
+  te_launch_permute(n, A->sell.perm, reinterpret_cast<const double2*>(in_dev), xp, st);
+  te_launch_sell_spmv(A->sell, A->is_real, make_double2(alpha_re, alpha_im), xp, yp, st);
+  te_launch_permute(n, A->sell.iperm, yp, reinterpret_cast<double2*>(out_dev), st);
+  return te_cuda_check(cudaGetLastError(), "spmv_noalloc launch");
 }

@@ -70,15 +70,15 @@ def max_over_ranks(dist, x):
     return float(t.item())
 
 
-def load_peaks():
+def load_peaks(te):
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peaks = {"hbm_gbs": 6800.0, "source": "fallback"}
     if os.path.exists(p):
         with open(p) as f:
             d = json.load(f)
         peaks = {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
-    # FP64 FMA throughput measured on this machine's GB300 (profiles/fp64_peak_gb300.md)
-    peaks["fp64_tflops"] = 1.19
+    # FP64 FMA throughput of this GPU, measured live (independent FMA chains on every SM)
+    peaks["fp64_tflops"] = te.probe_fp64_tflops()
     return peaks
 
 
@@ -228,7 +228,7 @@ def run_gb300(args):
             dist.destroy_process_group()
         return
     value = ms / 1000.0 / args.steps / ws
-    peaks = load_peaks()
+    peaks = load_peaks(te)
     b_apply = apply_kernel_bytes(n, nnz, info["real"])
     f_apply = apply_kernel_flops(n, nnz, info["real"])
     avg_apply_s = apply_ms / 1000.0 / max(1, apply_n)
@@ -250,6 +250,7 @@ def run_gb300(args):
                      "traffic": traffic, "algorithmic_bytes_per_launch": b_apply,
                      "avg_launch_us": avg_apply_s * 1e6, "launches": apply_n,
                      "fp64": {"achieved_tflops": f_apply / avg_apply_s / 1e12, "peak_tflops": peaks["fp64_tflops"],
+                              "peak_source": "measured (te_probe_fp64_tflops)",
                               "frac": f_apply / avg_apply_s / 1e12 / peaks["fp64_tflops"],
                               "flops_per_launch": f_apply}},
         "kernel_ms_per_solve": {k: round(v_[0] / args.steps, 3) for k, v_ in kernel_ms.items()},
@@ -308,6 +309,17 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def ncu_case(t_final):
+    """A short solve of the same workload for ncu captures (t_final instead of 10)."""
+    import timeevolver_gb300 as te
+    te.build()
+    te.lib().te_set_device(0)
+    n, Hc, Oc, v = build_problem()
+    out = te.evolve(Hc, v, t_final, t_final, [("sparse", Oc)], tol=TOL * t_final / T_FINAL, m=M_KRYLOV)
+    print("ncu case: t=%g, %d Krylov steps, status %d, %d launches" % (t_final, out["n_steps"], out["status"],
+                                                                      out["launches"]))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -315,7 +327,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ncu-case", type=float, default=None, metavar="T",
+                    help="run one short solve to time T (for ncu captures) and exit")
     args = ap.parse_args()
+    if args.ncu_case is not None:
+        ncu_case(args.ncu_case)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -24,9 +24,18 @@ def test_library_exports_all_declared_symbols():
     import timeevolver_gb300 as te
     te.build()
     lib = ctypes.CDLL(te.LIB_PATH)
-    missing = [n for n in _declared("tegpu.h") if not hasattr(lib, n)]
+    declared = _declared("tegpu.h") + _declared("te_diag.h")
+    missing = [n for n in declared if not hasattr(lib, n)]
     assert not missing, missing
-    assert set(_declared("tegpu.h")) <= set(te.SIGNATURES)
+    assert set(declared) <= set(te.SIGNATURES)
+
+
+def test_model_library_exports_all_declared_symbols():
+    import timeevolver_gb300 as te
+    te.build()
+    lib = ctypes.CDLL(os.path.join(os.path.dirname(te.LIB_PATH), "libtimeevolver.so"))
+    missing = [n for n in _declared("te_model.h") if not hasattr(lib, n)]
+    assert not missing, missing
 
 
 def test_missing_library_fails_loudly(tmp_path, monkeypatch):

@@ -81,6 +81,7 @@ SIGNATURES = {
     "te_evolver_stream": (_P, [_P]),
     "te_evolver_profile": (_I, [_P, _I]),
     "te_evolver_kernel_time": (_I, [_P, _I, _P, _P]),
+    "te_probe_fp64_tflops": (_I, [_P]),
 }
 
 _lib = None
@@ -111,6 +112,13 @@ def lib():
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+def probe_fp64_tflops():
+    """Measured FP64 FMA throughput of the current device (TFLOP/s)."""
+    x = ctypes.c_double()
+    _check(lib().te_probe_fp64_tflops(ctypes.byref(x)), "te_probe_fp64_tflops")
+    return x.value
 
 
 def _check(rc, where):

@@ -20,7 +20,8 @@ HOST = os.path.join(HERE, "host")
 LIB_TEGPU = os.path.join(BUILD, "libtegpu.so")
 LIB_HOST = os.path.join(BUILD, "libtimeevolver.so")
 
-CUDA_SOURCES = ["te_common.cu", "te_matrix.cu", "te_lanczos.cu", "te_krylov.cu", "te_sample.cu", "te_evolver.cu"]
+CUDA_SOURCES = ["te_common.cu", "te_matrix.cu", "te_lanczos.cu", "te_krylov.cu", "te_sample.cu", "te_evolver.cu",
+                "te_probe.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC"]
 HOST_SOURCES = ["matrixDataTypes.cpp", "krylovObservables.cpp", "krylovTimeEvolver.cpp", "krylovLogger.cpp",
@@ -61,7 +62,7 @@ def _run(cmd):
 def build_tegpu(force=False, verbose=False):
     os.makedirs(BUILD, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
-    headers.append(os.path.join(ROOT, "include", "tegpu.h"))
+    headers += [os.path.join(ROOT, "include", h) for h in ("tegpu.h", "te_diag.h")]
     srcs = [os.path.join(CSRC, f) for f in CUDA_SOURCES]
     if not force and not _stale(LIB_TEGPU, srcs + headers):
         return LIB_TEGPU

@@ -129,7 +129,11 @@ typedef struct te_params {
   int32_t m;             /* Krylov dimension (clamped to the Hilbert dimension) */
   int32_t fast_integration; /* Gauss 15/7 instead of tanh-sinh */
   int32_t progress_bar;  /* accepted for API parity; the GPU path prints nothing */
-  int32_t reserved;
+  int32_t reorth;        /* 0: the reference's three-term Lanczos recurrence
+                            (krylovTimeEvolver.cpp:537-546); 1: classical
+                            Gram-Schmidt against all previous basis vectors
+                            plus one reorthogonalisation pass (no counterpart
+                            in the reference; numerically stable basis) */
 } te_params;
 
 /* Result record of one evolution (krylovReturn, krylovTimeEvolver.h:32-51). */

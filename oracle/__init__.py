@@ -58,7 +58,7 @@ def lib():
         L = ctypes.CDLL(LIB_PATH)
         P = ctypes.c_void_p
         I64, D, I = ctypes.c_int64, ctypes.c_double, ctypes.c_int
-        L.oracle_evolve.argtypes = [I64, I64, P, P, P, P, D, D, D, D, I, I, I, P, P, P, P, P, I64, P, I]
+        L.oracle_evolve.argtypes = [I64, I64, P, P, P, P, D, D, D, D, I, I, I, I, P, P, P, P, P, I64, P, I]
         L.oracle_evolve.restype = I
         L.oracle_spmv.argtypes = [I64, I64, P, P, P, D, D, P, P]
         L.oracle_norm1.argtypes = [I64, I64, P, P]
@@ -85,7 +85,7 @@ def _coo(H):
 
 
 def evolve(H, v, t, sampling_step, observables=(), exp_factor=1.0, tol=1e-6, m=40, fast_integration=False,
-           n_threads=0, trace=False, max_trace=100000):
+           n_threads=0, trace=False, max_trace=100000, reorth=False):
     """Run the oracle evolution.  H is a COO triple (row, col, val) of size n.
 
     ``observables`` is a list of ("sparse", (row, col, val)), ("vector", o) or
@@ -122,7 +122,8 @@ def evolve(H, v, t, sampling_step, observables=(), exp_factor=1.0, tol=1e-6, m=4
     tr = (OracleStep * max_trace)() if trace else None
     ntr = ctypes.c_int64(0)
     rc = lib().oracle_evolve(n, len(val), _p(row), _p(col), _p(val), _p(v), t, sampling_step, exp_factor, tol, m,
-                             int(fast_integration), len(observables), ctypes.addressof(obs_arr), _p(samples),
+                             int(fast_integration), int(reorth), len(observables), ctypes.addressof(obs_arr),
+                             _p(samples),
                              _p(state), ctypes.byref(res), ctypes.addressof(tr) if tr is not None else None,
                              max_trace, ctypes.byref(ntr), n_threads)
     if rc != 0:

@@ -342,6 +342,7 @@ struct Evolver {
   cd expFactor;
   size_t m, Hsize;
   bool fastIntegration;
+  int reorth = 0;  // 1: classical Gram-Schmidt + one reorthogonalisation pass
   double matrixNorm;
   // observables
   struct Obs {
@@ -465,19 +466,31 @@ struct Evolver {
     return code;
   }
 
-  // arnoldiAlgorithm (core/krylovTimeEvolver.cpp:523-571)
+  // arnoldiAlgorithm (core/krylovTimeEvolver.cpp:523-571); with reorth != 0
+  // the three-term update is replaced by classical Gram-Schmidt against all
+  // previous vectors plus one reorthogonalisation pass (CGS2), keeping the
+  // tridiagonal coefficients H[j,j] = p1_j + p2_j and beta = ||w||.
   bool lanczos(double tolRate, std::vector<cd>& Hm, std::vector<cd>& V, double* hRet, size_t* mRet) {
     const int64_t n = (int64_t)Hsize;
     std::copy(currentVec.begin(), currentVec.end(), V.begin());
     for (size_t j = 0; j < m; ++j) {
       cd* vj = V.data() + j * n;
       spmv(H, expFactor, vj, tmpBlasVec.data());
+      if (reorth) {
+        std::vector<cd> p1(j + 1), p2(j + 1);
+        for (size_t i = 0; i <= j; ++i) p1[i] = zdotc(n, V.data() + i * n, tmpBlasVec.data());
+        for (size_t i = 0; i <= j; ++i) zaxpy(n, -p1[i], V.data() + i * n, tmpBlasVec.data());
+        for (size_t i = 0; i <= j; ++i) p2[i] = zdotc(n, V.data() + i * n, tmpBlasVec.data());
+        for (size_t i = 0; i <= j; ++i) zaxpy(n, -p2[i], V.data() + i * n, tmpBlasVec.data());
+        Hm[j + j * m] = p1[j] + p2[j];
+      } else {
       if (j != 0) {
         cd negH = -1.0 * Hm[j - 1 + j * m];
         zaxpy(n, negH, V.data() + (j - 1) * n, tmpBlasVec.data());
       }
       Hm[j + j * m] = zdotc(n, vj, tmpBlasVec.data());
       zaxpy(n, -1.0 * Hm[j + j * m], vj, tmpBlasVec.data());
+      }
       double normy = dznrm2(n, tmpBlasVec.data());
       if (normy < tolRate) {
         *mRet = j + 1;
@@ -659,9 +672,9 @@ double norm1_coo(int64_t n, int64_t nnz, const int64_t* col, const double* val) 
 
 extern "C" int oracle_evolve(int64_t n, int64_t nnz, const int64_t* row, const int64_t* col, const double* val,
                              const double* v, double t, double sampling_step, double exp_factor, double tol,
-                             int m, int fast_integration, int n_obs, const oracle_obs* obs, double* samples,
-                             double* state_out, oracle_result* result, oracle_step* trace, int64_t max_trace,
-                             int64_t* n_trace, int n_threads) {
+                             int m, int fast_integration, int reorth, int n_obs, const oracle_obs* obs,
+                             double* samples, double* state_out, oracle_result* result, oracle_step* trace,
+                             int64_t max_trace, int64_t* n_trace, int n_threads) {
 #ifdef _OPENMP
   if (n_threads > 0) omp_set_num_threads(n_threads);
 #else
@@ -677,6 +690,7 @@ extern "C" int oracle_evolve(int64_t n, int64_t nnz, const int64_t* row, const i
   E.tol = tol;
   E.expFactor = cd(0, -1 * exp_factor);
   E.fastIntegration = fast_integration != 0;
+  E.reorth = reorth;
   E.matrixNorm = norm1_coo(n, nnz, col, val);
   E.Hsize = (size_t)n;
   E.m = std::min<size_t>((size_t)m, E.Hsize);

@@ -59,6 +59,8 @@ typedef struct oracle_step {
 } oracle_step;
 
 /* Full evolution, restating krylovTimeEvolver(...) + timeEvolve().
+ * reorth != 0 replaces the three-term Lanczos update by classical
+ * Gram-Schmidt with one reorthogonalisation pass (the GPU's stable mode).
  * samples: n_obs * n_samples_total doubles (row per observable), may be NULL.
  * state_out: complex n (the last sampled state), may be NULL.
  * trace: up to max_trace step records (may be NULL); *n_trace receives the count.
@@ -66,7 +68,7 @@ typedef struct oracle_step {
  * would exit(1) there). */
 int oracle_evolve(int64_t n, int64_t nnz, const int64_t* row, const int64_t* col, const double* val,
                   const double* v, double t, double sampling_step, double exp_factor, double tol,
-                  int m, int fast_integration, int n_obs, const oracle_obs* obs, double* samples,
+                  int m, int fast_integration, int reorth, int n_obs, const oracle_obs* obs, double* samples,
                   double* state_out, oracle_result* result, oracle_step* trace, int64_t max_trace,
                   int64_t* n_trace, int n_threads);
 

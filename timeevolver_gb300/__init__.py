@@ -33,7 +33,7 @@ STATUS = {0: "ok", 1: "lucky breakdown", 2: "analytic error below roundoff estim
 class TeParams(ctypes.Structure):
     _fields_ = [("t", ctypes.c_double), ("sampling_step", ctypes.c_double), ("exp_factor", ctypes.c_double),
                 ("tol", ctypes.c_double), ("m", ctypes.c_int32), ("fast_integration", ctypes.c_int32),
-                ("progress_bar", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("progress_bar", ctypes.c_int32), ("reorth", ctypes.c_int32)]
 
 
 class TeResult(ctypes.Structure):
@@ -180,11 +180,11 @@ class Evolver:
     (requestStopException)."""
 
     def __init__(self, H, v, t, sampling_step, observables=(), exp_factor=1.0, tol=1e-6, m=40,
-                 fast_integration=False):
+                 fast_integration=False, reorth=False):
         self.H = H
         self.n = H.n
         v = np.ascontiguousarray(v, dtype=np.complex128)
-        p = TeParams(t, sampling_step, exp_factor, tol, int(m), int(bool(fast_integration)), 0, 0)
+        p = TeParams(t, sampling_step, exp_factor, tol, int(m), int(bool(fast_integration)), 0, int(bool(reorth)))
         self.handle = ctypes.c_void_p()
         _check(lib().te_evolver_create(H.handle, _ptr(v), ctypes.byref(p), ctypes.byref(self.handle)),
                "te_evolver_create")
@@ -287,7 +287,7 @@ class StopEvolution(Exception):
 
 
 def evolve(H_coo, v, t, sampling_step, observables=(), exp_factor=1.0, tol=1e-6, m=40, fast_integration=False,
-           trace=False):
+           trace=False, reorth=False):
     """One-call evolution with COO inputs, mirroring the oracle's signature.
 
     ``observables``: ("sparse", (row, col, val)), ("vector", o) or
@@ -300,7 +300,7 @@ def evolve(H_coo, v, t, sampling_step, observables=(), exp_factor=1.0, tol=1e-6,
             obs.append(("sparse", Matrix.from_coo(n, data)))
         else:
             obs.append((kind, data))
-    ev = Evolver(H, v, t, sampling_step, obs, exp_factor, tol, m, fast_integration)
+    ev = Evolver(H, v, t, sampling_step, obs, exp_factor, tol, m, fast_integration, reorth)
     try:
         return ev.time_evolve(trace=trace)
     finally:

@@ -304,17 +304,28 @@ int run(te_evolver ev, te_result* out) {
     err_prev = S->err;
     // STEP 1: Lanczos (:338)
     for (int j = 0; j < m; ++j) {
+      const bool cgs2 = ev->p.reorth != 0;
       {
         ProfScope ps(ev, 0);
-        te_launch_lanczos_apply(ev->H->sell, ev->H->is_real, ev->cols[j], j > 0 ? ev->cols[j - 1] : nullptr, ev->w,
-                                ev->ds, ev->partials, j, st);
+        te_launch_lanczos_apply(ev->H->sell, ev->H->is_real, ev->cols[j],
+                                (j > 0 && !cgs2) ? ev->cols[j - 1] : nullptr, ev->w, ev->ds, ev->partials, j, st);
       }
-      {
+      if (!cgs2) {
         ProfScope ps(ev, 1);
         te_launch_lanczos_update(n, ev->w, ev->cols[j], j + 1 < m ? ev->cols[j + 1] : nullptr, ev->ds, ev->partials,
                                  j, st);
+        ev->launches += 2;
+      } else {
+        // classical Gram-Schmidt against u_0..u_j, then one reorthogonalisation pass
+        TeBasisPtrs V{};
+        for (int i = 0; i <= j; ++i) V.u[i] = ev->cols[i];
+        ProfScope ps(ev, 1);
+        te_launch_gs_project(n, V, j + 1, ev->w, ev->ds, ev->partials, st);
+        te_launch_gs_update_project(n, V, j + 1, ev->w, ev->ds, ev->partials, st);
+        te_launch_gs_update_norm(n, V, j + 1, ev->w, j + 1 < m ? ev->cols[j + 1] : nullptr, ev->ds, ev->partials, j,
+                                 st);
+        ev->launches += 4;
       }
-      ev->launches += 2;
     }
     // STEP 1b-3: Krylov-space kernel (eigen data, step search, w, first batch)
     {
@@ -448,8 +459,9 @@ extern "C" int te_evolver_create(te_matrix H, const double* v_host, const te_par
     return TE_ERR_INVALID_ARG;
   }
   const te_params& p = *params;
-  if (!(p.t > 0.0) || !(p.sampling_step > 0.0) || !(p.tol > 0.0) || p.m < 1 || !std::isfinite(p.exp_factor)) {
-    te_set_error("te_evolver_create: t, sampling_step, tol must be positive and m >= 1");
+  if (!(p.t > 0.0) || !(p.sampling_step > 0.0) || !(p.tol > 0.0) || p.m < 1 || !std::isfinite(p.exp_factor) ||
+      p.reorth < 0 || p.reorth > 1) {
+    te_set_error("te_evolver_create: t, sampling_step, tol must be positive, m >= 1, reorth 0 or 1");
     return TE_ERR_INVALID_ARG;
   }
   const int64_t n = H->n_rows;

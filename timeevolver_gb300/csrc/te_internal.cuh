@@ -70,6 +70,9 @@ struct TeDevState {
   // reduction counters ("last block finishes" pattern)
   unsigned int counter[4];
   double norm2_final;  // ||sampledState||^2 of the final norm check
+  // Gram-Schmidt projections of the reorthogonalising mode (two passes)
+  double2 proj1[TE_MMAX];
+  double2 proj2[TE_MMAX];
 };
 
 // SELL-32 matrix in the sorted (permuted) basis.
@@ -122,6 +125,17 @@ void te_launch_lanczos_apply(const TeSell& A, bool is_real, const double2* u_j, 
                              TeDevState* ds, double* partials, int j, cudaStream_t st);
 void te_launch_lanczos_update(int64_t n, const double2* w, const double2* u_j, double2* u_jp1, TeDevState* ds,
                               double* partials, int j, cudaStream_t st);
+// Gram-Schmidt passes of the reorthogonalising Lanczos mode (te_lanczos.cu)
+#define TE_GS_ROWS 2048  // rows per block of the Gram-Schmidt passes
+struct TeBasisPtrs {
+  const double2* u[TE_MMAX];
+};
+void te_launch_gs_project(int64_t n, const TeBasisPtrs& V, int nvec, const double2* w, TeDevState* ds,
+                          double* partials, cudaStream_t st);
+void te_launch_gs_update_project(int64_t n, const TeBasisPtrs& V, int nvec, double2* w, TeDevState* ds,
+                                 double* partials, cudaStream_t st);
+void te_launch_gs_update_norm(int64_t n, const TeBasisPtrs& V, int nvec, const double2* w, double2* u_next,
+                              TeDevState* ds, double* partials, int j, cudaStream_t st);
 // te_krylov.cu
 int te_upload_quad_tables();
 void te_launch_krylov_step(TeDevState* ds, cudaStream_t st);

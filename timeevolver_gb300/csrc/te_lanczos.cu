@@ -13,6 +13,8 @@
 // a vector.  Each pass finishes its reduction in the last block to complete
 // (fixed order), so the Krylov coefficients never leave the device.  Pass 1
 // runs on the SELL-32 layout: a warp owns 32 equal-length rows.
+#include <algorithm>
+
 #include "te_internal.cuh"
 #include "te_reduce.cuh"
 #include "te_sell.cuh"
@@ -104,18 +106,207 @@ __global__ void __launch_bounds__(TE_THREADS) lanczos_update_kernel(int64_t n, c
   }
 }
 
+// --------------------------------------------------------------------------
+// Reorthogonalising mode: classical Gram-Schmidt with one reorthogonalisation
+// pass (CGS2) against all previous basis vectors.  Iteration j, after
+// w = A v_j (apply kernel without the three-term term):
+//   project:          p1_i = <v_i, w>                         i = 0..j
+//   update + project: w' = w - sum_i p1_i v_i,  p2_i = <v_i, w'>
+//   update + norm:    u_{j+1} = w' - sum_i p2_i v_i, beta_{j+1} = ||u_{j+1}||
+// alpha_j = p1_j + p2_j; the tridiagonal Krylov matrix keeps alpha and beta
+// (the remaining projections vanish up to rounding for an anti-Hermitian A).
+// A block owns TE_GS_ROWS consecutive rows and keeps its slice of w in shared
+// memory; each warp accumulates the projections of its share of the basis
+// vectors over the block's rows (coalesced reads of every u_i).
+
+__device__ __forceinline__ int gs_row_begin(int64_t n) {
+  return (int)min((int64_t)blockIdx.x * TE_GS_ROWS, n);
+}
+
+// Per-warp projections <u_i, w_s> over the block's rows, i = warp, warp + 8, ...;
+// partial sums (re, im) of vector i go to partials[(2 i + c) * gridDim.x + block].
+__device__ void gs_block_projections(int rows, int64_t r0, const double2* const* u_s, int nvec,
+                                     const double2* w_s, double* partials) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int i = warp; i < nvec; i += nw) {
+    const double2* __restrict__ u = u_s[i] + r0;
+    double re = 0.0, im = 0.0;
+    for (int r = lane; r < rows; r += 32) {
+      const double2 a = u[r], b = w_s[r];
+      re = fma(a.x, b.x, fma(a.y, b.y, re));
+      im = fma(a.x, b.y, fma(-a.y, b.x, im));
+    }
+    re = te_warp_sum(re);
+    im = te_warp_sum(im);
+    if (lane == 0) {
+      partials[(2 * i) * gridDim.x + blockIdx.x] = re;
+      partials[(2 * i + 1) * gridDim.x + blockIdx.x] = im;
+      __threadfence();
+    }
+  }
+}
+
+// Last block: proj[i] = s_i * sum over blocks (fixed order), i < nvec.
+__device__ void gs_finish(int nvec, const double* partials, double2* proj, const TeDevState* ds) {
+  __shared__ double red[2][TE_MMAX];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int v = warp; v < 2 * nvec; v += nw) {
+    double s = 0.0;
+    for (int b = lane; b < (int)gridDim.x; b += 32) s += __ldcg(partials + (int64_t)v * gridDim.x + b);
+    s = te_warp_sum(s);
+    if (lane == 0) red[v & 1][v >> 1] = s;
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < nvec) {
+    const double si = ds->s[threadIdx.x];
+    proj[threadIdx.x] = make_double2(si * red[0][threadIdx.x], si * red[1][threadIdx.x]);
+  }
+}
+
+__device__ __forceinline__ bool gs_last_block(unsigned int* counter) {
+  __shared__ bool is_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    is_last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (is_last) __threadfence();
+  return is_last;
+}
+
+__global__ void __launch_bounds__(TE_THREADS) gs_project_kernel(int64_t n, TeBasisPtrs V, int nvec,
+                                                                const double2* __restrict__ w, TeDevState* ds,
+                                                                double* partials) {
+  __shared__ double2 w_s[TE_GS_ROWS];
+  __shared__ const double2* u_s[TE_MMAX];
+  if (te_step_inactive(ds)) return;
+  if ((int)threadIdx.x < nvec) u_s[threadIdx.x] = V.u[threadIdx.x];
+  const int64_t r0 = gs_row_begin(n);
+  const int rows = (int)min((int64_t)TE_GS_ROWS, n - r0);
+  for (int r = threadIdx.x; r < rows; r += blockDim.x) w_s[r] = w[r0 + r];
+  __syncthreads();
+  gs_block_projections(rows, r0, u_s, nvec, w_s, partials);
+  if (gs_last_block(&ds->counter[0])) {
+    gs_finish(nvec, partials, ds->proj1, ds);
+    if (threadIdx.x == 0) ds->counter[0] = 0u;
+  }
+}
+
+__global__ void __launch_bounds__(TE_THREADS) gs_update_project_kernel(int64_t n, TeBasisPtrs V, int nvec,
+                                                                       double2* __restrict__ w, TeDevState* ds,
+                                                                       double* partials) {
+  __shared__ double2 w_s[TE_GS_ROWS];
+  __shared__ double2 c_s[TE_MMAX];
+  __shared__ const double2* u_s[TE_MMAX];
+  if (te_step_inactive(ds)) return;
+  if ((int)threadIdx.x < nvec) {
+    const double si = ds->s[threadIdx.x];
+    const double2 p = ds->proj1[threadIdx.x];
+    c_s[threadIdx.x] = make_double2(p.x * si, p.y * si);  // w -= p1_i v_i = (p1_i s_i) u_i
+    u_s[threadIdx.x] = V.u[threadIdx.x];
+  }
+  __syncthreads();
+  const int64_t r0 = gs_row_begin(n);
+  const int rows = (int)min((int64_t)TE_GS_ROWS, n - r0);
+  for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+    double2 x = w[r0 + r];
+    for (int i = 0; i < nvec; ++i) {
+      const double2 u = u_s[i][r0 + r], c = c_s[i];
+      x.x = fma(-c.x, u.x, fma(c.y, u.y, x.x));
+      x.y = fma(-c.x, u.y, fma(-c.y, u.x, x.y));
+    }
+    w_s[r] = x;
+    w[r0 + r] = x;
+  }
+  __syncthreads();
+  gs_block_projections(rows, r0, u_s, nvec, w_s, partials);
+  if (gs_last_block(&ds->counter[0])) {
+    gs_finish(nvec, partials, ds->proj2, ds);
+    if (threadIdx.x == 0) ds->counter[0] = 0u;
+  }
+}
+
+__global__ void __launch_bounds__(TE_THREADS) gs_update_norm_kernel(int64_t n, TeBasisPtrs V, int nvec,
+                                                                    const double2* __restrict__ w,
+                                                                    double2* __restrict__ u_next, TeDevState* ds,
+                                                                    double* partials, int j) {
+  __shared__ double2 c_s[TE_MMAX];
+  __shared__ const double2* u_s[TE_MMAX];
+  __shared__ double scratch[32];
+  if (te_step_inactive(ds)) return;
+  if ((int)threadIdx.x < nvec) {
+    const double si = ds->s[threadIdx.x];
+    const double2 p = ds->proj2[threadIdx.x];
+    c_s[threadIdx.x] = make_double2(p.x * si, p.y * si);
+    u_s[threadIdx.x] = V.u[threadIdx.x];
+  }
+  __syncthreads();
+  double acc[1] = {0.0};
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    double2 x = w[r];
+    for (int i = 0; i < nvec; ++i) {
+      const double2 u = u_s[i][r], c = c_s[i];
+      x.x = fma(-c.x, u.x, fma(c.y, u.y, x.x));
+      x.y = fma(-c.x, u.y, fma(-c.y, u.x, x.y));
+    }
+    if (u_next) u_next[r] = x;
+    acc[0] = fma(x.x, x.x, fma(x.y, x.y, acc[0]));
+  }
+  te_block_sum<1>(acc, scratch);
+  if (te_publish_partials<1>(acc, partials, &ds->counter[1])) {
+    double tot[1];
+    te_final_sum<1>(tot, partials, &ds->counter[1], scratch);
+    if (threadIdx.x == 0) {
+      const double2 a1 = ds->proj1[j], a2 = ds->proj2[j];
+      ds->alpha[j] = make_double2(a1.x + a2.x, a1.y + a2.y);
+      const double beta = sqrt(tot[0]);
+      const int m = ds->m_cur;
+      if (beta < ds->tol_rate) {
+        ds->breakdown = 1;
+        ds->m_eff = j + 1;
+        ds->h = beta;
+      } else if (j + 1 != m) {
+        ds->beta[j + 1] = beta;
+        ds->s[j + 1] = 1.0 / beta;
+      } else {
+        ds->h = beta;
+        ds->m_eff = m;
+      }
+    }
+  }
+}
+
+static int gs_grid(int64_t n) { return (int)std::max<int64_t>(1, (n + TE_GS_ROWS - 1) / TE_GS_ROWS); }
+
+void te_launch_gs_project(int64_t n, const TeBasisPtrs& V, int nvec, const double2* w, TeDevState* ds,
+                          double* partials, cudaStream_t st) {
+  gs_project_kernel<<<gs_grid(n), TE_THREADS, 0, st>>>(n, V, nvec, w, ds, partials);
+}
+
+void te_launch_gs_update_project(int64_t n, const TeBasisPtrs& V, int nvec, double2* w, TeDevState* ds,
+                                 double* partials, cudaStream_t st) {
+  gs_update_project_kernel<<<gs_grid(n), TE_THREADS, 0, st>>>(n, V, nvec, w, ds, partials);
+}
+
+void te_launch_gs_update_norm(int64_t n, const TeBasisPtrs& V, int nvec, const double2* w, double2* u_next,
+                              TeDevState* ds, double* partials, int j, cudaStream_t st) {
+  gs_update_norm_kernel<<<te_grid_for(n, TE_THREADS, 8), TE_THREADS, 0, st>>>(n, V, nvec, w, u_next, ds, partials,
+                                                                                j);
+}
+
 void te_launch_lanczos_apply(const TeSell& A, bool is_real, const double2* u_j, const double2* u_jm1, double2* w,
                              TeDevState* ds, double* partials, int j, cudaStream_t st) {
   const int grid = te_grid_for(A.n_chunks * 32, TE_THREADS, 8);
   if (is_real) {
-    if (j > 0)
+    if (u_jm1)
       lanczos_apply_kernel<true, true><<<grid, TE_THREADS, 0, st>>>(A.n, A.n_chunks, A.chunk_off, A.col, A.val, u_j,
                                                                     u_jm1, w, ds, partials, j);
     else
       lanczos_apply_kernel<true, false><<<grid, TE_THREADS, 0, st>>>(A.n, A.n_chunks, A.chunk_off, A.col, A.val, u_j,
                                                                      u_jm1, w, ds, partials, j);
   } else {
-    if (j > 0)
+    if (u_jm1)
       lanczos_apply_kernel<false, true><<<grid, TE_THREADS, 0, st>>>(A.n, A.n_chunks, A.chunk_off, A.col, A.val, u_j,
                                                                      u_jm1, w, ds, partials, j);
     else

@@ -210,6 +210,34 @@ void* te_evolver_stream(te_evolver ev);
 int te_evolver_profile(te_evolver ev, int enable);
 int te_evolver_kernel_time(te_evolver ev, int kind, double* total_ms, int64_t* launches);
 
+/* ------------------------------------------------------- batched evolutions */
+
+/* Many independent evolutions of uneven dimension advanced together: each
+ * instance is a krylovTimeEvolver (own H, v, t, sampling step, tolerance,
+ * Krylov dimension, step size and status), all instances share every kernel
+ * launch of a Krylov step (segmented SELL-32 matrix over the concatenated
+ * rows, per-instance reductions, one Krylov-space block per instance), and the
+ * launches of one step are replayed as a CUDA graph.  No counterpart in the
+ * reference (which runs one evolution per krylovTimeEvolver); per instance
+ * the results equal those of te_evolver_run with the same inputs.
+ * Restrictions: reorth 0, up to 4 diagonal observables per instance. */
+typedef struct te_batch_s* te_batch;
+
+/* H[i] (square, caller-owned, must outlive the batch), v_host[i] (complex
+ * n_i, copied) and params[i] for i < n_instances. */
+int te_batch_create(int n_instances, const te_matrix* H, const double* const* v_host, const te_params* params,
+                    te_batch* out);
+int te_batch_destroy(te_batch b);
+/* A diagonal observable of one instance (Re <psi|O|psi>, krylovSpMatrixObservable). */
+int te_batch_add_observable(te_batch b, int instance, te_matrix O);
+/* Run every instance to its final time; results[i] as te_evolver_run (may be NULL).
+ * A batch can be run again (same inputs). */
+int te_batch_run(te_batch b, te_result* results);
+int te_batch_samples(te_batch b, int instance, int obs_index, double* out_host, int64_t count);
+int te_batch_state(te_batch b, int instance, double* out_host);
+int64_t te_batch_launch_count(te_batch b);
+void* te_batch_stream(te_batch b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -82,6 +82,14 @@ SIGNATURES = {
     "te_evolver_profile": (_I, [_P, _I]),
     "te_evolver_kernel_time": (_I, [_P, _I, _P, _P]),
     "te_probe_fp64_tflops": (_I, [_P]),
+    "te_batch_create": (_I, [_I, _P, _P, _P, _P]),
+    "te_batch_destroy": (_I, [_P]),
+    "te_batch_add_observable": (_I, [_P, _I, _P]),
+    "te_batch_run": (_I, [_P, _P]),
+    "te_batch_samples": (_I, [_P, _I, _I, _P, _I64]),
+    "te_batch_state": (_I, [_P, _I, _P]),
+    "te_batch_launch_count": (_I64, [_P]),
+    "te_batch_stream": (_P, [_P]),
 }
 
 _lib = None
@@ -273,6 +281,75 @@ class Evolver:
     def close(self):
         if self.handle:
             lib().te_evolver_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many independent evolutions advanced together (te_batch_*).
+
+    ``instances``: list of dicts with keys H (Matrix), v, t, sampling_step and
+    optional tol, m, exp_factor, fast_integration, observables (list of
+    diagonal Matrix objects)."""
+
+    def __init__(self, instances):
+        B = len(instances)
+        self._keep = []
+        Hs = (ctypes.c_void_p * B)()
+        vs = (ctypes.c_void_p * B)()
+        ps = (TeParams * B)()
+        self.n_samples, self.dims, self.n_obs = [], [], []
+        for i, ins in enumerate(instances):
+            v = np.ascontiguousarray(ins["v"], dtype=np.complex128)
+            self._keep += [v, ins["H"]]
+            Hs[i] = ins["H"].handle
+            vs[i] = v.ctypes.data
+            t, dt = float(ins["t"]), float(ins["sampling_step"])
+            ps[i] = TeParams(t, dt, float(ins.get("exp_factor", 1.0)), float(ins.get("tol", 1e-6)),
+                             int(ins.get("m", 40)), int(bool(ins.get("fast_integration", False))), 0, 0)
+            self.n_samples.append(int(np.floor(t / dt)) + 1)
+            self.dims.append(len(v))
+        self.handle = ctypes.c_void_p()
+        _check(lib().te_batch_create(B, Hs, vs, ps, ctypes.byref(self.handle)), "te_batch_create")
+        for i, ins in enumerate(instances):
+            obs = ins.get("observables", [])
+            for O in obs:
+                self._keep.append(O)
+                _check(lib().te_batch_add_observable(self.handle, i, O.handle), "te_batch_add_observable")
+            self.n_obs.append(len(obs))
+        self.B = B
+
+    def run(self):
+        res = (TeResult * self.B)()
+        _check(lib().te_batch_run(self.handle, res), "te_batch_run")
+        return [dict(err=r.err, evolved_time=r.evolved_time, num_samples=r.num_samples, n_steps=r.n_steps,
+                     dim=r.dim, krylov_dim=r.krylov_dim, status=r.status) for r in res]
+
+    def samples(self, i):
+        out = np.zeros((self.n_obs[i], self.n_samples[i]))
+        for k in range(self.n_obs[i]):
+            _check(lib().te_batch_samples(self.handle, i, k, _ptr(out[k]), self.n_samples[i]), "te_batch_samples")
+        return out
+
+    def state(self, i):
+        st = np.zeros(self.dims[i], dtype=np.complex128)
+        _check(lib().te_batch_state(self.handle, i, _ptr(st)), "te_batch_state")
+        return st
+
+    def launch_count(self):
+        return lib().te_batch_launch_count(self.handle)
+
+    def stream(self):
+        return lib().te_batch_stream(self.handle)
+
+    def close(self):
+        if self.handle:
+            lib().te_batch_destroy(self.handle)
             self.handle = ctypes.c_void_p()
 
     def __del__(self):

@@ -1,0 +1,795 @@
+// te_batch.cu -- many independent evolutions of uneven dimension at once.
+//
+// Every instance runs the algorithm of krylovTimeEvolver::timeEvolve
+// (core/krylovTimeEvolver.cpp:261-512) with its own H, v, t, tolerance, step
+// size, Krylov dimension and status; the instances advance together, one
+// Krylov step of every active instance per global step:
+//   * one segmented SELL-32 matrix over the concatenated (length-sorted) rows of
+//     all instances; a chunk of 32 rows never straddles two instances, so a warp
+//     always works for one instance and reads its scalars once;
+//   * each Lanczos iteration is one apply pass and one update pass over every
+//     active instance's rows, each followed by a per-instance reduction of
+//     per-chunk partials in a fixed order (deterministic);
+//   * the Krylov-space work (exponential, error integrals, step size, sample
+//     schedule) runs one thread block per instance;
+//   * the whole sequence of one global step (4 m_max Lanczos kernels, Krylov
+//     kernel, combine, observables, flag gather) is captured once as a CUDA
+//     graph and replayed; the host syncs once per global step.
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "te_internal.cuh"
+#include "te_reduce.cuh"
+#include "te_sell.cuh"
+
+#define TE_BATCH_MAX_OBS 4
+
+namespace {
+
+struct BatchGeom {
+  int64_t n_chunks;
+  const int32_t* chunk_inst;  // instance of every chunk
+  const int64_t* chunk_off;   // global SELL slot offsets (n_chunks + 1)
+  const int32_t* col;         // global row indices
+  const double* val;
+  const int64_t* inst_row;    // first global row of each instance
+  const int32_t* inst_n;      // dimension of each instance
+  const int64_t* inst_chunk;  // first chunk of each instance (n_inst + 1)
+  int64_t ld;                 // leading dimension of the basis (total padded rows)
+};
+
+__device__ __forceinline__ bool lanczos_skip(const TeDevState* ds, int j) {
+  return ds->fatal != 0 || ds->done != 0 || ds->breakdown != 0 || j >= ds->m_cur;
+}
+
+template <bool REAL, bool HAS_PREV>
+__global__ void __launch_bounds__(TE_THREADS) batch_apply_kernel(BatchGeom g, const double2* __restrict__ V,
+                                                                 double2* __restrict__ w, TeDevState* states,
+                                                                 double* chunk_partials, int j) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const double2* __restrict__ u_j = V + (int64_t)j * g.ld;
+  const double2* __restrict__ u_jm1 = HAS_PREV ? V + (int64_t)(j - 1) * g.ld : nullptr;
+  for (int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < g.n_chunks; c += warps) {
+    const int inst = __ldg(g.chunk_inst + c);
+    const TeDevState* ds = states + inst;
+    if (lanczos_skip(ds, j)) continue;
+    const double sj = ds->s[j];
+    const double gg = ds->exp_factor * sj;
+    const double cprev = HAS_PREV ? ds->beta[j] * ds->s[j - 1] : 0.0;
+    const double2 y = te_sell_row<REAL>(g.chunk_off, g.col, g.val, u_j, c, lane);
+    const int64_t r = c * 32 + lane;
+    const bool valid = (r - __ldg(g.inst_row + inst)) < __ldg(g.inst_n + inst);
+    double a0 = 0.0, a1 = 0.0;
+    double2 wr = make_double2(0.0, 0.0);
+    if (valid) {
+      if (HAS_PREV) {
+        const double2 up = u_jm1[r];
+        wr.x = fma(cprev, up.x, gg * y.y);
+        wr.y = fma(cprev, up.y, -gg * y.x);
+      } else {
+        wr.x = gg * y.y;
+        wr.y = -gg * y.x;
+      }
+      const double2 uj = u_j[r];
+      a0 = fma(uj.x, wr.x, uj.y * wr.y);
+      a1 = fma(uj.x, wr.y, -uj.y * wr.x);
+    }
+    w[r] = wr;
+    a0 = te_warp_sum(a0);
+    a1 = te_warp_sum(a1);
+    if (lane == 0) {
+      chunk_partials[2 * c] = a0;
+      chunk_partials[2 * c + 1] = a1;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(TE_THREADS) batch_update_kernel(BatchGeom g, double2* __restrict__ V,
+                                                                  const double2* __restrict__ w, TeDevState* states,
+                                                                  double* chunk_partials, int j) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const double2* __restrict__ u_j = V + (int64_t)j * g.ld;
+  double2* __restrict__ u_jp1 = V + (int64_t)(j + 1) * g.ld;
+  for (int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < g.n_chunks; c += warps) {
+    const int inst = __ldg(g.chunk_inst + c);
+    const TeDevState* ds = states + inst;
+    if (lanczos_skip(ds, j)) continue;
+    const double sj = ds->s[j];
+    const double2 al = ds->alpha[j];
+    const double gr = al.x * sj, gi = al.y * sj;
+    const int64_t r = c * 32 + lane;
+    const bool valid = (r - __ldg(g.inst_row + inst)) < __ldg(g.inst_n + inst);
+    double2 o = make_double2(0.0, 0.0);
+    if (valid) {
+      const double2 wv = w[r], u = u_j[r];
+      o.x = fma(-gr, u.x, fma(gi, u.y, wv.x));
+      o.y = fma(-gr, u.y, fma(-gi, u.x, wv.y));
+    }
+    if (j + 1 < ds->m_cur) u_jp1[r] = o;
+    double nrm = fma(o.x, o.x, o.y * o.y);
+    nrm = te_warp_sum(nrm);
+    if (lane == 0) chunk_partials[2 * c] = nrm;
+  }
+}
+
+// kind 0: alpha_j of every instance; kind 1: beta_{j+1}, breakdown, h.
+__global__ void __launch_bounds__(TE_THREADS) batch_reduce_kernel(BatchGeom g, TeDevState* states,
+                                                                  const double* chunk_partials, int j, int kind) {
+  __shared__ double scratch[2 * 32];
+  const int inst = blockIdx.x;
+  TeDevState* ds = states + inst;
+  if (lanczos_skip(ds, j)) return;
+  const int64_t c0 = g.inst_chunk[inst], c1 = g.inst_chunk[inst + 1];
+  double acc[2] = {0.0, 0.0};
+  for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
+    acc[0] += chunk_partials[2 * c];
+    if (kind == 0) acc[1] += chunk_partials[2 * c + 1];
+  }
+  te_block_sum<2>(acc, scratch);
+  if (threadIdx.x != 0) return;
+  if (kind == 0) {
+    const double sj = ds->s[j];
+    ds->alpha[j] = make_double2(sj * acc[0], sj * acc[1]);
+    return;
+  }
+  const double beta = sqrt(acc[0]);
+  const int m = ds->m_cur;
+  if (beta < ds->tol_rate) {
+    ds->breakdown = 1;
+    ds->m_eff = j + 1;
+    ds->h = beta;
+  } else if (j + 1 != m) {
+    ds->beta[j + 1] = beta;
+    ds->s[j + 1] = 1.0 / beta;
+  } else {
+    ds->h = beta;
+    ds->m_eff = m;
+  }
+}
+
+// Start vector of the next step: u_0 = the w of the previous step.
+__global__ void __launch_bounds__(TE_THREADS) batch_new_start_kernel(BatchGeom g, double2* __restrict__ V,
+                                                                     const double2* __restrict__ spare,
+                                                                     const TeDevState* states) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < g.n_chunks; c += warps) {
+    const int inst = __ldg(g.chunk_inst + c);
+    const TeDevState* ds = states + inst;
+    if (!ds->new_start || ds->fatal || ds->done) continue;
+    const int64_t r = c * 32 + lane;
+    V[r] = spare[r];
+  }
+}
+
+// Clear the new-start flags once the copies are done (one thread per instance).
+__global__ void batch_clear_start_kernel(TeDevState* states, int n_inst) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_inst; i += gridDim.x * blockDim.x)
+    states[i].new_start = 0;
+}
+
+// psi = sum_j u_j Y[slot][j] for each instance's outputs of this batch:
+// slot 0 (w) -> spare, slot 1 (the sample; batches hold one sample) -> sampled.
+template <int G>
+__device__ __forceinline__ void batch_combine_rows(const double2* __restrict__ V, int64_t ld, int64_t r, int m,
+                                                   const double2* Y, const int* slots, double2* spare,
+                                                   double2* sampled) {
+  double2 acc[G];
+#pragma unroll
+  for (int o = 0; o < G; ++o) acc[o] = make_double2(0.0, 0.0);
+  for (int j = 0; j < m; ++j) {
+    const double2 u = V[(int64_t)j * ld + r];
+#pragma unroll
+    for (int o = 0; o < G; ++o) {
+      const double2 y = Y[slots[o] * TE_MMAX + j];
+      acc[o].x = fma(u.x, y.x, fma(-u.y, y.y, acc[o].x));
+      acc[o].y = fma(u.x, y.y, fma(u.y, y.x, acc[o].y));
+    }
+  }
+#pragma unroll
+  for (int o = 0; o < G; ++o) {
+    if (slots[o] == 0)
+      spare[r] = acc[o];
+    else
+      sampled[r] = acc[o];
+  }
+}
+
+__global__ void __launch_bounds__(TE_THREADS) batch_combine_kernel(BatchGeom g, const double2* __restrict__ V,
+                                                                   double2* spare, double2* sampled,
+                                                                   const TeDevState* states, int m_override) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < g.n_chunks; c += warps) {
+    const int inst = __ldg(g.chunk_inst + c);
+    const TeDevState* ds = states + inst;
+    if (ds->fatal) continue;
+    const int want_w = ds->want_w, S = ds->samples_in_batch;
+    const int nout = want_w + S;
+    if (nout == 0) continue;
+    const int m = m_override > 0 ? m_override : ds->m_eff;
+    const int64_t r = c * 32 + lane;
+    int slots[2];
+    slots[0] = want_w ? 0 : 1;
+    slots[1] = 1;
+    if (nout == 1)
+      batch_combine_rows<1>(V, g.ld, r, m, ds->Y, slots, spare, sampled);
+    else
+      batch_combine_rows<2>(V, g.ld, r, m, ds->Y, slots, spare, sampled);
+  }
+}
+
+// Diagonal observables of every instance with a sample in this batch
+// (one block per instance): Re sum_i O_ii |psi_i|^2.
+__global__ void __launch_bounds__(TE_THREADS) batch_obs_kernel(BatchGeom g, const double2* __restrict__ sampled,
+                                                               const double* __restrict__ diag, const int* n_obs,
+                                                               const int64_t* result_off, double* results,
+                                                               TeDevState* states) {
+  __shared__ double scratch[TE_BATCH_MAX_OBS * 32];
+  const int inst = blockIdx.x;
+  TeDevState* ds = states + inst;
+  const int no = n_obs[inst];
+  if (ds->fatal || ds->samples_in_batch == 0 || no == 0) return;
+  const int64_t r0 = g.inst_row[inst];
+  const int n = g.inst_n[inst];
+  double acc[TE_BATCH_MAX_OBS] = {0.0, 0.0, 0.0, 0.0};
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double2 p = sampled[r0 + i];
+    const double p2 = fma(p.x, p.x, p.y * p.y);
+    for (int k = 0; k < no; ++k) acc[k] = fma(diag[(int64_t)k * g.ld + r0 + i], p2, acc[k]);
+  }
+  te_block_sum<TE_BATCH_MAX_OBS>(acc, scratch);
+  if (threadIdx.x == 0) {
+    const int s = ds->sample_base;
+    for (int k = 0; k < no; ++k) results[result_off[inst] + (int64_t)k * ds->n_samples + s] = acc[k];
+  }
+}
+
+// ||sampled||^2 of every instance (final norm check of :446).
+__global__ void __launch_bounds__(TE_THREADS) batch_norm_kernel(BatchGeom g, const double2* __restrict__ sampled,
+                                                                TeDevState* states) {
+  __shared__ double scratch[32];
+  const int inst = blockIdx.x;
+  const int64_t r0 = g.inst_row[inst];
+  const int n = g.inst_n[inst];
+  double acc[1] = {0.0};
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double2 p = sampled[r0 + i];
+    acc[0] = fma(p.x, p.x, fma(p.y, p.y, acc[0]));
+  }
+  te_block_sum<1>(acc, scratch);
+  if (threadIdx.x == 0) states[inst].norm2_final = acc[0];
+}
+
+// One flag word per instance: bit0 done, bit1 samples pending, bit2 fatal.
+__global__ void batch_flags_kernel(const TeDevState* states, int n_inst, int* flags) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_inst; i += gridDim.x * blockDim.x) {
+    const TeDevState& d = states[i];
+    flags[i] = (d.done ? 1 : 0) | (d.samples_pending && !d.done ? 2 : 0) | (d.fatal ? 4 : 0);
+  }
+}
+
+// global = local + offset (columns of one instance into the concatenated rows)
+__global__ void offset_copy_kernel(const int32_t* __restrict__ in, int32_t* __restrict__ out, int64_t count,
+                                   int32_t offset) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = in[i] + offset;
+}
+
+__global__ void real_to_complex_kernel(const double* __restrict__ in, double2* __restrict__ out, int64_t count) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = make_double2(in[i], 0.0);
+}
+
+__global__ void scatter_permuted_kernel(int64_t n, const int32_t* __restrict__ perm, const double2* __restrict__ in,
+                                        double2* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = in[perm[i]];
+}
+
+__global__ void gather_diag_kernel(int64_t n, const int32_t* __restrict__ perm, const double2* __restrict__ dc,
+                                   double* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = dc[perm[i]].x;
+}
+
+}  // namespace
+
+struct te_batch_s {
+  int B = 0;
+  int m_max = 0;
+  bool is_real = true;
+  cudaStream_t st = nullptr;
+  std::vector<te_matrix> H;
+  std::vector<te_params> p;
+  std::vector<int64_t> inst_row, inst_chunk, n_samples;
+  std::vector<int32_t> inst_n;
+  int64_t ld = 0, n_chunks = 0, slots = 0;
+  // device
+  int32_t* d_chunk_inst = nullptr;
+  int64_t* d_chunk_off = nullptr;
+  int32_t* d_col = nullptr;
+  double* d_val = nullptr;
+  int64_t* d_inst_row = nullptr;
+  int32_t* d_inst_n = nullptr;
+  int64_t* d_inst_chunk = nullptr;
+  TeDevState* ds = nullptr;
+  double2* V = nullptr;
+  double2* spare = nullptr;
+  double2* w = nullptr;
+  double2* sampled = nullptr;
+  double2* v0 = nullptr;  // start vectors (permuted), kept for reruns
+  double* partials = nullptr;
+  double* diag = nullptr;  // TE_BATCH_MAX_OBS x ld
+  int* d_nobs = nullptr;
+  int64_t* d_result_off = nullptr;
+  double* results = nullptr;
+  int* d_flags = nullptr;
+  int* h_flags = nullptr;  // pinned
+  std::vector<int> nobs;
+  std::vector<int64_t> result_off;
+  cudaGraphExec_t g_step = nullptr, g_batch = nullptr;
+  int64_t launches = 0;
+  bool ran = false;
+};
+
+namespace {
+
+BatchGeom geom(const te_batch_s* b) {
+  BatchGeom g;
+  g.n_chunks = b->n_chunks;
+  g.chunk_inst = b->d_chunk_inst;
+  g.chunk_off = b->d_chunk_off;
+  g.col = b->d_col;
+  g.val = b->d_val;
+  g.inst_row = b->d_inst_row;
+  g.inst_n = b->d_inst_n;
+  g.inst_chunk = b->d_inst_chunk;
+  g.ld = b->ld;
+  return g;
+}
+
+void free_batch(te_batch b) {
+  if (!b) return;
+  if (b->g_step) cudaGraphExecDestroy(b->g_step);
+  if (b->g_batch) cudaGraphExecDestroy(b->g_batch);
+  cudaFree(b->d_chunk_inst);
+  cudaFree(b->d_chunk_off);
+  cudaFree(b->d_col);
+  cudaFree(b->d_val);
+  cudaFree(b->d_inst_row);
+  cudaFree(b->d_inst_n);
+  cudaFree(b->d_inst_chunk);
+  cudaFree(b->ds);
+  cudaFree(b->V);
+  cudaFree(b->spare);
+  cudaFree(b->w);
+  cudaFree(b->sampled);
+  cudaFree(b->v0);
+  cudaFree(b->partials);
+  cudaFree(b->diag);
+  cudaFree(b->d_nobs);
+  cudaFree(b->d_result_off);
+  cudaFree(b->results);
+  cudaFree(b->d_flags);
+  cudaFreeHost(b->h_flags);
+  if (b->st) cudaStreamDestroy(b->st);
+  delete b;
+}
+
+int grid_chunks(const te_batch_s* b) { return te_grid_for(b->n_chunks * 32, TE_THREADS, 8); }
+
+// Record the kernels of one global step (or of one extra sample batch).
+int enqueue_step(te_batch b, bool full_step) {
+  const BatchGeom g = geom(b);
+  cudaStream_t st = b->st;
+  const int gc = grid_chunks(b);
+  int64_t k = 0;
+  if (full_step) {
+    batch_new_start_kernel<<<gc, TE_THREADS, 0, st>>>(g, b->V, b->spare, b->ds);
+    batch_clear_start_kernel<<<(b->B + 255) / 256, 256, 0, st>>>(b->ds, b->B);
+    k += 2;
+    for (int j = 0; j < b->m_max; ++j) {
+      if (b->is_real) {
+        if (j > 0)
+          batch_apply_kernel<true, true><<<gc, TE_THREADS, 0, st>>>(g, b->V, b->w, b->ds, b->partials, j);
+        else
+          batch_apply_kernel<true, false><<<gc, TE_THREADS, 0, st>>>(g, b->V, b->w, b->ds, b->partials, j);
+      } else {
+        if (j > 0)
+          batch_apply_kernel<false, true><<<gc, TE_THREADS, 0, st>>>(g, b->V, b->w, b->ds, b->partials, j);
+        else
+          batch_apply_kernel<false, false><<<gc, TE_THREADS, 0, st>>>(g, b->V, b->w, b->ds, b->partials, j);
+      }
+      batch_reduce_kernel<<<b->B, TE_THREADS, 0, st>>>(g, b->ds, b->partials, j, 0);
+      batch_update_kernel<<<gc, TE_THREADS, 0, st>>>(g, b->V, b->w, b->ds, b->partials, j);
+      batch_reduce_kernel<<<b->B, TE_THREADS, 0, st>>>(g, b->ds, b->partials, j, 1);
+      k += 4;
+    }
+  }
+  te_launch_krylov_batch(b->ds, b->B, full_step ? 0 : 1, st);
+  batch_combine_kernel<<<gc, TE_THREADS, 0, st>>>(g, b->V, b->spare, b->sampled, b->ds, 0);
+  batch_obs_kernel<<<b->B, TE_THREADS, 0, st>>>(g, b->sampled, b->diag, b->d_nobs, b->d_result_off, b->results,
+                                                b->ds);
+  batch_flags_kernel<<<(b->B + 255) / 256, 256, 0, st>>>(b->ds, b->B, b->d_flags);
+  k += 4;
+  TE_CUDA(cudaMemcpyAsync(b->h_flags, b->d_flags, sizeof(int) * b->B, cudaMemcpyDeviceToHost, st));
+  b->launches += 0;  // counted per replay
+  (void)k;
+  return te_cuda_check(cudaGetLastError(), "batch enqueue");
+}
+
+int64_t kernels_per_replay(const te_batch_s* b, bool full_step) {
+  return (full_step ? 2 + 4 * (int64_t)b->m_max : 0) + 4;
+}
+
+int capture(te_batch b, bool full_step, cudaGraphExec_t* exec) {
+  cudaGraph_t graph = nullptr;
+  TE_CUDA(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_step(b, full_step);
+  cudaError_t e = cudaStreamEndCapture(b->st, &graph);
+  if (rc != TE_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  TE_CUDA(e);
+  rc = te_cuda_check(cudaGraphInstantiate(exec, graph, 0), "graph instantiate");
+  cudaGraphDestroy(graph);
+  return rc;
+}
+
+int reset_states(te_batch b) {
+  const BatchGeom g = geom(b);
+  std::vector<TeDevState> hs(b->B);
+  for (int i = 0; i < b->B; ++i) {
+    TeDevState& s = hs[i];
+    std::memset(&s, 0, sizeof(TeDevState));
+    const te_params& p = b->p[i];
+    const int m = (int)std::min<int64_t>(p.m, b->inst_n[i]);
+    s.t = p.t;
+    s.sampling_step = p.sampling_step;
+    s.tol = p.tol;
+    s.tol_rate = p.tol / p.t;
+    s.exp_factor = p.exp_factor;
+    s.num_err_est = (double)b->inst_n[i] * b->H[i]->norm1 * DBL_EPSILON;
+    s.m_max = m;
+    s.n_samples = (int)b->n_samples[i];
+    s.integ_long = p.fast_integration ? 0 : 2;
+    s.integ_short = p.fast_integration ? 1 : 2;
+    s.max_batch = 1;
+    s.t_step = 0.1;
+    s.m_cur = m;
+    s.m_eff = m;
+    s.s[0] = 1.0;
+    s.samples_in_batch = 1;  // the sample at t = 0 (:306-313)
+    s.sample_base = 0;
+    s.index_samples = 1;
+    s.Y[1 * TE_MMAX + 0] = make_double2(1.0, 0.0);
+    s.n_steps = b->n_samples[i] > 1 ? 1 : 0;
+    s.done = b->n_samples[i] > 1 ? 0 : 1;
+  }
+  TE_CUDA(cudaMemcpyAsync(b->ds, hs.data(), sizeof(TeDevState) * b->B, cudaMemcpyHostToDevice, b->st));
+  TE_CUDA(cudaMemcpyAsync(b->V, b->v0, sizeof(double2) * b->ld, cudaMemcpyDeviceToDevice, b->st));
+  batch_combine_kernel<<<grid_chunks(b), TE_THREADS, 0, b->st>>>(g, b->V, b->spare, b->sampled, b->ds, 1);
+  batch_obs_kernel<<<b->B, TE_THREADS, 0, b->st>>>(g, b->sampled, b->diag, b->d_nobs, b->d_result_off, b->results,
+                                                   b->ds);
+  b->launches += 2;
+  TE_CUDA(cudaStreamSynchronize(b->st));
+  return TE_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ C ABI
+
+extern "C" int te_batch_create(int n_instances, const te_matrix* H, const double* const* v_host,
+                               const te_params* params, te_batch* out) {
+  if (n_instances <= 0 || !H || !v_host || !params || !out) {
+    te_set_error("te_batch_create: invalid arguments");
+    return TE_ERR_INVALID_ARG;
+  }
+  int rc = te_upload_quad_tables();
+  if (rc != TE_OK) return rc;
+  te_batch b = new te_batch_s();
+  auto fail = [&](int code) {
+    free_batch(b);
+    return code;
+  };
+  b->B = n_instances;
+  for (int i = 0; i < n_instances; ++i) {
+    const te_params& p = params[i];
+    if (!H[i] || !v_host[i] || H[i]->n_rows != H[i]->n_cols || !(p.t > 0.0) || !(p.sampling_step > 0.0) ||
+        !(p.tol > 0.0) || p.m < 1 || p.reorth != 0) {
+      te_set_error("te_batch_create: instance %d: invalid matrix or parameters (reorth is not batched)", i);
+      return fail(TE_ERR_INVALID_ARG);
+    }
+    const int64_t n = H[i]->n_rows;
+    double nrm = 0.0;
+    for (int64_t k = 0; k < 2 * n; ++k) nrm += v_host[i][k] * v_host[i][k];
+    if (std::fabs(std::sqrt(nrm) - 1.0) > p.tol) {
+      te_set_error("te_batch_create: instance %d: Initial vector is not normalized", i);
+      return fail(TE_ERR_NOT_NORMALIZED);
+    }
+    const int m = (int)std::min<int64_t>(p.m, n);
+    if (m > TE_MMAX) {
+      te_set_error("te_batch_create: instance %d: Krylov dimension above %d", i, TE_MMAX);
+      return fail(TE_ERR_UNSUPPORTED);
+    }
+    b->m_max = std::max(b->m_max, m);
+    b->H.push_back(H[i]);
+    b->p.push_back(p);
+    b->is_real = b->is_real && H[i]->is_real;
+    b->n_samples.push_back((int64_t)std::floor(p.t / p.sampling_step) + 1);
+  }
+  // geometry: instance rows padded to whole chunks
+  b->inst_row.resize(n_instances + 1);
+  b->inst_chunk.resize(n_instances + 1);
+  b->inst_n.resize(n_instances);
+  int64_t rows = 0, chunks = 0, slots = 0;
+  std::vector<int64_t> slot_begin(n_instances);
+  for (int i = 0; i < n_instances; ++i) {
+    b->inst_row[i] = rows;
+    b->inst_chunk[i] = chunks;
+    b->inst_n[i] = (int32_t)b->H[i]->n_rows;
+    slot_begin[i] = slots;
+    rows += b->H[i]->sell.n_chunks * 32;
+    chunks += b->H[i]->sell.n_chunks;
+    slots += b->H[i]->sell.slots;
+  }
+  b->inst_row[n_instances] = rows;
+  b->inst_chunk[n_instances] = chunks;
+  b->ld = rows;
+  b->n_chunks = chunks;
+  b->slots = slots;
+  if (rows >= ((int64_t)1 << 31)) {
+    te_set_error("te_batch_create: the instances together exceed 2^31 rows");
+    return fail(TE_ERR_UNSUPPORTED);
+  }
+  if ((rc = te_cuda_check(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking), "stream")) != TE_OK)
+    return fail(rc);
+  cudaStream_t st = b->st;
+  std::vector<int64_t> off(chunks + 1);
+  std::vector<int32_t> cinst(chunks);
+  for (int i = 0; i < n_instances; ++i) {
+    const TeSell& S = b->H[i]->sell;
+    std::vector<int64_t> loc(S.n_chunks + 1);
+    if ((rc = te_cuda_check(cudaMemcpy(loc.data(), S.chunk_off, sizeof(int64_t) * (S.n_chunks + 1),
+                                       cudaMemcpyDeviceToHost), "chunk_off")) != TE_OK)
+      return fail(rc);
+    for (int64_t c = 0; c < S.n_chunks; ++c) {
+      off[b->inst_chunk[i] + c] = slot_begin[i] + loc[c];
+      cinst[b->inst_chunk[i] + c] = i;
+    }
+  }
+  off[chunks] = slots;
+  auto alloc = [&](void** p, size_t bytes) { return te_cuda_check(cudaMalloc(p, std::max<size_t>(bytes, 16)), "alloc"); };
+  const int vw = b->is_real ? 1 : 2;
+  if ((rc = alloc((void**)&b->d_chunk_off, sizeof(int64_t) * (chunks + 1))) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_chunk_inst, sizeof(int32_t) * chunks)) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_col, sizeof(int32_t) * slots)) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_val, sizeof(double) * vw * slots)) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_inst_row, sizeof(int64_t) * (n_instances + 1))) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_inst_chunk, sizeof(int64_t) * (n_instances + 1))) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_inst_n, sizeof(int32_t) * n_instances)) != TE_OK) return fail(rc);
+  TE_CUDA(cudaMemcpy(b->d_chunk_off, off.data(), sizeof(int64_t) * (chunks + 1), cudaMemcpyHostToDevice));
+  TE_CUDA(cudaMemcpy(b->d_chunk_inst, cinst.data(), sizeof(int32_t) * chunks, cudaMemcpyHostToDevice));
+  TE_CUDA(cudaMemcpy(b->d_inst_row, b->inst_row.data(), sizeof(int64_t) * (n_instances + 1), cudaMemcpyHostToDevice));
+  TE_CUDA(cudaMemcpy(b->d_inst_chunk, b->inst_chunk.data(), sizeof(int64_t) * (n_instances + 1),
+                     cudaMemcpyHostToDevice));
+  TE_CUDA(cudaMemcpy(b->d_inst_n, b->inst_n.data(), sizeof(int32_t) * n_instances, cudaMemcpyHostToDevice));
+  for (int i = 0; i < n_instances; ++i) {
+    const TeSell& S = b->H[i]->sell;
+    const int gr = te_grid_for(S.slots, 256, 4);
+    offset_copy_kernel<<<gr, 256, 0, st>>>(S.col, b->d_col + slot_begin[i], S.slots, (int32_t)b->inst_row[i]);
+    if (b->is_real)
+      TE_CUDA(cudaMemcpyAsync(b->d_val + slot_begin[i], S.val, sizeof(double) * S.slots, cudaMemcpyDeviceToDevice, st));
+    else if (b->H[i]->is_real)
+      real_to_complex_kernel<<<gr, 256, 0, st>>>(S.val, reinterpret_cast<double2*>(b->d_val) + slot_begin[i],
+                                                 S.slots);
+    else
+      TE_CUDA(cudaMemcpyAsync(b->d_val + 2 * slot_begin[i], S.val, sizeof(double2) * S.slots,
+                              cudaMemcpyDeviceToDevice, st));
+  }
+  const int64_t ld = b->ld;
+  if ((rc = alloc((void**)&b->ds, sizeof(TeDevState) * n_instances)) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->V, sizeof(double2) * ld * b->m_max)) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->spare, sizeof(double2) * ld)) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->w, sizeof(double2) * ld)) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->sampled, sizeof(double2) * ld)) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->v0, sizeof(double2) * ld)) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->partials, sizeof(double) * 2 * std::max<int64_t>(chunks, 1))) != TE_OK)
+    return fail(rc);
+  if ((rc = alloc((void**)&b->diag, sizeof(double) * TE_BATCH_MAX_OBS * ld)) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_nobs, sizeof(int) * n_instances)) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_result_off, sizeof(int64_t) * n_instances)) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_flags, sizeof(int) * n_instances)) != TE_OK) return fail(rc);
+  TE_CUDA(cudaMallocHost(&b->h_flags, sizeof(int) * n_instances));
+  TE_CUDA(cudaMemsetAsync(b->V, 0, sizeof(double2) * ld * b->m_max, st));
+  TE_CUDA(cudaMemsetAsync(b->spare, 0, sizeof(double2) * ld, st));
+  TE_CUDA(cudaMemsetAsync(b->w, 0, sizeof(double2) * ld, st));
+  TE_CUDA(cudaMemsetAsync(b->v0, 0, sizeof(double2) * ld, st));
+  TE_CUDA(cudaMemsetAsync(b->diag, 0, sizeof(double) * TE_BATCH_MAX_OBS * ld, st));
+  // start vectors into the instances' sorted order
+  double2* tmp = nullptr;
+  int64_t nmax = 0;
+  for (int i = 0; i < n_instances; ++i) nmax = std::max<int64_t>(nmax, b->inst_n[i]);
+  if ((rc = alloc((void**)&tmp, sizeof(double2) * nmax)) != TE_OK) return fail(rc);
+  for (int i = 0; i < n_instances; ++i) {
+    TE_CUDA(cudaMemcpyAsync(tmp, v_host[i], sizeof(double2) * b->inst_n[i], cudaMemcpyHostToDevice, st));
+    scatter_permuted_kernel<<<te_grid_for(b->inst_n[i], 256, 4), 256, 0, st>>>(b->inst_n[i], b->H[i]->sell.perm, tmp,
+                                                                              b->v0 + b->inst_row[i]);
+    TE_CUDA(cudaStreamSynchronize(st));
+  }
+  cudaFree(tmp);
+  b->nobs.assign(n_instances, 0);
+  TE_CUDA(cudaMemcpy(b->d_nobs, b->nobs.data(), sizeof(int) * n_instances, cudaMemcpyHostToDevice));
+  *out = b;
+  return TE_OK;
+}
+
+extern "C" int te_batch_add_observable(te_batch b, int instance, te_matrix O) {
+  if (!b || !O || instance < 0 || instance >= b->B) {
+    te_set_error("te_batch_add_observable: invalid arguments");
+    return TE_ERR_INVALID_ARG;
+  }
+  if (O->n_rows != b->inst_n[instance] || O->n_cols != b->inst_n[instance]) {
+    te_set_error("Incompatible dimensions");
+    return TE_ERR_DIM;
+  }
+  if (!O->is_diag || b->nobs[instance] >= TE_BATCH_MAX_OBS) {
+    te_set_error("te_batch_add_observable: batched evolutions take up to %d diagonal observables per instance",
+                 TE_BATCH_MAX_OBS);
+    return TE_ERR_UNSUPPORTED;
+  }
+  const int k = b->nobs[instance]++;
+  gather_diag_kernel<<<te_grid_for(b->inst_n[instance], 256, 4), 256, 0, b->st>>>(
+      b->inst_n[instance], b->H[instance]->sell.perm, O->diag_c, b->diag + (int64_t)k * b->ld + b->inst_row[instance]);
+  TE_CUDA(cudaStreamSynchronize(b->st));
+  TE_CUDA(cudaMemcpy(b->d_nobs, b->nobs.data(), sizeof(int) * b->B, cudaMemcpyHostToDevice));
+  return TE_OK;
+}
+
+extern "C" int te_batch_run(te_batch b, te_result* results) {
+  if (!b) {
+    te_set_error("te_batch_run: null batch");
+    return TE_ERR_INVALID_ARG;
+  }
+  b->launches = 0;
+  // result table
+  if (!b->results) {
+    b->result_off.assign(b->B, 0);
+    int64_t tot = 0;
+    for (int i = 0; i < b->B; ++i) {
+      b->result_off[i] = tot;
+      tot += (int64_t)std::max(1, b->nobs[i]) * b->n_samples[i];
+    }
+    TE_CUDA(cudaMalloc(&b->results, sizeof(double) * std::max<int64_t>(tot, 1)));
+    TE_CUDA(cudaMemset(b->results, 0, sizeof(double) * std::max<int64_t>(tot, 1)));
+    TE_CUDA(cudaMemcpy(b->d_result_off, b->result_off.data(), sizeof(int64_t) * b->B, cudaMemcpyHostToDevice));
+  }
+  int rc = reset_states(b);
+  if (rc != TE_OK) return rc;
+  if (!b->g_step) {
+    if ((rc = capture(b, true, &b->g_step)) != TE_OK) return rc;
+    if ((rc = capture(b, false, &b->g_batch)) != TE_OK) return rc;
+  }
+  const int64_t per_step = kernels_per_replay(b, true), per_batch = kernels_per_replay(b, false);
+  for (int64_t guard = 0; guard < ((int64_t)1 << 30); ++guard) {
+    TE_CUDA(cudaGraphLaunch(b->g_step, b->st));
+    TE_CUDA(cudaStreamSynchronize(b->st));
+    b->launches += per_step;
+    bool pending = false, all_done = true, fatal = false;
+    for (int i = 0; i < b->B; ++i) {
+      pending |= (b->h_flags[i] & 2) != 0;
+      all_done &= (b->h_flags[i] & 1) != 0;
+      fatal |= (b->h_flags[i] & 4) != 0;
+    }
+    while (pending && !fatal) {
+      TE_CUDA(cudaGraphLaunch(b->g_batch, b->st));
+      TE_CUDA(cudaStreamSynchronize(b->st));
+      b->launches += per_batch;
+      pending = false;
+      all_done = true;
+      for (int i = 0; i < b->B; ++i) {
+        pending |= (b->h_flags[i] & 2) != 0;
+        all_done &= (b->h_flags[i] & 1) != 0;
+        fatal |= (b->h_flags[i] & 4) != 0;
+      }
+    }
+    if (fatal || all_done) break;
+  }
+  batch_norm_kernel<<<b->B, TE_THREADS, 0, b->st>>>(geom(b), b->sampled, b->ds);
+  b->launches += 1;
+  std::vector<TeDevState> hs(b->B);
+  TE_CUDA(cudaMemcpyAsync(hs.data(), b->ds, sizeof(TeDevState) * b->B, cudaMemcpyDeviceToHost, b->st));
+  TE_CUDA(cudaStreamSynchronize(b->st));
+  int first_fatal = 0;
+  for (int i = 0; i < b->B; ++i) {
+    const TeDevState& S = hs[i];
+    if (S.fatal && !first_fatal) first_fatal = S.fatal;
+    // final checks of :445-504
+    int status = S.status, nbErrors = 0;
+    if (std::fabs(std::sqrt(S.norm2_final) - 1.0) > b->p[i].tol) {
+      nbErrors++;
+      status = TE_STATUS_NORM;
+    }
+    const double numErrTotal = S.num_err_est * S.n_steps;
+    if (S.nb_err_roundoff != 0) {
+      nbErrors++;
+      status = TE_STATUS_ROUNDOFF;
+    }
+    if (S.nb_err_int != 0) {
+      nbErrors++;
+      status = TE_STATUS_INTEGRATION;
+    }
+    if (numErrTotal > S.err && S.nb_err_roundoff == 0) {
+      if (numErrTotal > b->p[i].tol) {
+        status = TE_STATUS_ROUNDOFF_TOTAL;
+        nbErrors++;
+      } else if (status != TE_STATUS_LUCKY_BREAKDOWN) {
+        status = TE_STATUS_BELOW_ROUNDOFF;
+      }
+    }
+    if (nbErrors > 1) status = TE_STATUS_MULTIPLE;
+    if (results) {
+      te_result& r = results[i];
+      r = te_result{};
+      r.err = S.err;
+      r.evolved_time = S.t_now;
+      r.num_samples = S.index_samples;
+      r.n_steps = S.n_steps;
+      r.dim = b->inst_n[i];
+      r.krylov_dim = S.m_cur;
+      r.status = S.fatal ? S.fatal : status;
+      r.nb_err_roundoff = S.nb_err_roundoff;
+      r.nb_err_int = S.nb_err_int;
+    }
+  }
+  b->ran = true;
+  if (first_fatal) {
+    te_set_error("device-side failure %d in a batched evolution", first_fatal);
+    return first_fatal;
+  }
+  return TE_OK;
+}
+
+extern "C" int te_batch_samples(te_batch b, int instance, int obs_index, double* out_host, int64_t count) {
+  if (!b || !b->ran || instance < 0 || instance >= b->B || obs_index < 0 || obs_index >= b->nobs[instance] ||
+      !out_host || count < 0) {
+    te_set_error("te_batch_samples: invalid arguments");
+    return TE_ERR_INVALID_ARG;
+  }
+  const int64_t k = std::min<int64_t>(count, b->n_samples[instance]);
+  TE_CUDA(cudaMemcpy(out_host, b->results + b->result_off[instance] + (int64_t)obs_index * b->n_samples[instance],
+                     sizeof(double) * k, cudaMemcpyDeviceToHost));
+  for (int64_t i = k; i < count; ++i) out_host[i] = 0.0;
+  return TE_OK;
+}
+
+extern "C" int te_batch_state(te_batch b, int instance, double* out_host) {
+  if (!b || !b->ran || instance < 0 || instance >= b->B || !out_host) {
+    te_set_error("te_batch_state: invalid arguments");
+    return TE_ERR_INVALID_ARG;
+  }
+  const int64_t n = b->inst_n[instance];
+  double2* tmp = nullptr;
+  TE_CUDA(cudaMalloc(&tmp, sizeof(double2) * n));
+  te_launch_permute(n, b->H[instance]->sell.iperm, b->sampled + b->inst_row[instance], tmp, b->st);
+  int rc = te_cuda_check(cudaMemcpyAsync(out_host, tmp, sizeof(double2) * n, cudaMemcpyDeviceToHost, b->st), "D2H");
+  if (rc == TE_OK) rc = te_cuda_check(cudaStreamSynchronize(b->st), "sync");
+  cudaFree(tmp);
+  return rc;
+}
+
+extern "C" int64_t te_batch_launch_count(te_batch b) { return b ? b->launches : 0; }
+
+extern "C" void* te_batch_stream(te_batch b) { return b ? (void*)b->st : nullptr; }
+
+extern "C" int te_batch_destroy(te_batch b) {
+  free_batch(b);
+  return TE_OK;
+}

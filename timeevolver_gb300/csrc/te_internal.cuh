@@ -73,6 +73,10 @@ struct TeDevState {
   // Gram-Schmidt projections of the reorthogonalising mode (two passes)
   double2 proj1[TE_MMAX];
   double2 proj2[TE_MMAX];
+  // batched evolutions: the step produced a new start vector (copied into u_0
+  // at the beginning of the next step)
+  int new_start;
+  int pad_tail[3];
 };
 
 // SELL-32 matrix in the sorted (permuted) basis.
@@ -140,6 +144,7 @@ void te_launch_gs_update_norm(int64_t n, const TeBasisPtrs& V, int nvec, const d
 int te_upload_quad_tables();
 void te_launch_krylov_step(TeDevState* ds, cudaStream_t st);
 void te_launch_schedule_samples(TeDevState* ds, cudaStream_t st);
+void te_launch_krylov_batch(TeDevState* states, int n_instances, int mode, cudaStream_t st);
 // te_sample.cu
 struct TeCombineArgs {
   const double2* cols[TE_MMAX];

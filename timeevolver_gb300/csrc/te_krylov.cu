@@ -759,13 +759,19 @@ __device__ void load_krylov_data(KCtx& C) {
   __syncthreads();
 }
 
+// One Krylov-space step of one evolution (block-cooperative).
 // mode 0: full step (matrix setup, step search, w, first sample batch);
 // mode 1: next sample batch of the same Krylov space.
-__global__ void __launch_bounds__(TE_THREADS) krylov_kernel(TeDevState* ds, int mode) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  KSmem* S = reinterpret_cast<KSmem*>(smem_raw);
+__device__ void krylov_step_body(TeDevState* ds, int mode, KSmem* S) {
   if (ds->fatal != 0) return;
-  if (mode == 0 && ds->done != 0) return;
+  if ((mode == 0 && ds->done != 0) || (mode == 1 && ds->samples_pending == 0)) {
+    // nothing to do for this evolution: make the combine/observable passes skip it
+    if (threadIdx.x == 0) {
+      ds->samples_in_batch = 0;
+      ds->want_w = 0;
+    }
+    return;
+  }
   KCtx C;
   C.ds = ds;
   C.sm = S;
@@ -790,6 +796,7 @@ __global__ void __launch_bounds__(TE_THREADS) krylov_kernel(TeDevState* ds, int 
       ds->m_cur = C.m;
       ds->status = TE_STATUS_LUCKY_BREAKDOWN;
       ds->want_w = 0;
+      ds->new_start = 0;
     }
   } else {
     const double s0 = 0.97 * ds->t_step;
@@ -805,6 +812,7 @@ __global__ void __launch_bounds__(TE_THREADS) krylov_kernel(TeDevState* ds, int 
       ds->err_step = err_step;
       ds->err_code_find = code;
       ds->want_w = 1;
+      ds->new_start = 1;
     }
     __syncthreads();
     double dts[1] = {t_step};
@@ -826,6 +834,17 @@ __global__ void __launch_bounds__(TE_THREADS) krylov_kernel(TeDevState* ds, int 
   if (ds->fatal != 0) return;
   schedule_batch(C);
   save_krylov_data(C);
+}
+
+__global__ void __launch_bounds__(TE_THREADS) krylov_kernel(TeDevState* ds, int mode) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  krylov_step_body(ds, mode, reinterpret_cast<KSmem*>(smem_raw));
+}
+
+// Batched evolutions: block b runs the step of instance b.
+__global__ void __launch_bounds__(TE_THREADS) krylov_batch_kernel(TeDevState* states, int mode) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  krylov_step_body(states + blockIdx.x, mode, reinterpret_cast<KSmem*>(smem_raw));
 }
 
 // ---------------------------------------------------------------- host side
@@ -893,6 +912,7 @@ int te_upload_quad_tables() {
   gauss(7, T.g7_x, T.g7_w);
   TE_CUDA(cudaMemcpyToSymbol(c_quad, &T, sizeof(T)));
   TE_CUDA(cudaFuncSetAttribute(krylov_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(KSmem)));
+  TE_CUDA(cudaFuncSetAttribute(krylov_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(KSmem)));
   g_tables_uploaded = true;
   return TE_OK;
 }
@@ -903,4 +923,8 @@ void te_launch_krylov_step(TeDevState* ds, cudaStream_t st) {
 
 void te_launch_schedule_samples(TeDevState* ds, cudaStream_t st) {
   krylov_kernel<<<1, TE_THREADS, sizeof(KSmem), st>>>(ds, 1);
+}
+
+void te_launch_krylov_batch(TeDevState* states, int n_instances, int mode, cudaStream_t st) {
+  krylov_batch_kernel<<<n_instances, TE_THREADS, sizeof(KSmem), st>>>(states, mode);
 }

@@ -309,6 +309,84 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+BATCH_METRIC = "batched solves/s (256 Bose-Hubbard chains L=6..10, N=L, m=32, tol 1e-8)"
+BATCH_WORKLOAD = ("256 open Bose-Hubbard chains, L~U{6..10}, N=L (dims 462..92378), J~U(0.5,1.5), U~U(0,4), "
+                  "t~U(1,20), v = all bosons on site 0, tol=1e-8, m=32, <n_0> at 0 and t; numpy default_rng(4)")
+
+
+def batched_instances(count=256, seed=4):
+    """The batched workload: seeded random chains (the C++ model builder)."""
+    from timeevolver_gb300 import models
+    rng = np.random.default_rng(seed)
+    out = []
+    cache = {}
+    for _ in range(count):
+        L = int(rng.integers(6, 11))
+        J = float(rng.uniform(0.5, 1.5))
+        U = float(rng.uniform(0.0, 4.0))
+        t = float(rng.uniform(1.0, 20.0))
+        B, H = models.bose_hubbard(L, L, J, U)
+        if L not in cache:
+            cache[L] = (B, models.operator_matrix([models.number_operator(0, 1.0)], B))
+        Bb, O = cache[L]
+        v = np.zeros(len(B), dtype=np.complex128)
+        v[B.index([L] + [0] * (L - 1))] = 1.0
+        out.append(dict(L=L, coo=H, n0=O, v=v, t=t, n=len(B)))
+    return out
+
+
+def run_batched(args):
+    """Batched launch vs a per-instance loop of the plain GPU evolver."""
+    import torch
+    import timeevolver_gb300 as te
+    te.lib().te_set_device(0)
+    specs = batched_instances()
+    mats = [(te.Matrix.from_coo(s["n"], s["coo"]), te.Matrix.from_coo(s["n"], s["n0"])) for s in specs]
+    inst = [dict(H=H, v=s["v"], t=s["t"], sampling_step=s["t"], tol=1e-8, m=32, observables=[O])
+            for s, (H, O) in zip(specs, mats)]
+    batch = te.Batch(inst)
+    stream = torch.cuda.ExternalStream(batch.stream())
+    for _ in range(args.warmup):
+        batch.run()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    launches = 0
+    start.record(stream)
+    for _ in range(args.steps):
+        res = batch.run()
+        launches += batch.launch_count()
+    stop.record(stream)
+    stop.synchronize()
+    batch_ms = start.elapsed_time(stop) / args.steps
+    # per-instance loop of the plain evolver (evolvers created once, reset and run)
+    evs = [te.Evolver(H, s["v"], s["t"], s["t"], [("sparse", O)], tol=1e-8, m=32) for s, (H, O) in zip(specs, mats)]
+    for ev, s in zip(evs, specs):
+        ev.run()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loop_launches = 0
+    single = []
+    for ev, s in zip(evs, specs):
+        ev.reset(s["v"])
+        single.append(ev.run())
+        loop_launches += te.lib().te_evolver_launch_count(ev.handle)
+    torch.cuda.synchronize()
+    loop_ms = (time.perf_counter() - t0) * 1e3
+    same_steps = sum(int(r["n_steps"] == x.n_steps) for r, x in zip(res, single))
+    steps = [r["n_steps"] for r in res]
+    line = {"metric": BATCH_METRIC, "value": len(specs) / (batch_ms / 1e3), "unit": "solves/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": batch_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "complex128 (FP64)",
+            "data": "synthetic (seeded Bose-Hubbard chains)",
+            "config": {"workload": BATCH_WORKLOAD, "total_rows": int(sum(s["n"] for s in specs)),
+                       "krylov_steps_min_mean_max": [int(min(steps)), float(np.mean(steps)), int(max(steps))]},
+            "per_instance_loop": {"value": len(specs) / (loop_ms / 1e3), "unit": "solves/s", "ms": loop_ms,
+                                  "gpu_launches": int(loop_launches),
+                                  "instances_with_equal_step_count": same_steps},
+            "speedup_vs_loop": loop_ms / batch_ms, "gpu_launches": int(launches)}
+    print(json.dumps(line), flush=True)
+
+
 def ncu_case(t_final):
     """A short solve of the same workload for ncu captures (t_final instead of 10)."""
     import timeevolver_gb300 as te
@@ -327,6 +405,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--config", default="plain", choices=["plain", "batched"],
+                    help="plain: the L=12 single evolution (headline); batched: 256 chains in one batch")
     ap.add_argument("--ncu-case", type=float, default=None, metavar="T",
                     help="run one short solve to time T (for ncu captures) and exit")
     args = ap.parse_args()
@@ -335,6 +415,10 @@ def main():
         return
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == "batched":
+        import timeevolver_gb300 as te
+        te.build()
+        run_batched(args)
     else:
         import timeevolver_gb300 as te
         te.build()

@@ -70,6 +70,9 @@ struct te_evolver_s {
   bool ran = false;
   int64_t launches = 0;
   double2* host_state = nullptr;  // pinned buffer for callbacks
+  double* sample_times = nullptr;  // explicit sample times (device), optional
+  double2* state_store = nullptr;  // store for every sampled state (caller-owned), optional
+  int64_t store_ld = 0;
   // per-kernel event timing
   bool profiling = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -207,6 +210,7 @@ void free_evolver(te_evolver ev) {
   cudaFree(ev->orig_tmp);
   cudaFree(ev->partials);
   cudaFree(ev->results);
+  cudaFree(ev->sample_times);
   for (auto& o : ev->obs) {
     cudaFree(o.diag_perm);
     cudaFree(o.vec_perm);
@@ -265,6 +269,9 @@ int run(te_evolver ev, te_result* out) {
   hs->Y[1 * TE_MMAX + 0] = make_double2(1.0, 0.0);
   hs->n_steps = ev->n_samples > 1 ? 1 : 0;
   hs->done = ev->n_samples > 1 ? 0 : 1;
+  hs->sample_times = ev->sample_times;
+  hs->state_store = ev->state_store;
+  hs->store_ld = ev->store_ld;
   rc = te_cuda_check(cudaMemcpyAsync(ev->ds, hs, sizeof(TeDevState), cudaMemcpyHostToDevice, st), "state upload");
   TE_CUDA(cudaStreamSynchronize(st));
   delete hs;
@@ -657,6 +664,30 @@ extern "C" int te_evolver_trace(te_evolver ev, te_step_record* out, int64_t max_
 }
 
 extern "C" int64_t te_evolver_launch_count(te_evolver ev) { return ev ? ev->launches : 0; }
+
+// Sample at the given ascending times (times[0] = 0, times[count-1] <= t)
+// instead of multiples of sampling_step, and optionally store every sampled
+// state (evolver row order) at store_dev + k * store_ld.
+int te_evolver_set_schedule(te_evolver ev, const double* times_host, int64_t count, double2* store_dev,
+                            int64_t store_ld) {
+  if (!ev || count < 1 || !times_host || times_host[0] != 0.0) {
+    te_set_error("te_evolver_set_schedule: invalid arguments");
+    return TE_ERR_INVALID_ARG;
+  }
+  for (int64_t i = 1; i < count; ++i)
+    if (!(times_host[i] >= times_host[i - 1]) || times_host[i] > ev->p.t) {
+      te_set_error("te_evolver_set_schedule: sample times must ascend within [0, t]");
+      return TE_ERR_INVALID_ARG;
+    }
+  cudaFree(ev->sample_times);
+  ev->sample_times = nullptr;
+  TE_CUDA(cudaMalloc(&ev->sample_times, sizeof(double) * count));
+  TE_CUDA(cudaMemcpy(ev->sample_times, times_host, sizeof(double) * count, cudaMemcpyHostToDevice));
+  ev->n_samples = count;
+  ev->state_store = store_dev;
+  ev->store_ld = store_ld;
+  return TE_OK;
+}
 
 extern "C" int te_evolver_reset(te_evolver ev, const double* v, int v_is_device) {
   if (!ev || !v) {

@@ -77,6 +77,12 @@ struct TeDevState {
   // at the beginning of the next step)
   int new_start;
   int pad_tail[3];
+  // optional explicit sample times (ascending, sample_times[0] = 0) instead of
+  // multiples of sampling_step, and an optional store for every sampled state
+  // (sample k at state_store + k * store_ld, in the evolver's row order)
+  const double* sample_times;
+  double2* state_store;
+  int64_t store_ld;
 };
 
 // SELL-32 matrix in the sorted (permuted) basis.
@@ -146,6 +152,9 @@ void te_launch_krylov_step(TeDevState* ds, cudaStream_t st);
 void te_launch_schedule_samples(TeDevState* ds, cudaStream_t st);
 void te_launch_krylov_batch(TeDevState* states, int n_instances, int mode, cudaStream_t st);
 // te_sample.cu
+// internal: explicit sample times and stored sampled states (te_evolver.cu)
+int te_evolver_set_schedule(te_evolver ev, const double* times_host, int64_t count, double2* store_dev,
+                            int64_t store_ld);
 struct TeCombineArgs {
   const double2* cols[TE_MMAX];
   int m;

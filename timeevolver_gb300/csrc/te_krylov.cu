@@ -627,11 +627,14 @@ __device__ void schedule_batch(KCtx& C) {
     double ts = ds->t_sampling;
     int cnt = 0;
     ds->sample_base = idx;
+    const double* times = ds->sample_times;
     auto cond = [&](int i, double tsv) {
-      return i < ns && (tsv + ss <= t_now + t_step || (i == ns - 1 && fabs(t_now + t_step - t) <= DBL_EPSILON));
+      if (i >= ns) return false;
+      const double next = times ? times[i] : tsv + ss;
+      return next <= t_now + t_step || (i == ns - 1 && fabs(t_now + t_step - t) <= DBL_EPSILON);
     };
     while (cnt < ds->max_batch && cond(idx, ts)) {
-      ts += ss;
+      ts = times ? times[idx] : ts + ss;
       dts[cnt] = ts - t_now;
       ++cnt;
       ++idx;

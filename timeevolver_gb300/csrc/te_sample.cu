@@ -22,7 +22,7 @@
 template <int G>
 __device__ __forceinline__ void combine_rows(const TeCombineArgs& a, const double2* const* cols, int m,
                                              const double2 (*ys)[TE_MMAX], const int* slot_s, int S,
-                                             double2* last_out) {
+                                             double2* last_out, double2* store, int64_t store_ld, int base) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < a.n; r += (int64_t)gridDim.x * blockDim.x) {
     double2 acc[G];
 #pragma unroll
@@ -44,6 +44,7 @@ __device__ __forceinline__ void combine_rows(const TeCombineArgs& a, const doubl
       } else {
         a.sample_out[(int64_t)(slot - 1) * a.n + r] = acc[o];
         if (slot == S) last_out[r] = acc[o];
+        if (store) store[(int64_t)(base + slot - 1) * store_ld + r] = acc[o];
       }
     }
   }
@@ -75,11 +76,14 @@ __global__ void __launch_bounds__(TE_THREADS) combine_kernel(TeCombineArgs a, Te
       ys[o][j] = j < m ? ds->Y[slot_s[o] * TE_MMAX + j] : make_double2(0.0, 0.0);
     }
     __syncthreads();
+    double2* store = ds->state_store;
+    const int64_t sld = ds->store_ld;
+    const int base = ds->sample_base;
     switch (G) {
-      case 1: combine_rows<1>(a, cols, m, ys, slot_s, S, last_out); break;
-      case 2: combine_rows<2>(a, cols, m, ys, slot_s, S, last_out); break;
-      case 3: combine_rows<3>(a, cols, m, ys, slot_s, S, last_out); break;
-      default: combine_rows<4>(a, cols, m, ys, slot_s, S, last_out); break;
+      case 1: combine_rows<1>(a, cols, m, ys, slot_s, S, last_out, store, sld, base); break;
+      case 2: combine_rows<2>(a, cols, m, ys, slot_s, S, last_out, store, sld, base); break;
+      case 3: combine_rows<3>(a, cols, m, ys, slot_s, S, last_out, store, sld, base); break;
+      default: combine_rows<4>(a, cols, m, ys, slot_s, S, last_out, store, sld, base); break;
     }
   }
 }

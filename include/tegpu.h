@@ -238,6 +238,29 @@ int te_batch_state(te_batch b, int instance, double* out_host);
 int64_t te_batch_launch_count(te_batch b);
 void* te_batch_stream(te_batch b);
 
+/* ------------------------------------------------------------------ adjoint */
+
+/* Gradient of L(theta) = <psi(T)|O|psi(T)>, psi(T) = exp(-i H(theta) T) v,
+ * H(theta) = sum_k theta_k H_k, by the adjoint method:
+ * dL/dtheta_k = 2 Im int_0^T <lambda(s)|H_k|psi(s)> ds with the costate
+ * lambda(s) = exp(+i H (T - s)) O psi(T) evolved backward on the GPU, the time
+ * integral by Gauss-Legendre with nodes_per_interval nodes on every
+ * checkpoint interval of length checkpoint_interval, and the bilinear forms of
+ * all terms in one fused pass.  The forward evolution is krylovTimeEvolver's
+ * algorithm (expFactor 1, tolerance tol, Krylov dimension m); no counterpart
+ * in the reference, which has no differentiation.  terms, O (caller-owned)
+ * must outlive the object; v (complex n) is copied. */
+typedef struct te_adjoint_s* te_adjoint;
+int te_adjoint_create(int n_terms, const te_matrix* terms, te_matrix O, const double* v_host, double T, double tol,
+                      int m, double checkpoint_interval, int nodes_per_interval, te_adjoint* out);
+int te_adjoint_destroy(te_adjoint a);
+/* loss and gradient (n_terms doubles) at theta */
+int te_adjoint_run(te_adjoint a, const double* theta, double* loss, double* grad);
+/* loss only: one plain forward evolution sampled at 0 and T */
+int te_adjoint_forward(te_adjoint a, const double* theta, double* loss);
+/* results of the last forward / backward evolutions, kernel launches of the last call, sample nodes */
+int te_adjoint_stats(te_adjoint a, te_result* forward, te_result* backward, int64_t* launches, int64_t* n_nodes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -90,6 +90,11 @@ SIGNATURES = {
     "te_batch_state": (_I, [_P, _I, _P]),
     "te_batch_launch_count": (_I64, [_P]),
     "te_batch_stream": (_P, [_P]),
+    "te_adjoint_create": (_I, [_I, _P, _P, _P, _D, _D, _I, _D, _I, _P]),
+    "te_adjoint_destroy": (_I, [_P]),
+    "te_adjoint_run": (_I, [_P, _P, _P, _P]),
+    "te_adjoint_forward": (_I, [_P, _P, _P]),
+    "te_adjoint_stats": (_I, [_P, _P, _P, _P, _P]),
 }
 
 _lib = None
@@ -357,6 +362,74 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class Adjoint:
+    """Gradients of <psi(T)|O|psi(T)> with respect to the couplings theta of
+    H = sum_k theta_k H_k (te_adjoint_*).  ``terms``: list of Matrix; ``O``: Matrix."""
+
+    def __init__(self, terms, O, v, T, tol=1e-10, m=40, checkpoint_interval=0.5, nodes_per_interval=24):
+        self._keep = list(terms) + [O]
+        arr = (ctypes.c_void_p * len(terms))(*[t.handle.value for t in terms])
+        v = np.ascontiguousarray(v, dtype=np.complex128)
+        self.K = len(terms)
+        self.handle = ctypes.c_void_p()
+        _check(lib().te_adjoint_create(self.K, arr, O.handle, _ptr(v), float(T), float(tol), int(m),
+                                       float(checkpoint_interval), int(nodes_per_interval), ctypes.byref(self.handle)),
+               "te_adjoint_create")
+
+    def run(self, theta):
+        th = np.ascontiguousarray(theta, dtype=np.float64)
+        loss = ctypes.c_double()
+        grad = np.zeros(self.K)
+        _check(lib().te_adjoint_run(self.handle, _ptr(th), ctypes.byref(loss), _ptr(grad)), "te_adjoint_run")
+        return loss.value, grad
+
+    def forward(self, theta):
+        th = np.ascontiguousarray(theta, dtype=np.float64)
+        loss = ctypes.c_double()
+        _check(lib().te_adjoint_forward(self.handle, _ptr(th), ctypes.byref(loss)), "te_adjoint_forward")
+        return loss.value
+
+    def stats(self):
+        f, b = TeResult(), TeResult()
+        launches, nodes = ctypes.c_int64(), ctypes.c_int64()
+        _check(lib().te_adjoint_stats(self.handle, ctypes.byref(f), ctypes.byref(b), ctypes.byref(launches),
+                                      ctypes.byref(nodes)), "te_adjoint_stats")
+        return dict(forward_steps=f.n_steps, forward_status=f.status, forward_err=f.err, backward_steps=b.n_steps,
+                    backward_status=b.status, backward_err=b.err, launches=launches.value, nodes=nodes.value)
+
+    def close(self):
+        if self.handle:
+            lib().te_adjoint_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def expectation_function():
+    """torch.autograd.Function over te_adjoint_run: ``f.apply(theta, adjoint)``
+    returns <psi(T)|O|psi(T)> as a 0-d float64 tensor whose backward is the
+    adjoint gradient."""
+    import torch
+
+    class KrylovExpectation(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, theta, adjoint):
+            loss, grad = adjoint.run(theta.detach().cpu().numpy().astype(np.float64))
+            ctx.save_for_backward(torch.from_numpy(grad).to(theta.device, theta.dtype))
+            return torch.tensor(loss, dtype=theta.dtype, device=theta.device)
+
+        @staticmethod
+        def backward(ctx, g):
+            (grad,) = ctx.saved_tensors
+            return g * grad, None
+
+    return KrylovExpectation
 
 
 class StopEvolution(Exception):

@@ -147,3 +147,20 @@ def bose_hubbard(L, N, J, U, mu=0.0):
             terms.append(number_operator(i, -mu))
     B = Basis(N, L, 0, 0)
     return B, operator_matrix(terms, B)
+
+
+def bose_hubbard_term_matrices(L, N):
+    """Terms of H(theta) = sum_b J_b H_hop,b + U H_int for the adjoint:
+    H_hop,b = -(a_b^dag a_{b+1} + h.c.) for the L-1 bonds, H_int = 1/2 sum_i
+    n_i (n_i - 1), in the basis(N, L) order.  Returns (basis, [COO, ...])."""
+    B = Basis(N, L, 0, 0)
+    mats = []
+    for b in range(L - 1):
+        mats.append(operator_matrix([lin_interaction(b, b + 1, 0, 0, False, -1.0),
+                                     lin_interaction(b, b + 1, 0, 0, True, -1.0)], B))
+    inter = []
+    for i in range(L):
+        inter.append(four_point_a(i, i, i, i, 0, 0, 0, 0, 0.5))
+        inter.append(number_operator(i, -0.5))
+    mats.append(operator_matrix(inter, B))
+    return B, mats

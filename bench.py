@@ -387,6 +387,64 @@ def run_batched(args):
     print(json.dumps(line), flush=True)
 
 
+ADJ_METRIC = "grads/s (adjoint d<n_0(T)>/d(J_1..J_9, U), Bose-Hubbard L=10 N=10, T=5, tol 1e-10, m=40)"
+ADJ_WORKLOAD = ("Bose-Hubbard open chain L=10 N=10 (dim 92378), H = sum_b J_b H_hop,b + U H_int, J_b~U(0.8,1.2) "
+                "(numpy default_rng(2)), U=2; v = all bosons on site 0; loss <n_0(T)>, T=5, tol=1e-10, m=40; "
+                "checkpoint interval 0.5, Gauss-Legendre nodes per interval")
+
+
+def run_adjoint(args, nodes=24):
+    """Adjoint gradient vs one plain forward evolution, and central FD on the GPU."""
+    import torch
+    import timeevolver_gb300 as te
+    from timeevolver_gb300 import models
+    te.lib().te_set_device(0)
+    L = 10
+    B, mats = models.bose_hubbard_term_matrices(L, L)
+    n = len(B)
+    rng = np.random.default_rng(2)
+    theta = np.concatenate([rng.uniform(0.8, 1.2, L - 1), [2.0]])
+    v = np.zeros(n, dtype=np.complex128)
+    v[B.index([L] + [0] * (L - 1))] = 1.0
+    terms = [te.Matrix.from_coo(n, m) for m in mats]
+    O = te.Matrix.from_coo(n, models.operator_matrix([models.number_operator(0, 1.0)], B))
+    adj = te.Adjoint(terms, O, v, T=5.0, tol=1e-10, m=40, checkpoint_interval=0.5, nodes_per_interval=nodes)
+    for _ in range(args.warmup):
+        adj.run(theta)
+        adj.forward(theta)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        loss, grad = adj.run(theta)
+    torch.cuda.synchronize()
+    t_grad = (time.perf_counter() - t0) / args.steps
+    st = adj.stats()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        loss_f = adj.forward(theta)
+    torch.cuda.synchronize()
+    t_fwd = (time.perf_counter() - t0) / args.steps
+    fwd_steps = adj.stats()["forward_steps"]
+    h = 1e-5
+    fd = np.zeros_like(theta)
+    for k in range(len(theta)):
+        e = np.zeros_like(theta)
+        e[k] = h
+        fd[k] = (adj.forward(theta + e) - adj.forward(theta - e)) / (2 * h)
+    rel = float(np.max(np.abs(grad - fd)) / np.max(np.abs(fd)))
+    line = {"metric": ADJ_METRIC, "value": 1.0 / t_grad, "unit": "grads/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_grad * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "complex128 (FP64)", "data": "synthetic (seeded couplings)",
+            "config": {"workload": ADJ_WORKLOAD, "n": n, "nodes_per_interval": nodes, "sample_nodes": st["nodes"],
+                       "loss": loss, "plain_forward_loss": loss_f},
+            "cost_vs_forward": t_grad / t_fwd, "forward_s": t_fwd,
+            "forward_krylov_steps": {"plain": fwd_steps, "adjoint_forward": st["forward_steps"],
+                                     "costate": st["backward_steps"]},
+            "fd_check": {"step": h, "max_abs_diff_rel": rel, "grad": grad.tolist(), "fd": fd.tolist()},
+            "gpu_launches_per_gradient": int(st["launches"])}
+    print(json.dumps(line), flush=True)
+
+
 def ncu_case(t_final):
     """A short solve of the same workload for ncu captures (t_final instead of 10)."""
     import timeevolver_gb300 as te
@@ -405,8 +463,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--config", default="plain", choices=["plain", "batched"],
-                    help="plain: the L=12 single evolution (headline); batched: 256 chains in one batch")
+    ap.add_argument("--config", default="plain", choices=["plain", "batched", "adjoint"],
+                    help="plain: the L=12 single evolution (headline); batched: 256 chains in one batch; "
+                         "adjoint: gradients of <n_0(T)> for L=10")
     ap.add_argument("--ncu-case", type=float, default=None, metavar="T",
                     help="run one short solve to time T (for ncu captures) and exit")
     args = ap.parse_args()
@@ -419,6 +478,10 @@ def main():
         import timeevolver_gb300 as te
         te.build()
         run_batched(args)
+    elif args.config == "adjoint":
+        import timeevolver_gb300 as te
+        te.build()
+        run_adjoint(args)
     else:
         import timeevolver_gb300 as te
         te.build()

@@ -248,8 +248,8 @@ void* te_batch_stream(te_batch b);
  * checkpoint interval of length checkpoint_interval, and the bilinear forms of
  * all terms in one fused pass.  The forward evolution is krylovTimeEvolver's
  * algorithm (expFactor 1, tolerance tol, Krylov dimension m); no counterpart
- * in the reference, which has no differentiation.  terms, O (caller-owned)
- * must outlive the object; v (complex n) is copied. */
+ * in the reference, which has no differentiation.  The terms are copied at
+ * creation; O (caller-owned) must outlive the object; v (complex n) is copied. */
 typedef struct te_adjoint_s* te_adjoint;
 int te_adjoint_create(int n_terms, const te_matrix* terms, te_matrix O, const double* v_host, double T, double tol,
                       int m, double checkpoint_interval, int nodes_per_interval, te_adjoint* out);
@@ -260,6 +260,9 @@ int te_adjoint_run(te_adjoint a, const double* theta, double* loss, double* grad
 int te_adjoint_forward(te_adjoint a, const double* theta, double* loss);
 /* results of the last forward / backward evolutions, kernel launches of the last call, sample nodes */
 int te_adjoint_stats(te_adjoint a, te_result* forward, te_result* backward, int64_t* launches, int64_t* n_nodes);
+/* host wall time (ms) of the last call's phases: ms[0] coupling refresh, ms[1]
+ * forward evolution, ms[2] costate evolution, ms[3] bilinear pass */
+int te_adjoint_phase_times(te_adjoint a, double* ms);
 
 #ifdef __cplusplus
 }

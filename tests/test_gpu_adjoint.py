@@ -86,3 +86,23 @@ def test_torch_autograd_binding(problem):
     ref_loss, ref_grad = adj.run(theta)
     assert abs(loss.item() - ref_loss) < 1e-14
     assert np.allclose(th.grad.numpy(), ref_grad, rtol=0, atol=1e-14)
+
+
+def test_theta_refresh_is_stateless(problem):
+    """H(theta) keeps one pattern and rescales its values on the device: the
+    result for theta must not depend on the couplings used before."""
+    adj, theta = problem["adj"], problem["theta"]
+    l1, g1 = adj.run(theta)
+    adj.run(theta * 1.3)
+    adj.forward(theta[::-1].copy())
+    l2, g2 = adj.run(theta)
+    assert l1 == l2
+    assert np.array_equal(g1, g2)
+
+
+def test_forward_loss_matches_oracle(problem, oracle_lib):
+    adj, theta = problem["adj"], problem["theta"]
+    for th in (theta, 0.7 * theta[::-1].copy()):
+        r = oracle_lib.evolve(_sum(problem["mats"], th), problem["v"], 2.0, 2.0, [("sparse", problem["O"])],
+                              tol=1e-12, m=30)
+        assert abs(adj.forward(th) - r["samples"][0][-1]) < 1e-9

@@ -95,6 +95,7 @@ SIGNATURES = {
     "te_adjoint_run": (_I, [_P, _P, _P, _P]),
     "te_adjoint_forward": (_I, [_P, _P, _P]),
     "te_adjoint_stats": (_I, [_P, _P, _P, _P, _P]),
+    "te_adjoint_phase_times": (_I, [_P, _P]),
 }
 
 _lib = None
@@ -369,7 +370,7 @@ class Adjoint:
     H = sum_k theta_k H_k (te_adjoint_*).  ``terms``: list of Matrix; ``O``: Matrix."""
 
     def __init__(self, terms, O, v, T, tol=1e-10, m=40, checkpoint_interval=0.5, nodes_per_interval=24):
-        self._keep = list(terms) + [O]
+        self._keep = [O]  # the terms are copied at creation
         arr = (ctypes.c_void_p * len(terms))(*[t.handle.value for t in terms])
         v = np.ascontiguousarray(v, dtype=np.complex128)
         self.K = len(terms)
@@ -398,6 +399,12 @@ class Adjoint:
                                       ctypes.byref(nodes)), "te_adjoint_stats")
         return dict(forward_steps=f.n_steps, forward_status=f.status, forward_err=f.err, backward_steps=b.n_steps,
                     backward_status=b.status, backward_err=b.err, launches=launches.value, nodes=nodes.value)
+
+    def phase_times(self):
+        """Host wall time (ms) of the last call's phases."""
+        ms = np.zeros(4)
+        _check(lib().te_adjoint_phase_times(self.handle, _ptr(ms)), "te_adjoint_phase_times")
+        return dict(theta_refresh=ms[0], forward=ms[1], costate=ms[2], bilinear=ms[3])
 
     def close(self):
         if self.handle:

@@ -64,6 +64,8 @@ struct te_evolver_s {
   double* partials = nullptr;
   double* results = nullptr;  // n_obs x n_samples
   int max_batch = 1;
+  int batch_cap = 0;         // states the batch buffer holds
+  size_t results_cap = 0;    // doubles the results buffer holds
   std::vector<HostObs> obs;
   std::vector<te_step_record> trace;
   te_result res{};
@@ -220,12 +222,17 @@ void free_evolver(te_evolver ev) {
   delete ev;
 }
 
+// Sample results, zeroed for every run; the buffer is kept while it is large enough.
 int alloc_results(te_evolver ev) {
-  cudaFree(ev->results);
-  ev->results = nullptr;
   size_t count = std::max<size_t>(1, ev->obs.size()) * (size_t)ev->n_samples;
-  TE_CUDA(cudaMalloc(&ev->results, sizeof(double) * count));
-  TE_CUDA(cudaMemset(ev->results, 0, sizeof(double) * count));
+  if (count > ev->results_cap) {
+    cudaFree(ev->results);
+    ev->results = nullptr;
+    ev->results_cap = 0;
+    TE_CUDA(cudaMalloc(&ev->results, sizeof(double) * count));
+    ev->results_cap = count;
+  }
+  TE_CUDA(cudaMemsetAsync(ev->results, 0, sizeof(double) * count, ev->st));
   return TE_OK;
 }
 
@@ -237,9 +244,13 @@ int run(te_evolver ev, te_result* out) {
   bool need_host = false;
   for (auto& o : ev->obs) need_host |= (o.kind == 2 || o.kind == 3);
   ev->max_batch = need_host ? 1 : (int)std::max<int64_t>(1, std::min<int64_t>(TE_SCAP, ((int64_t)256 << 20) / (16 * n)));
-  cudaFree(ev->batch);
-  ev->batch = nullptr;
-  TE_CUDA(cudaMalloc(&ev->batch, sizeof(double2) * n * ev->max_batch));
+  if (ev->max_batch > ev->batch_cap) {  // kept across runs while large enough
+    cudaFree(ev->batch);
+    ev->batch = nullptr;
+    ev->batch_cap = 0;
+    TE_CUDA(cudaMalloc(&ev->batch, sizeof(double2) * n * ev->max_batch));
+    ev->batch_cap = ev->max_batch;
+  }
   int rc = alloc_results(ev);
   if (rc != TE_OK) return rc;
 

@@ -381,7 +381,15 @@ void free_batch(te_batch b) {
   delete b;
 }
 
-int grid_chunks(const te_batch_s* b) { return te_grid_for(b->n_chunks * 32, TE_THREADS, 8); }
+// One resident wave of the chunk-strided kernels (apply, update, combine).
+int grid_chunks(const te_batch_s* b) {
+  const void* k[] = {(const void*)batch_apply_kernel<true, true>,  (const void*)batch_apply_kernel<true, false>,
+                     (const void*)batch_apply_kernel<false, true>, (const void*)batch_apply_kernel<false, false>,
+                     (const void*)batch_update_kernel,             (const void*)batch_combine_kernel};
+  int bps = 8;
+  for (const void* f : k) bps = std::min(bps, te_kernel_blocks_per_sm(f, TE_THREADS, 0));
+  return (int)std::min<int64_t>((b->n_chunks * 32 + TE_THREADS - 1) / TE_THREADS, (int64_t)te_num_sms() * bps);
+}
 
 // Record the kernels of one global step (or of one extra sample batch).
 int enqueue_step(te_batch b, bool full_step) {

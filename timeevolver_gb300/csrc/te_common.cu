@@ -2,6 +2,10 @@
 #include <cstdarg>
 #include <cstdio>
 
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "te_internal.cuh"
 
 static thread_local char g_last_error[512] = "";
@@ -37,6 +41,38 @@ int te_grid_for(int64_t n_items, int threads, int blocks_per_sm) {
   int64_t cap = (int64_t)te_num_sms() * blocks_per_sm;
   if (need < 1) need = 1;
   return (int)(need < cap ? need : cap);
+}
+
+int te_grid_balanced(int64_t n_items, int threads, int blocks_per_sm) {
+  const int64_t cap = (int64_t)te_grid_for(n_items, threads, blocks_per_sm) * threads;
+  const int64_t per_thread = (n_items + cap - 1) / cap;  // items per thread in the capped grid
+  if (per_thread <= 1) return te_grid_for(n_items, threads, blocks_per_sm);
+  const int64_t threads_needed = (n_items + per_thread - 1) / per_thread;
+  return (int)((threads_needed + threads - 1) / threads);
+}
+
+int te_kernel_blocks_per_sm(const void* kernel, int threads, size_t dyn_smem) {
+  static std::mutex mu;
+  static std::map<std::tuple<const void*, int, size_t>, int> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_tuple(kernel, threads, dyn_smem);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  int blocks = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kernel, threads, dyn_smem) != cudaSuccess || blocks < 1) {
+    cudaGetLastError();
+    blocks = 1;
+  }
+  cache[key] = blocks;
+  return blocks;
+}
+
+int te_grid_fit(const void* kernel, int64_t n_items, int threads, size_t dyn_smem) {
+  const int64_t cap = (int64_t)te_num_sms() * te_kernel_blocks_per_sm(kernel, threads, dyn_smem);
+  const int64_t need = (n_items + threads - 1) / threads;
+  if (need <= cap) return (int)std::max<int64_t>(need, 1);
+  const int64_t per_thread = (n_items + cap * threads - 1) / (cap * threads);
+  return (int)((n_items + per_thread * threads - 1) / (per_thread * threads));
 }
 
 extern "C" const char* te_last_error(void) { return g_last_error; }

@@ -95,6 +95,11 @@ struct TeSell {
   double* val = nullptr;  // real: slots doubles; complex: 2*slots doubles
   int32_t* perm = nullptr;   // permuted index -> original index
   int32_t* iperm = nullptr;  // original index -> permuted index
+  // Static schedule of the SpMV passes: warp w of a grid of `grid` blocks of
+  // TE_THREADS owns chunks [warp_chunk[w], warp_chunk[w + 1]), contiguous
+  // ranges of equal FP64 work (slots plus the per-row epilogue).
+  int32_t* warp_chunk = nullptr;
+  int grid = 0;
 };
 
 struct te_matrix_s {
@@ -123,6 +128,17 @@ int te_cuda_check(cudaError_t e, const char* what);
 // launch shapes
 int te_num_sms();
 int te_grid_for(int64_t n_items, int threads, int blocks_per_sm);
+// Like te_grid_for, but shrinks the grid so that a grid-stride loop gives
+// every thread the same number of items (up to one).
+int te_grid_balanced(int64_t n_items, int threads, int blocks_per_sm);
+// Resident blocks per SM of a kernel at this block size (occupancy query, cached).
+int te_kernel_blocks_per_sm(const void* kernel, int threads, size_t dyn_smem);
+// One wave of a grid-stride kernel: at most every SM's resident blocks, and
+// shrunk so that every thread gets the same number of items (up to one).
+int te_grid_fit(const void* kernel, int64_t n_items, int threads, size_t dyn_smem = 0);
+// Resident blocks per SM shared by the SELL SpMV passes of a matrix (the
+// Lanczos apply variants and the plain SpMV), which run on one static schedule.
+int te_sell_blocks_per_sm(bool is_real);
 
 // ---------------------------------------------------------------- launches
 // te_matrix.cu

@@ -23,9 +23,11 @@ __device__ __forceinline__ bool te_step_inactive(const TeDevState* ds) {
   return ds->fatal != 0 || ds->done != 0 || ds->breakdown != 0;
 }
 
+// 6 (real H: at most 40 registers) or 5 (complex H) resident blocks of 256;
+// the static chunk schedule of the matrix assumes the whole grid is resident.
 template <bool REAL, bool HAS_PREV>
-__global__ void __launch_bounds__(TE_THREADS) lanczos_apply_kernel(
-    int64_t n, int64_t n_chunks, const int64_t* __restrict__ chunk_off, const int32_t* __restrict__ col,
+__global__ void __launch_bounds__(TE_THREADS, REAL ? 6 : 5) lanczos_apply_kernel(
+    int64_t n, const int32_t* __restrict__ warp_chunk, const int64_t* __restrict__ chunk_off, const int32_t* __restrict__ col,
     const double* __restrict__ val, const double2* __restrict__ u_j, const double2* __restrict__ u_jm1,
     double2* __restrict__ w, TeDevState* ds, double* partials, int j) {
   __shared__ double scratch[2 * 32];
@@ -35,8 +37,9 @@ __global__ void __launch_bounds__(TE_THREADS) lanczos_apply_kernel(
   const double g = ds->exp_factor * sj;  // A v_j = -i g H u_j
   const double cprev = HAS_PREV ? ds->beta[j] * ds->s[j - 1] : 0.0;
   double acc[2] = {0.0, 0.0};
-  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < n_chunks; c += warps) {
+  const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int64_t c_end = warp_chunk[wid + 1];
+  for (int64_t c = warp_chunk[wid]; c < c_end; ++c) {
     double2 y = te_sell_row<REAL>(chunk_off, col, val, u_j, c, lane);
     const int64_t r = c * 32 + lane;
     if (r < n) {
@@ -295,29 +298,23 @@ void te_launch_gs_update_norm(int64_t n, const TeBasisPtrs& V, int nvec, const d
                                                                                 j);
 }
 
+int te_sell_blocks_per_sm(bool is_real) {
+  const void* k[2] = {is_real ? (const void*)lanczos_apply_kernel<true, true> : (const void*)lanczos_apply_kernel<false, true>,
+                      is_real ? (const void*)lanczos_apply_kernel<true, false>
+                              : (const void*)lanczos_apply_kernel<false, false>};
+  return std::min(te_kernel_blocks_per_sm(k[0], TE_THREADS, 0), te_kernel_blocks_per_sm(k[1], TE_THREADS, 0));
+}
+
 void te_launch_lanczos_apply(const TeSell& A, bool is_real, const double2* u_j, const double2* u_jm1, double2* w,
                              TeDevState* ds, double* partials, int j, cudaStream_t st) {
-  const int grid = te_grid_for(A.n_chunks * 32, TE_THREADS, 8);
-  if (is_real) {
-    if (u_jm1)
-      lanczos_apply_kernel<true, true><<<grid, TE_THREADS, 0, st>>>(A.n, A.n_chunks, A.chunk_off, A.col, A.val, u_j,
-                                                                    u_jm1, w, ds, partials, j);
-    else
-      lanczos_apply_kernel<true, false><<<grid, TE_THREADS, 0, st>>>(A.n, A.n_chunks, A.chunk_off, A.col, A.val, u_j,
-                                                                     u_jm1, w, ds, partials, j);
-  } else {
-    if (u_jm1)
-      lanczos_apply_kernel<false, true><<<grid, TE_THREADS, 0, st>>>(A.n, A.n_chunks, A.chunk_off, A.col, A.val, u_j,
-                                                                     u_jm1, w, ds, partials, j);
-    else
-      lanczos_apply_kernel<false, false><<<grid, TE_THREADS, 0, st>>>(A.n, A.n_chunks, A.chunk_off, A.col, A.val,
-                                                                      u_j, u_jm1, w, ds, partials, j);
-  }
+  auto k = is_real ? (u_jm1 ? lanczos_apply_kernel<true, true> : lanczos_apply_kernel<true, false>)
+                   : (u_jm1 ? lanczos_apply_kernel<false, true> : lanczos_apply_kernel<false, false>);
+  k<<<A.grid, TE_THREADS, 0, st>>>(A.n, A.warp_chunk, A.chunk_off, A.col, A.val, u_j, u_jm1, w, ds, partials, j);
 }
 
 void te_launch_lanczos_update(int64_t n, const double2* w, const double2* u_j, double2* u_jp1, TeDevState* ds,
                               double* partials, int j, cudaStream_t st) {
-  const int grid = te_grid_for(n, TE_THREADS, 8);
+  const int grid = te_grid_fit((const void*)lanczos_update_kernel<true>, n, TE_THREADS);
   if (u_jp1)
     lanczos_update_kernel<true><<<grid, TE_THREADS, 0, st>>>(n, w, u_j, u_jp1, ds, partials, j);
   else

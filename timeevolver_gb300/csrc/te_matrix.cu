@@ -25,15 +25,16 @@
 // ---------------------------------------------------------------- kernels
 
 template <bool REAL>
-__global__ void __launch_bounds__(TE_THREADS) sell_spmv_kernel(int64_t n, int64_t n_chunks,
+__global__ void __launch_bounds__(TE_THREADS) sell_spmv_kernel(int64_t n, const int32_t* __restrict__ warp_chunk,
                                                                const int64_t* __restrict__ chunk_off,
                                                                const int32_t* __restrict__ col,
                                                                const double* __restrict__ val, double2 alpha,
                                                                const double2* __restrict__ x,
                                                                double2* __restrict__ y) {
   const int lane = threadIdx.x & 31;
-  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < n_chunks; c += warps) {
+  const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int64_t c_end = warp_chunk[wid + 1];
+  for (int64_t c = warp_chunk[wid]; c < c_end; ++c) {
     double2 acc = te_sell_row<REAL>(chunk_off, col, val, x, c, lane);
     int64_t r = c * 32 + lane;
     if (r < n) y[r] = make_double2(alpha.x * acc.x - alpha.y * acc.y, alpha.x * acc.y + alpha.y * acc.x);
@@ -61,12 +62,11 @@ __global__ void permute_kernel(int64_t n, const int32_t* __restrict__ idx, const
 
 void te_launch_sell_spmv(const TeSell& A, bool is_real, double2 alpha, const double2* x_perm, double2* y_perm,
                          cudaStream_t st) {
-  int grid = te_grid_for(A.n_chunks * 32, TE_THREADS, 8);
   if (is_real)
-    sell_spmv_kernel<true><<<grid, TE_THREADS, 0, st>>>(A.n, A.n_chunks, A.chunk_off, A.col, A.val, alpha, x_perm,
+    sell_spmv_kernel<true><<<A.grid, TE_THREADS, 0, st>>>(A.n, A.warp_chunk, A.chunk_off, A.col, A.val, alpha, x_perm,
                                                         y_perm);
   else
-    sell_spmv_kernel<false><<<grid, TE_THREADS, 0, st>>>(A.n, A.n_chunks, A.chunk_off, A.col, A.val, alpha, x_perm,
+    sell_spmv_kernel<false><<<A.grid, TE_THREADS, 0, st>>>(A.n, A.warp_chunk, A.chunk_off, A.col, A.val, alpha, x_perm,
                                                          y_perm);
 }
 
@@ -79,7 +79,7 @@ void te_launch_csr_spmv(const te_matrix_s& A, double2 alpha, const double2* x, d
 }
 
 void te_launch_permute(int64_t n, const int32_t* idx, const double2* in, double2* out, cudaStream_t st) {
-  permute_kernel<<<te_grid_for(n, TE_THREADS, 8), TE_THREADS, 0, st>>>(n, idx, in, out);
+  permute_kernel<<<te_grid_fit((const void*)permute_kernel, n, TE_THREADS), TE_THREADS, 0, st>>>(n, idx, in, out);
 }
 
 // ------------------------------------------------------------ host build
@@ -97,6 +97,7 @@ void free_matrix(te_matrix_s* M) {
   cudaFree(M->sell.val);
   cudaFree(M->sell.perm);
   cudaFree(M->sell.iperm);
+  cudaFree(M->sell.warp_chunk);
   delete M;
 }
 
@@ -199,6 +200,26 @@ int build_matrix(te_matrix_s* M, const std::vector<int32_t>& rp, const std::vect
   if ((rc = upload(&S.val, sval.data(), sval.size())) != TE_OK) return rc;
   if ((rc = upload(&S.perm, perm.data(), perm.size())) != TE_OK) return rc;
   if ((rc = upload(&S.iperm, iperm.data(), iperm.size())) != TE_OK) return rc;
+  // static warp schedule: equal FP64 work per warp (te_sell_row issues 2 (real)
+  // or 4 (complex) FMAs per slot; the SpMV epilogues about 8 per row)
+  const int bps = std::min(te_sell_blocks_per_sm(real),
+                           te_kernel_blocks_per_sm(real ? (const void*)sell_spmv_kernel<true>
+                                                        : (const void*)sell_spmv_kernel<false>,
+                                                   TE_THREADS, 0));
+  S.grid = (int)std::min<int64_t>((S.n_chunks * 32 + TE_THREADS - 1) / TE_THREADS, (int64_t)te_num_sms() * bps);
+  const int64_t W = (int64_t)S.grid * (TE_THREADS / 32);
+  const double w_slot = real ? 2.0 : 4.0, w_chunk = 8.0 * 32;
+  auto cost = [&](int64_t c) { return w_slot * (double)off[c] + w_chunk * (double)c; };
+  const double total = cost(S.n_chunks);
+  std::vector<int32_t> wc(W + 1);
+  int64_t c = 0;
+  for (int64_t w = 0; w < W; ++w) {
+    const double target = total * (double)w / (double)W;
+    while (c < S.n_chunks && cost(c) < target) ++c;
+    wc[w] = (int32_t)c;
+  }
+  wc[W] = (int32_t)S.n_chunks;
+  if ((rc = upload(&S.warp_chunk, wc.data(), wc.size())) != TE_OK) return rc;
   return TE_OK;
 }
 

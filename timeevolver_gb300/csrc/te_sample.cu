@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(TE_THREADS) combine_kernel(TeCombineArgs a, Te
 }
 
 void te_launch_combine(const TeCombineArgs& a, TeDevState* ds, double2* last_out, cudaStream_t st) {
-  combine_kernel<<<te_grid_for(a.n, TE_THREADS, 8), TE_THREADS, 0, st>>>(a, ds, last_out);
+  combine_kernel<<<te_grid_fit((const void*)combine_kernel, a.n, TE_THREADS), TE_THREADS, 0, st>>>(a, ds, last_out);
 }
 
 // Diagonal observables: Re sum_i O_ii |psi_i|^2 (= Re zdotc(psi, O psi) for a
@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(TE_THREADS) fused_obs_kernel(int64_t n, const 
 template <int ND, int NV>
 static void launch_fused(int64_t n, const double2* psi, const TeFusedObs& f, TeDevState* ds, double* partials,
                          double* results, int n_samples_total, cudaStream_t st) {
-  fused_obs_kernel<ND, NV><<<te_grid_for(n, TE_THREADS, 4), TE_THREADS, 0, st>>>(n, psi, f, ds, partials, results,
+  fused_obs_kernel<ND, NV><<<te_grid_fit((const void*)fused_obs_kernel<ND, NV>, n, TE_THREADS), TE_THREADS, 0, st>>>(n, psi, f, ds, partials, results,
                                                                                  n_samples_total);
 }
 
@@ -235,5 +235,5 @@ __global__ void __launch_bounds__(TE_THREADS) norm2_kernel(int64_t n, const doub
 }
 
 void te_launch_norm2(int64_t n, const double2* x, double* partials, TeDevState* ds, cudaStream_t st) {
-  norm2_kernel<<<te_grid_for(n, TE_THREADS, 8), TE_THREADS, 0, st>>>(n, x, ds, partials);
+  norm2_kernel<<<te_grid_fit((const void*)norm2_kernel, n, TE_THREADS), TE_THREADS, 0, st>>>(n, x, ds, partials);
 }

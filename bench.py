@@ -455,6 +455,110 @@ def run_adjoint(args, nodes=16):
     print(json.dumps(line), flush=True)
 
 
+ZIPF_N, ZIPF_T = 10_000_000, 100.0
+ZIPF_METRIC = "exp(-iHt)v s (synthetic Zipf(1.5) Hermitian, dim 1e7, t=100, tol 1e-8, m=40)"
+ZIPF_WORKLOAD = ("synthetic complex Hermitian H=(A+A^H)/2, dim 1e7, rows of A with Zipf(1.5) lengths clipped to "
+                 "[2,256], distinct uniform columns, re/im ~ N(0,1) (device generator, seed 1), scaled by a "
+                 "30-step power-iteration estimate of ||H||_2; v complex Gaussian (numpy default_rng(1)); t=100, "
+                 "tol=1e-8, m=40, samples at 0 and t")
+ZIPF_CPU_N, ZIPF_CPU_T = 1_000_000, 10.0
+
+
+def run_zipf(args):
+    """The load-imbalanced workload: one solve per step with H and v in HBM,
+    the apply kernel's roofline, and a CPU sample on a smaller instance."""
+    import torch
+    import timeevolver_gb300 as te
+    te.lib().te_set_device(0)
+    t0 = time.perf_counter()
+    H, est = te.Matrix.zipf(ZIPF_N, 1.5, 2, 256, 1, 30)
+    gen_s = time.perf_counter() - t0
+    info = H.info()
+    n, nnz = info["n_rows"], info["nnz"]
+    rng = np.random.default_rng(1)
+    v = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    v /= np.linalg.norm(v)
+    v_dev = torch.from_numpy(v.view(np.float64).copy()).cuda()
+    ev = te.Evolver(H, v, ZIPF_T, ZIPF_T, [], tol=TOL, m=M_KRYLOV)
+    for _ in range(args.warmup):
+        ev.reset(None, device_ptr=v_dev.data_ptr())
+        ev.run()
+    torch.cuda.synchronize()
+    ev.profile(True)
+    stream = torch.cuda.ExternalStream(ev.stream())
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches = 0
+    with ClockSampler(0) as clk:
+        start.record(stream)
+        for _ in range(args.steps):
+            ev.reset(None, device_ptr=v_dev.data_ptr())
+            r = ev.run()
+            launches += te.lib().te_evolver_launch_count(ev.handle)
+        stop.record(stream)
+        stop.synchronize()
+    value = start.elapsed_time(stop) / 1e3 / args.steps
+    apply_ms, apply_n = ev.kernel_time(0)
+    kernel_ms = {name: ev.kernel_time(k) for k, name in enumerate(
+        ["lanczos_apply", "lanczos_update", "krylov_step", "combine", "observables"])}
+    ev.profile(False)
+    ev.close()
+    # end to end through the public call: start vector from the host, state back
+    e2e = []
+    for _ in range(max(1, args.steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = te.evolve(H, v, ZIPF_T, ZIPF_T, [], tol=TOL, m=M_KRYLOV)
+        torch.cuda.synchronize()
+        e2e.append(time.perf_counter() - t0)
+    peaks = load_peaks(te)
+    b_apply = apply_kernel_bytes(n, nnz, info["real"])
+    f_apply = apply_kernel_flops(n, nnz, info["real"])
+    avg = apply_ms / 1e3 / max(1, apply_n)
+    line = {"metric": ZIPF_METRIC, "value": value, "unit": "s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "complex128 (FP64)", "data": "synthetic (device generator, seeded)",
+            "config": {"workload": ZIPF_WORKLOAD, "n": n, "nnz": nnz, "norm_estimate": est,
+                       "generation_s": gen_s, "krylov_steps_per_solve": r.n_steps, "status": r.status,
+                       "err": r.err, "l2": "inputs larger than L2 (H %.1f GB)" % (nnz * 20 / 1e9)},
+            "e2e": {"value": float(np.mean(e2e)), "unit": "s", "h2d_bytes_per_step": 16 * n,
+                    "d2h_bytes_per_step": 16 * n + 16},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "kernel": "lanczos_apply_kernel (SELL-32 SpMV, complex H)",
+                         "achieved": b_apply / avg / 1e9, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": b_apply / avg / 1e9 / peaks["hbm_gbs"], "peak_source": peaks["source"],
+                         "traffic": None, "algorithmic_bytes_per_launch": b_apply, "avg_launch_us": avg * 1e6,
+                         "launches": apply_n,
+                         "fp64": {"achieved_tflops": f_apply / avg / 1e12, "peak_tflops": peaks["fp64_tflops"],
+                                  "frac": f_apply / avg / 1e12 / peaks["fp64_tflops"],
+                                  "flops_per_launch": f_apply}},
+            "kernel_ms_per_solve": {k: round(v_[0] / args.steps, 3) for k, v_ in kernel_ms.items()},
+            "clocks": clk.summary()}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = zipf_cpu_baseline(te, nnz, r.n_steps)
+    print(json.dumps(line), flush=True)
+
+
+def zipf_cpu_baseline(te, nnz_full, steps_full):
+    """The oracle on all host cores on the same generator at dim 1e6, one
+    solve to t=10, scaled by the non-zeros and the Krylov step counts."""
+    import oracle
+    oracle.build()
+    Hs, _ = te.Matrix.zipf(ZIPF_CPU_N, 1.5, 2, 256, 1, 30)
+    coo = Hs.to_coo()
+    rng = np.random.default_rng(1)
+    v = rng.standard_normal(ZIPF_CPU_N) + 1j * rng.standard_normal(ZIPF_CPU_N)
+    v /= np.linalg.norm(v)
+    cores = os.cpu_count()
+    t0 = time.perf_counter()
+    r = oracle.evolve(coo, v, ZIPF_CPU_T, ZIPF_CPU_T, [], tol=TOL, m=M_KRYLOV, n_threads=cores)
+    el = time.perf_counter() - t0
+    per_step = el / max(1, r["n_steps"]) * nnz_full / len(coo[2])
+    return {"value": per_step * steps_full, "unit": "s", "cores": cores, "kind": "port",
+            "sample": "same generator at dim 1e6 (%d non-zeros), t=%g: %d Krylov steps in %.1f s; scaled by the "
+                      "non-zero ratio to %.3f s per Krylov step at dim 1e7 and to the %d steps of the full solve "
+                      "(extrapolated)" % (len(coo[2]), ZIPF_CPU_T, r["n_steps"], el, per_step, steps_full)}
+
+
 def ncu_case(t_final):
     """A short solve of the same workload for ncu captures (t_final instead of 10)."""
     import timeevolver_gb300 as te
@@ -473,9 +577,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--config", default="plain", choices=["plain", "batched", "adjoint"],
+    ap.add_argument("--config", default="plain", choices=["plain", "batched", "adjoint", "zipf"],
                     help="plain: the L=12 single evolution (headline); batched: 256 chains in one batch; "
-                         "adjoint: gradients of <n_0(T)> for L=10")
+                         "adjoint: gradients of <n_0(T)> for L=10; zipf: the dim-1e7 load-imbalanced matrix")
     ap.add_argument("--ncu-case", type=float, default=None, metavar="T",
                     help="run one short solve to time T (for ncu captures) and exit")
     args = ap.parse_args()
@@ -492,6 +596,10 @@ def main():
         import timeevolver_gb300 as te
         te.build()
         run_adjoint(args)
+    elif args.config == "zipf":
+        import timeevolver_gb300 as te
+        te.build()
+        run_zipf(args)
     else:
         import timeevolver_gb300 as te
         te.build()

@@ -89,6 +89,33 @@ int te_matrix_create_coo(int64_t n_rows, int64_t n_cols, int64_t nnz, const uint
 int te_matrix_create_csr(int64_t n_rows, int64_t n_cols, int64_t nnz, const int64_t* row_ptr,
                          const int32_t* col_idx, const double* values, int values_complex, te_matrix* out);
 
+/* Same from a CSR already in device memory (row_ptr_dev: n_rows + 1 int32;
+ * col_dev: nnz int32; values_dev: nnz complex or real doubles); the arrays are
+ * copied.  The layout is built on the device; the 1-norm is accumulated in
+ * 64-bit fixed point (independent of the order of the device's atomics,
+ * resolution ~1e-12 of the largest |entry|) instead of the reference's
+ * floating-point column sums.  No counterpart in the reference (which builds
+ * every matrix on the host). */
+int te_matrix_create_csr_device(int64_t n_rows, int64_t n_cols, int64_t nnz, const int32_t* row_ptr_dev,
+                                const int32_t* col_dev, const double* values_dev, int values_complex,
+                                te_matrix* out);
+
+/* Synthetic load-imbalanced workload, generated on the device (no
+ * counterpart in the reference): H = (A + A^H) / 2 where row r of A has k_r
+ * distinct uniformly random columns, k_r drawn from the Zipf law
+ * P(k) ~ k^-exponent truncated to [min_len, max_len], and entries with
+ * independent N(0, 1) real and imaginary parts; H is then divided by a
+ * spectral-norm estimate from power_iters power iterations (returned in
+ * *norm_estimate; power_iters = 0 leaves H unscaled).  Every random number is
+ * a counter-based hash of (seed, row, draw, stream), so the matrix does not
+ * depend on the launch shape.  Needs n >= 4 max_len. */
+int te_matrix_create_zipf(int64_t n, double exponent, int32_t min_len, int32_t max_len, uint64_t seed,
+                          int32_t power_iters, double* norm_estimate, te_matrix* out);
+
+/* Copy a matrix's original-order CSR to host buffers: row_ptr (n_rows + 1),
+ * col_idx (nnz), values (nnz interleaved complex doubles). */
+int te_matrix_download_csr(te_matrix A, int32_t* row_ptr, int32_t* col_idx, double* values);
+
 int te_matrix_destroy(te_matrix A);
 
 /* n_rows, n_cols, nnz, flags (bit0 real values, bit1 diagonal), and the

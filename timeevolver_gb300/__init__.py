@@ -66,6 +66,9 @@ SIGNATURES = {
     "te_matrix_spmv": (_I, [_P, _D, _D, _P, _P, _P]),
     "te_matrix_spmv_host": (_I, [_P, _D, _D, _P, _P]),
     "te_matrix_spmv_noalloc": (_I, [_P, _D, _D, _P, _P, _P]),
+    "te_matrix_create_csr_device": (_I, [_I64, _I64, _I64, _P, _P, _P, _I, _P]),
+    "te_matrix_download_csr": (_I, [_P, _P, _P, _P]),
+    "te_matrix_create_zipf": (_I, [_I64, _D, ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_int32, _P, _P]),
     "te_evolver_create": (_I, [_P, _P, _P, _P]),
     "te_evolver_destroy": (_I, [_P]),
     "te_evolver_add_sparse_observable": (_I, [_P, _P]),
@@ -159,6 +162,54 @@ class Matrix:
     @classmethod
     def from_coo(cls, n, coo):
         return cls(n, coo[0], coo[1], coo[2])
+
+    @classmethod
+    def _adopt(cls, handle):
+        M = cls.__new__(cls)
+        M.handle = handle
+        M.n = M.info()["n_rows"]
+        return M
+
+    @classmethod
+    def from_device_csr(cls, n_rows, row_ptr, col, values, n_cols=None):
+        """From a CSR already on the GPU (torch tensors: int32 row_ptr and
+        col, complex128 or float64 values); the arrays are copied."""
+        import torch
+        assert row_ptr.dtype == torch.int32 and col.dtype == torch.int32 and row_ptr.is_cuda
+        cplx = values.dtype == torch.complex128
+        vals = torch.view_as_real(values.contiguous()) if cplx else values.contiguous()
+        h = ctypes.c_void_p()
+        _check(lib().te_matrix_create_csr_device(int(n_rows), int(n_cols or n_rows), int(col.numel()),
+                                                 ctypes.c_void_p(row_ptr.data_ptr()), ctypes.c_void_p(col.data_ptr()),
+                                                 ctypes.c_void_p(vals.data_ptr()), int(cplx), ctypes.byref(h)),
+               "te_matrix_create_csr_device")
+        return cls._adopt(h)
+
+    @classmethod
+    def zipf(cls, n, exponent=1.5, min_len=2, max_len=256, seed=1, power_iters=30):
+        """The synthetic load-imbalanced Hermitian matrix generated on the
+        device (te_matrix_create_zipf).  Returns (Matrix, norm_estimate)."""
+        h = ctypes.c_void_p()
+        est = ctypes.c_double(0.0)
+        _check(lib().te_matrix_create_zipf(int(n), float(exponent), int(min_len), int(max_len), int(seed),
+                                           int(power_iters), ctypes.byref(est), ctypes.byref(h)),
+               "te_matrix_create_zipf")
+        return cls._adopt(h), est.value
+
+    def to_csr(self):
+        """(row_ptr int32, col int32, values complex128) of the original-order CSR, on the host."""
+        inf = self.info()
+        rp = np.zeros(inf["n_rows"] + 1, dtype=np.int32)
+        ci = np.zeros(max(1, inf["nnz"]), dtype=np.int32)
+        val = np.zeros(max(1, inf["nnz"]), dtype=np.complex128)
+        _check(lib().te_matrix_download_csr(self.handle, _ptr(rp), _ptr(ci), _ptr(val)), "te_matrix_download_csr")
+        return rp, ci[:inf["nnz"]], val[:inf["nnz"]]
+
+    def to_coo(self):
+        """(row, col, values) COO triple of the matrix, on the host."""
+        rp, ci, val = self.to_csr()
+        row = np.repeat(np.arange(len(rp) - 1, dtype=np.int64), np.diff(rp))
+        return row, ci.astype(np.int64), val
 
     def info(self):
         nr, nc, nnz, fl, n1 = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int(), ctypes.c_double()
@@ -447,10 +498,10 @@ def evolve(H_coo, v, t, sampling_step, observables=(), exp_factor=1.0, tol=1e-6,
            trace=False, reorth=False):
     """One-call evolution with COO inputs, mirroring the oracle's signature.
 
-    ``observables``: ("sparse", (row, col, val)), ("vector", o) or
-    ("callback", fn)."""
+    ``H_coo`` may also be a Matrix already on the device.  ``observables``:
+    ("sparse", (row, col, val)), ("vector", o) or ("callback", fn)."""
     n = len(v)
-    H = Matrix.from_coo(n, H_coo)
+    H = H_coo if isinstance(H_coo, Matrix) else Matrix.from_coo(n, H_coo)
     obs = []
     for kind, data in observables:
         if kind == "sparse":

@@ -12,6 +12,7 @@
 //   TeDevState: the scalar state of the evolution (coefficients, step
 //     control, sampling cursor, reduction counters), written only by kernels.
 #pragma once
+#include <vector>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -115,6 +116,11 @@ struct te_matrix_s {
   TeSell sell;                // square matrices only
   int device = 0;
 };
+
+// Adopt a device CSR (int32 row pointers, columns, complex values; the matrix
+// frees them) -- the device-side build of te_matrix_create_csr_device.
+int te_matrix_adopt_device_csr(int64_t n_rows, int64_t n_cols, const std::vector<int32_t>& rp_host, int32_t* d_rp,
+                               int32_t* d_ci, double2* d_v, te_matrix* out);
 
 // error reporting
 void te_set_error(const char* fmt, ...);

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <cstring>
 #include <mutex>
 #include <numeric>
 #include <vector>
@@ -82,6 +83,115 @@ void te_launch_permute(int64_t n, const int32_t* idx, const double2* in, double2
   permute_kernel<<<te_grid_fit((const void*)permute_kernel, n, TE_THREADS), TE_THREADS, 0, st>>>(n, idx, in, out);
 }
 
+// ------------------------------------------------- device build (kernels)
+
+enum { TE_CSR_BAD_COL = 1, TE_CSR_COMPLEX = 2, TE_CSR_OFFDIAG = 4 };
+
+// One thread per row: column range, any imaginary part, any off-diagonal
+// entry (flag bits above) and the largest |value| (bit pattern of a
+// non-negative double, so the maximum does not depend on the order).
+__global__ void csr_scan_kernel(int64_t n_rows, int64_t n_cols, const int32_t* __restrict__ rp,
+                                const int32_t* __restrict__ ci, const double2* __restrict__ v, unsigned int* flags,
+                                unsigned long long* vmax_bits) {
+  unsigned int f = 0;
+  double vmax = 0.0;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_rows; r += (int64_t)gridDim.x * blockDim.x) {
+    for (int32_t p = rp[r]; p < rp[r + 1]; ++p) {
+      const int32_t c = ci[p];
+      const double2 x = v[p];
+      if (c < 0 || c >= n_cols) f |= TE_CSR_BAD_COL;
+      if (x.y != 0.0) f |= TE_CSR_COMPLEX;
+      if (c != r) f |= TE_CSR_OFFDIAG;
+      vmax = fmax(vmax, hypot(x.x, x.y));
+    }
+  }
+  if (f) atomicOr(flags, f);
+  atomicMax(vmax_bits, (unsigned long long)__double_as_longlong(vmax));
+}
+
+// Column sums of |value| in 64-bit fixed point (scale 2^e): integer additions
+// commute, so the sums do not depend on the order of the atomics.
+__global__ void colsum_fixed_kernel(int64_t n_rows, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                    const double2* __restrict__ v, double scale, unsigned long long* colsum) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_rows; r += (int64_t)gridDim.x * blockDim.x)
+    for (int32_t p = rp[r]; p < rp[r + 1]; ++p) {
+      const double2 x = v[p];
+      atomicAdd(&colsum[ci[p]], (unsigned long long)(hypot(x.x, x.y) * scale));
+    }
+}
+
+__global__ void max_u64_kernel(int64_t n, const unsigned long long* __restrict__ a, unsigned long long* out) {
+  unsigned long long m = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    m = max(m, a[i]);
+  atomicMax(out, m);
+}
+
+__global__ void real_part_kernel(int64_t n, const double2* __restrict__ v, double* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = v[i].x;
+}
+
+__global__ void widen_real_kernel(int64_t n, const double* __restrict__ v, double2* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = make_double2(v[i], 0.0);
+}
+
+// Diagonal of a diagonal matrix (entries of a row summed in order).
+__global__ void diag_sum_kernel(int64_t n, const int32_t* __restrict__ rp, const double2* __restrict__ v,
+                                double* __restrict__ dre, double2* __restrict__ dc) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    double2 acc = make_double2(0.0, 0.0);
+    for (int32_t p = rp[r]; p < rp[r + 1]; ++p) {
+      acc.x += v[p].x;
+      acc.y += v[p].y;
+    }
+    dre[r] = acc.x;
+    dc[r] = acc;
+  }
+}
+
+// SELL-32 slots from the CSR: one thread per (chunk, lane), i.e. per sorted
+// row index; padding slots point at the row itself with value 0.
+template <bool REAL>
+__global__ void fill_sell_kernel(int64_t n, int64_t n_chunks, const int64_t* __restrict__ off,
+                                 const int32_t* __restrict__ perm, const int32_t* __restrict__ iperm,
+                                 const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                 const double2* __restrict__ v, int32_t* __restrict__ scol, double* __restrict__ sval) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n_chunks * 32;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = t >> 5;
+    const int lane = (int)(t & 31);
+    const int64_t len = (off[c + 1] - off[c]) / 32;
+    int64_t p0 = 0, rlen = 0;
+    if (t < n) {
+      const int32_t r = perm[t];
+      p0 = rp[r];
+      rlen = rp[r + 1] - p0;
+    }
+    const int32_t pad = (int32_t)min(t, n - 1);
+    for (int64_t k = 0; k < len; ++k) {
+      const int64_t sidx = off[c] + 32 * k + lane;
+      if (k < rlen) {
+        const double2 x = v[p0 + k];
+        scol[sidx] = iperm[ci[p0 + k]];
+        if (REAL) {
+          sval[sidx] = x.x;
+        } else {
+          reinterpret_cast<double2*>(sval)[sidx] = x;
+        }
+      } else {
+        scol[sidx] = pad;
+        if (REAL) {
+          sval[sidx] = 0.0;
+        } else {
+          reinterpret_cast<double2*>(sval)[sidx] = make_double2(0.0, 0.0);
+        }
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------------ host build
 
 namespace {
@@ -106,6 +216,59 @@ int upload(T** dst, const T* src, size_t count) {
   TE_CUDA(cudaMalloc(dst, sizeof(T) * std::max<size_t>(count, 1)));
   if (count) TE_CUDA(cudaMemcpy(*dst, src, sizeof(T) * count, cudaMemcpyHostToDevice));
   return TE_OK;
+}
+
+// SELL-32 layout of a square matrix from its row pointers (host): rows sorted
+// by length (descending, stable), chunk offsets in slots, and the static warp
+// schedule of the SpMV passes (equal FP64 work per warp: te_sell_row issues 2
+// (real) or 4 (complex) FMAs per slot, the SpMV epilogues about 8 per row).
+// Uploads chunk_off, perm, iperm and warp_chunk; returns perm, iperm and the
+// offsets for filling col/val.
+int sell_layout(te_matrix_s* M, const std::vector<int32_t>& rp, bool real, std::vector<int32_t>& perm,
+                std::vector<int32_t>& iperm, std::vector<int64_t>& off) {
+  const int64_t n = M->n_rows;
+  TeSell& S = M->sell;
+  S.n = n;
+  S.n_chunks = (n + 31) / 32;
+  // stable counting sort by length, longest first
+  int32_t max_len = 0;
+  for (int64_t r = 0; r < n; ++r) max_len = std::max(max_len, rp[r + 1] - rp[r]);
+  std::vector<int64_t> start(max_len + 2, 0);
+  for (int64_t r = 0; r < n; ++r) start[max_len - (rp[r + 1] - rp[r]) + 1]++;
+  for (int32_t b = 0; b <= max_len; ++b) start[b + 1] += start[b];
+  perm.assign(n, 0);
+  iperm.assign(n, 0);
+  for (int64_t r = 0; r < n; ++r) perm[start[max_len - (rp[r + 1] - rp[r])]++] = (int32_t)r;
+  for (int64_t i = 0; i < n; ++i) iperm[perm[i]] = (int32_t)i;
+  off.assign(S.n_chunks + 1, 0);
+  for (int64_t c = 0; c < S.n_chunks; ++c) {
+    int32_t r0 = perm[c * 32];
+    int64_t len = rp[r0 + 1] - rp[r0];  // longest row of the chunk comes first
+    off[c + 1] = off[c] + 32 * len;
+  }
+  S.slots = off[S.n_chunks];
+  int rc;
+  if ((rc = upload(&S.chunk_off, off.data(), off.size())) != TE_OK) return rc;
+  if ((rc = upload(&S.perm, perm.data(), perm.size())) != TE_OK) return rc;
+  if ((rc = upload(&S.iperm, iperm.data(), iperm.size())) != TE_OK) return rc;
+  const int bps = std::min(te_sell_blocks_per_sm(real),
+                           te_kernel_blocks_per_sm(real ? (const void*)sell_spmv_kernel<true>
+                                                        : (const void*)sell_spmv_kernel<false>,
+                                                   TE_THREADS, 0));
+  S.grid = (int)std::min<int64_t>((S.n_chunks * 32 + TE_THREADS - 1) / TE_THREADS, (int64_t)te_num_sms() * bps);
+  const int64_t W = (int64_t)S.grid * (TE_THREADS / 32);
+  const double w_slot = real ? 2.0 : 4.0, w_chunk = 8.0 * 32;
+  auto cost = [&](int64_t c) { return w_slot * (double)off[c] + w_chunk * (double)c; };
+  const double total = cost(S.n_chunks);
+  std::vector<int32_t> wc(W + 1);
+  int64_t c = 0;
+  for (int64_t w = 0; w < W; ++w) {
+    const double target = total * (double)w / (double)W;
+    while (c < S.n_chunks && cost(c) < target) ++c;
+    wc[w] = (int32_t)c;
+  }
+  wc[W] = (int32_t)S.n_chunks;
+  return upload(&S.warp_chunk, wc.data(), wc.size());
 }
 
 // rp/ci/vv: original-order CSR with interleaved complex values.
@@ -150,22 +313,10 @@ int build_matrix(te_matrix_s* M, const std::vector<int32_t>& rp, const std::vect
   }
   if (M->n_rows != M->n_cols) return TE_OK;
 
-  // SELL-32 with rows sorted by length (descending, stable)
+  std::vector<int32_t> perm, iperm;
+  std::vector<int64_t> off;
+  if ((rc = sell_layout(M, rp, real, perm, iperm, off)) != TE_OK) return rc;
   TeSell& S = M->sell;
-  S.n = n;
-  S.n_chunks = (n + 31) / 32;
-  std::vector<int32_t> perm(n), iperm(n);
-  std::iota(perm.begin(), perm.end(), 0);
-  std::stable_sort(perm.begin(), perm.end(),
-                   [&](int32_t a, int32_t b) { return (rp[a + 1] - rp[a]) > (rp[b + 1] - rp[b]); });
-  for (int64_t i = 0; i < n; ++i) iperm[perm[i]] = (int32_t)i;
-  std::vector<int64_t> off(S.n_chunks + 1, 0);
-  for (int64_t c = 0; c < S.n_chunks; ++c) {
-    int32_t r0 = perm[c * 32];
-    int64_t len = rp[r0 + 1] - rp[r0];  // longest row of the chunk comes first
-    off[c + 1] = off[c] + 32 * len;
-  }
-  S.slots = off[S.n_chunks];
   std::vector<int32_t> scol(S.slots);
   std::vector<double> sval((real ? 1 : 2) * S.slots, 0.0);
   for (int64_t c = 0; c < S.n_chunks; ++c) {
@@ -195,31 +346,8 @@ int build_matrix(te_matrix_s* M, const std::vector<int32_t>& rp, const std::vect
       }
     }
   }
-  if ((rc = upload(&S.chunk_off, off.data(), off.size())) != TE_OK) return rc;
   if ((rc = upload(&S.col, scol.data(), scol.size())) != TE_OK) return rc;
   if ((rc = upload(&S.val, sval.data(), sval.size())) != TE_OK) return rc;
-  if ((rc = upload(&S.perm, perm.data(), perm.size())) != TE_OK) return rc;
-  if ((rc = upload(&S.iperm, iperm.data(), iperm.size())) != TE_OK) return rc;
-  // static warp schedule: equal FP64 work per warp (te_sell_row issues 2 (real)
-  // or 4 (complex) FMAs per slot; the SpMV epilogues about 8 per row)
-  const int bps = std::min(te_sell_blocks_per_sm(real),
-                           te_kernel_blocks_per_sm(real ? (const void*)sell_spmv_kernel<true>
-                                                        : (const void*)sell_spmv_kernel<false>,
-                                                   TE_THREADS, 0));
-  S.grid = (int)std::min<int64_t>((S.n_chunks * 32 + TE_THREADS - 1) / TE_THREADS, (int64_t)te_num_sms() * bps);
-  const int64_t W = (int64_t)S.grid * (TE_THREADS / 32);
-  const double w_slot = real ? 2.0 : 4.0, w_chunk = 8.0 * 32;
-  auto cost = [&](int64_t c) { return w_slot * (double)off[c] + w_chunk * (double)c; };
-  const double total = cost(S.n_chunks);
-  std::vector<int32_t> wc(W + 1);
-  int64_t c = 0;
-  for (int64_t w = 0; w < W; ++w) {
-    const double target = total * (double)w / (double)W;
-    while (c < S.n_chunks && cost(c) < target) ++c;
-    wc[w] = (int32_t)c;
-  }
-  wc[W] = (int32_t)S.n_chunks;
-  if ((rc = upload(&S.warp_chunk, wc.data(), wc.size())) != TE_OK) return rc;
   return TE_OK;
 }
 
@@ -239,7 +367,131 @@ int finish_create(int64_t n_rows, int64_t n_cols, const std::vector<int32_t>& rp
   return TE_OK;
 }
 
+// Device build: the CSR (int32 row pointers, columns, complex values) is
+// already on the device and becomes the matrix's own (the caller's buffers
+// are adopted: M frees them).  rp_host is a host copy of the row pointers.
+// The 1-norm is the maximum column sum of |a| accumulated in 64-bit fixed
+// point (relative resolution ~1e-12 of the largest entry), so it does not
+// depend on the order of the device atomics.
+int build_matrix_device(te_matrix_s* M, const std::vector<int32_t>& rp_host, int32_t* d_rp, int32_t* d_ci,
+                        double2* d_v) {
+  const int64_t n = M->n_rows, nnz = M->nnz;
+  M->row_ptr = d_rp;
+  M->col = d_ci;
+  unsigned int* d_flags = nullptr;
+  unsigned long long *d_u64 = nullptr, *d_colsum = nullptr;
+  auto cleanup = [&]() {
+    cudaFree(d_flags);
+    cudaFree(d_u64);
+    cudaFree(d_colsum);
+  };
+  auto fail = [&](int rc) {
+    cudaFree(d_v);
+    cleanup();
+    return rc;
+  };
+  if (te_cuda_check(cudaMalloc(&d_flags, sizeof(unsigned int)), "flags") != TE_OK) return fail(TE_ERR_CUDA);
+  if (te_cuda_check(cudaMalloc(&d_u64, 2 * sizeof(unsigned long long)), "flags") != TE_OK) return fail(TE_ERR_CUDA);
+  cudaMemset(d_flags, 0, sizeof(unsigned int));
+  cudaMemset(d_u64, 0, 2 * sizeof(unsigned long long));
+  const int gr = te_grid_fit((const void*)csr_scan_kernel, n, TE_THREADS);
+  csr_scan_kernel<<<gr, TE_THREADS>>>(n, M->n_cols, d_rp, d_ci, d_v, d_flags, d_u64);
+  unsigned int flags = 0;
+  unsigned long long vmax_bits = 0;
+  if (te_cuda_check(cudaMemcpy(&flags, d_flags, sizeof(flags), cudaMemcpyDeviceToHost), "flags") != TE_OK ||
+      te_cuda_check(cudaMemcpy(&vmax_bits, d_u64, sizeof(vmax_bits), cudaMemcpyDeviceToHost), "flags") != TE_OK)
+    return fail(TE_ERR_CUDA);
+  if (flags & TE_CSR_BAD_COL) {
+    te_set_error("te_matrix_create_csr_device: a column index is out of range");
+    return fail(TE_ERR_INVALID_ARG);
+  }
+  const bool real = !(flags & TE_CSR_COMPLEX);
+  const bool diag = (M->n_rows == M->n_cols) && !(flags & TE_CSR_OFFDIAG);
+  M->is_real = real;
+  M->is_diag = diag;
+  // 1-norm
+  double vmax;
+  std::memcpy(&vmax, &vmax_bits, sizeof(vmax));
+  M->norm1 = 0.0;
+  if (vmax > 0.0 && nnz > 0) {
+    const int e = 62 - (int)std::ceil(std::log2(vmax * (double)std::max<int64_t>(n, 1)));
+    const double scale = std::ldexp(1.0, e);
+    if (te_cuda_check(cudaMalloc(&d_colsum, sizeof(unsigned long long) * M->n_cols), "colsum") != TE_OK)
+      return fail(TE_ERR_CUDA);
+    cudaMemset(d_colsum, 0, sizeof(unsigned long long) * M->n_cols);
+    colsum_fixed_kernel<<<gr, TE_THREADS>>>(n, d_rp, d_ci, d_v, scale, d_colsum);
+    max_u64_kernel<<<te_grid_fit((const void*)max_u64_kernel, M->n_cols, TE_THREADS), TE_THREADS>>>(
+        M->n_cols, d_colsum, d_u64 + 1);
+    unsigned long long mx = 0;
+    if (te_cuda_check(cudaMemcpy(&mx, d_u64 + 1, sizeof(mx), cudaMemcpyDeviceToHost), "norm1") != TE_OK)
+      return fail(TE_ERR_CUDA);
+    M->norm1 = std::ldexp((double)mx, -e);
+  }
+  // values: real matrices keep the real parts
+  if (real) {
+    double* vr = nullptr;
+    if (te_cuda_check(cudaMalloc(&vr, sizeof(double) * std::max<int64_t>(nnz, 1)), "values") != TE_OK)
+      return fail(TE_ERR_CUDA);
+    real_part_kernel<<<te_grid_fit((const void*)real_part_kernel, nnz, TE_THREADS), TE_THREADS>>>(nnz, d_v, vr);
+    M->val = vr;
+  } else {
+    M->val = reinterpret_cast<double*>(d_v);
+  }
+  if (diag) {
+    if (te_cuda_check(cudaMalloc(&M->diag_re, sizeof(double) * n), "diag") != TE_OK ||
+        te_cuda_check(cudaMalloc(&M->diag_c, sizeof(double2) * n), "diag") != TE_OK) {
+      if (real) cudaFree(d_v);
+      cleanup();
+      return TE_ERR_CUDA;
+    }
+    diag_sum_kernel<<<te_grid_fit((const void*)diag_sum_kernel, n, TE_THREADS), TE_THREADS>>>(n, d_rp, d_v,
+                                                                                             M->diag_re, M->diag_c);
+  }
+  int rc = TE_OK;
+  if (M->n_rows == M->n_cols) {
+    std::vector<int32_t> perm, iperm;
+    std::vector<int64_t> off;
+    rc = sell_layout(M, rp_host, real, perm, iperm, off);
+    TeSell& S = M->sell;
+    if (rc == TE_OK) rc = te_cuda_check(cudaMalloc(&S.col, sizeof(int32_t) * std::max<int64_t>(S.slots, 1)), "sell");
+    if (rc == TE_OK)
+      rc = te_cuda_check(cudaMalloc(&S.val, sizeof(double) * (real ? 1 : 2) * std::max<int64_t>(S.slots, 1)), "sell");
+    if (rc == TE_OK) {
+      const int gf = te_grid_fit(real ? (const void*)fill_sell_kernel<true> : (const void*)fill_sell_kernel<false>,
+                                 S.n_chunks * 32, TE_THREADS);
+      if (real)
+        fill_sell_kernel<true><<<gf, TE_THREADS>>>(n, S.n_chunks, S.chunk_off, S.perm, S.iperm, d_rp, d_ci, d_v, S.col,
+                                                   S.val);
+      else
+        fill_sell_kernel<false><<<gf, TE_THREADS>>>(n, S.n_chunks, S.chunk_off, S.perm, S.iperm, d_rp, d_ci, d_v,
+                                                    S.col, S.val);
+    }
+  }
+  if (rc == TE_OK) rc = te_cuda_check(cudaDeviceSynchronize(), "device build");
+  if (real) cudaFree(d_v);
+  cleanup();
+  return rc;
+}
+
 }  // namespace
+
+// Adopt a device CSR (see build_matrix_device); used by the device-side
+// workload generators.  On failure the buffers are freed.
+int te_matrix_adopt_device_csr(int64_t n_rows, int64_t n_cols, const std::vector<int32_t>& rp_host, int32_t* d_rp,
+                               int32_t* d_ci, double2* d_v, te_matrix* out) {
+  te_matrix_s* M = new te_matrix_s();
+  cudaGetDevice(&M->device);
+  M->n_rows = n_rows;
+  M->n_cols = n_cols;
+  M->nnz = rp_host[n_rows];
+  int rc = build_matrix_device(M, rp_host, d_rp, d_ci, d_v);
+  if (rc != TE_OK) {
+    free_matrix(M);
+    return rc;
+  }
+  *out = M;
+  return TE_OK;
+}
 
 // ------------------------------------------------------------------ C ABI
 
@@ -308,6 +560,80 @@ extern "C" int te_matrix_create_csr(int64_t n_rows, int64_t n_cols, int64_t nnz,
     vv[2 * i + 1] = values_complex ? values[2 * i + 1] : 0.0;
   }
   return finish_create(n_rows, n_cols, rp, ci, vv, out);
+}
+
+extern "C" int te_matrix_create_csr_device(int64_t n_rows, int64_t n_cols, int64_t nnz, const int32_t* row_ptr_dev,
+                                           const int32_t* col_dev, const double* values_dev, int values_complex,
+                                           te_matrix* out) {
+  if (!out || n_rows <= 0 || n_cols <= 0 || nnz < 0 || !row_ptr_dev || (nnz > 0 && (!col_dev || !values_dev))) {
+    te_set_error("te_matrix_create_csr_device: invalid arguments");
+    return n_rows == 0 || n_cols == 0 ? TE_ERR_EMPTY : TE_ERR_INVALID_ARG;
+  }
+  if (nnz >= ((int64_t)1 << 31) || n_rows >= ((int64_t)1 << 31) || n_cols >= ((int64_t)1 << 31)) {
+    te_set_error("te_matrix_create_csr_device: sizes must stay below 2^31 (int32 indices)");
+    return TE_ERR_UNSUPPORTED;
+  }
+  std::vector<int32_t> rp(n_rows + 1);
+  TE_CUDA(cudaMemcpy(rp.data(), row_ptr_dev, sizeof(int32_t) * (n_rows + 1), cudaMemcpyDeviceToHost));
+  if (rp[0] != 0 || rp[n_rows] != nnz) {
+    te_set_error("te_matrix_create_csr_device: row_ptr must start at 0 and end at nnz");
+    return TE_ERR_INVALID_ARG;
+  }
+  for (int64_t r = 0; r < n_rows; ++r)
+    if (rp[r + 1] < rp[r]) {
+      te_set_error("te_matrix_create_csr_device: row_ptr decreases at row %lld", (long long)(r + 1));
+      return TE_ERR_INVALID_ARG;
+    }
+  // private copies (the matrix owns its arrays)
+  int32_t *d_rp = nullptr, *d_ci = nullptr;
+  double2* d_v = nullptr;
+  auto fail = [&](int rc) {
+    cudaFree(d_rp);
+    cudaFree(d_ci);
+    cudaFree(d_v);
+    return rc;
+  };
+  if (te_cuda_check(cudaMalloc(&d_rp, sizeof(int32_t) * (n_rows + 1)), "csr") != TE_OK ||
+      te_cuda_check(cudaMalloc(&d_ci, sizeof(int32_t) * std::max<int64_t>(nnz, 1)), "csr") != TE_OK ||
+      te_cuda_check(cudaMalloc(&d_v, sizeof(double2) * std::max<int64_t>(nnz, 1)), "csr") != TE_OK)
+    return fail(TE_ERR_CUDA);
+  if (te_cuda_check(cudaMemcpy(d_rp, row_ptr_dev, sizeof(int32_t) * (n_rows + 1), cudaMemcpyDeviceToDevice), "csr") !=
+      TE_OK)
+    return fail(TE_ERR_CUDA);
+  if (nnz > 0) {
+    if (te_cuda_check(cudaMemcpy(d_ci, col_dev, sizeof(int32_t) * nnz, cudaMemcpyDeviceToDevice), "csr") != TE_OK)
+      return fail(TE_ERR_CUDA);
+    if (values_complex) {
+      if (te_cuda_check(cudaMemcpy(d_v, values_dev, sizeof(double2) * nnz, cudaMemcpyDeviceToDevice), "csr") != TE_OK)
+        return fail(TE_ERR_CUDA);
+    } else {
+      widen_real_kernel<<<te_grid_fit((const void*)widen_real_kernel, nnz, TE_THREADS), TE_THREADS>>>(nnz, values_dev,
+                                                                                                    d_v);
+    }
+  }
+  return te_matrix_adopt_device_csr(n_rows, n_cols, rp, d_rp, d_ci, d_v, out);
+}
+
+extern "C" int te_matrix_download_csr(te_matrix A, int32_t* row_ptr, int32_t* col_idx, double* values) {
+  if (!A || !row_ptr || (A->nnz > 0 && (!col_idx || !values))) {
+    te_set_error("te_matrix_download_csr: invalid arguments");
+    return TE_ERR_INVALID_ARG;
+  }
+  const int64_t nnz = A->nnz;
+  TE_CUDA(cudaMemcpy(row_ptr, A->row_ptr, sizeof(int32_t) * (A->n_rows + 1), cudaMemcpyDeviceToHost));
+  if (nnz == 0) return TE_OK;
+  TE_CUDA(cudaMemcpy(col_idx, A->col, sizeof(int32_t) * nnz, cudaMemcpyDeviceToHost));
+  if (A->is_real) {
+    std::vector<double> re(nnz);
+    TE_CUDA(cudaMemcpy(re.data(), A->val, sizeof(double) * nnz, cudaMemcpyDeviceToHost));
+    for (int64_t p = 0; p < nnz; ++p) {
+      values[2 * p] = re[p];
+      values[2 * p + 1] = 0.0;
+    }
+  } else {
+    TE_CUDA(cudaMemcpy(values, A->val, sizeof(double2) * nnz, cudaMemcpyDeviceToHost));
+  }
+  return TE_OK;
 }
 
 extern "C" int te_matrix_destroy(te_matrix A) {

@@ -321,17 +321,19 @@ int run(te_evolver ev, te_result* out) {
     t_prev = S->t_now;
     err_prev = S->err;
     // STEP 1: Lanczos (:338)
+    const bool cgs2 = ev->p.reorth != 0;
+    const bool fold = !cgs2 && ev->p.exp_factor != 0.0;
     for (int j = 0; j < m; ++j) {
-      const bool cgs2 = ev->p.reorth != 0;
       {
         ProfScope ps(ev, 0);
         te_launch_lanczos_apply(ev->H->sell, ev->H->is_real, ev->cols[j],
-                                (j > 0 && !cgs2) ? ev->cols[j - 1] : nullptr, ev->w, ev->ds, ev->partials, j, st);
+                                (j > 0 && !cgs2) ? ev->cols[j - 1] : nullptr, ev->w, ev->ds, ev->partials, j, fold,
+                                st);
       }
       if (!cgs2) {
         ProfScope ps(ev, 1);
         te_launch_lanczos_update(n, ev->w, ev->cols[j], j + 1 < m ? ev->cols[j + 1] : nullptr, ev->ds, ev->partials,
-                                 j, st);
+                                 j, fold, st);
         ev->launches += 2;
       } else {
         // classical Gram-Schmidt against u_0..u_j, then one reorthogonalisation pass

@@ -122,6 +122,28 @@ struct te_matrix_s {
 int te_matrix_adopt_device_csr(int64_t n_rows, int64_t n_cols, const std::vector<int32_t>& rp_host, int32_t* d_rp,
                                int32_t* d_ci, double2* d_v, te_matrix* out);
 
+// Programmatic dependent launch: a kernel launched with te_launch_pdl may be
+// scheduled while its predecessor in the stream is still finishing (hiding the
+// launch and block ramp); it must call te_pdl_wait() before touching anything
+// the predecessor writes.  Both are no-ops for a kernel launched normally.
+__device__ __forceinline__ void te_pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void te_pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+cudaError_t te_launch_pdl(void (*kernel)(KArgs...), int grid, int block, cudaStream_t st, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // error reporting
 void te_set_error(const char* fmt, ...);
 int te_cuda_check(cudaError_t e, const char* what);
@@ -153,10 +175,12 @@ void te_launch_sell_spmv(const TeSell& A, bool is_real, double2 alpha, const dou
 void te_launch_csr_spmv(const te_matrix_s& A, double2 alpha, const double2* x, double2* y, cudaStream_t st);
 void te_launch_permute(int64_t n, const int32_t* idx, const double2* in, double2* out, cudaStream_t st);
 // te_lanczos.cu
+// fold: store w / (expFactor s_j) instead of w (three-term mode with a
+// non-zero expFactor; the update kernel then takes the factor into s_{j+1}).
 void te_launch_lanczos_apply(const TeSell& A, bool is_real, const double2* u_j, const double2* u_jm1, double2* w,
-                             TeDevState* ds, double* partials, int j, cudaStream_t st);
+                             TeDevState* ds, double* partials, int j, bool fold, cudaStream_t st);
 void te_launch_lanczos_update(int64_t n, const double2* w, const double2* u_j, double2* u_jp1, TeDevState* ds,
-                              double* partials, int j, cudaStream_t st);
+                              double* partials, int j, bool fold, cudaStream_t st);
 // Gram-Schmidt passes of the reorthogonalising Lanczos mode (te_lanczos.cu)
 #define TE_GS_ROWS 2048  // rows per block of the Gram-Schmidt passes
 struct TeBasisPtrs {

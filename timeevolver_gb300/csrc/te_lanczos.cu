@@ -25,17 +25,25 @@ __device__ __forceinline__ bool te_step_inactive(const TeDevState* ds) {
 
 // 6 (real H: at most 40 registers) or 5 (complex H) resident blocks of 256;
 // the static chunk schedule of the matrix assumes the whole grid is resident.
-template <bool REAL, bool HAS_PREV>
+//
+// FOLD (three-term mode, expFactor != 0): with g = expFactor s_j the kernel
+// stores w' = w / g = -i H u_j + (beta_j s_{j-1} / g) u_{j-1}, which saves the
+// two multiplications by g per row (FP64 issue is the bound); alpha_j is
+// still the reference's <v_j, w> = s_j g <u_j, w'>.
+template <bool REAL, bool HAS_PREV, bool FOLD>
 __global__ void __launch_bounds__(TE_THREADS, REAL ? 6 : 5) lanczos_apply_kernel(
     int64_t n, const int32_t* __restrict__ warp_chunk, const int64_t* __restrict__ chunk_off, const int32_t* __restrict__ col,
     const double* __restrict__ val, const double2* __restrict__ u_j, const double2* __restrict__ u_jm1,
     double2* __restrict__ w, TeDevState* ds, double* partials, int j) {
   __shared__ double scratch[2 * 32];
+  te_pdl_trigger();
+  te_pdl_wait();
   if (te_step_inactive(ds)) return;
   const int lane = threadIdx.x & 31;
   const double sj = ds->s[j];
   const double g = ds->exp_factor * sj;  // A v_j = -i g H u_j
   const double cprev = HAS_PREV ? ds->beta[j] * ds->s[j - 1] : 0.0;
+  const double cw = FOLD ? cprev / g : cprev;
   double acc[2] = {0.0, 0.0};
   const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int64_t c_end = warp_chunk[wid + 1];
@@ -44,10 +52,19 @@ __global__ void __launch_bounds__(TE_THREADS, REAL ? 6 : 5) lanczos_apply_kernel
     const int64_t r = c * 32 + lane;
     if (r < n) {
       double2 wr;
-      if (HAS_PREV) {
+      if (FOLD) {
+        if (HAS_PREV) {
+          double2 up = u_jm1[r];
+          wr.x = fma(cw, up.x, y.y);
+          wr.y = fma(cw, up.y, -y.x);
+        } else {
+          wr.x = y.y;
+          wr.y = -y.x;
+        }
+      } else if (HAS_PREV) {
         double2 up = u_jm1[r];
-        wr.x = fma(cprev, up.x, g * y.y);
-        wr.y = fma(cprev, up.y, -g * y.x);
+        wr.x = fma(cw, up.x, g * y.y);
+        wr.y = fma(cw, up.y, -g * y.x);
       } else {
         wr.x = g * y.y;
         wr.y = -g * y.x;
@@ -63,20 +80,28 @@ __global__ void __launch_bounds__(TE_THREADS, REAL ? 6 : 5) lanczos_apply_kernel
   if (te_publish_partials<2>(acc, partials, &ds->counter[0])) {
     double tot[2];
     te_final_sum<2>(tot, partials, &ds->counter[0], scratch);
-    if (threadIdx.x == 0) ds->alpha[j] = make_double2(sj * tot[0], sj * tot[1]);
+    const double f = FOLD ? sj * g : sj;
+    if (threadIdx.x == 0) ds->alpha[j] = make_double2(f * tot[0], f * tot[1]);
   }
 }
 
+// u_{j+1} = w - alpha_j v_j and beta_{j+1} = ||u_{j+1}||.  With a folded w'
+// (fold != 0) the kernel forms u'_{j+1} = w' - (alpha_j s_j / g) u_j = u_{j+1} / g
+// and keeps the factor in the scale: beta_{j+1} = |g| ||u'||, s_{j+1} = g / beta_{j+1}.
 template <bool STORE>
 __global__ void __launch_bounds__(TE_THREADS) lanczos_update_kernel(int64_t n, const double2* __restrict__ w,
                                                                     const double2* __restrict__ u_j,
                                                                     double2* __restrict__ u_jp1, TeDevState* ds,
-                                                                    double* partials, int j) {
+                                                                    double* partials, int j, int fold) {
   __shared__ double scratch[32];
+  te_pdl_trigger();
+  te_pdl_wait();
   if (te_step_inactive(ds)) return;
   const double sj = ds->s[j];
+  const double g = fold ? ds->exp_factor * sj : 1.0;
   const double2 a = ds->alpha[j];
-  const double gr = a.x * sj, gi = a.y * sj;  // gamma = alpha_j s_j
+  const double q = fold ? sj / g : sj;
+  const double gr = a.x * q, gi = a.y * q;  // gamma = alpha_j s_j (/ g)
   double acc[1] = {0.0};
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
     double2 wv = w[r];
@@ -92,7 +117,7 @@ __global__ void __launch_bounds__(TE_THREADS) lanczos_update_kernel(int64_t n, c
     double tot[1];
     te_final_sum<1>(tot, partials, &ds->counter[1], scratch);
     if (threadIdx.x == 0) {
-      const double beta = sqrt(tot[0]);
+      const double beta = fabs(g) * sqrt(tot[0]);
       const int m = ds->m_cur;
       if (beta < ds->tol_rate) {  // lucky breakdown (:551-555)
         ds->breakdown = 1;
@@ -100,7 +125,7 @@ __global__ void __launch_bounds__(TE_THREADS) lanczos_update_kernel(int64_t n, c
         ds->h = beta;
       } else if (j + 1 != m) {
         ds->beta[j + 1] = beta;
-        ds->s[j + 1] = 1.0 / beta;
+        ds->s[j + 1] = g / beta;
       } else {
         ds->h = beta;
         ds->m_eff = m;
@@ -299,24 +324,34 @@ void te_launch_gs_update_norm(int64_t n, const TeBasisPtrs& V, int nvec, const d
 }
 
 int te_sell_blocks_per_sm(bool is_real) {
-  const void* k[2] = {is_real ? (const void*)lanczos_apply_kernel<true, true> : (const void*)lanczos_apply_kernel<false, true>,
-                      is_real ? (const void*)lanczos_apply_kernel<true, false>
-                              : (const void*)lanczos_apply_kernel<false, false>};
-  return std::min(te_kernel_blocks_per_sm(k[0], TE_THREADS, 0), te_kernel_blocks_per_sm(k[1], TE_THREADS, 0));
+  const void* k[4] = {
+      is_real ? (const void*)lanczos_apply_kernel<true, true, true> : (const void*)lanczos_apply_kernel<false, true, true>,
+      is_real ? (const void*)lanczos_apply_kernel<true, false, true> : (const void*)lanczos_apply_kernel<false, false, true>,
+      is_real ? (const void*)lanczos_apply_kernel<true, true, false> : (const void*)lanczos_apply_kernel<false, true, false>,
+      is_real ? (const void*)lanczos_apply_kernel<true, false, false>
+              : (const void*)lanczos_apply_kernel<false, false, false>};
+  int b = 8;
+  for (const void* f : k) b = std::min(b, te_kernel_blocks_per_sm(f, TE_THREADS, 0));
+  return b;
 }
 
 void te_launch_lanczos_apply(const TeSell& A, bool is_real, const double2* u_j, const double2* u_jm1, double2* w,
-                             TeDevState* ds, double* partials, int j, cudaStream_t st) {
-  auto k = is_real ? (u_jm1 ? lanczos_apply_kernel<true, true> : lanczos_apply_kernel<true, false>)
-                   : (u_jm1 ? lanczos_apply_kernel<false, true> : lanczos_apply_kernel<false, false>);
-  k<<<A.grid, TE_THREADS, 0, st>>>(A.n, A.warp_chunk, A.chunk_off, A.col, A.val, u_j, u_jm1, w, ds, partials, j);
+                             TeDevState* ds, double* partials, int j, bool fold, cudaStream_t st) {
+  using K = void (*)(int64_t, const int32_t*, const int64_t*, const int32_t*, const double*, const double2*,
+                     const double2*, double2*, TeDevState*, double*, int);
+  static const K table[2][2][2] = {
+      {{lanczos_apply_kernel<false, false, false>, lanczos_apply_kernel<false, false, true>},
+       {lanczos_apply_kernel<false, true, false>, lanczos_apply_kernel<false, true, true>}},
+      {{lanczos_apply_kernel<true, false, false>, lanczos_apply_kernel<true, false, true>},
+       {lanczos_apply_kernel<true, true, false>, lanczos_apply_kernel<true, true, true>}}};
+  const K k = table[is_real ? 1 : 0][u_jm1 ? 1 : 0][fold ? 1 : 0];
+  te_launch_pdl(k, A.grid, TE_THREADS, st, A.n, A.warp_chunk, A.chunk_off, A.col, A.val, u_j, u_jm1, w, ds, partials,
+                j);
 }
 
 void te_launch_lanczos_update(int64_t n, const double2* w, const double2* u_j, double2* u_jp1, TeDevState* ds,
-                              double* partials, int j, cudaStream_t st) {
+                              double* partials, int j, bool fold, cudaStream_t st) {
   const int grid = te_grid_fit((const void*)lanczos_update_kernel<true>, n, TE_THREADS);
-  if (u_jp1)
-    lanczos_update_kernel<true><<<grid, TE_THREADS, 0, st>>>(n, w, u_j, u_jp1, ds, partials, j);
-  else
-    lanczos_update_kernel<false><<<grid, TE_THREADS, 0, st>>>(n, w, u_j, u_jp1, ds, partials, j);
+  te_launch_pdl(u_jp1 ? lanczos_update_kernel<true> : lanczos_update_kernel<false>, grid, TE_THREADS, st, n, w, u_j,
+                u_jp1, ds, partials, j, (int)fold);
 }

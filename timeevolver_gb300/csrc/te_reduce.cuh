@@ -60,10 +60,13 @@ template <int NV>
 __device__ __forceinline__ void te_final_sum(double (&out)[NV], const double* partials, unsigned int* counter,
                                              double* scratch) {
 #pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    double s = 0.0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += __ldcg(partials + k * gridDim.x + b);
-    out[k] = s;
+  for (int k = 0; k < NV; ++k) out[k] = 0.0;
+  // blocks ascending per thread for every value (the loads of consecutive
+  // iterations are independent, so the unrolled loop keeps several in flight)
+#pragma unroll 4
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) out[k] += __ldcg(partials + k * gridDim.x + b);
   }
   te_block_sum<NV>(out, scratch);
   if (threadIdx.x == 0) *counter = 0u;

@@ -566,11 +566,21 @@ def zipf_cpu_baseline(te, nnz_full, steps_full):
                       "(extrapolated)" % (len(coo[2]), ZIPF_CPU_T, r["n_steps"], el, per_step, steps_full)}
 
 
-def ncu_case(t_final):
-    """A short solve of the same workload for ncu captures (t_final instead of 10)."""
+def ncu_case(t_final, config="plain", zipf_n=2_000_000):
+    """A short solve of the same workload for ncu captures (t_final instead of
+    the full time; the Zipf matrix at a smaller dimension)."""
     import timeevolver_gb300 as te
     te.build()
     te.lib().te_set_device(0)
+    if config == "zipf":
+        H, est = te.Matrix.zipf(zipf_n, 1.5, 2, 256, 1, 30)
+        rng = np.random.default_rng(1)
+        v = rng.standard_normal(zipf_n) + 1j * rng.standard_normal(zipf_n)
+        v /= np.linalg.norm(v)
+        out = te.evolve(H, v, t_final, t_final, [], tol=TOL, m=M_KRYLOV)
+        print("ncu case: zipf n=%d nnz=%d t=%g, %d Krylov steps, status %d, %d launches"
+              % (zipf_n, H.info()["nnz"], t_final, out["n_steps"], out["status"], out["launches"]))
+        return
     n, Hc, Oc, v = build_problem()
     out = te.evolve(Hc, v, t_final, t_final, [("sparse", Oc)], tol=TOL * t_final / T_FINAL, m=M_KRYLOV)
     print("ncu case: t=%g, %d Krylov steps, status %d, %d launches" % (t_final, out["n_steps"], out["status"],
@@ -589,9 +599,11 @@ def main():
                          "adjoint: gradients of <n_0(T)> for L=10; zipf: the dim-1e7 load-imbalanced matrix")
     ap.add_argument("--ncu-case", type=float, default=None, metavar="T",
                     help="run one short solve to time T (for ncu captures) and exit")
+    ap.add_argument("--zipf-n", type=int, default=2_000_000,
+                    help="dimension of the Zipf matrix in --ncu-case runs of --config zipf")
     args = ap.parse_args()
     if args.ncu_case is not None:
-        ncu_case(args.ncu_case)
+        ncu_case(args.ncu_case, args.config, args.zipf_n)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -463,6 +463,7 @@ int reset_states(te_batch b) {
     s.tol = p.tol;
     s.tol_rate = p.tol / p.t;
     s.exp_factor = p.exp_factor;
+    s.inv_exp_factor = p.exp_factor != 0.0 ? 1.0 / p.exp_factor : 0.0;
     s.num_err_est = (double)b->inst_n[i] * b->H[i]->norm1 * DBL_EPSILON;
     s.m_max = m;
     s.n_samples = (int)b->n_samples[i];

@@ -262,6 +262,7 @@ int run(te_evolver ev, te_result* out) {
   hs->tol = ev->p.tol;
   hs->tol_rate = ev->p.tol / ev->p.t;                                            // :287
   hs->exp_factor = ev->p.exp_factor;
+  hs->inv_exp_factor = ev->p.exp_factor != 0.0 ? 1.0 / ev->p.exp_factor : 0.0;
   hs->num_err_est = (double)n * ev->H->norm1 * DBL_EPSILON;                      // :289
   hs->m_max = ev->m;
   hs->n_samples = (int)ev->n_samples;

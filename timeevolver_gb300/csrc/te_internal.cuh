@@ -84,6 +84,9 @@ struct TeDevState {
   const double* sample_times;
   double2* state_store;
   int64_t store_ld;
+  // 1 / expFactor (0 when expFactor is 0): the folded three-term passes use
+  // beta_j^2 / expFactor^2 and alpha_j / expFactor without a division per thread
+  double inv_exp_factor;
 };
 
 // SELL-32 matrix in the sorted (permuted) basis.

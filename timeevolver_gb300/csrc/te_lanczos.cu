@@ -42,8 +42,14 @@ __global__ void __launch_bounds__(TE_THREADS, REAL ? 6 : 5) lanczos_apply_kernel
   const int lane = threadIdx.x & 31;
   const double sj = ds->s[j];
   const double g = ds->exp_factor * sj;  // A v_j = -i g H u_j
-  const double cprev = HAS_PREV ? ds->beta[j] * ds->s[j - 1] : 0.0;
-  const double cw = FOLD ? cprev / g : cprev;
+  // the u_{j-1} term: beta_j s_{j-1}, divided by g when folded; the folded
+  // update sets s_j = expFactor s_{j-1} / beta_j, so that is beta_j^2 / expFactor^2
+  double cw = 0.0;
+  if (HAS_PREV) {
+    const double bj = ds->beta[j];
+    const double ie = ds->inv_exp_factor;
+    cw = FOLD ? (bj * ie) * (bj * ie) : bj * ds->s[j - 1];
+  }
   double acc[2] = {0.0, 0.0};
   const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int64_t c_end = warp_chunk[wid + 1];
@@ -100,8 +106,8 @@ __global__ void __launch_bounds__(TE_THREADS) lanczos_update_kernel(int64_t n, c
   const double sj = ds->s[j];
   const double g = fold ? ds->exp_factor * sj : 1.0;
   const double2 a = ds->alpha[j];
-  const double q = fold ? sj / g : sj;
-  const double gr = a.x * q, gi = a.y * q;  // gamma = alpha_j s_j (/ g)
+  const double q = fold ? ds->inv_exp_factor : sj;  // alpha_j s_j / g = alpha_j / expFactor
+  const double gr = a.x * q, gi = a.y * q;
   double acc[1] = {0.0};
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
     double2 wv = w[r];

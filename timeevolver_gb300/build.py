@@ -71,7 +71,8 @@ def build_tegpu(force=False, verbose=False):
     def one(src):
         obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
         if force or _stale(obj, [src] + headers):
-            out = _run([nvcc] + NVCC_FLAGS + (["-Xptxas", "-v"] if verbose else []) + ["-c", src, "-o", obj])
+            extra = os.environ.get("TE_NVCC_FLAGS", "").split()  # e.g. -DTE_NO_PDL
+            out = _run([nvcc] + NVCC_FLAGS + extra + (["-Xptxas", "-v"] if verbose else []) + ["-c", src, "-o", obj])
             if verbose:
                 print(out)
         return obj

@@ -75,6 +75,11 @@ int te_grid_fit(const void* kernel, int64_t n_items, int threads, size_t dyn_sme
   return (int)((n_items + per_thread * threads - 1) / (per_thread * threads));
 }
 
+bool te_grid_saturated(const void* kernel, int64_t n_items, int threads, size_t dyn_smem) {
+  const int64_t cap = (int64_t)te_num_sms() * te_kernel_blocks_per_sm(kernel, threads, dyn_smem);
+  return (n_items + threads - 1) / threads > cap;
+}
+
 extern "C" const char* te_last_error(void) { return g_last_error; }
 extern "C" int te_abi_version(void) { return TEGPU_ABI_VERSION; }
 extern "C" int te_set_device(int device) { return te_cuda_check(cudaSetDevice(device), "cudaSetDevice"); }

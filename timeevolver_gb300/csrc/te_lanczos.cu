@@ -351,13 +351,14 @@ void te_launch_lanczos_apply(const TeSell& A, bool is_real, const double2* u_j, 
       {{lanczos_apply_kernel<true, false, false>, lanczos_apply_kernel<true, false, true>},
        {lanczos_apply_kernel<true, true, false>, lanczos_apply_kernel<true, true, true>}}};
   const K k = table[is_real ? 1 : 0][u_jm1 ? 1 : 0][fold ? 1 : 0];
-  te_launch_pdl(k, A.grid, TE_THREADS, st, A.n, A.warp_chunk, A.chunk_off, A.col, A.val, u_j, u_jm1, w, ds, partials,
-                j);
+  te_launch_pdl(A.saturated, k, A.grid, TE_THREADS, st, A.n, A.warp_chunk, A.chunk_off, A.col, A.val, u_j, u_jm1, w,
+                ds, partials, j);
 }
 
 void te_launch_lanczos_update(int64_t n, const double2* w, const double2* u_j, double2* u_jp1, TeDevState* ds,
                               double* partials, int j, bool fold, cudaStream_t st) {
-  const int grid = te_grid_fit((const void*)lanczos_update_kernel<true>, n, TE_THREADS);
-  te_launch_pdl(u_jp1 ? lanczos_update_kernel<true> : lanczos_update_kernel<false>, grid, TE_THREADS, st, n, w, u_j,
-                u_jp1, ds, partials, j, (int)fold);
+  const void* kk = (const void*)lanczos_update_kernel<true>;
+  const int grid = te_grid_fit(kk, n, TE_THREADS);
+  te_launch_pdl(te_grid_saturated(kk, n, TE_THREADS), u_jp1 ? lanczos_update_kernel<true> : lanczos_update_kernel<false>,
+                grid, TE_THREADS, st, n, w, u_j, u_jp1, ds, partials, j, (int)fold);
 }

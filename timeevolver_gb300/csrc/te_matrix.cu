@@ -255,7 +255,9 @@ int sell_layout(te_matrix_s* M, const std::vector<int32_t>& rp, bool real, std::
                            te_kernel_blocks_per_sm(real ? (const void*)sell_spmv_kernel<true>
                                                         : (const void*)sell_spmv_kernel<false>,
                                                    TE_THREADS, 0));
-  S.grid = (int)std::min<int64_t>((S.n_chunks * 32 + TE_THREADS - 1) / TE_THREADS, (int64_t)te_num_sms() * bps);
+  const int64_t need = (S.n_chunks * 32 + TE_THREADS - 1) / TE_THREADS;
+  S.grid = (int)std::min<int64_t>(need, (int64_t)te_num_sms() * bps);
+  S.saturated = need > (int64_t)te_num_sms() * bps;
   const int64_t W = (int64_t)S.grid * (TE_THREADS / 32);
   const double w_slot = real ? 2.0 : 4.0, w_chunk = 8.0 * 32;
   auto cost = [&](int64_t c) { return w_slot * (double)off[c] + w_chunk * (double)c; };

@@ -1,0 +1,68 @@
+"""Matrix upload (needs a GB300): the device conversion of large row-sorted
+COO input, the host fallback for unsorted input, and the reference's 1-norm
+(column sums of |a| in entry order, matrixDataTypes.cpp:67-79) in both."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+N = 200_000
+PER_ROW = 3  # 600k entries: above the device-conversion threshold of 2^18
+
+
+def _coo(seed, sort_rows=True, real=False):
+    rng = np.random.default_rng(seed)
+    row = np.repeat(np.arange(N, dtype=np.int64), PER_ROW)
+    col = rng.integers(0, N, size=len(row)).astype(np.int64)
+    val = rng.standard_normal(len(row)) + (0 if real else 1j) * rng.standard_normal(len(row))
+    if not sort_rows:
+        p = rng.permutation(len(row))
+        row, col, val = row[p], col[p], val[p]
+    return row, col, val.astype(np.complex128)
+
+
+def _reference_norm1(col, val):
+    s = np.zeros(N)
+    np.add.at(s, col, np.abs(val))  # sequential in entry order
+    return s.max()
+
+
+def _expected_csr(row, col, val):
+    order = np.argsort(row, kind="stable")
+    rp = np.zeros(N + 1, dtype=np.int64)
+    np.add.at(rp, row + 1, 1)
+    return np.cumsum(rp), col[order], val[order]
+
+
+@pytest.mark.parametrize("sort_rows", [True, False])
+def test_coo_upload(te_gpu, sort_rows):
+    row, col, val = _coo(1, sort_rows)
+    M = te_gpu.Matrix(N, row, col, val)
+    rp, ci, v = M.to_csr()
+    rp0, ci0, v0 = _expected_csr(row, col, val)
+    assert np.array_equal(rp, rp0) and np.array_equal(ci, ci0) and np.array_equal(v, v0)
+    info = M.info()
+    assert info["norm1"] == _reference_norm1(col, val)
+    assert not info["real"] and not info["diagonal"]
+    x = np.random.default_rng(2).standard_normal(N) + 0j
+    y = np.zeros(N, dtype=np.complex128)
+    np.add.at(y, row, val * x[col])
+    assert np.max(np.abs(M.spmv(x) - y)) < 1e-12 * np.max(np.abs(y))
+
+
+def test_coo_upload_real_and_diagonal(te_gpu):
+    row, col, val = _coo(3, True, real=True)
+    M = te_gpu.Matrix(N, row, col, val)
+    assert M.info()["real"]
+    d = np.arange(N, dtype=np.int64)
+    D = te_gpu.Matrix(N, np.repeat(d, 2), np.repeat(d, 2), np.ones(2 * N, dtype=np.complex128))
+    inf = D.info()
+    assert inf["diagonal"] and inf["real"] and inf["norm1"] == 2.0
+
+
+def test_coo_upload_rejects_out_of_range(te_gpu):
+    row, col, val = _coo(4, True)
+    col = col.copy()
+    col[123_456] = N
+    with pytest.raises(RuntimeError, match="entry 123456 out of range"):
+        te_gpu.Matrix(N, row, col, val)

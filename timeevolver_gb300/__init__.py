@@ -147,12 +147,20 @@ def _ptr(a):
     return a.ctypes.data_as(ctypes.c_void_p)
 
 
+def _as_u64(a):
+    """Index array as uint64 (int64 input is reinterpreted without a copy;
+    negative entries become out-of-range indices, which the library rejects)."""
+    a = np.ascontiguousarray(a)
+    if a.dtype == np.int64:
+        return a.view(np.uint64)
+    return np.ascontiguousarray(a, dtype=np.uint64)
+
+
 class Matrix:
     """Device sparse matrix (TE::smatrix): from COO arrays (row, col, values)."""
 
     def __init__(self, n, row, col, val, n_cols=None):
-        row = np.ascontiguousarray(row, dtype=np.uint64)
-        col = np.ascontiguousarray(col, dtype=np.uint64)
+        row, col = _as_u64(row), _as_u64(col)
         val = np.ascontiguousarray(val, dtype=np.complex128)
         self.handle = ctypes.c_void_p()
         self.n = int(n)

@@ -123,8 +123,10 @@ struct te_matrix_s {
 
 // Adopt a device CSR (int32 row pointers, columns, complex values; the matrix
 // frees them) -- the device-side build of te_matrix_create_csr_device.
+// norm1: the 1-norm if the caller computed it, NAN to accumulate it on the
+// device in fixed point.
 int te_matrix_adopt_device_csr(int64_t n_rows, int64_t n_cols, const std::vector<int32_t>& rp_host, int32_t* d_rp,
-                               int32_t* d_ci, double2* d_v, te_matrix* out);
+                               int32_t* d_ci, double2* d_v, te_matrix* out, double norm1);
 
 // Programmatic dependent launch: a kernel launched with te_launch_pdl may be
 // scheduled while its predecessor in the stream is still finishing (hiding the

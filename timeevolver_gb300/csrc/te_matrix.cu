@@ -17,6 +17,7 @@
 #include <cstring>
 #include <mutex>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 #include "te_internal.cuh"
@@ -192,6 +193,35 @@ __global__ void fill_sell_kernel(int64_t n, int64_t n_chunks, const int64_t* __r
   }
 }
 
+enum { TE_COO_BAD = 1, TE_COO_UNSORTED = 2 };
+
+// COO input checks on the device: indices in range (the first bad entry is
+// kept) and rows in non-decreasing order.
+__global__ void coo_scan_kernel(int64_t nnz, uint64_t n_rows, uint64_t n_cols, const uint64_t* __restrict__ row,
+                                const uint64_t* __restrict__ col, unsigned int* flags,
+                                unsigned long long* first_bad) {
+  unsigned int f = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nnz; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t r = row[i];
+    if (r >= n_rows || col[i] >= n_cols) {
+      f |= TE_COO_BAD;
+      atomicMin(first_bad, (unsigned long long)i);
+    }
+    if (i > 0 && row[i - 1] > r) f |= TE_COO_UNSORTED;
+  }
+  if (f) atomicOr(flags, f);
+}
+
+__global__ void row_count_kernel(int64_t nnz, const uint64_t* __restrict__ row, int32_t* __restrict__ count) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nnz; i += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&count[row[i]], 1);
+}
+
+__global__ void narrow_index_kernel(int64_t nnz, const uint64_t* __restrict__ in, int32_t* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nnz; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (int32_t)in[i];
+}
+
 // ------------------------------------------------------------ host build
 
 namespace {
@@ -275,7 +305,7 @@ int sell_layout(te_matrix_s* M, const std::vector<int32_t>& rp, bool real, std::
 
 // rp/ci/vv: original-order CSR with interleaved complex values.
 int build_matrix(te_matrix_s* M, const std::vector<int32_t>& rp, const std::vector<int32_t>& ci,
-                 const std::vector<double>& vv) {
+                 const std::vector<double>& vv, double norm1_given) {
   const int64_t n = M->n_rows, nnz = M->nnz;
   bool real = true;
   for (int64_t i = 0; i < nnz && real; ++i) real = (vv[2 * i + 1] == 0.0);
@@ -288,10 +318,15 @@ int build_matrix(te_matrix_s* M, const std::vector<int32_t>& rp, const std::vect
       }
   M->is_real = real;
   M->is_diag = diag;
-  // 1-norm as in matrixDataTypes.cpp:223-235 (max absolute column sum)
-  std::vector<double> colsum(M->n_cols, 0.0);
-  for (int64_t p = 0; p < nnz; ++p) colsum[ci[p]] += std::abs(std::complex<double>(vv[2 * p], vv[2 * p + 1]));
-  M->norm1 = *std::max_element(colsum.begin(), colsum.end());
+  // 1-norm as in matrixDataTypes.cpp:223-235 (max absolute column sum), unless
+  // the caller computed it in its own entry order
+  if (std::isnan(norm1_given)) {
+    std::vector<double> colsum(M->n_cols, 0.0);
+    for (int64_t p = 0; p < nnz; ++p) colsum[ci[p]] += std::abs(std::complex<double>(vv[2 * p], vv[2 * p + 1]));
+    M->norm1 = *std::max_element(colsum.begin(), colsum.end());
+  } else {
+    M->norm1 = norm1_given;
+  }
 
   std::vector<double> vr;
   if (real) {
@@ -354,13 +389,13 @@ int build_matrix(te_matrix_s* M, const std::vector<int32_t>& rp, const std::vect
 }
 
 int finish_create(int64_t n_rows, int64_t n_cols, const std::vector<int32_t>& rp, const std::vector<int32_t>& ci,
-                  const std::vector<double>& vv, te_matrix* out) {
+                  const std::vector<double>& vv, te_matrix* out, double norm1_given = NAN) {
   te_matrix_s* M = new te_matrix_s();
   cudaGetDevice(&M->device);
   M->n_rows = n_rows;
   M->n_cols = n_cols;
   M->nnz = (int64_t)ci.size();
-  int rc = build_matrix(M, rp, ci, vv);
+  int rc = build_matrix(M, rp, ci, vv, norm1_given);
   if (rc != TE_OK) {
     free_matrix(M);
     return rc;
@@ -376,7 +411,7 @@ int finish_create(int64_t n_rows, int64_t n_cols, const std::vector<int32_t>& rp
 // point (relative resolution ~1e-12 of the largest entry), so it does not
 // depend on the order of the device atomics.
 int build_matrix_device(te_matrix_s* M, const std::vector<int32_t>& rp_host, int32_t* d_rp, int32_t* d_ci,
-                        double2* d_v) {
+                        double2* d_v, double norm1_given) {
   const int64_t n = M->n_rows, nnz = M->nnz;
   M->row_ptr = d_rp;
   M->col = d_ci;
@@ -414,8 +449,8 @@ int build_matrix_device(te_matrix_s* M, const std::vector<int32_t>& rp_host, int
   // 1-norm
   double vmax;
   std::memcpy(&vmax, &vmax_bits, sizeof(vmax));
-  M->norm1 = 0.0;
-  if (vmax > 0.0 && nnz > 0) {
+  M->norm1 = std::isnan(norm1_given) ? 0.0 : norm1_given;
+  if (std::isnan(norm1_given) && vmax > 0.0 && nnz > 0) {
     const int e = 62 - (int)std::ceil(std::log2(vmax * (double)std::max<int64_t>(n, 1)));
     const double scale = std::ldexp(1.0, e);
     if (te_cuda_check(cudaMalloc(&d_colsum, sizeof(unsigned long long) * M->n_cols), "colsum") != TE_OK)
@@ -480,13 +515,13 @@ int build_matrix_device(te_matrix_s* M, const std::vector<int32_t>& rp_host, int
 // Adopt a device CSR (see build_matrix_device); used by the device-side
 // workload generators.  On failure the buffers are freed.
 int te_matrix_adopt_device_csr(int64_t n_rows, int64_t n_cols, const std::vector<int32_t>& rp_host, int32_t* d_rp,
-                               int32_t* d_ci, double2* d_v, te_matrix* out) {
+                               int32_t* d_ci, double2* d_v, te_matrix* out, double norm1) {
   te_matrix_s* M = new te_matrix_s();
   cudaGetDevice(&M->device);
   M->n_rows = n_rows;
   M->n_cols = n_cols;
   M->nnz = rp_host[n_rows];
-  int rc = build_matrix_device(M, rp_host, d_rp, d_ci, d_v);
+  int rc = build_matrix_device(M, rp_host, d_rp, d_ci, d_v, norm1);
   if (rc != TE_OK) {
     free_matrix(M);
     return rc;
@@ -497,22 +532,37 @@ int te_matrix_adopt_device_csr(int64_t n_rows, int64_t n_cols, const std::vector
 
 // ------------------------------------------------------------------ C ABI
 
-extern "C" int te_matrix_create_coo(int64_t n_rows, int64_t n_cols, int64_t nnz, const uint64_t* row_index,
-                                    const uint64_t* columns, const double* values, te_matrix* out) {
-  if (!out || n_rows <= 0 || n_cols <= 0 || nnz < 0 || (nnz > 0 && (!row_index || !columns || !values))) {
-    te_set_error("te_matrix_create_coo: invalid arguments");
-    return n_rows == 0 || n_cols == 0 ? TE_ERR_EMPTY : TE_ERR_INVALID_ARG;
-  }
-  if (nnz >= ((int64_t)1 << 31) || n_rows >= ((int64_t)1 << 31) || n_cols >= ((int64_t)1 << 31)) {
-    te_set_error("te_matrix_create_coo: sizes must stay below 2^31 (int32 indices)");
-    return TE_ERR_UNSUPPORTED;
-  }
+namespace {
+
+// The reference's 1-norm (matrixDataTypes.cpp:67-79): column sums of |a| in the
+// order of the COO entries.  Threads own disjoint column ranges and each scans
+// all entries, so every column is summed in exactly that order.  Entries with
+// an out-of-range column are skipped (the caller rejects them).
+double coo_norm1(int64_t n_cols, int64_t nnz, const uint64_t* col, const double* val) {
+  const int T = (int)std::max<unsigned>(1u, std::min<unsigned>(8u, std::thread::hardware_concurrency()));
+  std::vector<double> colsum(n_cols, 0.0);
+  auto work = [&](int t) {
+    const uint64_t c0 = (uint64_t)(n_cols * t / T), c1 = (uint64_t)(n_cols * (t + 1) / T);
+    for (int64_t i = 0; i < nnz; ++i) {
+      const uint64_t c = col[i];
+      if (c >= c0 && c < c1) colsum[c] += std::abs(std::complex<double>(val[2 * i], val[2 * i + 1]));
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < T; ++t) pool.emplace_back(work, t);
+  work(0);
+  for (auto& th : pool) th.join();
+  return n_cols > 0 ? *std::max_element(colsum.begin(), colsum.end()) : 0.0;
+}
+
+// Host conversion: stable COO -> CSR (entries of one row keep their input order).
+int create_coo_host(int64_t n_rows, int64_t n_cols, int64_t nnz, const uint64_t* row_index, const uint64_t* columns,
+                    const double* values, double norm1, te_matrix* out) {
   for (int64_t i = 0; i < nnz; ++i)
     if (row_index[i] >= (uint64_t)n_rows || columns[i] >= (uint64_t)n_cols) {
       te_set_error("te_matrix_create_coo: entry %lld out of range", (long long)i);
       return TE_ERR_INVALID_ARG;
     }
-  // stable COO -> CSR: entries of one row keep their input order
   std::vector<int32_t> rp(n_rows + 1, 0), ci(nnz);
   std::vector<double> vv(2 * nnz);
   for (int64_t i = 0; i < nnz; ++i) rp[row_index[i] + 1]++;
@@ -524,7 +574,109 @@ extern "C" int te_matrix_create_coo(int64_t n_rows, int64_t n_cols, int64_t nnz,
     vv[2 * p] = values[2 * i];
     vv[2 * p + 1] = values[2 * i + 1];
   }
-  return finish_create(n_rows, n_cols, rp, ci, vv, out);
+  return finish_create(n_rows, n_cols, rp, ci, vv, out, norm1);
+}
+
+// Device conversion of a row-sorted COO (the order TE::Hamiltonian::createMatrix
+// produces): the arrays are copied to the GPU as they are, the row pointers come
+// from per-row counts, and the layout is built by kernels.  Returns
+// TE_ERR_UNSUPPORTED (nothing built, no error set) for unsorted input.
+int create_coo_device(int64_t n_rows, int64_t n_cols, int64_t nnz, const uint64_t* row_index, const uint64_t* columns,
+                      const double* values, double norm1, te_matrix* out) {
+  uint64_t *d_row = nullptr, *d_col = nullptr;
+  double2* d_v = nullptr;
+  int32_t *d_cnt = nullptr, *d_rp = nullptr, *d_ci = nullptr;
+  unsigned int* d_flags = nullptr;
+  unsigned long long* d_bad = nullptr;
+  auto release = [&]() {
+    cudaFree(d_row);
+    cudaFree(d_col);
+    cudaFree(d_cnt);
+    cudaFree(d_flags);
+    cudaFree(d_bad);
+  };
+  auto fail = [&](int rc) {
+    release();
+    cudaFree(d_v);
+    cudaFree(d_rp);
+    cudaFree(d_ci);
+    return rc;
+  };
+  if (te_cuda_check(cudaMalloc(&d_row, sizeof(uint64_t) * nnz), "coo") != TE_OK ||
+      te_cuda_check(cudaMalloc(&d_col, sizeof(uint64_t) * nnz), "coo") != TE_OK ||
+      te_cuda_check(cudaMalloc(&d_v, sizeof(double2) * nnz), "coo") != TE_OK ||
+      te_cuda_check(cudaMalloc(&d_flags, sizeof(unsigned int)), "coo") != TE_OK ||
+      te_cuda_check(cudaMalloc(&d_bad, sizeof(unsigned long long)), "coo") != TE_OK)
+    return fail(TE_ERR_CUDA);
+  const unsigned long long none = ~0ull;
+  if (te_cuda_check(cudaMemcpy(d_row, row_index, sizeof(uint64_t) * nnz, cudaMemcpyHostToDevice), "coo") != TE_OK ||
+      te_cuda_check(cudaMemcpy(d_col, columns, sizeof(uint64_t) * nnz, cudaMemcpyHostToDevice), "coo") != TE_OK ||
+      te_cuda_check(cudaMemcpy(d_v, values, sizeof(double2) * nnz, cudaMemcpyHostToDevice), "coo") != TE_OK ||
+      te_cuda_check(cudaMemset(d_flags, 0, sizeof(unsigned int)), "coo") != TE_OK ||
+      te_cuda_check(cudaMemcpy(d_bad, &none, sizeof(none), cudaMemcpyHostToDevice), "coo") != TE_OK)
+    return fail(TE_ERR_CUDA);
+  coo_scan_kernel<<<te_grid_fit((const void*)coo_scan_kernel, nnz, TE_THREADS), TE_THREADS>>>(
+      nnz, (uint64_t)n_rows, (uint64_t)n_cols, d_row, d_col, d_flags, d_bad);
+  unsigned int flags = 0;
+  unsigned long long bad = 0;
+  if (te_cuda_check(cudaMemcpy(&flags, d_flags, sizeof(flags), cudaMemcpyDeviceToHost), "coo") != TE_OK ||
+      te_cuda_check(cudaMemcpy(&bad, d_bad, sizeof(bad), cudaMemcpyDeviceToHost), "coo") != TE_OK)
+    return fail(TE_ERR_CUDA);
+  if (flags & TE_COO_BAD) {
+    te_set_error("te_matrix_create_coo: entry %lld out of range", (long long)bad);
+    return fail(TE_ERR_INVALID_ARG);
+  }
+  if (flags & TE_COO_UNSORTED) return fail(TE_ERR_UNSUPPORTED);
+  // row pointers from the per-row counts (rows are sorted, so CSR order = input order)
+  if (te_cuda_check(cudaMalloc(&d_cnt, sizeof(int32_t) * n_rows), "coo") != TE_OK ||
+      te_cuda_check(cudaMemset(d_cnt, 0, sizeof(int32_t) * n_rows), "coo") != TE_OK)
+    return fail(TE_ERR_CUDA);
+  row_count_kernel<<<te_grid_fit((const void*)row_count_kernel, nnz, TE_THREADS), TE_THREADS>>>(nnz, d_row, d_cnt);
+  std::vector<int32_t> cnt(n_rows), rp(n_rows + 1, 0);
+  if (te_cuda_check(cudaMemcpy(cnt.data(), d_cnt, sizeof(int32_t) * n_rows, cudaMemcpyDeviceToHost), "coo") != TE_OK)
+    return fail(TE_ERR_CUDA);
+  for (int64_t r = 0; r < n_rows; ++r) rp[r + 1] = rp[r] + cnt[r];
+  if (te_cuda_check(cudaMalloc(&d_rp, sizeof(int32_t) * (n_rows + 1)), "coo") != TE_OK ||
+      te_cuda_check(cudaMalloc(&d_ci, sizeof(int32_t) * nnz), "coo") != TE_OK ||
+      te_cuda_check(cudaMemcpy(d_rp, rp.data(), sizeof(int32_t) * (n_rows + 1), cudaMemcpyHostToDevice), "coo") !=
+          TE_OK)
+    return fail(TE_ERR_CUDA);
+  narrow_index_kernel<<<te_grid_fit((const void*)narrow_index_kernel, nnz, TE_THREADS), TE_THREADS>>>(nnz, d_col,
+                                                                                                   d_ci);
+  if (te_cuda_check(cudaDeviceSynchronize(), "coo") != TE_OK) return fail(TE_ERR_CUDA);
+  release();
+  return te_matrix_adopt_device_csr(n_rows, n_cols, rp, d_rp, d_ci, d_v, out, norm1);
+}
+
+// Below this many entries the host conversion is as fast as the device one.
+const int64_t kDeviceCooMinEntries = (int64_t)1 << 18;
+
+}  // namespace
+
+extern "C" int te_matrix_create_coo(int64_t n_rows, int64_t n_cols, int64_t nnz, const uint64_t* row_index,
+                                    const uint64_t* columns, const double* values, te_matrix* out) {
+  if (!out || n_rows <= 0 || n_cols <= 0 || nnz < 0 || (nnz > 0 && (!row_index || !columns || !values))) {
+    te_set_error("te_matrix_create_coo: invalid arguments");
+    return n_rows == 0 || n_cols == 0 ? TE_ERR_EMPTY : TE_ERR_INVALID_ARG;
+  }
+  if (nnz >= ((int64_t)1 << 31) || n_rows >= ((int64_t)1 << 31) || n_cols >= ((int64_t)1 << 31)) {
+    te_set_error("te_matrix_create_coo: sizes must stay below 2^31 (int32 indices)");
+    return TE_ERR_UNSUPPORTED;
+  }
+  if (nnz < kDeviceCooMinEntries)
+    return create_coo_host(n_rows, n_cols, nnz, row_index, columns, values, coo_norm1(n_cols, nnz, columns, values),
+                           out);
+  // the 1-norm on host threads while the device converts the layout
+  double norm1 = 0.0;
+  std::thread norm_thread([&]() { norm1 = coo_norm1(n_cols, nnz, columns, values); });
+  int rc = create_coo_device(n_rows, n_cols, nnz, row_index, columns, values, 0.0, out);
+  norm_thread.join();
+  if (rc == TE_OK) {
+    (*out)->norm1 = norm1;
+    return TE_OK;
+  }
+  if (rc != TE_ERR_UNSUPPORTED) return rc;
+  return create_coo_host(n_rows, n_cols, nnz, row_index, columns, values, norm1, out);
 }
 
 extern "C" int te_matrix_create_csr(int64_t n_rows, int64_t n_cols, int64_t nnz, const int64_t* row_ptr,
@@ -613,7 +765,7 @@ extern "C" int te_matrix_create_csr_device(int64_t n_rows, int64_t n_cols, int64
                                                                                                     d_v);
     }
   }
-  return te_matrix_adopt_device_csr(n_rows, n_cols, rp, d_rp, d_ci, d_v, out);
+  return te_matrix_adopt_device_csr(n_rows, n_cols, rp, d_rp, d_ci, d_v, out, NAN);
 }
 
 extern "C" int te_matrix_download_csr(te_matrix A, int32_t* row_ptr, int32_t* col_idx, double* values) {

@@ -112,6 +112,19 @@ int te_matrix_create_csr_device(int64_t n_rows, int64_t n_cols, int64_t nnz, con
 int te_matrix_create_zipf(int64_t n, double exponent, int32_t min_len, int32_t max_len, uint64_t seed,
                           int32_t power_iters, double* norm_estimate, te_matrix* out);
 
+/* Lanes per row of the matrix's SELL-32 SpMV passes (no counterpart in the
+ * reference).  1: one lane per row (the layout's native form); 2 or 4: each
+ * row's entries are split over 2 or 4 lanes of a warp, which multiplies the
+ * warps in flight for matrices too small to fill the GPU.  0 (the default):
+ * te_evolver_create tunes it by timing the Lanczos pass for 1, 2 and 4 on the
+ * matrix and keeps 2 or 4 only when more than 10% faster; the choice changes
+ * the summation order of a row (results differ by rounding), so it is made
+ * once per matrix.  Setting 1, 2 or 4 pins it. */
+int te_matrix_set_spmv_lanes(te_matrix A, int lanes);
+/* Current lanes per row (1, 2, 4), tuning first if tune_now != 0 and the
+ * choice is still open; a negative value is an error code. */
+int te_matrix_spmv_lanes(te_matrix A, int tune_now);
+
 /* Copy a matrix's original-order CSR to host buffers: row_ptr (n_rows + 1),
  * col_idx (nnz), values (nnz interleaved complex doubles). */
 int te_matrix_download_csr(te_matrix A, int32_t* row_ptr, int32_t* col_idx, double* values);

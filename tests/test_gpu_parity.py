@@ -247,3 +247,34 @@ def test_reorthogonalised_mode_l12(te_gpu, oracle_lib):
     gpu = te_gpu.evolve(H, v, 0.5, 0.25, obs, tol=1e-8, m=40, reorth=True)
     ref = oracle_lib.evolve(H, v, 0.5, 0.25, obs, tol=1e-8, m=40, reorth=True)
     _compare(gpu, ref, 1e-8, strict=True)
+
+
+@pytest.mark.parametrize("lanes", [1, 2, 4])
+def test_spmv_lanes_variants(te_gpu, oracle_lib, lanes):
+    """Every lanes-per-row variant of the SpMV passes against the oracle: the
+    product to 1e-13 and a full L=8 evolution within the parity bounds."""
+    states, H = models.bose_hubbard(8, 8, 1.0, 2.0)
+    n = len(states)
+    M = te_gpu.Matrix.from_coo(n, H)
+    M.set_spmv_lanes(lanes)
+    assert M.spmv_lanes(tune=False) == lanes
+    x = _random_state(n, 7)
+    ref = oracle_lib.spmv(H, x, -1j)
+    assert np.linalg.norm(M.spmv(x, -1j) - ref) <= 1e-13 * np.linalg.norm(ref)
+    v = _fock(states, [8] + [0] * 7)
+    obs = [("sparse", o) for o in models.number_operator_observables(states)]
+    O = [("sparse", te_gpu.Matrix.from_coo(n, o)) for _, o in obs]
+    ev = te_gpu.Evolver(M, v, 10.0, 0.1, O, tol=1e-8, m=40)
+    gpu = ev.time_evolve()
+    ev.close()
+    assert M.spmv_lanes(tune=False) == lanes  # a pinned choice is kept by the evolver
+    ref = oracle_lib.evolve(H, v, 10.0, 0.1, obs, tol=1e-8, m=40)
+    _compare(gpu, ref, 1e-8, obs_norm=8.0, strict=False)
+
+
+def test_spmv_lanes_tuning(te_gpu):
+    states, H = models.bose_hubbard(10, 10, 1.0, 2.0)
+    M = te_gpu.Matrix.from_coo(len(states), H)
+    k = M.spmv_lanes(tune=True)
+    assert k in (1, 2, 4)
+    assert M.spmv_lanes(tune=True) == k  # tuned once

@@ -68,6 +68,8 @@ SIGNATURES = {
     "te_matrix_spmv_noalloc": (_I, [_P, _D, _D, _P, _P, _P]),
     "te_matrix_create_csr_device": (_I, [_I64, _I64, _I64, _P, _P, _P, _I, _P]),
     "te_matrix_download_csr": (_I, [_P, _P, _P, _P]),
+    "te_matrix_set_spmv_lanes": (_I, [_P, _I]),
+    "te_matrix_spmv_lanes": (_I, [_P, _I]),
     "te_matrix_create_zipf": (_I, [_I64, _D, ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_int32, _P, _P]),
     "te_evolver_create": (_I, [_P, _P, _P, _P]),
     "te_evolver_destroy": (_I, [_P]),
@@ -212,6 +214,17 @@ class Matrix:
         val = np.zeros(max(1, inf["nnz"]), dtype=np.complex128)
         _check(lib().te_matrix_download_csr(self.handle, _ptr(rp), _ptr(ci), _ptr(val)), "te_matrix_download_csr")
         return rp, ci[:inf["nnz"]], val[:inf["nnz"]]
+
+    def spmv_lanes(self, tune=True):
+        """Lanes per row of the SpMV passes (tuned on first use unless pinned)."""
+        k = lib().te_matrix_spmv_lanes(self.handle, int(bool(tune)))
+        if k < 0:
+            _check(k, "te_matrix_spmv_lanes")
+        return k
+
+    def set_spmv_lanes(self, lanes):
+        """Pin the lanes per row (1, 2, 4) or reopen the choice (0)."""
+        _check(lib().te_matrix_set_spmv_lanes(self.handle, int(lanes)), "te_matrix_set_spmv_lanes")
 
     def to_coo(self):
         """(row, col, values) COO triple of the matrix, on the host."""

@@ -505,6 +505,8 @@ extern "C" int te_evolver_create(te_matrix H, const double* v_host, const te_par
   }
   int rc = te_upload_quad_tables();
   if (rc != TE_OK) return rc;
+  rc = te_tune_sell_lanes(H);  // once per matrix (lanes per row of the SpMV passes)
+  if (rc != TE_OK) return rc;
   te_evolver ev = new te_evolver_s();
   ev->H = H;
   ev->p = p;

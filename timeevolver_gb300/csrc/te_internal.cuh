@@ -105,6 +105,10 @@ struct TeSell {
   int32_t* warp_chunk = nullptr;
   int grid = 0;
   bool saturated = false;  // the grid is capped at every SM's resident blocks
+  // lanes per row of the SpMV passes (1, 2 or 4), chosen by te_tune_sell_lanes
+  // or set through te_matrix_set_spmv_lanes; lanes_fixed once chosen
+  int lanes = 1;
+  bool lanes_fixed = false;
 };
 
 struct te_matrix_s {
@@ -199,6 +203,8 @@ void te_launch_lanczos_apply(const TeSell& A, bool is_real, const double2* u_j, 
                              TeDevState* ds, double* partials, int j, bool fold, cudaStream_t st);
 void te_launch_lanczos_update(int64_t n, const double2* w, const double2* u_j, double2* u_jp1, TeDevState* ds,
                               double* partials, int j, bool fold, cudaStream_t st);
+// Choose the lanes per row of a square matrix's SpMV passes (te_lanczos.cu).
+int te_tune_sell_lanes(te_matrix_s* A);
 // Gram-Schmidt passes of the reorthogonalising Lanczos mode (te_lanczos.cu)
 #define TE_GS_ROWS 2048  // rows per block of the Gram-Schmidt passes
 struct TeBasisPtrs {

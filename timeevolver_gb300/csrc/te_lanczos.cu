@@ -14,6 +14,7 @@
 // (fixed order), so the Krylov coefficients never leave the device.  Pass 1
 // runs on the SELL-32 layout: a warp owns 32 equal-length rows.
 #include <algorithm>
+#include <cstring>
 
 #include "te_internal.cuh"
 #include "te_reduce.cuh"
@@ -23,18 +24,55 @@ __device__ __forceinline__ bool te_step_inactive(const TeDevState* ds) {
   return ds->fatal != 0 || ds->done != 0 || ds->breakdown != 0;
 }
 
-// 6 (real H: at most 40 registers) or 5 (complex H) resident blocks of 256;
-// the static chunk schedule of the matrix assumes the whole grid is resident.
+// The recurrence epilogue of one row r (A u_j row sum y): writes w (or the
+// folded w') and accumulates conj(u_j) w.
+template <bool HAS_PREV, bool FOLD>
+__device__ __forceinline__ void apply_row_epilogue(int64_t r, double2 y, double g, double cw,
+                                                   const double2* __restrict__ u_j,
+                                                   const double2* __restrict__ u_jm1, double2* __restrict__ w,
+                                                   double (&acc)[2]) {
+  double2 wr;
+  if (FOLD) {
+    if (HAS_PREV) {
+      double2 up = u_jm1[r];
+      wr.x = fma(cw, up.x, y.y);
+      wr.y = fma(cw, up.y, -y.x);
+    } else {
+      wr.x = y.y;
+      wr.y = -y.x;
+    }
+  } else if (HAS_PREV) {
+    double2 up = u_jm1[r];
+    wr.x = fma(cw, up.x, g * y.y);
+    wr.y = fma(cw, up.y, -g * y.x);
+  } else {
+    wr.x = g * y.y;
+    wr.y = -g * y.x;
+  }
+  w[r] = wr;
+  double2 uj = u_j[r];
+  // conj(u_j) * w
+  acc[0] = fma(uj.x, wr.x, fma(uj.y, wr.y, acc[0]));
+  acc[1] = fma(uj.x, wr.y, fma(-uj.y, wr.x, acc[1]));
+}
+
+// 6 (real H: at most 40 registers) or 5 (complex H, or K > 1) resident blocks
+// of 256; the static chunk schedule of the matrix assumes the whole grid is
+// resident.
 //
 // FOLD (three-term mode, expFactor != 0): with g = expFactor s_j the kernel
 // stores w' = w / g = -i H u_j + (beta_j s_{j-1} / g) u_{j-1}, which saves the
 // two multiplications by g per row (FP64 issue is the bound); alpha_j is
 // still the reference's <v_j, w> = s_j g <u_j, w'>.
-template <bool REAL, bool HAS_PREV, bool FOLD>
-__global__ void __launch_bounds__(TE_THREADS, REAL ? 6 : 5) lanczos_apply_kernel(
-    int64_t n, const int32_t* __restrict__ warp_chunk, const int64_t* __restrict__ chunk_off, const int32_t* __restrict__ col,
-    const double* __restrict__ val, const double2* __restrict__ u_j, const double2* __restrict__ u_jm1,
-    double2* __restrict__ w, TeDevState* ds, double* partials, int j) {
+//
+// K lanes per row: K = 1 walks the matrix's static chunk schedule; K = 2, 4
+// (small matrices, chosen by te_tune_sell_lanes) give each warp 32/K rows and
+// stride over (chunk, part) units.
+template <bool REAL, bool HAS_PREV, bool FOLD, int K>
+__global__ void __launch_bounds__(TE_THREADS, (REAL && K == 1) ? 6 : 5) lanczos_apply_kernel(
+    int64_t n, int64_t n_chunks, const int32_t* __restrict__ warp_chunk, const int64_t* __restrict__ chunk_off,
+    const int32_t* __restrict__ col, const double* __restrict__ val, const double2* __restrict__ u_j,
+    const double2* __restrict__ u_jm1, double2* __restrict__ w, TeDevState* ds, double* partials, int j) {
   __shared__ double scratch[2 * 32];
   te_pdl_trigger();
   te_pdl_wait();
@@ -52,34 +90,21 @@ __global__ void __launch_bounds__(TE_THREADS, REAL ? 6 : 5) lanczos_apply_kernel
   }
   double acc[2] = {0.0, 0.0};
   const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int64_t c_end = warp_chunk[wid + 1];
-  for (int64_t c = warp_chunk[wid]; c < c_end; ++c) {
-    double2 y = te_sell_row<REAL>(chunk_off, col, val, u_j, c, lane);
-    const int64_t r = c * 32 + lane;
-    if (r < n) {
-      double2 wr;
-      if (FOLD) {
-        if (HAS_PREV) {
-          double2 up = u_jm1[r];
-          wr.x = fma(cw, up.x, y.y);
-          wr.y = fma(cw, up.y, -y.x);
-        } else {
-          wr.x = y.y;
-          wr.y = -y.x;
-        }
-      } else if (HAS_PREV) {
-        double2 up = u_jm1[r];
-        wr.x = fma(cw, up.x, g * y.y);
-        wr.y = fma(cw, up.y, -g * y.x);
-      } else {
-        wr.x = g * y.y;
-        wr.y = -g * y.x;
-      }
-      w[r] = wr;
-      double2 uj = u_j[r];
-      // conj(u_j) * w
-      acc[0] = fma(uj.x, wr.x, fma(uj.y, wr.y, acc[0]));
-      acc[1] = fma(uj.x, wr.y, fma(-uj.y, wr.x, acc[1]));
+  if (K == 1) {
+    const int64_t c_end = warp_chunk[wid + 1];
+    for (int64_t c = warp_chunk[wid]; c < c_end; ++c) {
+      const double2 y = te_sell_row<REAL>(chunk_off, col, val, u_j, c, lane);
+      const int64_t r = c * 32 + lane;
+      if (r < n) apply_row_epilogue<HAS_PREV, FOLD>(r, y, g, cw, u_j, u_jm1, w, acc);
+    }
+  } else {
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t u = wid; u < n_chunks * K; u += warps) {
+      const int64_t c = u / K;
+      const int part = (int)(u - c * K);
+      const double2 y = te_sell_row_k<REAL, K>(chunk_off, col, val, u_j, c, part, lane);
+      const int64_t r = c * 32 + part * (32 / K) + lane / K;
+      if (lane % K == 0 && r < n) apply_row_epilogue<HAS_PREV, FOLD>(r, y, g, cw, u_j, u_jm1, w, acc);
     }
   }
   te_block_sum<2>(acc, scratch);
@@ -329,30 +354,131 @@ void te_launch_gs_update_norm(int64_t n, const TeBasisPtrs& V, int nvec, const d
                                                                                 j);
 }
 
+namespace {
+
+using ApplyKernel = void (*)(int64_t, int64_t, const int32_t*, const int64_t*, const int32_t*, const double*,
+                             const double2*, const double2*, double2*, TeDevState*, double*, int);
+
+template <int K>
+ApplyKernel apply_kernel_for(bool is_real, bool has_prev, bool fold) {
+  static const ApplyKernel table[2][2][2] = {
+      {{lanczos_apply_kernel<false, false, false, K>, lanczos_apply_kernel<false, false, true, K>},
+       {lanczos_apply_kernel<false, true, false, K>, lanczos_apply_kernel<false, true, true, K>}},
+      {{lanczos_apply_kernel<true, false, false, K>, lanczos_apply_kernel<true, false, true, K>},
+       {lanczos_apply_kernel<true, true, false, K>, lanczos_apply_kernel<true, true, true, K>}}};
+  return table[is_real ? 1 : 0][has_prev ? 1 : 0][fold ? 1 : 0];
+}
+
+ApplyKernel apply_kernel(int lanes, bool is_real, bool has_prev, bool fold) {
+  switch (lanes) {
+    case 2: return apply_kernel_for<2>(is_real, has_prev, fold);
+    case 4: return apply_kernel_for<4>(is_real, has_prev, fold);
+    default: return apply_kernel_for<1>(is_real, has_prev, fold);
+  }
+}
+
+// Blocks of the apply kernel for K > 1: one warp per (chunk, part) unit, at
+// most one resident wave.
+int apply_grid_k(const TeSell& A, int lanes, ApplyKernel k) {
+  const int64_t units = A.n_chunks * lanes;
+  const int64_t cap = (int64_t)te_num_sms() * te_kernel_blocks_per_sm((const void*)k, TE_THREADS, 0);
+  return (int)std::max<int64_t>(1, std::min<int64_t>((units + 7) / 8, cap));
+}
+
+}  // namespace
+
 int te_sell_blocks_per_sm(bool is_real) {
-  const void* k[4] = {
-      is_real ? (const void*)lanczos_apply_kernel<true, true, true> : (const void*)lanczos_apply_kernel<false, true, true>,
-      is_real ? (const void*)lanczos_apply_kernel<true, false, true> : (const void*)lanczos_apply_kernel<false, false, true>,
-      is_real ? (const void*)lanczos_apply_kernel<true, true, false> : (const void*)lanczos_apply_kernel<false, true, false>,
-      is_real ? (const void*)lanczos_apply_kernel<true, false, false>
-              : (const void*)lanczos_apply_kernel<false, false, false>};
   int b = 8;
-  for (const void* f : k) b = std::min(b, te_kernel_blocks_per_sm(f, TE_THREADS, 0));
+  for (int hp = 0; hp < 2; ++hp)
+    for (int f = 0; f < 2; ++f)
+      b = std::min(b, te_kernel_blocks_per_sm((const void*)apply_kernel(1, is_real, hp, f), TE_THREADS, 0));
   return b;
 }
 
 void te_launch_lanczos_apply(const TeSell& A, bool is_real, const double2* u_j, const double2* u_jm1, double2* w,
                              TeDevState* ds, double* partials, int j, bool fold, cudaStream_t st) {
-  using K = void (*)(int64_t, const int32_t*, const int64_t*, const int32_t*, const double*, const double2*,
-                     const double2*, double2*, TeDevState*, double*, int);
-  static const K table[2][2][2] = {
-      {{lanczos_apply_kernel<false, false, false>, lanczos_apply_kernel<false, false, true>},
-       {lanczos_apply_kernel<false, true, false>, lanczos_apply_kernel<false, true, true>}},
-      {{lanczos_apply_kernel<true, false, false>, lanczos_apply_kernel<true, false, true>},
-       {lanczos_apply_kernel<true, true, false>, lanczos_apply_kernel<true, true, true>}}};
-  const K k = table[is_real ? 1 : 0][u_jm1 ? 1 : 0][fold ? 1 : 0];
-  te_launch_pdl(A.saturated, k, A.grid, TE_THREADS, st, A.n, A.warp_chunk, A.chunk_off, A.col, A.val, u_j, u_jm1, w,
-                ds, partials, j);
+  const int lanes = A.lanes;
+  const ApplyKernel k = apply_kernel(lanes, is_real, u_jm1 != nullptr, fold);
+  const int grid = lanes == 1 ? A.grid : apply_grid_k(A, lanes, k);
+  te_launch_pdl(lanes == 1 && A.saturated, k, grid, TE_THREADS, st, A.n, A.n_chunks, A.warp_chunk, A.chunk_off,
+                A.col, A.val, u_j, u_jm1, w, ds, partials, j);
+}
+
+// Autotuning of the lanes per row: time the three-term apply pass (the
+// dominant kernel) for K = 1, 2, 4 on the matrix itself, with scratch vectors
+// and a scratch state, and keep K > 1 only when it is clearly (> 10%) faster,
+// so that the choice -- which changes the rounding of the row sums -- is
+// stable from run to run.  Matrices that give every resident warp at least 8
+// chunks keep K = 1 without timing.
+int te_tune_sell_lanes(te_matrix_s* A) {
+  TeSell& S = A->sell;
+  if (S.lanes_fixed) return TE_OK;
+  const int64_t resident_warps = (int64_t)te_num_sms() * te_sell_blocks_per_sm(A->is_real) * (TE_THREADS / 32);
+  S.lanes = 1;
+  if (S.n_chunks >= 8 * resident_warps) {
+    S.lanes_fixed = true;
+    return TE_OK;
+  }
+  const int64_t n = S.n;
+  double2 *x = nullptr, *xp = nullptr, *w = nullptr;
+  double* partials = nullptr;
+  TeDevState* ds = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  auto cleanup = [&]() {
+    cudaFree(x);
+    cudaFree(xp);
+    cudaFree(w);
+    cudaFree(partials);
+    cudaFree(ds);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+  };
+  int rc = TE_OK;
+  if ((rc = te_cuda_check(cudaMalloc(&x, sizeof(double2) * n), "tune")) == TE_OK &&
+      (rc = te_cuda_check(cudaMalloc(&xp, sizeof(double2) * n), "tune")) == TE_OK &&
+      (rc = te_cuda_check(cudaMalloc(&w, sizeof(double2) * n), "tune")) == TE_OK &&
+      (rc = te_cuda_check(cudaMalloc(&partials, sizeof(double) * 2 * 8 * 4096), "tune")) == TE_OK &&
+      (rc = te_cuda_check(cudaMalloc(&ds, sizeof(TeDevState)), "tune")) == TE_OK &&
+      (rc = te_cuda_check(cudaEventCreate(&e0), "tune")) == TE_OK &&
+      (rc = te_cuda_check(cudaEventCreate(&e1), "tune")) == TE_OK) {
+    TeDevState* hs = new TeDevState();
+    std::memset(hs, 0, sizeof(TeDevState));
+    hs->exp_factor = 1.0;
+    hs->inv_exp_factor = 1.0;
+    hs->m_cur = 2;
+    hs->s[0] = hs->s[1] = 1.0;
+    hs->beta[1] = 1.0;
+    rc = te_cuda_check(cudaMemcpy(ds, hs, sizeof(TeDevState), cudaMemcpyHostToDevice), "tune");
+    delete hs;
+    if (rc == TE_OK) rc = te_cuda_check(cudaMemset(x, 0, sizeof(double2) * n), "tune");
+    if (rc == TE_OK) rc = te_cuda_check(cudaMemset(xp, 0, sizeof(double2) * n), "tune");
+  }
+  float best[3] = {0, 0, 0};
+  const int cand[3] = {1, 2, 4};
+  for (int v = 0; v < 3 && rc == TE_OK; ++v) {
+    S.lanes = cand[v];
+    float t_min = 1e30f;
+    for (int rep = 0; rep < 6 && rc == TE_OK; ++rep) {
+      cudaEventRecord(e0, 0);
+      te_launch_lanczos_apply(S, A->is_real, x, xp, w, ds, partials, 1, true, 0);
+      cudaEventRecord(e1, 0);
+      rc = te_cuda_check(cudaEventSynchronize(e1), "tune");
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) t_min = std::min(t_min, ms);  // the first launch warms the caches
+    }
+    best[v] = t_min;
+  }
+  cleanup();
+  S.lanes = 1;
+  if (rc != TE_OK) return rc;
+  int pick = 0;
+  for (int v = 1; v < 3; ++v)
+    if (best[v] < best[pick]) pick = v;
+  if (pick != 0 && best[pick] > 0.9f * best[0]) pick = 0;
+  S.lanes = cand[pick];
+  S.lanes_fixed = true;
+  return TE_OK;
 }
 
 void te_launch_lanczos_update(int64_t n, const double2* w, const double2* u_j, double2* u_jp1, TeDevState* ds,

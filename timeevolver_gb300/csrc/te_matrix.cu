@@ -26,8 +26,11 @@
 
 // ---------------------------------------------------------------- kernels
 
-template <bool REAL>
-__global__ void __launch_bounds__(TE_THREADS) sell_spmv_kernel(int64_t n, const int32_t* __restrict__ warp_chunk,
+// K lanes per row as in lanczos_apply_kernel: K = 1 follows the static chunk
+// schedule, K = 2, 4 stride over (chunk, part) units.
+template <bool REAL, int K>
+__global__ void __launch_bounds__(TE_THREADS) sell_spmv_kernel(int64_t n, int64_t n_chunks,
+                                                               const int32_t* __restrict__ warp_chunk,
                                                                const int64_t* __restrict__ chunk_off,
                                                                const int32_t* __restrict__ col,
                                                                const double* __restrict__ val, double2 alpha,
@@ -35,11 +38,23 @@ __global__ void __launch_bounds__(TE_THREADS) sell_spmv_kernel(int64_t n, const 
                                                                double2* __restrict__ y) {
   const int lane = threadIdx.x & 31;
   const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int64_t c_end = warp_chunk[wid + 1];
-  for (int64_t c = warp_chunk[wid]; c < c_end; ++c) {
-    double2 acc = te_sell_row<REAL>(chunk_off, col, val, x, c, lane);
-    int64_t r = c * 32 + lane;
-    if (r < n) y[r] = make_double2(alpha.x * acc.x - alpha.y * acc.y, alpha.x * acc.y + alpha.y * acc.x);
+  if (K == 1) {
+    const int64_t c_end = warp_chunk[wid + 1];
+    for (int64_t c = warp_chunk[wid]; c < c_end; ++c) {
+      double2 acc = te_sell_row<REAL>(chunk_off, col, val, x, c, lane);
+      int64_t r = c * 32 + lane;
+      if (r < n) y[r] = make_double2(alpha.x * acc.x - alpha.y * acc.y, alpha.x * acc.y + alpha.y * acc.x);
+    }
+  } else {
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t u = wid; u < n_chunks * K; u += warps) {
+      const int64_t c = u / K;
+      const int part = (int)(u - c * K);
+      const double2 acc = te_sell_row_k<REAL, K>(chunk_off, col, val, x, c, part, lane);
+      const int64_t r = c * 32 + part * (32 / K) + lane / K;
+      if (lane % K == 0 && r < n)
+        y[r] = make_double2(alpha.x * acc.x - alpha.y * acc.y, alpha.x * acc.y + alpha.y * acc.x);
+    }
   }
 }
 
@@ -64,12 +79,18 @@ __global__ void permute_kernel(int64_t n, const int32_t* __restrict__ idx, const
 
 void te_launch_sell_spmv(const TeSell& A, bool is_real, double2 alpha, const double2* x_perm, double2* y_perm,
                          cudaStream_t st) {
-  if (is_real)
-    sell_spmv_kernel<true><<<A.grid, TE_THREADS, 0, st>>>(A.n, A.warp_chunk, A.chunk_off, A.col, A.val, alpha, x_perm,
-                                                        y_perm);
-  else
-    sell_spmv_kernel<false><<<A.grid, TE_THREADS, 0, st>>>(A.n, A.warp_chunk, A.chunk_off, A.col, A.val, alpha, x_perm,
-                                                         y_perm);
+  using K = void (*)(int64_t, int64_t, const int32_t*, const int64_t*, const int32_t*, const double*, double2,
+                     const double2*, double2*);
+  static const K table[2][3] = {{sell_spmv_kernel<false, 1>, sell_spmv_kernel<false, 2>, sell_spmv_kernel<false, 4>},
+                                {sell_spmv_kernel<true, 1>, sell_spmv_kernel<true, 2>, sell_spmv_kernel<true, 4>}};
+  const int li = A.lanes == 4 ? 2 : A.lanes == 2 ? 1 : 0;
+  const K k = table[is_real ? 1 : 0][li];
+  int grid = A.grid;
+  if (A.lanes > 1) {
+    const int64_t cap = (int64_t)te_num_sms() * te_kernel_blocks_per_sm((const void*)k, TE_THREADS, 0);
+    grid = (int)std::max<int64_t>(1, std::min<int64_t>((A.n_chunks * A.lanes + 7) / 8, cap));
+  }
+  k<<<grid, TE_THREADS, 0, st>>>(A.n, A.n_chunks, A.warp_chunk, A.chunk_off, A.col, A.val, alpha, x_perm, y_perm);
 }
 
 void te_launch_csr_spmv(const te_matrix_s& A, double2 alpha, const double2* x, double2* y, cudaStream_t st) {
@@ -282,8 +303,8 @@ int sell_layout(te_matrix_s* M, const std::vector<int32_t>& rp, bool real, std::
   if ((rc = upload(&S.perm, perm.data(), perm.size())) != TE_OK) return rc;
   if ((rc = upload(&S.iperm, iperm.data(), iperm.size())) != TE_OK) return rc;
   const int bps = std::min(te_sell_blocks_per_sm(real),
-                           te_kernel_blocks_per_sm(real ? (const void*)sell_spmv_kernel<true>
-                                                        : (const void*)sell_spmv_kernel<false>,
+                           te_kernel_blocks_per_sm(real ? (const void*)sell_spmv_kernel<true, 1>
+                                                        : (const void*)sell_spmv_kernel<false, 1>,
                                                    TE_THREADS, 0));
   const int64_t need = (S.n_chunks * 32 + TE_THREADS - 1) / TE_THREADS;
   S.grid = (int)std::min<int64_t>(need, (int64_t)te_num_sms() * bps);
@@ -788,6 +809,28 @@ extern "C" int te_matrix_download_csr(te_matrix A, int32_t* row_ptr, int32_t* co
     TE_CUDA(cudaMemcpy(values, A->val, sizeof(double2) * nnz, cudaMemcpyDeviceToHost));
   }
   return TE_OK;
+}
+
+extern "C" int te_matrix_set_spmv_lanes(te_matrix A, int lanes) {
+  if (!A || A->n_rows != A->n_cols || !(lanes == 0 || lanes == 1 || lanes == 2 || lanes == 4)) {
+    te_set_error("te_matrix_set_spmv_lanes: square matrix and lanes 0 (tune), 1, 2 or 4 required");
+    return TE_ERR_INVALID_ARG;
+  }
+  A->sell.lanes = lanes == 0 ? 1 : lanes;
+  A->sell.lanes_fixed = lanes != 0;
+  return TE_OK;
+}
+
+extern "C" int te_matrix_spmv_lanes(te_matrix A, int tune_now) {
+  if (!A || A->n_rows != A->n_cols) {
+    te_set_error("te_matrix_spmv_lanes: square matrix required");
+    return TE_ERR_INVALID_ARG;
+  }
+  if (tune_now) {
+    int rc = te_tune_sell_lanes(A);
+    if (rc != TE_OK) return rc;
+  }
+  return A->sell.lanes;
 }
 
 extern "C" int te_matrix_destroy(te_matrix A) {

@@ -61,3 +61,57 @@ __device__ __forceinline__ double2 te_sell_row(const int64_t* __restrict__ chunk
   }
   return make_double2(re, im);
 }
+
+// K lanes per row (K = 2 or 4), for matrices too small to fill the GPU with
+// one lane per row: a warp owns the part-th group of 32/K rows of a chunk;
+// lane l works on row part * (32/K) + l/K and takes that row's entries
+// k = l%K, l%K + K, ...; the K partial sums are combined by xor shuffles, so
+// every lane of the row ends with the same value.  The entries are summed in
+// a different order than te_sell_row (interleaved by K): results differ from
+// the K = 1 kernel by rounding only.
+template <bool REAL, int K>
+__device__ __forceinline__ double2 te_sell_row_k(const int64_t* __restrict__ chunk_off,
+                                                 const int32_t* __restrict__ col, const double* __restrict__ val,
+                                                 const double2* __restrict__ x, int64_t chunk, int part, int lane) {
+  const int64_t off = __ldg(chunk_off + chunk);
+  const int64_t len = (__ldg(chunk_off + chunk + 1) - off) >> 5;
+  const int rloc = part * (32 / K) + lane / K;
+  double re = 0.0, im = 0.0;
+  int64_t k = lane % K;
+  if (REAL) {
+    for (; k + K < len; k += 2 * K) {
+      const int64_t s0 = off + 32 * k + rloc, s1 = s0 + 32 * K;
+      const int32_t c0 = __ldcs(col + s0), c1 = __ldcs(col + s1);
+      const double a0 = __ldcs(val + s0), a1 = __ldcs(val + s1);
+      const double2 x0 = __ldg(x + c0), x1 = __ldg(x + c1);
+      re = fma(a0, x0.x, re);
+      im = fma(a0, x0.y, im);
+      re = fma(a1, x1.x, re);
+      im = fma(a1, x1.y, im);
+    }
+    for (; k < len; k += K) {
+      const int64_t s = off + 32 * k + rloc;
+      const double a = __ldcs(val + s);
+      const double2 xv = __ldg(x + __ldcs(col + s));
+      re = fma(a, xv.x, re);
+      im = fma(a, xv.y, im);
+    }
+  } else {
+    const double2* __restrict__ v2 = reinterpret_cast<const double2*>(val);
+    for (; k < len; k += K) {
+      const int64_t s = off + 32 * k + rloc;
+      const double2 a = __ldcs(v2 + s);
+      const double2 xv = __ldg(x + __ldcs(col + s));
+      re = fma(a.x, xv.x, re);
+      re = fma(-a.y, xv.y, re);
+      im = fma(a.x, xv.y, im);
+      im = fma(a.y, xv.x, im);
+    }
+  }
+#pragma unroll
+  for (int o = 1; o < K; o <<= 1) {
+    re += __shfl_xor_sync(0xffffffffu, re, o);
+    im += __shfl_xor_sync(0xffffffffu, im, o);
+  }
+  return make_double2(re, im);
+}

@@ -233,6 +233,17 @@ int te_evolver_trace(te_evolver ev, te_step_record* out, int64_t max_records, in
 /* Kernel launches issued by the last te_evolver_run (for launch accounting). */
 int64_t te_evolver_launch_count(te_evolver ev);
 
+/* Evolver options (no counterpart in the reference).
+ * TE_OPT_FUSED_LANCZOS: run the three-term Lanczos iterations of a Krylov step
+ * as one persistent cooperative kernel with grid barriers instead of two
+ * launches per iteration (same step sequence; the norm sums round
+ * differently).  0: never; 1 (default): for matrices of fewer than 2048
+ * 32-row chunks, where launch costs dominate (measured on GB300: 20% faster
+ * at dim 6435, equal at dim 92378, slower from dim 352716); 2: always, where
+ * a cooperative launch of the matrix's schedule is possible. */
+#define TE_OPT_FUSED_LANCZOS 1
+int te_evolver_set_option(te_evolver ev, int option, int value);
+
 /* Prepare another run of the same evolution (same H, parameters and
  * observables, device buffers reused) from the start vector v (complex n):
  * v_is_device != 0 reads v from device memory, else from host memory.  No

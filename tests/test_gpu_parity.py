@@ -278,3 +278,28 @@ def test_spmv_lanes_tuning(te_gpu):
     k = M.spmv_lanes(tune=True)
     assert k in (1, 2, 4)
     assert M.spmv_lanes(tune=True) == k  # tuned once
+
+
+@pytest.mark.parametrize("L,t,sampling", [(8, 10.0, 0.1), (11, 2.0, 0.5)])
+def test_fused_and_per_iteration_lanczos_agree(te_gpu, oracle_lib, L, t, sampling):
+    """The persistent Lanczos kernel and the per-iteration passes: same step
+    sequence and status, states within the Krylov truncation error, and both
+    within the bounds against the oracle."""
+    states, H = models.bose_hubbard(L, L, 1.0, 2.0)
+    n = len(states)
+    v = _fock(states, [L] + [0] * (L - 1))
+    O = models.create_matrix([models.number_operator(0, 1.0)], states)
+    M = te_gpu.Matrix.from_coo(n, H)
+    Om = te_gpu.Matrix.from_coo(n, O)
+    out = {}
+    for fused in (2, 0):  # always fused / never fused
+        ev = te_gpu.Evolver(M, v, t, sampling, [("sparse", Om)], tol=1e-8, m=40)
+        ev.set_option(te_gpu.OPT_FUSED_LANCZOS, fused)
+        out[fused] = ev.time_evolve()
+        ev.close()
+    a, b = out[2], out[0]
+    assert a["n_steps"] == b["n_steps"] and a["status"] == b["status"] and a["num_samples"] == b["num_samples"]
+    assert np.linalg.norm(a["state"] - b["state"]) < 2e-8
+    ref = oracle_lib.evolve(H, v, t, sampling, [("sparse", O)], tol=1e-8, m=40)
+    for r in (a, b):
+        _compare(r, ref, 1e-8, obs_norm=float(L), strict=False)

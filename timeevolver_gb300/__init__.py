@@ -95,6 +95,7 @@ SIGNATURES = {
     "te_batch_state": (_I, [_P, _I, _P]),
     "te_batch_launch_count": (_I64, [_P]),
     "te_batch_stream": (_P, [_P]),
+    "te_evolver_set_option": (_I, [_P, _I, _I]),
     "te_adjoint_create": (_I, [_I, _P, _P, _P, _D, _D, _I, _D, _I, _P]),
     "te_adjoint_destroy": (_I, [_P]),
     "te_adjoint_run": (_I, [_P, _P, _P, _P]),
@@ -156,6 +157,9 @@ def _as_u64(a):
     if a.dtype == np.int64:
         return a.view(np.uint64)
     return np.ascontiguousarray(a, dtype=np.uint64)
+
+
+OPT_FUSED_LANCZOS = 1
 
 
 class Matrix:
@@ -349,6 +353,10 @@ class Evolver:
 
     def profile(self, enable=True):
         _check(lib().te_evolver_profile(self.handle, int(enable)), "te_evolver_profile")
+
+    def set_option(self, option, value):
+        """te_evolver_set_option (e.g. OPT_FUSED_LANCZOS)."""
+        _check(lib().te_evolver_set_option(self.handle, int(option), int(value)), "te_evolver_set_option")
 
     def kernel_time(self, kind):
         ms, cnt = ctypes.c_double(), ctypes.c_int64()

@@ -64,6 +64,7 @@ struct te_evolver_s {
   double* partials = nullptr;
   double* results = nullptr;  // n_obs x n_samples
   int max_batch = 1;
+  int fused_lanczos = 1;  // TE_OPT_FUSED_LANCZOS: 0 never, 1 automatic, 2 always
   int batch_cap = 0;         // states the batch buffer holds
   size_t results_cap = 0;    // doubles the results buffer holds
   std::vector<HostObs> obs;
@@ -324,7 +325,17 @@ int run(te_evolver ev, te_result* out) {
     // STEP 1: Lanczos (:338)
     const bool cgs2 = ev->p.reorth != 0;
     const bool fold = !cgs2 && ev->p.exp_factor != 0.0;
-    for (int j = 0; j < m; ++j) {
+    bool fused = false;
+    // all m iterations in one persistent launch: measured faster than the
+    // per-iteration passes only while launch costs dominate (dim 6435: -20%;
+    // dim 92378: equal; dim >= 352716: slower), hence the automatic size rule
+    const bool want_fused = ev->fused_lanczos == 2 || (ev->fused_lanczos == 1 && ev->H->sell.n_chunks < 2048);
+    if (fold && want_fused) {
+      ProfScope ps(ev, 0);
+      fused = te_launch_lanczos_step(ev->H->sell, ev->H->is_real, ev->cols, m, ev->w, ev->ds, ev->partials, st);
+      if (fused) ++ev->launches;
+    }
+    for (int j = 0; j < m && !fused; ++j) {
       {
         ProfScope ps(ev, 0);
         te_launch_lanczos_apply(ev->H->sell, ev->H->is_real, ev->cols[j],
@@ -727,6 +738,22 @@ extern "C" int te_evolver_reset(te_evolver ev, const double* v, int v_is_device)
   te_launch_permute(n, ev->H->sell.perm, ev->orig_tmp, ev->cols[0], ev->st);
   ev->ran = false;
   return te_cuda_check(cudaGetLastError(), "te_evolver_reset");
+}
+
+extern "C" int te_evolver_set_option(te_evolver ev, int option, int value) {
+  if (!ev) return TE_ERR_INVALID_ARG;
+  switch (option) {
+    case TE_OPT_FUSED_LANCZOS:
+      if (value < 0 || value > 2) {
+        te_set_error("te_evolver_set_option: TE_OPT_FUSED_LANCZOS takes 0, 1 or 2");
+        return TE_ERR_INVALID_ARG;
+      }
+      ev->fused_lanczos = value;
+      return TE_OK;
+    default:
+      te_set_error("te_evolver_set_option: unknown option %d", option);
+      return TE_ERR_INVALID_ARG;
+  }
 }
 
 extern "C" void* te_evolver_stream(te_evolver ev) { return ev ? (void*)ev->st : nullptr; }

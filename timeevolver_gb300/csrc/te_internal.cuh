@@ -87,6 +87,8 @@ struct TeDevState {
   // 1 / expFactor (0 when expFactor is 0): the folded three-term passes use
   // beta_j^2 / expFactor^2 and alpha_j / expFactor without a division per thread
   double inv_exp_factor;
+  // grid barrier of the persistent Lanczos kernel (arrivals, generation)
+  unsigned int bar_count, bar_gen;
 };
 
 // SELL-32 matrix in the sorted (permuted) basis.
@@ -203,6 +205,13 @@ void te_launch_lanczos_apply(const TeSell& A, bool is_real, const double2* u_j, 
                              TeDevState* ds, double* partials, int j, bool fold, cudaStream_t st);
 void te_launch_lanczos_update(int64_t n, const double2* w, const double2* u_j, double2* u_jp1, TeDevState* ds,
                               double* partials, int j, bool fold, cudaStream_t st);
+// All m three-term Lanczos iterations of one Krylov step in one cooperative
+// launch (te_lanczos.cu).  Returns false (nothing launched) when the matrix's
+// static schedule does not fit the persistent kernel's residency, or the
+// device has no cooperative launch; the caller then runs the per-iteration
+// passes.  cols[j]: the basis columns of the step.
+bool te_launch_lanczos_step(const TeSell& A, bool is_real, double2* const* cols, int m, double2* w, TeDevState* ds,
+                            double* partials, cudaStream_t st);
 // Choose the lanes per row of a square matrix's SpMV passes (te_lanczos.cu).
 int te_tune_sell_lanes(te_matrix_s* A);
 // Gram-Schmidt passes of the reorthogonalising Lanczos mode (te_lanczos.cu)

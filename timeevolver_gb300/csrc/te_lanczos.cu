@@ -26,7 +26,7 @@ __device__ __forceinline__ bool te_step_inactive(const TeDevState* ds) {
 
 // The recurrence epilogue of one row r (A u_j row sum y): writes w (or the
 // folded w') and accumulates conj(u_j) w.
-template <bool HAS_PREV, bool FOLD>
+template <bool HAS_PREV, bool FOLD, bool CG = false>
 __device__ __forceinline__ void apply_row_epilogue(int64_t r, double2 y, double g, double cw,
                                                    const double2* __restrict__ u_j,
                                                    const double2* __restrict__ u_jm1, double2* __restrict__ w,
@@ -34,7 +34,7 @@ __device__ __forceinline__ void apply_row_epilogue(int64_t r, double2 y, double 
   double2 wr;
   if (FOLD) {
     if (HAS_PREV) {
-      double2 up = u_jm1[r];
+      double2 up = CG ? __ldca(u_jm1 + r) : u_jm1[r];
       wr.x = fma(cw, up.x, y.y);
       wr.y = fma(cw, up.y, -y.x);
     } else {
@@ -50,7 +50,7 @@ __device__ __forceinline__ void apply_row_epilogue(int64_t r, double2 y, double 
     wr.y = -g * y.x;
   }
   w[r] = wr;
-  double2 uj = u_j[r];
+  double2 uj = CG ? __ldca(u_j + r) : u_j[r];
   // conj(u_j) * w
   acc[0] = fma(uj.x, wr.x, fma(uj.y, wr.y, acc[0]));
   acc[1] = fma(uj.x, wr.y, fma(-uj.y, wr.x, acc[1]));
@@ -114,6 +114,212 @@ __global__ void __launch_bounds__(TE_THREADS, (REAL && K == 1) ? 6 : 5) lanczos_
     const double f = FOLD ? sj * g : sj;
     if (threadIdx.x == 0) ds->alpha[j] = make_double2(f * tot[0], f * tot[1]);
   }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent three-term Lanczos: all m iterations of a Krylov step in one
+// cooperative launch on the matrix's static chunk schedule.  Per iteration:
+//   apply (as lanczos_apply_kernel, folded) -> grid barrier -> every block sums
+//   the alpha partials in the fixed order of te_final_sum (so alpha_j is the
+//   same in every block and identical to the two-kernel path) -> update of the
+//   warp's own rows (u'_{j+1} = w' - (alpha_j / e) u_j) -> grid barrier ->
+//   every block sums the beta partials -> breakdown test, same in all blocks.
+// This removes two launches, two block ramps and two serial last-block
+// reductions per iteration, which dominate small problems.
+
+#define TE_BARRIER_SPIN_LIMIT (1u << 22)  // ~ seconds of polling; a co-resident grid arrives in microseconds
+
+struct TeLanczosArgs {
+  int64_t n;
+  const int32_t* warp_chunk;
+  const int64_t* chunk_off;
+  const int32_t* col;
+  const double* val;
+  double2* w;
+  double* partials;  // 3 * gridDim.x: alpha (re, im), beta
+  int m;
+  double2* u[TE_MMAX];
+};
+
+// Grid barrier with a bounded wait.  Arrival after a fence; the last block
+// resets the count and bumps the generation.  A wait that gives up sets
+// fatal = TE_ERR_DEVICE_TIMEOUT and returns false (the kernel then exits).
+__device__ __forceinline__ bool te_grid_barrier(unsigned int* count, unsigned int* gen, int* fatal) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    volatile unsigned int* vgen = gen;
+    const unsigned int g0 = *vgen;
+    __threadfence();
+    if (atomicAdd(count, 1u) == gridDim.x - 1) {
+      atomicExch(count, 0u);
+      __threadfence();
+      atomicAdd(gen, 1u);
+    } else {
+      unsigned int spins = 0;
+      while (*vgen == g0) {
+        __nanosleep(32);
+        if (++spins > TE_BARRIER_SPIN_LIMIT) {
+          ok = 0;
+          atomicExch(fatal, TE_ERR_DEVICE_TIMEOUT);
+          break;
+        }
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// Sum of NV partial arrays (stride gridDim.x) in the order of te_final_sum;
+// the result is returned to every thread of the block.
+template <int NV>
+__device__ __forceinline__ void te_grid_partials_sum(double (&out)[NV], const double* partials, double* scratch,
+                                                     double* bcast) {
+#pragma unroll
+  for (int k = 0; k < NV; ++k) out[k] = 0.0;
+#pragma unroll 4
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) out[k] += __ldcg(partials + k * gridDim.x + b);
+  }
+  te_block_sum<NV>(out, scratch);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) bcast[k] = out[k];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < NV; ++k) out[k] = bcast[k];
+}
+
+template <bool REAL>
+__global__ void __launch_bounds__(TE_THREADS, REAL ? 6 : 5) lanczos_step_kernel(TeLanczosArgs a, TeDevState* ds) {
+  __shared__ double scratch[2 * 32];
+  __shared__ double bcast[2];
+  if (te_step_inactive(ds)) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int64_t c_begin = a.warp_chunk[wid], c_end = a.warp_chunk[wid + 1];
+  const bool leader = blockIdx.x == 0 && threadIdx.x == 0;
+  const double e = ds->exp_factor, ie = ds->inv_exp_factor, tol_rate = ds->tol_rate;
+  const int m = min(a.m, ds->m_cur);
+  const int G = gridDim.x;
+  double sj = ds->s[0], bj = 0.0;
+  for (int j = 0; j < m; ++j) {
+    const double2* __restrict__ uj = a.u[j];
+    const double g = e * sj;
+    // apply: w' = -i H u_j + (beta_j / e)^2 u_{j-1}, partials of <u_j, w'>
+    double acc[2] = {0.0, 0.0};
+    if (j > 0) {
+      const double cw = (bj * ie) * (bj * ie);
+      const double2* __restrict__ ujm1 = a.u[j - 1];
+      for (int64_t c = c_begin; c < c_end; ++c) {
+        const double2 y = te_sell_row<REAL, true>(a.chunk_off, a.col, a.val, uj, c, lane);
+        const int64_t r = c * 32 + lane;
+        if (r < a.n) apply_row_epilogue<true, true, true>(r, y, g, cw, uj, ujm1, a.w, acc);
+      }
+    } else {
+      for (int64_t c = c_begin; c < c_end; ++c) {
+        const double2 y = te_sell_row<REAL, true>(a.chunk_off, a.col, a.val, uj, c, lane);
+        const int64_t r = c * 32 + lane;
+        if (r < a.n) apply_row_epilogue<false, true, true>(r, y, g, 0.0, uj, nullptr, a.w, acc);
+      }
+    }
+    te_block_sum<2>(acc, scratch);
+    if (threadIdx.x == 0) {
+      a.partials[blockIdx.x] = acc[0];
+      a.partials[G + blockIdx.x] = acc[1];
+    }
+    if (!te_grid_barrier(&ds->bar_count, &ds->bar_gen, &ds->fatal)) return;
+    double tot[2];
+    te_grid_partials_sum<2>(tot, a.partials, scratch, bcast);
+    const double f = sj * g;
+    const double2 alpha = make_double2(f * tot[0], f * tot[1]);
+    if (leader) ds->alpha[j] = alpha;
+    // update of this warp's rows: u'_{j+1} = w' - (alpha_j / e) u_j
+    const double gr = alpha.x * ie, gi = alpha.y * ie;
+    double2* __restrict__ ujp1 = j + 1 < m ? a.u[j + 1] : nullptr;
+    double nrm[1] = {0.0};
+    for (int64_t c = c_begin; c < c_end; ++c) {
+      const int64_t r = c * 32 + lane;
+      if (r < a.n) {
+        const double2 wv = __ldca(a.w + r);
+        const double2 u = __ldca(uj + r);
+        double2 o;
+        o.x = fma(-gr, u.x, fma(gi, u.y, wv.x));
+        o.y = fma(-gr, u.y, fma(-gi, u.x, wv.y));
+        if (ujp1) ujp1[r] = o;
+        nrm[0] = fma(o.x, o.x, fma(o.y, o.y, nrm[0]));
+      }
+    }
+    te_block_sum<1>(nrm, scratch);
+    if (threadIdx.x == 0) a.partials[2 * G + blockIdx.x] = nrm[0];
+    if (!te_grid_barrier(&ds->bar_count, &ds->bar_gen, &ds->fatal)) return;
+    double t2[1];
+    te_grid_partials_sum<1>(t2, a.partials + 2 * G, scratch, bcast);
+    const double beta = fabs(g) * sqrt(t2[0]);
+    if (beta < tol_rate) {  // lucky breakdown (:551-555)
+      if (leader) {
+        ds->breakdown = 1;
+        ds->m_eff = j + 1;
+        ds->h = beta;
+      }
+      return;
+    }
+    if (j + 1 != m) {
+      if (leader) {
+        ds->beta[j + 1] = beta;
+        ds->s[j + 1] = g / beta;
+      }
+      bj = beta;
+      sj = g / beta;
+    } else if (leader) {
+      ds->h = beta;
+      ds->m_eff = m;
+    }
+  }
+}
+
+bool te_launch_lanczos_step(const TeSell& A, bool is_real, double2* const* cols, int m, double2* w, TeDevState* ds,
+                            double* partials, cudaStream_t st) {
+  if (A.lanes != 1 || m < 1 || m > TE_MMAX) return false;
+  static int coop = -1;
+  if (coop < 0) {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrCooperativeLaunch, dev);
+    coop = v;
+  }
+  if (!coop) return false;
+  auto k = is_real ? lanczos_step_kernel<true> : lanczos_step_kernel<false>;
+  if ((int64_t)te_num_sms() * te_kernel_blocks_per_sm((const void*)k, TE_THREADS, 0) < A.grid) return false;
+  TeLanczosArgs a;
+  a.n = A.n;
+  a.warp_chunk = A.warp_chunk;
+  a.chunk_off = A.chunk_off;
+  a.col = A.col;
+  a.val = A.val;
+  a.w = w;
+  a.partials = partials;
+  a.m = m;
+  for (int j = 0; j < TE_MMAX; ++j) a.u[j] = j < m ? cols[j] : nullptr;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(A.grid);
+  cfg.blockDim = dim3(TE_THREADS);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, k, a, ds) != cudaSuccess) {
+    cudaGetLastError();  // a refused launch is not an error of the evolution: the caller falls back
+    return false;
+  }
+  return true;
 }
 
 // u_{j+1} = w - alpha_j v_j and beta_{j+1} = ||u_{j+1}||.  With a folded w'
@@ -409,13 +615,14 @@ void te_launch_lanczos_apply(const TeSell& A, bool is_real, const double2* u_j, 
 // and a scratch state, and keep K > 1 only when it is clearly (> 10%) faster,
 // so that the choice -- which changes the rounding of the row sums -- is
 // stable from run to run.  Matrices that give every resident warp at least 8
-// chunks keep K = 1 without timing.
+// chunks keep K = 1 without timing, and so do matrices of fewer than 2048
+// chunks, whose Lanczos iterations run in the persistent kernel (K = 1).
 int te_tune_sell_lanes(te_matrix_s* A) {
   TeSell& S = A->sell;
   if (S.lanes_fixed) return TE_OK;
   const int64_t resident_warps = (int64_t)te_num_sms() * te_sell_blocks_per_sm(A->is_real) * (TE_THREADS / 32);
   S.lanes = 1;
-  if (S.n_chunks >= 8 * resident_warps) {
+  if (S.n_chunks >= 8 * resident_warps || S.n_chunks < 2048) {
     S.lanes_fixed = true;
     return TE_OK;
   }

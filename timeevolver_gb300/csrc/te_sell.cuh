@@ -8,7 +8,17 @@
 #pragma once
 #include "te_internal.cuh"
 
-template <bool REAL>
+// Loads of x: through the read-only (non-coherent) cache by default; XCG
+// selects ordinary cached loads (ld.global.ca) for x written earlier in the
+// same kernel by other SMs (the persistent Lanczos kernel), which are coherent
+// after that kernel's grid barrier (release/acquire fences) where the
+// read-only path is not.
+template <bool XCG>
+__device__ __forceinline__ double2 te_load_x(const double2* __restrict__ x, int32_t c) {
+  return XCG ? __ldca(x + c) : __ldg(x + c);
+}
+
+template <bool REAL, bool XCG = false>
 __device__ __forceinline__ double2 te_sell_row(const int64_t* __restrict__ chunk_off,
                                                const int32_t* __restrict__ col, const double* __restrict__ val,
                                                const double2* __restrict__ x, int64_t chunk, int lane) {
@@ -19,7 +29,8 @@ __device__ __forceinline__ double2 te_sell_row(const int64_t* __restrict__ chunk
     for (; s + 96 < e; s += 128) {
       int32_t c0 = __ldcs(col + s), c1 = __ldcs(col + s + 32), c2 = __ldcs(col + s + 64), c3 = __ldcs(col + s + 96);
       double a0 = __ldcs(val + s), a1 = __ldcs(val + s + 32), a2 = __ldcs(val + s + 64), a3 = __ldcs(val + s + 96);
-      double2 x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
+      double2 x0 = te_load_x<XCG>(x, c0), x1 = te_load_x<XCG>(x, c1), x2 = te_load_x<XCG>(x, c2),
+              x3 = te_load_x<XCG>(x, c3);
       re = fma(a0, x0.x, re);
       im = fma(a0, x0.y, im);
       re = fma(a1, x1.x, re);
@@ -31,7 +42,7 @@ __device__ __forceinline__ double2 te_sell_row(const int64_t* __restrict__ chunk
     }
     for (; s < e; s += 32) {
       double a = __ldcs(val + s);
-      double2 xv = __ldg(x + __ldcs(col + s));
+      double2 xv = te_load_x<XCG>(x, __ldcs(col + s));
       re = fma(a, xv.x, re);
       im = fma(a, xv.y, im);
     }
@@ -40,7 +51,7 @@ __device__ __forceinline__ double2 te_sell_row(const int64_t* __restrict__ chunk
     for (; s + 32 < e; s += 64) {
       int32_t c0 = __ldcs(col + s), c1 = __ldcs(col + s + 32);
       double2 a0 = __ldcs(v2 + s), a1 = __ldcs(v2 + s + 32);
-      double2 x0 = __ldg(x + c0), x1 = __ldg(x + c1);
+      double2 x0 = te_load_x<XCG>(x, c0), x1 = te_load_x<XCG>(x, c1);
       re = fma(a0.x, x0.x, re);
       re = fma(-a0.y, x0.y, re);
       im = fma(a0.x, x0.y, im);
@@ -52,7 +63,7 @@ __device__ __forceinline__ double2 te_sell_row(const int64_t* __restrict__ chunk
     }
     for (; s < e; s += 32) {
       double2 a = __ldcs(v2 + s);
-      double2 xv = __ldg(x + __ldcs(col + s));
+      double2 xv = te_load_x<XCG>(x, __ldcs(col + s));
       re = fma(a.x, xv.x, re);
       re = fma(-a.y, xv.y, re);
       im = fma(a.x, xv.y, im);

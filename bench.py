@@ -46,13 +46,15 @@ def dist_info():
     return ws, rank, local
 
 
-def init_dist(ws, local):
+def init_dist(ws, local, backend="nccl"):
+    """One process per GPU (replicas); NCCL on the GPUs, gloo for host-only runs."""
     if ws <= 1:
         return None
     import torch
     import torch.distributed as dist
-    torch.cuda.set_device(local)
-    dist.init_process_group("nccl")
+    if backend == "nccl":
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend)
     return dist
 
 
@@ -62,12 +64,20 @@ def barrier(dist):
 
 
 def max_over_ranks(dist, x):
+    """The slowest rank's value (the timing rule for replicas)."""
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_seconds_per_solve(max_ms, steps, world_size):
+    """Whole-job seconds per solve of N replicas, each timing `steps` solves
+    (the slowest rank's time): N solves finish every max_ms / steps."""
+    return max_ms / 1000.0 / steps / world_size
 
 
 def load_peaks(te):
@@ -238,7 +248,7 @@ def run_gb300(args):
         if dist is not None:
             dist.destroy_process_group()
         return
-    value = ms / 1000.0 / args.steps / ws
+    value = replica_seconds_per_solve(ms, args.steps, ws)
     peaks = load_peaks(te)
     b_apply = apply_kernel_bytes(n, nnz, info["real"])
     f_apply = apply_kernel_flops(n, nnz, info["real"])

@@ -38,7 +38,41 @@ struct BatchGeom {
   const int32_t* inst_n;      // dimension of each instance
   const int64_t* inst_chunk;  // first chunk of each instance (n_inst + 1)
   int64_t ld;                 // leading dimension of the basis (total padded rows)
+  // chunks of the instances still running at the start of the global step
+  // (null: every chunk); late global steps, when few instances are left, then
+  // cost no more than those instances' work
+  const int32_t* active;
+  const int* active_count;
 };
+
+// The i-th chunk of a pass and the number of chunks to visit.
+__device__ __forceinline__ int64_t batch_chunk_count(const BatchGeom& g) {
+  return g.active ? (int64_t)*g.active_count : g.n_chunks;
+}
+__device__ __forceinline__ int64_t batch_chunk(const BatchGeom& g, int64_t i) {
+  return g.active ? (int64_t)__ldg(g.active + i) : i;
+}
+
+// Compact the chunks of the running instances (one thread per chunk, one
+// atomic per warp).  The order of the list does not matter: every pass writes
+// chunk-indexed partials that are reduced per instance in chunk order.
+__global__ void batch_active_kernel(int64_t n_chunks, const int32_t* __restrict__ chunk_inst,
+                                    const TeDevState* states, int32_t* active, int* count) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n_chunks; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = base + threadIdx.x;
+    bool keep = false;
+    if (c < n_chunks) {
+      const TeDevState* ds = states + chunk_inst[c];
+      keep = !ds->done && !ds->fatal;
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, keep);
+    int pos = 0;
+    if (lane == 0 && mask) pos = atomicAdd(count, __popc(mask));
+    pos = __shfl_sync(0xffffffffu, pos, 0);
+    if (keep) active[pos + __popc(mask & ((1u << lane) - 1u))] = (int32_t)c;
+  }
+}
 
 __device__ __forceinline__ bool lanczos_skip(const TeDevState* ds, int j) {
   return ds->fatal != 0 || ds->done != 0 || ds->breakdown != 0 || j >= ds->m_cur;
@@ -52,7 +86,9 @@ __global__ void __launch_bounds__(TE_THREADS) batch_apply_kernel(BatchGeom g, co
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   const double2* __restrict__ u_j = V + (int64_t)j * g.ld;
   const double2* __restrict__ u_jm1 = HAS_PREV ? V + (int64_t)(j - 1) * g.ld : nullptr;
-  for (int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < g.n_chunks; c += warps) {
+  const int64_t n_visit = batch_chunk_count(g);
+  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n_visit; i += warps) {
+    const int64_t c = batch_chunk(g, i);
     const int inst = __ldg(g.chunk_inst + c);
     const TeDevState* ds = states + inst;
     if (lanczos_skip(ds, j)) continue;
@@ -94,7 +130,9 @@ __global__ void __launch_bounds__(TE_THREADS) batch_update_kernel(BatchGeom g, d
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   const double2* __restrict__ u_j = V + (int64_t)j * g.ld;
   double2* __restrict__ u_jp1 = V + (int64_t)(j + 1) * g.ld;
-  for (int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < g.n_chunks; c += warps) {
+  const int64_t n_visit = batch_chunk_count(g);
+  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n_visit; i += warps) {
+    const int64_t c = batch_chunk(g, i);
     const int inst = __ldg(g.chunk_inst + c);
     const TeDevState* ds = states + inst;
     if (lanczos_skip(ds, j)) continue;
@@ -157,7 +195,9 @@ __global__ void __launch_bounds__(TE_THREADS) batch_new_start_kernel(BatchGeom g
                                                                      const TeDevState* states) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < g.n_chunks; c += warps) {
+  const int64_t n_visit = batch_chunk_count(g);
+  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n_visit; i += warps) {
+    const int64_t c = batch_chunk(g, i);
     const int inst = __ldg(g.chunk_inst + c);
     const TeDevState* ds = states + inst;
     if (!ds->new_start || ds->fatal || ds->done) continue;
@@ -204,7 +244,9 @@ __global__ void __launch_bounds__(TE_THREADS) batch_combine_kernel(BatchGeom g, 
                                                                    const TeDevState* states, int m_override) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t c = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); c < g.n_chunks; c += warps) {
+  const int64_t n_visit = batch_chunk_count(g);
+  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n_visit; i += warps) {
+    const int64_t c = batch_chunk(g, i);
     const int inst = __ldg(g.chunk_inst + c);
     const TeDevState* ds = states + inst;
     if (ds->fatal) continue;
@@ -330,6 +372,8 @@ struct te_batch_s {
   double* results = nullptr;
   int* d_flags = nullptr;
   int* h_flags = nullptr;  // pinned
+  int32_t* d_active = nullptr;  // chunks of the running instances
+  int* d_active_count = nullptr;
   std::vector<int> nobs;
   std::vector<int64_t> result_off;
   cudaGraphExec_t g_step = nullptr, g_batch = nullptr;
@@ -350,6 +394,15 @@ BatchGeom geom(const te_batch_s* b) {
   g.inst_n = b->d_inst_n;
   g.inst_chunk = b->d_inst_chunk;
   g.ld = b->ld;
+  g.active = b->d_active;
+  g.active_count = b->d_active_count;
+  return g;
+}
+
+BatchGeom geom_all_chunks(const te_batch_s* b) {
+  BatchGeom g = geom(b);
+  g.active = nullptr;
+  g.active_count = nullptr;
   return g;
 }
 
@@ -377,6 +430,8 @@ void free_batch(te_batch b) {
   cudaFree(b->results);
   cudaFree(b->d_flags);
   cudaFreeHost(b->h_flags);
+  cudaFree(b->d_active);
+  cudaFree(b->d_active_count);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
 }
@@ -398,6 +453,9 @@ int enqueue_step(te_batch b, bool full_step) {
   const int gc = grid_chunks(b);
   int64_t k = 0;
   if (full_step) {
+    TE_CUDA(cudaMemsetAsync(b->d_active_count, 0, sizeof(int), st));
+    batch_active_kernel<<<te_grid_fit((const void*)batch_active_kernel, b->n_chunks, 256), 256, 0, st>>>(
+        b->n_chunks, b->d_chunk_inst, b->ds, b->d_active, b->d_active_count);
     batch_new_start_kernel<<<gc, TE_THREADS, 0, st>>>(g, b->V, b->spare, b->ds);
     batch_clear_start_kernel<<<(b->B + 255) / 256, 256, 0, st>>>(b->ds, b->B);
     k += 2;
@@ -432,7 +490,7 @@ int enqueue_step(te_batch b, bool full_step) {
 }
 
 int64_t kernels_per_replay(const te_batch_s* b, bool full_step) {
-  return (full_step ? 2 + 4 * (int64_t)b->m_max : 0) + 4;
+  return (full_step ? 3 + 4 * (int64_t)b->m_max : 0) + 4;
 }
 
 int capture(te_batch b, bool full_step, cudaGraphExec_t* exec) {
@@ -451,7 +509,7 @@ int capture(te_batch b, bool full_step, cudaGraphExec_t* exec) {
 }
 
 int reset_states(te_batch b) {
-  const BatchGeom g = geom(b);
+  const BatchGeom g = geom_all_chunks(b);
   std::vector<TeDevState> hs(b->B);
   for (int i = 0; i < b->B; ++i) {
     TeDevState& s = hs[i];
@@ -616,6 +674,8 @@ extern "C" int te_batch_create(int n_instances, const te_matrix* H, const double
   if ((rc = alloc((void**)&b->d_nobs, sizeof(int) * n_instances)) != TE_OK) return fail(rc);
   if ((rc = alloc((void**)&b->d_result_off, sizeof(int64_t) * n_instances)) != TE_OK) return fail(rc);
   if ((rc = alloc((void**)&b->d_flags, sizeof(int) * n_instances)) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_active, sizeof(int32_t) * std::max<int64_t>(chunks, 1))) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_active_count, sizeof(int))) != TE_OK) return fail(rc);
   TE_CUDA(cudaMallocHost(&b->h_flags, sizeof(int) * n_instances));
   TE_CUDA(cudaMemsetAsync(b->V, 0, sizeof(double2) * ld * b->m_max, st));
   TE_CUDA(cudaMemsetAsync(b->spare, 0, sizeof(double2) * ld, st));

@@ -8,8 +8,9 @@
 //     all instances; a chunk of 32 rows never straddles two instances, so a warp
 //     always works for one instance and reads its scalars once;
 //   * each Lanczos iteration is one apply pass and one update pass over every
-//     active instance's rows, each followed by a per-instance reduction of
-//     per-chunk partials in a fixed order (deterministic);
+//     active instance's rows on a per-step warp schedule of equal FP64 cost,
+//     each followed by a per-instance reduction of per-(warp, instance)
+//     partials in a fixed order (deterministic);
 //   * the Krylov-space work (exponential, error integrals, step size, sample
 //     schedule) runs one thread block per instance;
 //   * the whole sequence of one global step (4 m_max Lanczos kernels, Krylov
@@ -54,8 +55,8 @@ __device__ __forceinline__ int64_t batch_chunk(const BatchGeom& g, int64_t i) {
 }
 
 // Compact the chunks of the running instances (one thread per chunk, one
-// atomic per warp).  The order of the list does not matter: every pass writes
-// chunk-indexed partials that are reduced per instance in chunk order.
+// atomic per warp) for the once-per-step passes (new start vector, combine).
+// The order of the list does not matter: those passes write rows, not sums.
 __global__ void batch_active_kernel(int64_t n_chunks, const int32_t* __restrict__ chunk_inst,
                                     const TeDevState* states, int32_t* active, int* count) {
   const int lane = threadIdx.x & 31;
@@ -78,103 +79,259 @@ __device__ __forceinline__ bool lanczos_skip(const TeDevState* ds, int j) {
   return ds->fatal != 0 || ds->done != 0 || ds->breakdown != 0 || j >= ds->m_cur;
 }
 
+// ---------------------------------------------------------------------------
+// Lanczos passes over the segmented layout.
+//
+// A schedule, recomputed on the device at the start of every global step,
+// gives warp w the contiguous chunk range [warp_begin[w], warp_begin[w + 1])
+// of equal FP64 cost over the running instances (finished instances inside a
+// range are skipped whole).  A warp accumulates per lane across the chunks of
+// one instance and reduces once per (warp, instance) segment; segment s of
+// instance i goes to slot seg_base[i] + (w - inst_w0[i]), so the per-instance
+// sum runs over consecutive slots in a fixed order (deterministic).  The
+// recurrence is folded as in the single-instance passes: the apply pass
+// stores w' = w / (e s_j), the update forms u'_{j+1} = w' - (alpha_j / e) u_j
+// and sets s_{j+1} = e s_j / beta_{j+1}.
+
+struct BatchSched {
+  const int32_t* warp_begin;  // W + 1 global chunk indices
+  const int32_t* inst_w0;     // first warp covering each instance
+  const int32_t* inst_nseg;   // segments (warps) covering each running instance, 0 otherwise
+  const int32_t* seg_base;    // first segment slot of each instance
+  const int32_t* next_run;    // the next running instance after each instance (n_inst: none)
+};
+
+// Where a warp continues after the chunks of instance inst that it must skip:
+// past every finished instance at once, or past this instance only.
+__device__ __forceinline__ int64_t batch_skip_to(const BatchGeom& g, const BatchSched& sc, const TeDevState* ds,
+                                                 int inst, int64_t cend) {
+  const int64_t nxt = (ds->done || ds->fatal) ? (int64_t)g.inst_chunk[sc.next_run[inst]]
+                                              : (int64_t)g.inst_chunk[inst + 1];
+  return min(nxt, cend);
+}
+
+// One block: per-instance costs, warp boundaries by binary search, segment bases.
+__global__ void __launch_bounds__(1024) batch_schedule_kernel(BatchGeom g, const TeDevState* states, int n_inst,
+                                                              int n_warps, double w_slot, double* inst_cost,
+                                                              int32_t* warp_begin, int32_t* inst_w0,
+                                                              int32_t* inst_nseg, int32_t* seg_base,
+                                                              int32_t* next_run) {
+  const double w_chunk = 8.0 * 32.0;
+  __shared__ double total;
+  for (int i = threadIdx.x; i < n_inst; i += blockDim.x) {
+    const TeDevState& d = states[i];
+    const int64_t c0 = g.inst_chunk[i], c1 = g.inst_chunk[i + 1];
+    const bool run = !d.done && !d.fatal;
+    inst_cost[i + 1] = run ? w_slot * (double)(g.chunk_off[c1] - g.chunk_off[c0]) + w_chunk * (double)(c1 - c0) : 0.0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {  // exclusive prefix over instances (n_inst is small)
+    inst_cost[0] = 0.0;
+    for (int i = 0; i < n_inst; ++i) inst_cost[i + 1] += inst_cost[i];
+    total = inst_cost[n_inst];
+  }
+  __syncthreads();
+  for (int w = threadIdx.x; w <= n_warps; w += blockDim.x) {
+    int32_t c;
+    const double target = total * (double)w / (double)n_warps;
+    if (w == n_warps || !(total > 0.0)) {
+      c = (int32_t)g.n_chunks;
+    } else {
+      int lo = 0, hi = n_inst - 1;  // instance k: inst_cost[k] <= target < inst_cost[k + 1]
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (inst_cost[mid] <= target)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      int k = lo;
+      while (k < n_inst - 1 && !(inst_cost[k + 1] > target)) ++k;  // step over empty (finished) instances
+      const double rem = target - inst_cost[k];
+      const int64_t c0 = g.inst_chunk[k], c1 = g.inst_chunk[k + 1];
+      int64_t a = c0, b = c1;  // first chunk whose cost prefix within the instance reaches rem
+      while (a < b) {
+        const int64_t mid = (a + b) >> 1;
+        const double cm = w_slot * (double)(g.chunk_off[mid] - g.chunk_off[c0]) + w_chunk * (double)(mid - c0);
+        if (cm < rem)
+          a = mid + 1;
+        else
+          b = mid;
+      }
+      c = (int32_t)a;
+    }
+    warp_begin[w] = c;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n_inst; i += blockDim.x) {
+    const TeDevState& d = states[i];
+    const int64_t c0 = g.inst_chunk[i], c1 = g.inst_chunk[i + 1];
+    int nseg = 0, w0 = 0;
+    if (!d.done && !d.fatal && c1 > c0) {
+      auto last_warp_at_or_before = [&](int64_t c) {  // last w with warp_begin[w] <= c
+        int lo = 0, hi = n_warps;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (warp_begin[mid] <= c)
+            lo = mid;
+          else
+            hi = mid - 1;
+        }
+        return lo;
+      };
+      w0 = last_warp_at_or_before(c0);
+      nseg = last_warp_at_or_before(c1 - 1) - w0 + 1;
+    }
+    inst_w0[i] = w0;
+    inst_nseg[i] = nseg;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int32_t base = 0;
+    for (int i = 0; i < n_inst; ++i) {
+      seg_base[i] = base;
+      base += inst_nseg[i];
+    }
+  } else if (threadIdx.x == 32) {
+    int32_t nxt = n_inst;  // next running instance after i
+    for (int i = n_inst - 1; i >= 0; --i) {
+      next_run[i] = nxt;
+      if (!states[i].done && !states[i].fatal) nxt = i;
+    }
+  }
+}
+
 template <bool REAL, bool HAS_PREV>
-__global__ void __launch_bounds__(TE_THREADS) batch_apply_kernel(BatchGeom g, const double2* __restrict__ V,
+__global__ void __launch_bounds__(TE_THREADS, REAL ? 6 : 5) batch_apply_kernel(BatchGeom g, BatchSched sc,
+                                                                 const double2* __restrict__ V,
                                                                  double2* __restrict__ w, TeDevState* states,
-                                                                 double* chunk_partials, int j) {
+                                                                 double* seg_partials, int j) {
   const int lane = threadIdx.x & 31;
-  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const double2* __restrict__ u_j = V + (int64_t)j * g.ld;
   const double2* __restrict__ u_jm1 = HAS_PREV ? V + (int64_t)(j - 1) * g.ld : nullptr;
-  const int64_t n_visit = batch_chunk_count(g);
-  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n_visit; i += warps) {
-    const int64_t c = batch_chunk(g, i);
+  int64_t c = sc.warp_begin[wid];
+  const int64_t cend = sc.warp_begin[wid + 1];
+  while (c < cend) {
     const int inst = __ldg(g.chunk_inst + c);
     const TeDevState* ds = states + inst;
-    if (lanczos_skip(ds, j)) continue;
+    const int64_t c1 = min((int64_t)__ldg(g.inst_chunk + inst + 1), cend);
+    if (lanczos_skip(ds, j)) {
+      c = batch_skip_to(g, sc, ds, inst, cend);
+      continue;
+    }
     const double sj = ds->s[j];
     const double gg = ds->exp_factor * sj;
-    const double cprev = HAS_PREV ? ds->beta[j] * ds->s[j - 1] : 0.0;
-    const double2 y = te_sell_row<REAL>(g.chunk_off, g.col, g.val, u_j, c, lane);
-    const int64_t r = c * 32 + lane;
-    const bool valid = (r - __ldg(g.inst_row + inst)) < __ldg(g.inst_n + inst);
-    double a0 = 0.0, a1 = 0.0;
-    double2 wr = make_double2(0.0, 0.0);
-    if (valid) {
-      if (HAS_PREV) {
-        const double2 up = u_jm1[r];
-        wr.x = fma(cprev, up.x, gg * y.y);
-        wr.y = fma(cprev, up.y, -gg * y.x);
-      } else {
-        wr.x = gg * y.y;
-        wr.y = -gg * y.x;
-      }
-      const double2 uj = u_j[r];
-      a0 = fma(uj.x, wr.x, uj.y * wr.y);
-      a1 = fma(uj.x, wr.y, -uj.y * wr.x);
+    double cw = 0.0;
+    if (HAS_PREV) {
+      const double bie = ds->beta[j] * ds->inv_exp_factor;
+      cw = bie * bie;
     }
-    w[r] = wr;
+    const int64_t row0 = __ldg(g.inst_row + inst);
+    const int n_i = __ldg(g.inst_n + inst);
+    double a0 = 0.0, a1 = 0.0;
+    for (; c < c1; ++c) {
+      const double2 y = te_sell_row<REAL>(g.chunk_off, g.col, g.val, u_j, c, lane);
+      const int64_t r = c * 32 + lane;
+      double2 wr = make_double2(0.0, 0.0);
+      if (r - row0 < n_i) {
+        if (HAS_PREV) {
+          const double2 up = u_jm1[r];
+          wr.x = fma(cw, up.x, y.y);
+          wr.y = fma(cw, up.y, -y.x);
+        } else {
+          wr.x = y.y;
+          wr.y = -y.x;
+        }
+        const double2 uj = u_j[r];
+        a0 = fma(uj.x, wr.x, fma(uj.y, wr.y, a0));
+        a1 = fma(uj.x, wr.y, fma(-uj.y, wr.x, a1));
+      }
+      w[r] = wr;
+    }
+    (void)gg;
     a0 = te_warp_sum(a0);
     a1 = te_warp_sum(a1);
     if (lane == 0) {
-      chunk_partials[2 * c] = a0;
-      chunk_partials[2 * c + 1] = a1;
+      const int64_t seg = sc.seg_base[inst] + (wid - sc.inst_w0[inst]);
+      seg_partials[2 * seg] = a0;
+      seg_partials[2 * seg + 1] = a1;
     }
   }
 }
 
-__global__ void __launch_bounds__(TE_THREADS) batch_update_kernel(BatchGeom g, double2* __restrict__ V,
+__global__ void __launch_bounds__(TE_THREADS) batch_update_kernel(BatchGeom g, BatchSched sc,
+                                                                  double2* __restrict__ V,
                                                                   const double2* __restrict__ w, TeDevState* states,
-                                                                  double* chunk_partials, int j) {
+                                                                  double* seg_partials, int j) {
   const int lane = threadIdx.x & 31;
-  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const double2* __restrict__ u_j = V + (int64_t)j * g.ld;
   double2* __restrict__ u_jp1 = V + (int64_t)(j + 1) * g.ld;
-  const int64_t n_visit = batch_chunk_count(g);
-  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n_visit; i += warps) {
-    const int64_t c = batch_chunk(g, i);
+  int64_t c = sc.warp_begin[wid];
+  const int64_t cend = sc.warp_begin[wid + 1];
+  while (c < cend) {
     const int inst = __ldg(g.chunk_inst + c);
     const TeDevState* ds = states + inst;
-    if (lanczos_skip(ds, j)) continue;
-    const double sj = ds->s[j];
-    const double2 al = ds->alpha[j];
-    const double gr = al.x * sj, gi = al.y * sj;
-    const int64_t r = c * 32 + lane;
-    const bool valid = (r - __ldg(g.inst_row + inst)) < __ldg(g.inst_n + inst);
-    double2 o = make_double2(0.0, 0.0);
-    if (valid) {
-      const double2 wv = w[r], u = u_j[r];
-      o.x = fma(-gr, u.x, fma(gi, u.y, wv.x));
-      o.y = fma(-gr, u.y, fma(-gi, u.x, wv.y));
+    const int64_t c1 = min((int64_t)__ldg(g.inst_chunk + inst + 1), cend);
+    if (lanczos_skip(ds, j)) {
+      c = batch_skip_to(g, sc, ds, inst, cend);
+      continue;
     }
-    if (j + 1 < ds->m_cur) u_jp1[r] = o;
-    double nrm = fma(o.x, o.x, o.y * o.y);
+    const double2 al = ds->alpha[j];
+    const double q = ds->inv_exp_factor;  // alpha_j s_j / (e s_j)
+    const double gr = al.x * q, gi = al.y * q;
+    const bool store = j + 1 < ds->m_cur;
+    const int64_t row0 = __ldg(g.inst_row + inst);
+    const int n_i = __ldg(g.inst_n + inst);
+    double nrm = 0.0;
+    for (; c < c1; ++c) {
+      const int64_t r = c * 32 + lane;
+      double2 o = make_double2(0.0, 0.0);
+      if (r - row0 < n_i) {
+        const double2 wv = w[r], u = u_j[r];
+        o.x = fma(-gr, u.x, fma(gi, u.y, wv.x));
+        o.y = fma(-gr, u.y, fma(-gi, u.x, wv.y));
+        nrm = fma(o.x, o.x, fma(o.y, o.y, nrm));
+      }
+      if (store) u_jp1[r] = o;
+    }
     nrm = te_warp_sum(nrm);
-    if (lane == 0) chunk_partials[2 * c] = nrm;
+    if (lane == 0) seg_partials[sc.seg_base[inst] + (wid - sc.inst_w0[inst])] = nrm;
   }
 }
 
-// kind 0: alpha_j of every instance; kind 1: beta_{j+1}, breakdown, h.
-__global__ void __launch_bounds__(TE_THREADS) batch_reduce_kernel(BatchGeom g, TeDevState* states,
-                                                                  const double* chunk_partials, int j, int kind) {
+// kind 0: alpha_j of every instance; kind 1: beta_{j+1}, s_{j+1}, breakdown, h
+// (one block per instance, its segments summed in slot order).
+__global__ void __launch_bounds__(TE_THREADS) batch_reduce_kernel(BatchSched sc, TeDevState* states,
+                                                                  const double* seg_partials, int j, int kind) {
   __shared__ double scratch[2 * 32];
   const int inst = blockIdx.x;
   TeDevState* ds = states + inst;
   if (lanczos_skip(ds, j)) return;
-  const int64_t c0 = g.inst_chunk[inst], c1 = g.inst_chunk[inst + 1];
+  const int64_t s0 = sc.seg_base[inst], ns = sc.inst_nseg[inst];
+  const int w0 = sc.inst_w0[inst];
   double acc[2] = {0.0, 0.0};
-  for (int64_t c = c0 + threadIdx.x; c < c1; c += blockDim.x) {
-    acc[0] += chunk_partials[2 * c];
-    if (kind == 0) acc[1] += chunk_partials[2 * c + 1];
+  for (int64_t s = threadIdx.x; s < ns; s += blockDim.x) {
+    // slot s belongs to warp w0 + s; a warp whose chunk range is empty wrote nothing
+    if (!(sc.warp_begin[w0 + s] < sc.warp_begin[w0 + s + 1])) continue;
+    if (kind == 0) {
+      acc[0] += seg_partials[2 * (s0 + s)];
+      acc[1] += seg_partials[2 * (s0 + s) + 1];
+    } else {
+      acc[0] += seg_partials[s0 + s];
+    }
   }
   te_block_sum<2>(acc, scratch);
   if (threadIdx.x != 0) return;
+  const double sj = ds->s[j];
+  const double g = ds->exp_factor * sj;
   if (kind == 0) {
-    const double sj = ds->s[j];
-    ds->alpha[j] = make_double2(sj * acc[0], sj * acc[1]);
+    const double f = sj * g;
+    ds->alpha[j] = make_double2(f * acc[0], f * acc[1]);
     return;
   }
-  const double beta = sqrt(acc[0]);
+  const double beta = fabs(g) * sqrt(acc[0]);
   const int m = ds->m_cur;
   if (beta < ds->tol_rate) {
     ds->breakdown = 1;
@@ -182,7 +339,7 @@ __global__ void __launch_bounds__(TE_THREADS) batch_reduce_kernel(BatchGeom g, T
     ds->h = beta;
   } else if (j + 1 != m) {
     ds->beta[j + 1] = beta;
-    ds->s[j + 1] = 1.0 / beta;
+    ds->s[j + 1] = g / beta;
   } else {
     ds->h = beta;
     ds->m_eff = m;
@@ -365,7 +522,6 @@ struct te_batch_s {
   double2* w = nullptr;
   double2* sampled = nullptr;
   double2* v0 = nullptr;  // start vectors (permuted), kept for reruns
-  double* partials = nullptr;
   double* diag = nullptr;  // TE_BATCH_MAX_OBS x ld
   int* d_nobs = nullptr;
   int64_t* d_result_off = nullptr;
@@ -374,6 +530,15 @@ struct te_batch_s {
   int* h_flags = nullptr;  // pinned
   int32_t* d_active = nullptr;  // chunks of the running instances
   int* d_active_count = nullptr;
+  // Lanczos schedule of the current global step (batch_schedule_kernel)
+  int n_warps = 0;
+  int32_t* d_warp_begin = nullptr;
+  int32_t* d_inst_w0 = nullptr;
+  int32_t* d_inst_nseg = nullptr;
+  int32_t* d_seg_base = nullptr;
+  int32_t* d_next_run = nullptr;
+  double* d_inst_cost = nullptr;
+  double* seg_partials = nullptr;
   std::vector<int> nobs;
   std::vector<int64_t> result_off;
   cudaGraphExec_t g_step = nullptr, g_batch = nullptr;
@@ -423,7 +588,6 @@ void free_batch(te_batch b) {
   cudaFree(b->w);
   cudaFree(b->sampled);
   cudaFree(b->v0);
-  cudaFree(b->partials);
   cudaFree(b->diag);
   cudaFree(b->d_nobs);
   cudaFree(b->d_result_off);
@@ -432,18 +596,45 @@ void free_batch(te_batch b) {
   cudaFreeHost(b->h_flags);
   cudaFree(b->d_active);
   cudaFree(b->d_active_count);
+  cudaFree(b->d_warp_begin);
+  cudaFree(b->d_inst_w0);
+  cudaFree(b->d_inst_nseg);
+  cudaFree(b->d_seg_base);
+  cudaFree(b->d_next_run);
+  cudaFree(b->d_inst_cost);
+  cudaFree(b->seg_partials);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
 }
 
-// One resident wave of the chunk-strided kernels (apply, update, combine).
+// One resident wave of the chunk-strided kernels (new start, combine).
 int grid_chunks(const te_batch_s* b) {
-  const void* k[] = {(const void*)batch_apply_kernel<true, true>,  (const void*)batch_apply_kernel<true, false>,
-                     (const void*)batch_apply_kernel<false, true>, (const void*)batch_apply_kernel<false, false>,
-                     (const void*)batch_update_kernel,             (const void*)batch_combine_kernel};
+  const void* k[] = {(const void*)batch_new_start_kernel, (const void*)batch_combine_kernel};
   int bps = 8;
   for (const void* f : k) bps = std::min(bps, te_kernel_blocks_per_sm(f, TE_THREADS, 0));
   return (int)std::min<int64_t>((b->n_chunks * 32 + TE_THREADS - 1) / TE_THREADS, (int64_t)te_num_sms() * bps);
+}
+
+// Warps of the Lanczos passes: one resident wave of the apply/update kernels.
+int lanczos_warps(const te_batch_s* b) {
+  const void* k[] = {(const void*)batch_apply_kernel<true, true>,  (const void*)batch_apply_kernel<true, false>,
+                     (const void*)batch_apply_kernel<false, true>, (const void*)batch_apply_kernel<false, false>,
+                     (const void*)batch_update_kernel};
+  int bps = 8;
+  for (const void* f : k) bps = std::min(bps, te_kernel_blocks_per_sm(f, TE_THREADS, 0));
+  const int64_t blocks = std::min<int64_t>((b->n_chunks * 32 + TE_THREADS - 1) / TE_THREADS,
+                                           (int64_t)te_num_sms() * bps);
+  return (int)std::max<int64_t>(blocks, 1) * (TE_THREADS / 32);
+}
+
+BatchSched sched(const te_batch_s* b) {
+  BatchSched sc;
+  sc.warp_begin = b->d_warp_begin;
+  sc.inst_w0 = b->d_inst_w0;
+  sc.inst_nseg = b->d_inst_nseg;
+  sc.seg_base = b->d_seg_base;
+  sc.next_run = b->d_next_run;
+  return sc;
 }
 
 // Record the kernels of one global step (or of one extra sample batch).
@@ -459,21 +650,27 @@ int enqueue_step(te_batch b, bool full_step) {
     batch_new_start_kernel<<<gc, TE_THREADS, 0, st>>>(g, b->V, b->spare, b->ds);
     batch_clear_start_kernel<<<(b->B + 255) / 256, 256, 0, st>>>(b->ds, b->B);
     k += 2;
+    const BatchSched sc = sched(b);
+    const int gl = b->n_warps / (TE_THREADS / 32);
+    batch_schedule_kernel<<<1, 1024, 0, st>>>(g, b->ds, b->B, b->n_warps, b->is_real ? 2.0 : 4.0, b->d_inst_cost,
+                                              b->d_warp_begin, b->d_inst_w0, b->d_inst_nseg, b->d_seg_base,
+                                              b->d_next_run);
+    k += 1;
     for (int j = 0; j < b->m_max; ++j) {
       if (b->is_real) {
         if (j > 0)
-          batch_apply_kernel<true, true><<<gc, TE_THREADS, 0, st>>>(g, b->V, b->w, b->ds, b->partials, j);
+          batch_apply_kernel<true, true><<<gl, TE_THREADS, 0, st>>>(g, sc, b->V, b->w, b->ds, b->seg_partials, j);
         else
-          batch_apply_kernel<true, false><<<gc, TE_THREADS, 0, st>>>(g, b->V, b->w, b->ds, b->partials, j);
+          batch_apply_kernel<true, false><<<gl, TE_THREADS, 0, st>>>(g, sc, b->V, b->w, b->ds, b->seg_partials, j);
       } else {
         if (j > 0)
-          batch_apply_kernel<false, true><<<gc, TE_THREADS, 0, st>>>(g, b->V, b->w, b->ds, b->partials, j);
+          batch_apply_kernel<false, true><<<gl, TE_THREADS, 0, st>>>(g, sc, b->V, b->w, b->ds, b->seg_partials, j);
         else
-          batch_apply_kernel<false, false><<<gc, TE_THREADS, 0, st>>>(g, b->V, b->w, b->ds, b->partials, j);
+          batch_apply_kernel<false, false><<<gl, TE_THREADS, 0, st>>>(g, sc, b->V, b->w, b->ds, b->seg_partials, j);
       }
-      batch_reduce_kernel<<<b->B, TE_THREADS, 0, st>>>(g, b->ds, b->partials, j, 0);
-      batch_update_kernel<<<gc, TE_THREADS, 0, st>>>(g, b->V, b->w, b->ds, b->partials, j);
-      batch_reduce_kernel<<<b->B, TE_THREADS, 0, st>>>(g, b->ds, b->partials, j, 1);
+      batch_reduce_kernel<<<b->B, TE_THREADS, 0, st>>>(sc, b->ds, b->seg_partials, j, 0);
+      batch_update_kernel<<<gl, TE_THREADS, 0, st>>>(g, sc, b->V, b->w, b->ds, b->seg_partials, j);
+      batch_reduce_kernel<<<b->B, TE_THREADS, 0, st>>>(sc, b->ds, b->seg_partials, j, 1);
       k += 4;
     }
   }
@@ -490,7 +687,7 @@ int enqueue_step(te_batch b, bool full_step) {
 }
 
 int64_t kernels_per_replay(const te_batch_s* b, bool full_step) {
-  return (full_step ? 3 + 4 * (int64_t)b->m_max : 0) + 4;
+  return (full_step ? 4 + 4 * (int64_t)b->m_max : 0) + 4;
 }
 
 int capture(te_batch b, bool full_step, cudaGraphExec_t* exec) {
@@ -570,8 +767,9 @@ extern "C" int te_batch_create(int n_instances, const te_matrix* H, const double
   for (int i = 0; i < n_instances; ++i) {
     const te_params& p = params[i];
     if (!H[i] || !v_host[i] || H[i]->n_rows != H[i]->n_cols || !(p.t > 0.0) || !(p.sampling_step > 0.0) ||
-        !(p.tol > 0.0) || p.m < 1 || p.reorth != 0) {
-      te_set_error("te_batch_create: instance %d: invalid matrix or parameters (reorth is not batched)", i);
+        !(p.tol > 0.0) || p.m < 1 || p.reorth != 0 || p.exp_factor == 0.0 || !std::isfinite(p.exp_factor)) {
+      te_set_error("te_batch_create: instance %d: invalid matrix or parameters (reorth and expFactor 0 are not "
+                   "batched)", i);
       return fail(TE_ERR_INVALID_ARG);
     }
     const int64_t n = H[i]->n_rows;
@@ -668,14 +866,22 @@ extern "C" int te_batch_create(int n_instances, const te_matrix* H, const double
   if ((rc = alloc((void**)&b->w, sizeof(double2) * ld)) != TE_OK) return fail(rc);
   if ((rc = alloc((void**)&b->sampled, sizeof(double2) * ld)) != TE_OK) return fail(rc);
   if ((rc = alloc((void**)&b->v0, sizeof(double2) * ld)) != TE_OK) return fail(rc);
-  if ((rc = alloc((void**)&b->partials, sizeof(double) * 2 * std::max<int64_t>(chunks, 1))) != TE_OK)
-    return fail(rc);
   if ((rc = alloc((void**)&b->diag, sizeof(double) * TE_BATCH_MAX_OBS * ld)) != TE_OK) return fail(rc);
   if ((rc = alloc((void**)&b->d_nobs, sizeof(int) * n_instances)) != TE_OK) return fail(rc);
   if ((rc = alloc((void**)&b->d_result_off, sizeof(int64_t) * n_instances)) != TE_OK) return fail(rc);
   if ((rc = alloc((void**)&b->d_flags, sizeof(int) * n_instances)) != TE_OK) return fail(rc);
   if ((rc = alloc((void**)&b->d_active, sizeof(int32_t) * std::max<int64_t>(chunks, 1))) != TE_OK) return fail(rc);
   if ((rc = alloc((void**)&b->d_active_count, sizeof(int))) != TE_OK) return fail(rc);
+  b->n_warps = lanczos_warps(b);
+  if ((rc = alloc((void**)&b->d_warp_begin, sizeof(int32_t) * (b->n_warps + 1))) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_inst_w0, sizeof(int32_t) * n_instances)) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_inst_nseg, sizeof(int32_t) * n_instances)) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_seg_base, sizeof(int32_t) * n_instances)) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_next_run, sizeof(int32_t) * n_instances)) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_inst_cost, sizeof(double) * (n_instances + 1))) != TE_OK) return fail(rc);
+  // segments: every warp has at most one per instance it touches
+  if ((rc = alloc((void**)&b->seg_partials, sizeof(double) * 2 * ((int64_t)b->n_warps + n_instances + 1))) != TE_OK)
+    return fail(rc);
   TE_CUDA(cudaMallocHost(&b->h_flags, sizeof(int) * n_instances));
   TE_CUDA(cudaMemsetAsync(b->V, 0, sizeof(double2) * ld * b->m_max, st));
   TE_CUDA(cudaMemsetAsync(b->spare, 0, sizeof(double2) * ld, st));

@@ -8,12 +8,12 @@
 //     all instances; a chunk of 32 rows never straddles two instances, so a warp
 //     always works for one instance and reads its scalars once;
 //   * each Lanczos iteration is one apply pass and one update pass over every
-//     active instance's rows on a per-step warp schedule of equal FP64 cost,
-//     each followed by a per-instance reduction of per-(warp, instance)
-//     partials in a fixed order (deterministic);
+//     active instance's rows on a per-step warp schedule of equal FP64 cost;
+//     per-(warp, instance) partials are summed per instance in a fixed order
+//     by the warp that writes the instance's last one (deterministic);
 //   * the Krylov-space work (exponential, error integrals, step size, sample
 //     schedule) runs one thread block per instance;
-//   * the whole sequence of one global step (4 m_max Lanczos kernels, Krylov
+//   * the whole sequence of one global step (2 m_max Lanczos kernels, Krylov
 //     kernel, combine, observables, flag gather) is captured once as a CUDA
 //     graph and replayed; the host syncs once per global step.
 #include <cfloat>
@@ -99,6 +99,8 @@ struct BatchSched {
   const int32_t* inst_nseg;   // segments (warps) covering each running instance, 0 otherwise
   const int32_t* seg_base;    // first segment slot of each instance
   const int32_t* next_run;    // the next running instance after each instance (n_inst: none)
+  const int32_t* inst_nwrite; // segments of each instance that are written (non-empty warps)
+  unsigned int* arrivals;     // per instance: segments written so far (apply pass, update pass)
 };
 
 // Where a warp continues after the chunks of instance inst that it must skip:
@@ -115,7 +117,7 @@ __global__ void __launch_bounds__(1024) batch_schedule_kernel(BatchGeom g, const
                                                               int n_warps, double w_slot, double* inst_cost,
                                                               int32_t* warp_begin, int32_t* inst_w0,
                                                               int32_t* inst_nseg, int32_t* seg_base,
-                                                              int32_t* next_run) {
+                                                              int32_t* next_run, int32_t* inst_nwrite) {
   const double w_chunk = 8.0 * 32.0;
   __shared__ double total;
   for (int i = threadIdx.x; i < n_inst; i += blockDim.x) {
@@ -184,6 +186,9 @@ __global__ void __launch_bounds__(1024) batch_schedule_kernel(BatchGeom g, const
     }
     inst_w0[i] = w0;
     inst_nseg[i] = nseg;
+    int nw = 0;
+    for (int s = 0; s < nseg; ++s) nw += warp_begin[w0 + s] < warp_begin[w0 + s + 1];
+    inst_nwrite[i] = nw;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -199,6 +204,40 @@ __global__ void __launch_bounds__(1024) batch_schedule_kernel(BatchGeom g, const
       if (!states[i].done && !states[i].fatal) nxt = i;
     }
   }
+}
+
+// Lane 0 has written this warp's segment partial(s) of instance inst; the warp
+// that completes the instance's count sums its written segments in slot order
+// (the same order whichever warp comes last) and returns true with the sums in
+// every lane.  NV values per segment at seg_partials[NV * slot + k].
+template <int NV>
+__device__ __forceinline__ bool batch_segment_done(const BatchSched& sc, int inst, int which,
+                                                   const double* seg_partials, double (&tot)[NV]) {
+  const int lane = threadIdx.x & 31;
+  unsigned int prev = 0;
+  if (lane == 0) {
+    __threadfence();
+    prev = atomicAdd(&sc.arrivals[2 * inst + which], 1u);
+  }
+  prev = __shfl_sync(0xffffffffu, prev, 0);
+  if (prev + 1 != (unsigned int)sc.inst_nwrite[inst]) return false;
+  __threadfence();
+  const int64_t s0 = sc.seg_base[inst];
+  const int w0 = sc.inst_w0[inst], ns = sc.inst_nseg[inst];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) tot[k] = 0.0;
+  for (int s = lane; s < ns; s += 32) {
+    if (!(sc.warp_begin[w0 + s] < sc.warp_begin[w0 + s + 1])) continue;  // an empty warp wrote nothing
+#pragma unroll
+    for (int k = 0; k < NV; ++k) tot[k] += __ldcg(seg_partials + NV * (s0 + s) + k);
+  }
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    tot[k] = te_warp_sum(tot[k]);
+    tot[k] = __shfl_sync(0xffffffffu, tot[k], 0);
+  }
+  if (lane == 0) sc.arrivals[2 * inst + which] = 0u;  // ready for the next pass
+  return true;
 }
 
 template <bool REAL, bool HAS_PREV>
@@ -249,13 +288,17 @@ __global__ void __launch_bounds__(TE_THREADS, REAL ? 6 : 5) batch_apply_kernel(B
       }
       w[r] = wr;
     }
-    (void)gg;
     a0 = te_warp_sum(a0);
     a1 = te_warp_sum(a1);
     if (lane == 0) {
       const int64_t seg = sc.seg_base[inst] + (wid - sc.inst_w0[inst]);
       seg_partials[2 * seg] = a0;
       seg_partials[2 * seg + 1] = a1;
+    }
+    double tot[2];
+    if (batch_segment_done<2>(sc, inst, 0, seg_partials, tot) && lane == 0) {
+      const double f = sj * gg;  // alpha_j = s_j g <u_j, w'>
+      states[inst].alpha[j] = make_double2(f * tot[0], f * tot[1]);
     }
   }
 }
@@ -298,51 +341,24 @@ __global__ void __launch_bounds__(TE_THREADS) batch_update_kernel(BatchGeom g, B
     }
     nrm = te_warp_sum(nrm);
     if (lane == 0) seg_partials[sc.seg_base[inst] + (wid - sc.inst_w0[inst])] = nrm;
-  }
-}
-
-// kind 0: alpha_j of every instance; kind 1: beta_{j+1}, s_{j+1}, breakdown, h
-// (one block per instance, its segments summed in slot order).
-__global__ void __launch_bounds__(TE_THREADS) batch_reduce_kernel(BatchSched sc, TeDevState* states,
-                                                                  const double* seg_partials, int j, int kind) {
-  __shared__ double scratch[2 * 32];
-  const int inst = blockIdx.x;
-  TeDevState* ds = states + inst;
-  if (lanczos_skip(ds, j)) return;
-  const int64_t s0 = sc.seg_base[inst], ns = sc.inst_nseg[inst];
-  const int w0 = sc.inst_w0[inst];
-  double acc[2] = {0.0, 0.0};
-  for (int64_t s = threadIdx.x; s < ns; s += blockDim.x) {
-    // slot s belongs to warp w0 + s; a warp whose chunk range is empty wrote nothing
-    if (!(sc.warp_begin[w0 + s] < sc.warp_begin[w0 + s + 1])) continue;
-    if (kind == 0) {
-      acc[0] += seg_partials[2 * (s0 + s)];
-      acc[1] += seg_partials[2 * (s0 + s) + 1];
-    } else {
-      acc[0] += seg_partials[s0 + s];
+    double tot[1];
+    if (batch_segment_done<1>(sc, inst, 1, seg_partials, tot) && lane == 0) {
+      TeDevState* dw = states + inst;
+      const double g = dw->exp_factor * dw->s[j];
+      const double beta = fabs(g) * sqrt(tot[0]);
+      const int m = dw->m_cur;
+      if (beta < dw->tol_rate) {  // lucky breakdown (:551-555)
+        dw->breakdown = 1;
+        dw->m_eff = j + 1;
+        dw->h = beta;
+      } else if (j + 1 != m) {
+        dw->beta[j + 1] = beta;
+        dw->s[j + 1] = g / beta;
+      } else {
+        dw->h = beta;
+        dw->m_eff = m;
+      }
     }
-  }
-  te_block_sum<2>(acc, scratch);
-  if (threadIdx.x != 0) return;
-  const double sj = ds->s[j];
-  const double g = ds->exp_factor * sj;
-  if (kind == 0) {
-    const double f = sj * g;
-    ds->alpha[j] = make_double2(f * acc[0], f * acc[1]);
-    return;
-  }
-  const double beta = fabs(g) * sqrt(acc[0]);
-  const int m = ds->m_cur;
-  if (beta < ds->tol_rate) {
-    ds->breakdown = 1;
-    ds->m_eff = j + 1;
-    ds->h = beta;
-  } else if (j + 1 != m) {
-    ds->beta[j + 1] = beta;
-    ds->s[j + 1] = g / beta;
-  } else {
-    ds->h = beta;
-    ds->m_eff = m;
   }
 }
 
@@ -537,6 +553,8 @@ struct te_batch_s {
   int32_t* d_inst_nseg = nullptr;
   int32_t* d_seg_base = nullptr;
   int32_t* d_next_run = nullptr;
+  int32_t* d_inst_nwrite = nullptr;
+  unsigned int* d_arrivals = nullptr;  // 2 per instance
   double* d_inst_cost = nullptr;
   double* seg_partials = nullptr;
   std::vector<int> nobs;
@@ -601,6 +619,8 @@ void free_batch(te_batch b) {
   cudaFree(b->d_inst_nseg);
   cudaFree(b->d_seg_base);
   cudaFree(b->d_next_run);
+  cudaFree(b->d_inst_nwrite);
+  cudaFree(b->d_arrivals);
   cudaFree(b->d_inst_cost);
   cudaFree(b->seg_partials);
   if (b->st) cudaStreamDestroy(b->st);
@@ -634,6 +654,8 @@ BatchSched sched(const te_batch_s* b) {
   sc.inst_nseg = b->d_inst_nseg;
   sc.seg_base = b->d_seg_base;
   sc.next_run = b->d_next_run;
+  sc.inst_nwrite = b->d_inst_nwrite;
+  sc.arrivals = b->d_arrivals;
   return sc;
 }
 
@@ -654,7 +676,7 @@ int enqueue_step(te_batch b, bool full_step) {
     const int gl = b->n_warps / (TE_THREADS / 32);
     batch_schedule_kernel<<<1, 1024, 0, st>>>(g, b->ds, b->B, b->n_warps, b->is_real ? 2.0 : 4.0, b->d_inst_cost,
                                               b->d_warp_begin, b->d_inst_w0, b->d_inst_nseg, b->d_seg_base,
-                                              b->d_next_run);
+                                              b->d_next_run, b->d_inst_nwrite);
     k += 1;
     for (int j = 0; j < b->m_max; ++j) {
       if (b->is_real) {
@@ -668,10 +690,8 @@ int enqueue_step(te_batch b, bool full_step) {
         else
           batch_apply_kernel<false, false><<<gl, TE_THREADS, 0, st>>>(g, sc, b->V, b->w, b->ds, b->seg_partials, j);
       }
-      batch_reduce_kernel<<<b->B, TE_THREADS, 0, st>>>(sc, b->ds, b->seg_partials, j, 0);
       batch_update_kernel<<<gl, TE_THREADS, 0, st>>>(g, sc, b->V, b->w, b->ds, b->seg_partials, j);
-      batch_reduce_kernel<<<b->B, TE_THREADS, 0, st>>>(sc, b->ds, b->seg_partials, j, 1);
-      k += 4;
+      k += 2;
     }
   }
   te_launch_krylov_batch(b->ds, b->B, full_step ? 0 : 1, st);
@@ -687,7 +707,7 @@ int enqueue_step(te_batch b, bool full_step) {
 }
 
 int64_t kernels_per_replay(const te_batch_s* b, bool full_step) {
-  return (full_step ? 4 + 4 * (int64_t)b->m_max : 0) + 4;
+  return (full_step ? 4 + 2 * (int64_t)b->m_max : 0) + 4;
 }
 
 int capture(te_batch b, bool full_step, cudaGraphExec_t* exec) {
@@ -737,6 +757,7 @@ int reset_states(te_batch b) {
     s.done = b->n_samples[i] > 1 ? 0 : 1;
   }
   TE_CUDA(cudaMemcpyAsync(b->ds, hs.data(), sizeof(TeDevState) * b->B, cudaMemcpyHostToDevice, b->st));
+  TE_CUDA(cudaMemsetAsync(b->d_arrivals, 0, sizeof(unsigned int) * 2 * b->B, b->st));
   TE_CUDA(cudaMemcpyAsync(b->V, b->v0, sizeof(double2) * b->ld, cudaMemcpyDeviceToDevice, b->st));
   batch_combine_kernel<<<grid_chunks(b), TE_THREADS, 0, b->st>>>(g, b->V, b->spare, b->sampled, b->ds, 1);
   batch_obs_kernel<<<b->B, TE_THREADS, 0, b->st>>>(g, b->sampled, b->diag, b->d_nobs, b->d_result_off, b->results,
@@ -878,6 +899,8 @@ extern "C" int te_batch_create(int n_instances, const te_matrix* H, const double
   if ((rc = alloc((void**)&b->d_inst_nseg, sizeof(int32_t) * n_instances)) != TE_OK) return fail(rc);
   if ((rc = alloc((void**)&b->d_seg_base, sizeof(int32_t) * n_instances)) != TE_OK) return fail(rc);
   if ((rc = alloc((void**)&b->d_next_run, sizeof(int32_t) * n_instances)) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_inst_nwrite, sizeof(int32_t) * n_instances)) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_arrivals, sizeof(unsigned int) * 2 * n_instances)) != TE_OK) return fail(rc);
   if ((rc = alloc((void**)&b->d_inst_cost, sizeof(double) * (n_instances + 1))) != TE_OK) return fail(rc);
   // segments: every warp has at most one per instance it touches
   if ((rc = alloc((void**)&b->seg_partials, sizeof(double) * 2 * ((int64_t)b->n_warps + n_instances + 1))) != TE_OK)

@@ -3,7 +3,8 @@
 // compiled against the GB300 headers.  Prints one line per observable with
 // its samples, then a line with the krylovReturn fields.
 //
-//   dropin_driver simple            two coupled oscillators (dim 201), t=10, tol 1e-6
+//   dropin_driver simple [csv_prefix]  two coupled oscillators (dim 201), t=10, tol 1e-6;
+//                                     with csv_prefix the samples also go through saveResult
 //   dropin_driver blackhole N0 Nm K maxT samplingStep
 #include <cmath>
 #include <cstdio>
@@ -15,6 +16,7 @@
 
 #include "Basis.h"
 #include "hamiltonian.h"
+#include "krylovHelper.h"
 #include "krylovObservables.h"
 #include "krylovTimeEvolver.h"
 #include "matrixDataTypes.h"
@@ -35,12 +37,13 @@ static void print_result(krylovReturn* res) {
               res->n_steps, res->numSamples, res->krylovDim, res->err, res->evolvedTime);
 }
 
-static int run(basicBasis& b, Hamiltonian& ham, std::vector<int> init, double t, double dt, double tol, bool full) {
+static int run(basicBasis& b, Hamiltonian& ham, std::vector<int> init, double t, double dt, double tol, bool full,
+               const char* csv_prefix = nullptr) {
   std::unique_ptr<smatrix> H = ham.createHamiltonMatrix(&b);
   std::vector<std::unique_ptr<smatrix>> ops = ham.createNumberOperatorObservables(&b);
   std::vector<std::unique_ptr<krylovBasicObservable>> obs;
-  for (size_t i = 0; i < ops.size(); ++i)
-    obs.push_back(std::make_unique<krylovSpMatrixObservable>("mode" + std::to_string(i), std::move(ops[i])));
+  for (size_t i = 0; i < ops.size(); ++i)  // named by mode index, as in the reference's example
+    obs.push_back(std::make_unique<krylovSpMatrixObservable>(std::to_string(i), std::move(ops[i])));
   basisVector bv((unsigned)init.size());
   for (size_t i = 0; i < init.size(); ++i) bv.e[i] = init[i];
   std::vector<std::complex<double>> v(b.numberElements);
@@ -56,6 +59,10 @@ static int run(basicBasis& b, Hamiltonian& ham, std::vector<int> init, double t,
     res = ev.timeEvolve();
   }
   print_result(res);
+  if (csv_prefix) {
+    parameter_list none;
+    saveResult(res->observableList, none, csv_prefix);
+  }
   delete res;
   return 0;
 }
@@ -67,7 +74,8 @@ int main(int argc, char** argv) {
     Hamiltonian ham;
     ham.hamiltonOperator = {ham.createNumberOperator(0, 1.0), ham.createNumberOperator(1, 2.0),
                             ham.linInteraction(0, 1, 0, 0, false, 1.0), ham.linInteraction(0, 1, 0, 0, true, 1.0)};
-    return run(b, ham, {N0, 0}, 10.0, 0.01, 1e-6, false);  // 5-argument constructor: tol 1e-6, m 40
+    return run(b, ham, {N0, 0}, 10.0, 0.01, 1e-6, false,  // 5-argument constructor: tol 1e-6, m 40
+               argc >= 3 ? argv[2] : nullptr);
   }
   if (argc >= 7 && std::strcmp(argv[1], "blackhole") == 0) {
     const int N0 = std::atoi(argv[2]), Nm = std::atoi(argv[3]), K = std::atoi(argv[4]);

@@ -203,6 +203,21 @@ typedef int (*te_observable_fn)(void* user, const double* state, int64_t dim, do
 int te_evolver_create(te_matrix H, const double* v_host, const te_params* params, te_evolver* out);
 int te_evolver_destroy(te_evolver ev);
 
+/* Device-side stop condition (the requestStopException of an observable,
+ * krylovTimeEvolver.cpp:423-436, without a host round trip): the evolution
+ * stops at the first sample at which observable obs_index (in the order the
+ * observables were added) is >= threshold (direction > 0) or <= threshold
+ * (direction < 0); that sample is not counted, status 3 (0 at t = 0), as for
+ * a stop requested by a callback.  Up to 4 conditions; any one stops. */
+int te_evolver_add_stop_condition(te_evolver ev, int obs_index, double threshold, int direction);
+
+/* Dense observable Re <psi|O|psi> for a complex n x n O stored column-major
+ * (values: 2 n^2 doubles, the layout of TE::matrix), evaluated on the GPU for
+ * every sample (krylovMatrixObservable, krylovObservables.cpp:119-138, whose
+ * constructor the reference keeps private; 4 n^2 FMAs per sample, so meant for
+ * small n).  O is copied to the device. */
+int te_evolver_add_dense_observable(te_evolver ev, const double* values, int64_t n);
+
 /* Observables, sampled in the order added (krylovObservables.cpp).  A
  * sparse observable stores Re <psi|O|psi>; a vector observable stores
  * |<psi|o>|^2.  O stays owned by the caller. */

@@ -303,3 +303,53 @@ def test_fused_and_per_iteration_lanczos_agree(te_gpu, oracle_lib, L, t, samplin
     ref = oracle_lib.evolve(H, v, t, sampling, [("sparse", O)], tol=1e-8, m=40)
     for r in (a, b):
         _compare(r, ref, 1e-8, obs_norm=float(L), strict=False)
+
+
+def test_dense_observable(te_gpu, oracle_lib):
+    """A dense Hermitian observable on the GPU (te_evolver_add_dense_observable)
+    against the oracle with the same matrix as a full COO."""
+    states, H = models.bose_hubbard(5, 5, 1.0, 2.0)
+    n = len(states)
+    rng = np.random.default_rng(9)
+    A = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    D = (A + A.conj().T) / (2 * np.sqrt(n))
+    rr, cc = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    coo = (rr.ravel(), cc.ravel(), D.ravel())
+    v = _fock(states, [5, 0, 0, 0, 0])
+    ev = te_gpu.Evolver(te_gpu.Matrix.from_coo(n, H), v, 2.0, 0.25, [("dense", D)], tol=1e-8, m=30)
+    gpu = ev.time_evolve()
+    ev.close()
+    ref = oracle_lib.evolve(H, v, 2.0, 0.25, [("sparse", coo)], tol=1e-8, m=30)
+    d_norm = np.max(np.abs(np.linalg.eigvalsh(D)))
+    _compare(gpu, ref, 1e-8, obs_norm=d_norm, strict=False)
+    # the value at t = 0 is exact
+    assert abs(gpu["samples"][0][0] - np.real(v.conj() @ D @ v)) < 1e-13
+
+
+@pytest.mark.parametrize("fused_obs", [True, False])
+def test_device_stop_condition(te_gpu, oracle_lib, fused_obs):
+    """A device-side stop condition stops where an observable raising the stop
+    request at the same sample does (the oracle's stop at that index): status 3,
+    the samples before it, the time and error of the step start."""
+    states, H = models.bose_hubbard(4, 4, 1.0, 2.0)
+    n = len(states)
+    v = _fock(states, [4, 0, 0, 0])
+    obs = [("sparse", o) for o in models.number_operator_observables(states)]
+    full = oracle_lib.evolve(H, v, 2.0, 0.1, obs, tol=1e-8, m=20)
+    n0 = full["samples"][0]
+    k = int(np.argmax(n0 <= 3.6))  # first sample with <n_0> <= 3.6 (it falls from 4 to 3.46)
+    assert 0 < k < len(n0) - 1
+    ref = oracle_lib.evolve(H, v, 2.0, 0.1, obs + [("stop", k)], tol=1e-8, m=20)
+    M = te_gpu.Matrix.from_coo(n, H)
+    O = [("sparse", te_gpu.Matrix.from_coo(n, o)) for _, o in obs]
+    if not fused_obs:  # a general (non-diagonal) observable routes samples through the per-sample path
+        O.append(("sparse", te_gpu.Matrix.from_coo(n, H)))
+    ev = te_gpu.Evolver(M, v, 2.0, 0.1, O, tol=1e-8, m=20)
+    ev.add_stop_condition(0, 3.6, -1)
+    gpu = ev.time_evolve()
+    ev.close()
+    assert gpu["status"] == ref["status"] == 3
+    assert gpu["num_samples"] == ref["num_samples"] == k
+    assert abs(gpu["evolved_time"] - ref["evolved_time"]) < 1e-12
+    assert abs(gpu["err"] - ref["err"]) < 1e-12
+    assert np.max(np.abs(gpu["samples"][:4, :k] - ref["samples"][:, :k])) < OBS_TOL

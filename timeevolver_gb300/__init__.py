@@ -96,6 +96,8 @@ SIGNATURES = {
     "te_batch_launch_count": (_I64, [_P]),
     "te_batch_stream": (_P, [_P]),
     "te_evolver_set_option": (_I, [_P, _I, _I]),
+    "te_evolver_add_dense_observable": (_I, [_P, _P, _I64]),
+    "te_evolver_add_stop_condition": (_I, [_P, _I, _D, _I]),
     "te_adjoint_create": (_I, [_I, _P, _P, _P, _D, _D, _I, _D, _I, _P]),
     "te_adjoint_destroy": (_I, [_P]),
     "te_adjoint_run": (_I, [_P, _P, _P, _P]),
@@ -265,9 +267,9 @@ class Matrix:
 class Evolver:
     """One time evolution (krylovTimeEvolver): construct, add observables, run.
 
-    ``observables`` entries: ("sparse", Matrix), ("vector", ndarray) or
-    ("callback", fn) where ``fn(state) -> float`` may raise StopEvolution
-    (requestStopException)."""
+    ``observables`` entries: ("sparse", Matrix), ("vector", ndarray),
+    ("dense", n x n ndarray) or ("callback", fn) where ``fn(state) -> float``
+    may raise StopEvolution (requestStopException)."""
 
     def __init__(self, H, v, t, sampling_step, observables=(), exp_factor=1.0, tol=1e-6, m=40,
                  fast_integration=False, reorth=False):
@@ -291,6 +293,10 @@ class Evolver:
         elif kind == "vector":
             o = np.ascontiguousarray(data, dtype=np.complex128)
             _check(lib().te_evolver_add_vector_observable(self.handle, _ptr(o)), "add_vector_observable")
+        elif kind == "dense":
+            o = np.asfortranarray(data, dtype=np.complex128)  # column-major n x n
+            _check(lib().te_evolver_add_dense_observable(self.handle, _ptr(o.reshape(-1, order="F")), o.shape[0]),
+                   "add_dense_observable")
         elif kind == "callback":
             fn = data
 
@@ -353,6 +359,12 @@ class Evolver:
 
     def profile(self, enable=True):
         _check(lib().te_evolver_profile(self.handle, int(enable)), "te_evolver_profile")
+
+    def add_stop_condition(self, obs_index, threshold, direction):
+        """Stop at the first sample where observable obs_index >= threshold
+        (direction > 0) or <= threshold (direction < 0), on the device."""
+        _check(lib().te_evolver_add_stop_condition(self.handle, int(obs_index), float(threshold), int(direction)),
+               "te_evolver_add_stop_condition")
 
     def set_option(self, option, value):
         """te_evolver_set_option (e.g. OPT_FUSED_LANCZOS)."""

@@ -19,8 +19,9 @@
 namespace {
 
 struct HostObs {
-  int kind;  // 0 fused diagonal, 1 fused vector, 2 general sparse, 3 callback
+  int kind;  // 0 fused diagonal, 1 fused vector, 2 general sparse, 3 callback, 4 dense
   te_matrix O = nullptr;
+  double2* dense = nullptr;      // dense: column-major n x n (original order)
   double* diag_perm = nullptr;   // fused diagonal (permuted, Re)
   double2* vec_perm = nullptr;   // fused vector (permuted)
   te_observable_fn fn = nullptr;
@@ -35,7 +36,7 @@ struct Summary {
   double t_now, t_sampling, err, t_step;
   int index_samples, n_steps, m_cur, status;
   int err_code_find, nb_err_roundoff, nb_err_int, fatal;
-  int done, pad_p0, pad_p1, pad_p2;
+  int done, stop_flag, pad_p1, pad_p2;
   double err_step, h;
   int breakdown, m_eff, step_code, n_integrals;
   int samples_in_batch, samples_pending, want_w, sample_base;
@@ -68,6 +69,7 @@ struct te_evolver_s {
   int batch_cap = 0;         // states the batch buffer holds
   size_t results_cap = 0;    // doubles the results buffer holds
   std::vector<HostObs> obs;
+  TeStopConds stops{};  // device-side stop conditions
   std::vector<te_step_record> trace;
   te_result res{};
   bool ran = false;
@@ -169,8 +171,14 @@ int process_batch(te_evolver ev, int* stop_at, bool synced) {
     ++ev->launches;
   }
   bool need_host = false;
-  for (auto& o : ev->obs) need_host |= (o.kind == 2 || o.kind == 3);
-  if (!need_host) return TE_OK;
+  for (auto& o : ev->obs) need_host |= (o.kind == 2 || o.kind == 3 || o.kind == 4);
+  if (!need_host) {
+    if (ev->stops.count) {
+      te_launch_stop_check(ev->stops, ev->results, (int)ev->n_samples, ev->ds, ev->st);
+      ++ev->launches;
+    }
+    return TE_OK;
+  }
   if (!synced) {
     int rc = read_summary(ev);
     if (rc != TE_OK) return rc;
@@ -183,6 +191,10 @@ int process_batch(te_evolver ev, int* stop_at, bool synced) {
       HostObs& o = ev->obs[i];
       if (o.kind == 2) {
         te_launch_general_obs(*o.O, ev->orig_tmp, ev->ds, s, ev->partials, ev->results + i * ev->n_samples, ev->st);
+        ++ev->launches;
+      } else if (o.kind == 4) {
+        te_launch_dense_obs(ev->n, o.dense, ev->orig_tmp, ev->ds, s, ev->partials, ev->results + i * ev->n_samples,
+                            ev->st);
         ++ev->launches;
       } else if (o.kind == 3) {
         TE_CUDA(cudaMemcpyAsync(ev->host_state, ev->orig_tmp, sizeof(double2) * ev->n, cudaMemcpyDeviceToHost,
@@ -199,6 +211,10 @@ int process_batch(te_evolver ev, int* stop_at, bool synced) {
         TE_CUDA(cudaStreamSynchronize(ev->st));
       }
     }
+  }
+  if (ev->stops.count) {
+    te_launch_stop_check(ev->stops, ev->results, (int)ev->n_samples, ev->ds, ev->st);
+    ++ev->launches;
   }
   return TE_OK;
 }
@@ -217,6 +233,7 @@ void free_evolver(te_evolver ev) {
   for (auto& o : ev->obs) {
     cudaFree(o.diag_perm);
     cudaFree(o.vec_perm);
+    cudaFree(o.dense);
   }
   for (auto e : ev->ev_pool) cudaEventDestroy(e);
   if (ev->st) cudaStreamDestroy(ev->st);
@@ -243,7 +260,7 @@ int run(te_evolver ev, te_result* out) {
   ev->launches = 0;
   ev->trace.clear();
   bool need_host = false;
-  for (auto& o : ev->obs) need_host |= (o.kind == 2 || o.kind == 3);
+  for (auto& o : ev->obs) need_host |= (o.kind == 2 || o.kind == 3 || o.kind == 4);
   ev->max_batch = need_host ? 1 : (int)std::max<int64_t>(1, std::min<int64_t>(TE_SCAP, ((int64_t)256 << 20) / (16 * n)));
   if (ev->max_batch > ev->batch_cap) {  // kept across runs while large enough
     cudaFree(ev->batch);
@@ -305,6 +322,7 @@ int run(te_evolver ev, te_result* out) {
   rc = read_summary(ev);
   if (rc != TE_OK) return rc;
   Summary* S = ev->sum;
+  if (stop_at < 0 && S->stop_flag) stop_at = S->stop_flag - 1;
   te_result r{};
   r.dim = n;
   if (stop_at >= 0) {  // stop requested at t = 0: plain return, status 0 (:309-313)
@@ -377,6 +395,7 @@ int run(te_evolver ev, te_result* out) {
     if (rc != TE_OK) return rc;
     rc = read_summary(ev);
     if (rc != TE_OK) return rc;
+    if (stop_at < 0 && S->stop_flag) stop_at = S->stop_flag - 1;
     if (S->fatal) break;
     // the combine pass above used the step's own m (m_eff on a breakdown)
     te_step_record rec{};
@@ -406,6 +425,7 @@ int run(te_evolver ev, te_result* out) {
       if (rc != TE_OK) return rc;
       rc = read_summary(ev);
       if (rc != TE_OK) return rc;
+      if (stop_at < 0 && S->stop_flag) stop_at = S->stop_flag - 1;
     }
     if (S->fatal) break;
     if (stop_at >= 0) {
@@ -588,6 +608,44 @@ extern "C" int te_evolver_add_sparse_observable(te_evolver ev, te_matrix O) {
     o.O = O;
   }
   ev->obs.push_back(o);
+  return TE_OK;
+}
+
+extern "C" int te_evolver_add_dense_observable(te_evolver ev, const double* values_host, int64_t n) {
+  if (!ev || !values_host) {
+    te_set_error("te_evolver_add_dense_observable: invalid arguments");
+    return TE_ERR_INVALID_ARG;
+  }
+  if (n != ev->n) {
+    te_set_error("Incompatible dimensions");
+    return TE_ERR_DIM;
+  }
+  HostObs o;
+  o.kind = 4;
+  TE_CUDA(cudaMalloc(&o.dense, sizeof(double2) * n * n));
+  const cudaError_t e = cudaMemcpy(o.dense, values_host, sizeof(double2) * n * n, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(o.dense);
+    return te_cuda_check(e, "dense observable upload");
+  }
+  ev->obs.push_back(o);
+  return TE_OK;
+}
+
+extern "C" int te_evolver_add_stop_condition(te_evolver ev, int obs_index, double threshold, int direction) {
+  if (!ev || obs_index < 0 || obs_index >= (int)ev->obs.size() || direction == 0 || !std::isfinite(threshold)) {
+    te_set_error("te_evolver_add_stop_condition: an existing observable index, a finite threshold and a non-zero "
+                 "direction are required");
+    return TE_ERR_INVALID_ARG;
+  }
+  if (ev->stops.count >= TE_MAX_STOP_CONDITIONS) {
+    te_set_error("te_evolver_add_stop_condition: at most %d conditions", TE_MAX_STOP_CONDITIONS);
+    return TE_ERR_UNSUPPORTED;
+  }
+  const int k = ev->stops.count++;
+  ev->stops.obs[k] = obs_index;
+  ev->stops.direction[k] = direction > 0 ? 1 : -1;
+  ev->stops.threshold[k] = threshold;
   return TE_OK;
 }
 

@@ -49,7 +49,7 @@ struct TeDevState {
   double t_now, t_sampling, err, t_step;
   int index_samples, n_steps, m_cur, status;
   int err_code_find, nb_err_roundoff, nb_err_int, fatal;  // fatal: TE_ERR_* raised on the device
-  int done, pad_p0, pad_p1, pad_p2;
+  int done, stop_flag, pad_p1, pad_p2;  // stop_flag: k + 1 when a stop condition holds at batch sample k
   // current step
   double err_step, h;
   int breakdown, m_eff, step_code, n_integrals;
@@ -212,6 +212,21 @@ void te_launch_lanczos_update(int64_t n, const double2* w, const double2* u_j, d
 // passes.  cols[j]: the basis columns of the step.
 bool te_launch_lanczos_step(const TeSell& A, bool is_real, double2* const* cols, int m, double2* w, TeDevState* ds,
                             double* partials, cudaStream_t st);
+// Device-side stop conditions: after a batch of samples, ds->stop_flag = k + 1
+// for the first sample k of the batch at which results[obs][sample] >= threshold
+// (direction > 0) or <= threshold (direction < 0) for any condition (te_sample.cu).
+#define TE_MAX_STOP_CONDITIONS 4
+struct TeStopConds {
+  int count;
+  int obs[TE_MAX_STOP_CONDITIONS];
+  int direction[TE_MAX_STOP_CONDITIONS];
+  double threshold[TE_MAX_STOP_CONDITIONS];
+};
+void te_launch_stop_check(const TeStopConds& c, const double* results, int n_samples_total, TeDevState* ds,
+                          cudaStream_t st);
+// Re <psi|O|psi> of a dense column-major O on the original ordering (te_sample.cu).
+void te_launch_dense_obs(int64_t n, const double2* O, const double2* psi_orig, TeDevState* ds, int sample_in_batch,
+                         double* partials, double* results_row, cudaStream_t st);
 // Choose the lanes per row of a square matrix's SpMV passes (te_lanczos.cu).
 int te_tune_sell_lanes(te_matrix_s* A);
 // Gram-Schmidt passes of the reorthogonalising Lanczos mode (te_lanczos.cu)

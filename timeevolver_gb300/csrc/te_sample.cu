@@ -217,6 +217,76 @@ void te_launch_general_obs(const te_matrix_s& O, const double2* psi_orig, TeDevS
                                                            sample_in_batch, partials, results_row);
 }
 
+// Dense observable: Re sum_i conj(psi_i) (O psi)_i for a column-major complex O
+// on the original ordering (the zgemv + zdotc of krylovObservables.cpp:119-138).
+// One thread per row (column-major: a warp reads 32 consecutive entries of a
+// column); psi is staged through shared memory in tiles.
+#define TE_DENSE_TILE 1024
+__global__ void __launch_bounds__(TE_THREADS) dense_obs_kernel(int64_t n, const double2* __restrict__ O,
+                                                               const double2* __restrict__ psi, TeDevState* ds,
+                                                               int sample_in_batch, double* partials,
+                                                               double* results_row) {
+  __shared__ double2 tile[TE_DENSE_TILE];
+  __shared__ double scratch[32];
+  if (ds->fatal != 0) return;
+  double acc[1] = {0.0};
+  const int64_t rows_per_pass = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r0 = (int64_t)blockIdx.x * blockDim.x; r0 < n; r0 += rows_per_pass) {
+    const int64_t r = r0 + threadIdx.x;
+    double yr = 0.0, yi = 0.0;
+    for (int64_t j0 = 0; j0 < n; j0 += TE_DENSE_TILE) {
+      const int64_t jn = min((int64_t)TE_DENSE_TILE, n - j0);
+      __syncthreads();
+      for (int64_t k = threadIdx.x; k < jn; k += blockDim.x) tile[k] = psi[j0 + k];
+      __syncthreads();
+      if (r < n) {
+        const double2* __restrict__ col = O + j0 * n + r;
+        for (int64_t k = 0; k < jn; ++k) {
+          const double2 a = col[k * n];
+          const double2 x = tile[k];
+          yr = fma(a.x, x.x, fma(-a.y, x.y, yr));
+          yi = fma(a.x, x.y, fma(a.y, x.x, yi));
+        }
+      }
+    }
+    if (r < n) {
+      const double2 p = psi[r];
+      acc[0] = fma(p.x, yr, fma(p.y, yi, acc[0]));
+    }
+  }
+  te_block_sum<1>(acc, scratch);
+  if (te_publish_partials<1>(acc, partials, &ds->counter[3])) {
+    double tot[1];
+    te_final_sum<1>(tot, partials, &ds->counter[3], scratch);
+    if (threadIdx.x == 0) results_row[ds->sample_base + sample_in_batch] = tot[0];
+  }
+}
+
+void te_launch_dense_obs(int64_t n, const double2* O, const double2* psi_orig, TeDevState* ds, int sample_in_batch,
+                         double* partials, double* results_row, cudaStream_t st) {
+  const int grid = te_grid_fit((const void*)dense_obs_kernel, n, TE_THREADS);
+  dense_obs_kernel<<<grid, TE_THREADS, 0, st>>>(n, O, psi_orig, ds, sample_in_batch, partials, results_row);
+}
+
+__global__ void stop_check_kernel(TeStopConds c, const double* __restrict__ results, int n_samples_total,
+                                  TeDevState* ds) {
+  if (threadIdx.x != 0 || ds->fatal != 0 || ds->stop_flag != 0) return;
+  const int S = ds->samples_in_batch, base = ds->sample_base;
+  for (int s = 0; s < S; ++s)
+    for (int k = 0; k < c.count; ++k) {
+      const double v = results[(int64_t)c.obs[k] * n_samples_total + base + s];
+      if (c.direction[k] > 0 ? v >= c.threshold[k] : v <= c.threshold[k]) {
+        ds->stop_flag = s + 1;
+        return;
+      }
+    }
+}
+
+void te_launch_stop_check(const TeStopConds& c, const double* results, int n_samples_total, TeDevState* ds,
+                          cudaStream_t st) {
+  stop_check_kernel<<<1, 32, 0, st>>>(c, results, n_samples_total, ds);
+}
+
 // ||x||^2 into ds->norm2_final (cblas_dznrm2 of :446).
 __global__ void __launch_bounds__(TE_THREADS) norm2_kernel(int64_t n, const double2* __restrict__ x, TeDevState* ds,
                                                            double* partials) {

@@ -112,6 +112,12 @@ int te_matrix_create_csr_device(int64_t n_rows, int64_t n_cols, int64_t nnz, con
 int te_matrix_create_zipf(int64_t n, double exponent, int32_t min_len, int32_t max_len, uint64_t seed,
                           int32_t power_iters, double* norm_estimate, te_matrix* out);
 
+/* Layout of a square matrix: SELL-32 slots (stored entries plus padding), and
+ * the rows kept out of the chunks because they are longer than
+ * max(1024, 32 x the mean row length) (multiplied warp-per-row) with their
+ * entries.  No counterpart in the reference. */
+int te_matrix_layout(te_matrix A, int64_t* sell_slots, int64_t* long_rows, int64_t* long_entries);
+
 /* Lanes per row of the matrix's SELL-32 SpMV passes (no counterpart in the
  * reference).  1: one lane per row (the layout's native form); 2 or 4: each
  * row's entries are split over 2 or 4 lanes of a warp, which multiplies the

@@ -66,3 +66,51 @@ def test_coo_upload_rejects_out_of_range(te_gpu):
     col[123_456] = N
     with pytest.raises(RuntimeError, match="entry 123456 out of range"):
         te_gpu.Matrix(N, row, col, val)
+
+
+def _hub_matrix(n, hubs, hub_len, seed, complex_values=True):
+    """A Hermitian matrix with a few 'hub' rows far longer than the rest."""
+    rng = np.random.default_rng(seed)
+    ent = {}
+    for r in range(n):
+        for c in rng.integers(0, n, size=4):
+            ent[(r, int(c))] = ent.get((r, int(c)), 0) + rng.standard_normal() + (1j * rng.standard_normal()
+                                                                                     if complex_values else 0)
+    for h in hubs:
+        for c in rng.choice(n, size=hub_len, replace=False):
+            ent[(h, int(c))] = ent.get((h, int(c)), 0) + rng.standard_normal() + (1j * rng.standard_normal()
+                                                                                    if complex_values else 0)
+    herm = {}
+    for (r, c), v in ent.items():
+        herm[(r, c)] = herm.get((r, c), 0) + v / 2
+        herm[(c, r)] = herm.get((c, r), 0) + np.conj(v) / 2
+    keys = sorted(herm)
+    row = np.array([k[0] for k in keys], dtype=np.int64)
+    col = np.array([k[1] for k in keys], dtype=np.int64)
+    val = np.array([herm[k] for k in keys], dtype=np.complex128)
+    return row, col, val
+
+
+@pytest.mark.parametrize("n,complex_values", [(6000, True), (6000, False), (40000, True)])
+def test_long_rows_layout_and_evolution(te_gpu, oracle_lib, n, complex_values):
+    """Rows far longer than the rest (3 hubs of 3000 entries among rows of ~8)
+    are kept out of the SELL chunks and multiplied warp-per-row: no chunk
+    padding, exact SpMV, an evolution within the parity bounds.  n = 40000
+    exceeds the device-conversion threshold (the layout is built by kernels)."""
+    row, col, val = _hub_matrix(n, [17, n // 2, n - 1], 3000, 11, complex_values)
+    M = te_gpu.Matrix(n, row, col, val)
+    lay = M.layout()
+    assert lay["long_rows"] == 3
+    assert lay["sell_slots"] <= 1.05 * (len(val) - lay["long_entries"]) + 32 * 64  # a few padded chunks at most
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    y = np.zeros(n, dtype=np.complex128)
+    np.add.at(y, row, val * x[col])
+    assert np.max(np.abs(M.spmv(x) - y)) < 1e-12 * np.max(np.abs(y))
+    v = x / np.linalg.norm(x)
+    d = (np.arange(n), np.arange(n), rng.uniform(-1, 1, n).astype(np.complex128))
+    gpu = te_gpu.evolve(M, v, 1.0, 0.25, [("sparse", d)], tol=1e-8, m=30)
+    ref = oracle_lib.evolve((row, col, val), v, 1.0, 0.25, [("sparse", d)], tol=1e-8, m=30)
+    assert gpu["status"] == ref["status"] and gpu["n_steps"] == ref["n_steps"]
+    assert np.linalg.norm(gpu["state"] - ref["state"]) < 2e-8
+    assert np.max(np.abs(gpu["samples"] - ref["samples"])) < 4e-8

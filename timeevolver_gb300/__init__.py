@@ -69,6 +69,7 @@ SIGNATURES = {
     "te_matrix_create_csr_device": (_I, [_I64, _I64, _I64, _P, _P, _P, _I, _P]),
     "te_matrix_download_csr": (_I, [_P, _P, _P, _P]),
     "te_matrix_set_spmv_lanes": (_I, [_P, _I]),
+    "te_matrix_layout": (_I, [_P, _P, _P, _P]),
     "te_matrix_spmv_lanes": (_I, [_P, _I]),
     "te_matrix_create_zipf": (_I, [_I64, _D, ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_int32, _P, _P]),
     "te_evolver_create": (_I, [_P, _P, _P, _P]),
@@ -220,6 +221,13 @@ class Matrix:
         val = np.zeros(max(1, inf["nnz"]), dtype=np.complex128)
         _check(lib().te_matrix_download_csr(self.handle, _ptr(rp), _ptr(ci), _ptr(val)), "te_matrix_download_csr")
         return rp, ci[:inf["nnz"]], val[:inf["nnz"]]
+
+    def layout(self):
+        """SELL-32 slots, long rows and their entries (te_matrix_layout)."""
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _check(lib().te_matrix_layout(self.handle, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+               "te_matrix_layout")
+        return dict(sell_slots=a.value, long_rows=b.value, long_entries=c.value)
 
     def spmv_lanes(self, tune=True):
         """Lanes per row of the SpMV passes (tuned on first use unless pinned)."""

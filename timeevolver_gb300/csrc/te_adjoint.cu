@@ -309,6 +309,10 @@ int build_pattern(te_adjoint a, const std::vector<HostTerm>& terms) {
   int rc = te_matrix_create_csr(n, n, nnz, rp.data(), ci.data(), vv.data(), 1, &a->Hth);
   if (rc != TE_OK) return rc;
   te_matrix H = a->Hth;
+  if (H->sell.n_long > 0) {  // the bilinear pass walks the SELL slots only
+    te_set_error("te_adjoint_create: H has long rows (above max(1024, 32 x mean) entries); not supported");
+    return TE_ERR_UNSUPPORTED;
+  }
   const int vw = H->is_real ? 1 : 2;
   // SELL slot -> CSR entry (the layout built by te_matrix.cu: chunk c, lane l,
   // k-th entry of row perm[32 c + l] at chunk_off[c] + 32 k + l)

@@ -793,6 +793,11 @@ extern "C" int te_batch_create(int n_instances, const te_matrix* H, const double
                    "batched)", i);
       return fail(TE_ERR_INVALID_ARG);
     }
+    if (H[i]->sell.n_long > 0) {
+      te_set_error("te_batch_create: instance %d: matrices with long rows (above max(1024, 32 x mean) entries) are "
+                   "not batched", i);
+      return fail(TE_ERR_UNSUPPORTED);
+    }
     const int64_t n = H[i]->n_rows;
     double nrm = 0.0;
     for (int64_t k = 0; k < 2 * n; ++k) nrm += v_host[i][k] * v_host[i][k];

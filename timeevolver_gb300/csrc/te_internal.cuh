@@ -111,7 +111,24 @@ struct TeSell {
   // or set through te_matrix_set_spmv_lanes; lanes_fixed once chosen
   int lanes = 1;
   bool lanes_fixed = false;
+  // Long rows: rows longer than max(1024, 32 x mean length) -- the first n_long
+  // rows of the sorted order -- have no slots in the chunks (one of them would
+  // pad its chunk to 32 x its length); their entries form a CSR in the sorted
+  // basis that the SpMV passes multiply warp-per-row.
+  int64_t n_long = 0;
+  int64_t* long_ptr = nullptr;  // n_long + 1
+  int32_t* long_col = nullptr;  // sorted-basis columns
+  double* long_val = nullptr;   // real: 1, complex: 2 doubles per entry
 };
+
+// The long rows of a SELL matrix, by value for kernels.
+struct TeLongRows {
+  int64_t n;
+  const int64_t* ptr;
+  const int32_t* col;
+  const double* val;
+};
+inline TeLongRows te_long_rows(const TeSell& S) { return TeLongRows{S.n_long, S.long_ptr, S.long_col, S.long_val}; }
 
 struct te_matrix_s {
   int64_t n_rows = 0, n_cols = 0, nnz = 0;

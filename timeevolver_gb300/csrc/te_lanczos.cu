@@ -71,7 +71,7 @@ __device__ __forceinline__ void apply_row_epilogue(int64_t r, double2 y, double 
 template <bool REAL, bool HAS_PREV, bool FOLD, int K>
 __global__ void __launch_bounds__(TE_THREADS, (REAL && K == 1) ? 6 : 5) lanczos_apply_kernel(
     int64_t n, int64_t n_chunks, const int32_t* __restrict__ warp_chunk, const int64_t* __restrict__ chunk_off,
-    const int32_t* __restrict__ col, const double* __restrict__ val, const double2* __restrict__ u_j,
+    const int32_t* __restrict__ col, const double* __restrict__ val, TeLongRows L, const double2* __restrict__ u_j,
     const double2* __restrict__ u_jm1, double2* __restrict__ w, TeDevState* ds, double* partials, int j) {
   __shared__ double scratch[2 * 32];
   te_pdl_trigger();
@@ -91,11 +91,16 @@ __global__ void __launch_bounds__(TE_THREADS, (REAL && K == 1) ? 6 : 5) lanczos_
   double acc[2] = {0.0, 0.0};
   const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (K == 1) {
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t lr = wid; lr < L.n; lr += warps) {  // long rows (sorted rows 0..L.n-1), warp-per-row
+      const double2 y = te_long_row<REAL>(L, lr, u_j, lane);
+      if (lane == 0) apply_row_epilogue<HAS_PREV, FOLD>(lr, y, g, cw, u_j, u_jm1, w, acc);
+    }
     const int64_t c_end = warp_chunk[wid + 1];
     for (int64_t c = warp_chunk[wid]; c < c_end; ++c) {
       const double2 y = te_sell_row<REAL>(chunk_off, col, val, u_j, c, lane);
       const int64_t r = c * 32 + lane;
-      if (r < n) apply_row_epilogue<HAS_PREV, FOLD>(r, y, g, cw, u_j, u_jm1, w, acc);
+      if (r < n && r >= L.n) apply_row_epilogue<HAS_PREV, FOLD>(r, y, g, cw, u_j, u_jm1, w, acc);
     }
   } else {
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -285,7 +290,7 @@ __global__ void __launch_bounds__(TE_THREADS, REAL ? 6 : 5) lanczos_step_kernel(
 
 bool te_launch_lanczos_step(const TeSell& A, bool is_real, double2* const* cols, int m, double2* w, TeDevState* ds,
                             double* partials, cudaStream_t st) {
-  if (A.lanes != 1 || m < 1 || m > TE_MMAX) return false;
+  if (A.lanes != 1 || A.n_long > 0 || m < 1 || m > TE_MMAX) return false;
   static int coop = -1;
   if (coop < 0) {
     int dev = 0, v = 0;
@@ -563,7 +568,7 @@ void te_launch_gs_update_norm(int64_t n, const TeBasisPtrs& V, int nvec, const d
 namespace {
 
 using ApplyKernel = void (*)(int64_t, int64_t, const int32_t*, const int64_t*, const int32_t*, const double*,
-                             const double2*, const double2*, double2*, TeDevState*, double*, int);
+                             TeLongRows, const double2*, const double2*, double2*, TeDevState*, double*, int);
 
 template <int K>
 ApplyKernel apply_kernel_for(bool is_real, bool has_prev, bool fold) {
@@ -607,7 +612,7 @@ void te_launch_lanczos_apply(const TeSell& A, bool is_real, const double2* u_j, 
   const ApplyKernel k = apply_kernel(lanes, is_real, u_jm1 != nullptr, fold);
   const int grid = lanes == 1 ? A.grid : apply_grid_k(A, lanes, k);
   te_launch_pdl(lanes == 1 && A.saturated, k, grid, TE_THREADS, st, A.n, A.n_chunks, A.warp_chunk, A.chunk_off,
-                A.col, A.val, u_j, u_jm1, w, ds, partials, j);
+                A.col, A.val, te_long_rows(A), u_j, u_jm1, w, ds, partials, j);
 }
 
 // Autotuning of the lanes per row: time the three-term apply pass (the
@@ -622,7 +627,7 @@ int te_tune_sell_lanes(te_matrix_s* A) {
   if (S.lanes_fixed) return TE_OK;
   const int64_t resident_warps = (int64_t)te_num_sms() * te_sell_blocks_per_sm(A->is_real) * (TE_THREADS / 32);
   S.lanes = 1;
-  if (S.n_chunks >= 8 * resident_warps || S.n_chunks < 2048) {
+  if (S.n_chunks >= 8 * resident_warps || S.n_chunks < 2048 || S.n_long > 0) {
     S.lanes_fixed = true;
     return TE_OK;
   }

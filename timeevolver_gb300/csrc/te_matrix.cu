@@ -33,17 +33,23 @@ __global__ void __launch_bounds__(TE_THREADS) sell_spmv_kernel(int64_t n, int64_
                                                                const int32_t* __restrict__ warp_chunk,
                                                                const int64_t* __restrict__ chunk_off,
                                                                const int32_t* __restrict__ col,
-                                                               const double* __restrict__ val, double2 alpha,
-                                                               const double2* __restrict__ x,
+                                                               const double* __restrict__ val, TeLongRows L,
+                                                               double2 alpha, const double2* __restrict__ x,
                                                                double2* __restrict__ y) {
   const int lane = threadIdx.x & 31;
   const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (K == 1) {
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t lr = wid; lr < L.n; lr += warps) {  // long rows, warp-per-row
+      const double2 acc = te_long_row<REAL>(L, lr, x, lane);
+      if (lane == 0) y[lr] = make_double2(alpha.x * acc.x - alpha.y * acc.y, alpha.x * acc.y + alpha.y * acc.x);
+    }
     const int64_t c_end = warp_chunk[wid + 1];
     for (int64_t c = warp_chunk[wid]; c < c_end; ++c) {
       double2 acc = te_sell_row<REAL>(chunk_off, col, val, x, c, lane);
       int64_t r = c * 32 + lane;
-      if (r < n) y[r] = make_double2(alpha.x * acc.x - alpha.y * acc.y, alpha.x * acc.y + alpha.y * acc.x);
+      if (r < n && r >= L.n)
+        y[r] = make_double2(alpha.x * acc.x - alpha.y * acc.y, alpha.x * acc.y + alpha.y * acc.x);
     }
   } else {
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -79,8 +85,8 @@ __global__ void permute_kernel(int64_t n, const int32_t* __restrict__ idx, const
 
 void te_launch_sell_spmv(const TeSell& A, bool is_real, double2 alpha, const double2* x_perm, double2* y_perm,
                          cudaStream_t st) {
-  using K = void (*)(int64_t, int64_t, const int32_t*, const int64_t*, const int32_t*, const double*, double2,
-                     const double2*, double2*);
+  using K = void (*)(int64_t, int64_t, const int32_t*, const int64_t*, const int32_t*, const double*, TeLongRows,
+                     double2, const double2*, double2*);
   static const K table[2][3] = {{sell_spmv_kernel<false, 1>, sell_spmv_kernel<false, 2>, sell_spmv_kernel<false, 4>},
                                 {sell_spmv_kernel<true, 1>, sell_spmv_kernel<true, 2>, sell_spmv_kernel<true, 4>}};
   const int li = A.lanes == 4 ? 2 : A.lanes == 2 ? 1 : 0;
@@ -90,7 +96,8 @@ void te_launch_sell_spmv(const TeSell& A, bool is_real, double2 alpha, const dou
     const int64_t cap = (int64_t)te_num_sms() * te_kernel_blocks_per_sm((const void*)k, TE_THREADS, 0);
     grid = (int)std::max<int64_t>(1, std::min<int64_t>((A.n_chunks * A.lanes + 7) / 8, cap));
   }
-  k<<<grid, TE_THREADS, 0, st>>>(A.n, A.n_chunks, A.warp_chunk, A.chunk_off, A.col, A.val, alpha, x_perm, y_perm);
+  k<<<grid, TE_THREADS, 0, st>>>(A.n, A.n_chunks, A.warp_chunk, A.chunk_off, A.col, A.val, te_long_rows(A), alpha,
+                                 x_perm, y_perm);
 }
 
 void te_launch_csr_spmv(const te_matrix_s& A, double2 alpha, const double2* x, double2* y, cudaStream_t st) {
@@ -176,7 +183,7 @@ __global__ void diag_sum_kernel(int64_t n, const int32_t* __restrict__ rp, const
 // SELL-32 slots from the CSR: one thread per (chunk, lane), i.e. per sorted
 // row index; padding slots point at the row itself with value 0.
 template <bool REAL>
-__global__ void fill_sell_kernel(int64_t n, int64_t n_chunks, const int64_t* __restrict__ off,
+__global__ void fill_sell_kernel(int64_t n, int64_t n_long, int64_t n_chunks, const int64_t* __restrict__ off,
                                  const int32_t* __restrict__ perm, const int32_t* __restrict__ iperm,
                                  const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
                                  const double2* __restrict__ v, int32_t* __restrict__ scol, double* __restrict__ sval) {
@@ -186,7 +193,7 @@ __global__ void fill_sell_kernel(int64_t n, int64_t n_chunks, const int64_t* __r
     const int lane = (int)(t & 31);
     const int64_t len = (off[c + 1] - off[c]) / 32;
     int64_t p0 = 0, rlen = 0;
-    if (t < n) {
+    if (t < n && t >= n_long) {  // long rows take no chunk slots
       const int32_t r = perm[t];
       p0 = rp[r];
       rlen = rp[r + 1] - p0;
@@ -259,6 +266,9 @@ void free_matrix(te_matrix_s* M) {
   cudaFree(M->sell.perm);
   cudaFree(M->sell.iperm);
   cudaFree(M->sell.warp_chunk);
+  cudaFree(M->sell.long_ptr);
+  cudaFree(M->sell.long_col);
+  cudaFree(M->sell.long_val);
   delete M;
 }
 
@@ -291,10 +301,20 @@ int sell_layout(te_matrix_s* M, const std::vector<int32_t>& rp, bool real, std::
   iperm.assign(n, 0);
   for (int64_t r = 0; r < n; ++r) perm[start[max_len - (rp[r + 1] - rp[r])]++] = (int32_t)r;
   for (int64_t i = 0; i < n; ++i) iperm[perm[i]] = (int32_t)i;
+  // long rows: longer than max(1024, 32 x the mean row length); they lead the
+  // sorted order and take no chunk slots
+  const int64_t nnz = rp[n];
+  const int64_t long_min = std::max<int64_t>(1024, 32 * ((nnz + n - 1) / std::max<int64_t>(n, 1)));
+  S.n_long = 0;
+  while (S.n_long < n && rp[perm[S.n_long] + 1] - rp[perm[S.n_long]] > long_min) ++S.n_long;
   off.assign(S.n_chunks + 1, 0);
   for (int64_t c = 0; c < S.n_chunks; ++c) {
-    int32_t r0 = perm[c * 32];
-    int64_t len = rp[r0 + 1] - rp[r0];  // longest row of the chunk comes first
+    int64_t len = 0;  // rows are sorted: the first row of the chunk that is not long is the longest
+    for (int64_t i = c * 32; i < std::min<int64_t>(n, c * 32 + 32); ++i)
+      if (i >= S.n_long) {
+        len = rp[perm[i] + 1] - rp[perm[i]];
+        break;
+      }
     off[c + 1] = off[c] + 32 * len;
   }
   S.slots = off[S.n_chunks];
@@ -322,6 +342,30 @@ int sell_layout(te_matrix_s* M, const std::vector<int32_t>& rp, bool real, std::
   }
   wc[W] = (int32_t)S.n_chunks;
   return upload(&S.warp_chunk, wc.data(), wc.size());
+}
+
+// The long-row CSR (sorted basis) from host copies of the original CSR.
+int build_long_rows(te_matrix_s* M, const std::vector<int32_t>& rp, const std::vector<int32_t>& ci,
+                    const std::vector<double>& vv, bool real, const std::vector<int32_t>& perm,
+                    const std::vector<int32_t>& iperm) {
+  TeSell& S = M->sell;
+  if (S.n_long == 0) return TE_OK;
+  std::vector<int64_t> lp(S.n_long + 1, 0);
+  std::vector<int32_t> lc;
+  std::vector<double> lv;
+  for (int64_t i = 0; i < S.n_long; ++i) {
+    const int32_t r = perm[i];
+    for (int32_t p = rp[r]; p < rp[r + 1]; ++p) {
+      lc.push_back(iperm[ci[p]]);
+      lv.push_back(vv[2 * p]);
+      if (!real) lv.push_back(vv[2 * p + 1]);
+    }
+    lp[i + 1] = (int64_t)lc.size();
+  }
+  int rc;
+  if ((rc = upload(&S.long_ptr, lp.data(), lp.size())) != TE_OK) return rc;
+  if ((rc = upload(&S.long_col, lc.data(), lc.size())) != TE_OK) return rc;
+  return upload(&S.long_val, lv.data(), lv.size());
 }
 
 // rp/ci/vv: original-order CSR with interleaved complex values.
@@ -383,7 +427,7 @@ int build_matrix(te_matrix_s* M, const std::vector<int32_t>& rp, const std::vect
       int64_t rnew = c * 32 + lane;
       int32_t pad_col = (int32_t)std::min<int64_t>(rnew, n - 1);
       int64_t rlen = 0, p0 = 0;
-      if (rnew < n) {
+      if (rnew < n && rnew >= S.n_long) {
         int32_t r = perm[rnew];
         p0 = rp[r];
         rlen = rp[r + 1] - rp[r];
@@ -406,7 +450,7 @@ int build_matrix(te_matrix_s* M, const std::vector<int32_t>& rp, const std::vect
   }
   if ((rc = upload(&S.col, scol.data(), scol.size())) != TE_OK) return rc;
   if ((rc = upload(&S.val, sval.data(), sval.size())) != TE_OK) return rc;
-  return TE_OK;
+  return build_long_rows(M, rp, ci, vv, real, perm, iperm);
 }
 
 int finish_create(int64_t n_rows, int64_t n_cols, const std::vector<int32_t>& rp, const std::vector<int32_t>& ci,
@@ -518,14 +562,43 @@ int build_matrix_device(te_matrix_s* M, const std::vector<int32_t>& rp_host, int
       const int gf = te_grid_fit(real ? (const void*)fill_sell_kernel<true> : (const void*)fill_sell_kernel<false>,
                                  S.n_chunks * 32, TE_THREADS);
       if (real)
-        fill_sell_kernel<true><<<gf, TE_THREADS>>>(n, S.n_chunks, S.chunk_off, S.perm, S.iperm, d_rp, d_ci, d_v, S.col,
-                                                   S.val);
+        fill_sell_kernel<true><<<gf, TE_THREADS>>>(n, S.n_long, S.n_chunks, S.chunk_off, S.perm, S.iperm, d_rp, d_ci,
+                                                   d_v, S.col, S.val);
       else
-        fill_sell_kernel<false><<<gf, TE_THREADS>>>(n, S.n_chunks, S.chunk_off, S.perm, S.iperm, d_rp, d_ci, d_v,
-                                                    S.col, S.val);
+        fill_sell_kernel<false><<<gf, TE_THREADS>>>(n, S.n_long, S.n_chunks, S.chunk_off, S.perm, S.iperm, d_rp, d_ci,
+                                                    d_v, S.col, S.val);
     }
   }
   if (rc == TE_OK) rc = te_cuda_check(cudaDeviceSynchronize(), "device build");
+  if (rc == TE_OK && M->n_rows == M->n_cols && M->sell.n_long > 0) {
+    // the long rows are few: copy their entries to the host and build their CSR there
+    TeSell& S = M->sell;
+    std::vector<int32_t> perm(n), iperm(n);
+    rc = te_cuda_check(cudaMemcpy(perm.data(), S.perm, sizeof(int32_t) * n, cudaMemcpyDeviceToHost), "long rows");
+    if (rc == TE_OK)
+      rc = te_cuda_check(cudaMemcpy(iperm.data(), S.iperm, sizeof(int32_t) * n, cudaMemcpyDeviceToHost), "long rows");
+    std::vector<int64_t> lp(S.n_long + 1, 0);
+    std::vector<int32_t> lc;
+    std::vector<double> lv;
+    for (int64_t i = 0; i < S.n_long && rc == TE_OK; ++i) {
+      const int32_t r = perm[i];
+      const int64_t b = rp_host[r], len = rp_host[r + 1] - rp_host[r];
+      std::vector<int32_t> c(len);
+      std::vector<double2> v(len);
+      rc = te_cuda_check(cudaMemcpy(c.data(), d_ci + b, sizeof(int32_t) * len, cudaMemcpyDeviceToHost), "long rows");
+      if (rc == TE_OK)
+        rc = te_cuda_check(cudaMemcpy(v.data(), d_v + b, sizeof(double2) * len, cudaMemcpyDeviceToHost), "long rows");
+      for (int64_t k = 0; k < len && rc == TE_OK; ++k) {
+        lc.push_back(iperm[c[k]]);
+        lv.push_back(v[k].x);
+        if (!real) lv.push_back(v[k].y);
+      }
+      lp[i + 1] = (int64_t)lc.size();
+    }
+    if (rc == TE_OK) rc = upload(&S.long_ptr, lp.data(), lp.size());
+    if (rc == TE_OK) rc = upload(&S.long_col, lc.data(), lc.size());
+    if (rc == TE_OK) rc = upload(&S.long_val, lv.data(), lv.size());
+  }
   if (real) cudaFree(d_v);
   cleanup();
   return rc;
@@ -811,10 +884,30 @@ extern "C" int te_matrix_download_csr(te_matrix A, int32_t* row_ptr, int32_t* co
   return TE_OK;
 }
 
+extern "C" int te_matrix_layout(te_matrix A, int64_t* sell_slots, int64_t* long_rows, int64_t* long_entries) {
+  if (!A || A->n_rows != A->n_cols) {
+    te_set_error("te_matrix_layout: square matrix required");
+    return TE_ERR_INVALID_ARG;
+  }
+  if (sell_slots) *sell_slots = A->sell.slots;
+  if (long_rows) *long_rows = A->sell.n_long;
+  if (long_entries) {
+    int64_t e = 0;
+    if (A->sell.n_long > 0)
+      TE_CUDA(cudaMemcpy(&e, A->sell.long_ptr + A->sell.n_long, sizeof(int64_t), cudaMemcpyDeviceToHost));
+    *long_entries = e;
+  }
+  return TE_OK;
+}
+
 extern "C" int te_matrix_set_spmv_lanes(te_matrix A, int lanes) {
   if (!A || A->n_rows != A->n_cols || !(lanes == 0 || lanes == 1 || lanes == 2 || lanes == 4)) {
     te_set_error("te_matrix_set_spmv_lanes: square matrix and lanes 0 (tune), 1, 2 or 4 required");
     return TE_ERR_INVALID_ARG;
+  }
+  if (lanes > 1 && A->sell.n_long > 0) {
+    te_set_error("te_matrix_set_spmv_lanes: a matrix with long rows uses one lane per row");
+    return TE_ERR_UNSUPPORTED;
   }
   A->sell.lanes = lanes == 0 ? 1 : lanes;
   A->sell.lanes_fixed = lanes != 0;

@@ -126,3 +126,36 @@ __device__ __forceinline__ double2 te_sell_row_k(const int64_t* __restrict__ chu
   }
   return make_double2(re, im);
 }
+
+// One long row (row lr of the long-row CSR) by a whole warp: lanes stride over
+// its entries, then a warp sum; the result is returned to every lane.
+template <bool REAL, bool XCG = false>
+__device__ __forceinline__ double2 te_long_row(const TeLongRows& L, int64_t lr, const double2* __restrict__ x,
+                                               int lane) {
+  const int64_t b = __ldg(L.ptr + lr), e = __ldg(L.ptr + lr + 1);
+  double re = 0.0, im = 0.0;
+  if (REAL) {
+    for (int64_t p = b + lane; p < e; p += 32) {
+      const double a = __ldcs(L.val + p);
+      const double2 xv = te_load_x<XCG>(x, __ldcs(L.col + p));
+      re = fma(a, xv.x, re);
+      im = fma(a, xv.y, im);
+    }
+  } else {
+    const double2* __restrict__ v2 = reinterpret_cast<const double2*>(L.val);
+    for (int64_t p = b + lane; p < e; p += 32) {
+      const double2 a = __ldcs(v2 + p);
+      const double2 xv = te_load_x<XCG>(x, __ldcs(L.col + p));
+      re = fma(a.x, xv.x, re);
+      re = fma(-a.y, xv.y, re);
+      im = fma(a.x, xv.y, im);
+      im = fma(a.y, xv.x, im);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    re += __shfl_xor_sync(0xffffffffu, re, o);
+    im += __shfl_xor_sync(0xffffffffu, im, o);
+  }
+  return make_double2(re, im);
+}

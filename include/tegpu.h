@@ -131,6 +131,34 @@ int te_matrix_set_spmv_lanes(te_matrix A, int lanes);
  * choice is still open; a negative value is an error code. */
 int te_matrix_spmv_lanes(te_matrix A, int tune_now);
 
+/* ------------------------------------------------- models built on the GPU */
+
+/* One operator term, as TE::opTerm (helper/hamiltonian.h): coefficient times
+ * a sequence of n_ops ladder operations applied in order to the state,
+ * operation +1 (creation, blocked above capacity when capacity != 0) or -1
+ * (annihilation) on mode[k]; up to 8 operations. */
+typedef struct te_term {
+  double coef_re, coef_im;
+  int32_t n_ops;
+  int32_t operation[8];
+  int32_t mode[8];
+  int32_t capacity[8];
+} te_term;
+
+/* Matrix of sum_terms on the number-conserving basis basis(n_particles,
+ * n_modes, 0, 0, quant) of helper/Basis.cpp, built on the GPU in the
+ * reference's basis order and with createMatrix's rules
+ * (helper/hamiltonian.cpp:318-402: terms applied per row in order, equal
+ * columns merged in term order, columns ascending, |v| < DBL_EPSILON dropped),
+ * so the result equals the host builder's entry for entry.  The 1-norm is the
+ * reference's for Hermitian term lists.  Up to 64 modes, 255 particles, 64
+ * terms; *dim receives the dimension. */
+int te_model_create_device(int n_particles, int n_modes, int quant, const te_term* terms, int n_terms,
+                           te_matrix* out, int64_t* dim);
+/* Index of an occupation vector (n_modes ints) in that basis, -1 if it is not
+ * a basis state. */
+int te_model_state_index(int n_particles, int n_modes, int quant, const int32_t* occupation, int64_t* index);
+
 /* Copy a matrix's original-order CSR to host buffers: row_ptr (n_rows + 1),
  * col_idx (nnz), values (nnz interleaved complex doubles). */
 int te_matrix_download_csr(te_matrix A, int32_t* row_ptr, int32_t* col_idx, double* values);

@@ -70,6 +70,8 @@ SIGNATURES = {
     "te_matrix_download_csr": (_I, [_P, _P, _P, _P]),
     "te_matrix_set_spmv_lanes": (_I, [_P, _I]),
     "te_matrix_layout": (_I, [_P, _P, _P, _P]),
+    "te_model_create_device": (_I, [_I, _I, _I, _P, _I, _P, _P]),
+    "te_model_state_index": (_I, [_I, _I, _I, _P, _P]),
     "te_matrix_spmv_lanes": (_I, [_P, _I]),
     "te_matrix_create_zipf": (_I, [_I64, _D, ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_int32, _P, _P]),
     "te_evolver_create": (_I, [_P, _P, _P, _P]),
@@ -137,6 +139,15 @@ def lib():
     return _lib
 
 
+def state_index_device(n_particles, occupation, quant=1):
+    """Index of an occupation vector in basis(n_particles, len(occupation)) (te_model_state_index)."""
+    occ = np.ascontiguousarray(occupation, dtype=np.int32)
+    r = ctypes.c_int64()
+    _check(lib().te_model_state_index(int(n_particles), len(occ), int(quant), _ptr(occ), ctypes.byref(r)),
+           "te_model_state_index")
+    return r.value
+
+
 def probe_fp64_tflops():
     """Measured FP64 FMA throughput of the current device (TFLOP/s)."""
     x = ctypes.c_double()
@@ -163,6 +174,11 @@ def _as_u64(a):
 
 
 OPT_FUSED_LANCZOS = 1
+
+
+class TeTerm(ctypes.Structure):
+    _fields_ = [("coef_re", ctypes.c_double), ("coef_im", ctypes.c_double), ("n_ops", ctypes.c_int32),
+                ("operation", ctypes.c_int32 * 8), ("mode", ctypes.c_int32 * 8), ("capacity", ctypes.c_int32 * 8)]
 
 
 class Matrix:
@@ -212,6 +228,24 @@ class Matrix:
                                            int(power_iters), ctypes.byref(est), ctypes.byref(h)),
                "te_matrix_create_zipf")
         return cls._adopt(h), est.value
+
+    @classmethod
+    def from_terms_device(cls, n_particles, n_modes, terms, quant=1):
+        """Operator matrix built on the GPU (te_model_create_device) from terms
+        (coef, operations, modes, capacities) -- the tuples of
+        timeevolver_gb300.models -- on basis(n_particles, n_modes).
+        Returns (Matrix, dim)."""
+        arr = (TeTerm * len(terms))()
+        for t, (coef, ops, modes, caps) in zip(arr, terms):
+            c = complex(coef)
+            t.coef_re, t.coef_im, t.n_ops = c.real, c.imag, len(ops)
+            for k, (o, m_, cp) in enumerate(zip(ops, modes, caps)):
+                t.operation[k], t.mode[k], t.capacity[k] = o, m_, cp
+        h = ctypes.c_void_p()
+        dim = ctypes.c_int64()
+        _check(lib().te_model_create_device(int(n_particles), int(n_modes), int(quant), arr, len(terms),
+                                            ctypes.byref(h), ctypes.byref(dim)), "te_model_create_device")
+        return cls._adopt(h), dim.value
 
     def to_csr(self):
         """(row_ptr int32, col int32, values complex128) of the original-order CSR, on the host."""

@@ -149,6 +149,28 @@ def bose_hubbard(L, N, J, U, mu=0.0):
     return B, operator_matrix(terms, B)
 
 
+def bose_hubbard_terms(L, J, U, mu=0.0):
+    """The terms of bose_hubbard (same order)."""
+    Js = list(J) if np.ndim(J) else [J] * (L - 1)
+    terms = []
+    for b in range(L - 1):
+        terms.append(lin_interaction(b, b + 1, 0, 0, False, -Js[b]))
+        terms.append(lin_interaction(b, b + 1, 0, 0, True, -Js[b]))
+    for i in range(L):
+        terms.append(four_point_a(i, i, i, i, 0, 0, 0, 0, U / 2.0))
+        terms.append(number_operator(i, -U / 2.0))
+        if mu != 0.0:
+            terms.append(number_operator(i, -mu))
+    return terms
+
+
+def bose_hubbard_device(L, N, J, U, mu=0.0):
+    """bose_hubbard built on the GPU: returns (Matrix, dim); the basis and the
+    entries equal the host builder's."""
+    from . import Matrix
+    return Matrix.from_terms_device(N, L, bose_hubbard_terms(L, J, U, mu))
+
+
 def bose_hubbard_term_matrices(L, N):
     """Terms of H(theta) = sum_b J_b H_hop,b + U H_int for the adjoint:
     H_hop,b = -(a_b^dag a_{b+1} + h.c.) for the L-1 bonds, H_int = 1/2 sum_i

@@ -74,6 +74,7 @@ __global__ void __launch_bounds__(TE_THREADS, (REAL && K == 1) ? 6 : 5) lanczos_
     const int32_t* __restrict__ col, const double* __restrict__ val, TeLongRows L, const double2* __restrict__ u_j,
     const double2* __restrict__ u_jm1, double2* __restrict__ w, TeDevState* ds, double* partials, int j) {
   __shared__ double scratch[2 * 32];
+  __shared__ double wide[2 * TE_THREADS];
   te_pdl_trigger();
   te_pdl_wait();
   if (te_step_inactive(ds)) return;
@@ -112,7 +113,7 @@ __global__ void __launch_bounds__(TE_THREADS, (REAL && K == 1) ? 6 : 5) lanczos_
       if (lane % K == 0 && r < n) apply_row_epilogue<HAS_PREV, FOLD>(r, y, g, cw, u_j, u_jm1, w, acc);
     }
   }
-  te_block_sum<2>(acc, scratch);
+  te_block_sum_wide<2>(acc, wide);
   if (te_publish_partials<2>(acc, partials, &ds->counter[0])) {
     double tot[2];
     te_final_sum<2>(tot, partials, &ds->counter[0], scratch);
@@ -204,6 +205,7 @@ template <bool REAL>
 __global__ void __launch_bounds__(TE_THREADS, REAL ? 6 : 5) lanczos_step_kernel(TeLanczosArgs a, TeDevState* ds) {
   __shared__ double scratch[2 * 32];
   __shared__ double bcast[2];
+  __shared__ double wide[2 * TE_THREADS];
   if (te_step_inactive(ds)) return;
   const int lane = threadIdx.x & 31;
   const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -233,7 +235,7 @@ __global__ void __launch_bounds__(TE_THREADS, REAL ? 6 : 5) lanczos_step_kernel(
         if (r < a.n) apply_row_epilogue<false, true, true>(r, y, g, 0.0, uj, nullptr, a.w, acc);
       }
     }
-    te_block_sum<2>(acc, scratch);
+    te_block_sum_wide<2>(acc, wide);
     if (threadIdx.x == 0) {
       a.partials[blockIdx.x] = acc[0];
       a.partials[G + blockIdx.x] = acc[1];
@@ -260,7 +262,7 @@ __global__ void __launch_bounds__(TE_THREADS, REAL ? 6 : 5) lanczos_step_kernel(
         nrm[0] = fma(o.x, o.x, fma(o.y, o.y, nrm[0]));
       }
     }
-    te_block_sum<1>(nrm, scratch);
+    te_block_sum_wide<1>(nrm, wide);
     if (threadIdx.x == 0) a.partials[2 * G + blockIdx.x] = nrm[0];
     if (!te_grid_barrier(&ds->bar_count, &ds->bar_gen, &ds->fatal)) return;
     double t2[1];
@@ -336,6 +338,7 @@ __global__ void __launch_bounds__(TE_THREADS) lanczos_update_kernel(int64_t n, c
                                                                     double2* __restrict__ u_jp1, TeDevState* ds,
                                                                     double* partials, int j, int fold) {
   __shared__ double scratch[32];
+  __shared__ double wide[TE_THREADS];
   te_pdl_trigger();
   te_pdl_wait();
   if (te_step_inactive(ds)) return;
@@ -354,7 +357,7 @@ __global__ void __launch_bounds__(TE_THREADS) lanczos_update_kernel(int64_t n, c
     if (STORE) u_jp1[r] = o;
     acc[0] = fma(o.x, o.x, fma(o.y, o.y, acc[0]));
   }
-  te_block_sum<1>(acc, scratch);
+  te_block_sum_wide<1>(acc, wide);
   if (te_publish_partials<1>(acc, partials, &ds->counter[1])) {
     double tot[1];
     te_final_sum<1>(tot, partials, &ds->counter[1], scratch);

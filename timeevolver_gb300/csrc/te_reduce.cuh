@@ -37,6 +37,28 @@ __device__ __forceinline__ void te_block_sum(double (&v)[NV], double* scratch) {
   __syncthreads();
 }
 
+// Block sum through shared memory first: every thread stores its NV values
+// (wide: NV * blockDim.x doubles), then warp 0 adds blockDim.x / 32 values per
+// lane and finishes with one shuffle tree.  The FP64 pipe sees
+// blockDim.x / 32 + 5 warp-wide additions per value instead of 5 per warp and
+// 5 more, which matters for passes bound by FP64 issue.  Result in thread 0.
+template <int NV>
+__device__ __forceinline__ void te_block_sum_wide(double (&v)[NV], double* wide) {
+  const int t = threadIdx.x, B = blockDim.x;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) wide[k * B + t] = v[k];
+  __syncthreads();
+  if (t < 32) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double s = wide[k * B + t];
+      for (int i = t + 32; i < B; i += 32) s += wide[k * B + i];
+      v[k] = te_warp_sum(s);
+    }
+  }
+  __syncthreads();
+}
+
 // Publish NV per-block partials and return true in the block that must do
 // the final reduction.  Call from all threads; thread 0 holds the values.
 template <int NV>

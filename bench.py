@@ -160,18 +160,20 @@ def build_problem():
     return n, H, O, v
 
 
-def apply_kernel_bytes(n, nnz, real=True):
+def apply_kernel_bytes(n, nnz, real=True, fixed=False):
     """Algorithmic bytes of one Lanczos apply launch: the matrix (values +
     int32 columns), the SELL chunk offsets, x = u_j read once, u_{j-1} read,
-    w written."""
+    w written.  The fixed-point apply reads the fixed-point copy of u_j (16
+    bytes per row, gathered) and u_j itself for <u_j, w'> (16 more)."""
     chunks = (n + 31) // 32
-    return nnz * ((8 if real else 16) + 4) + 8 * (chunks + 1) + 3 * 16 * n
+    return nnz * ((8 if real else 16) + 4) + 8 * (chunks + 1) + (4 if fixed else 3) * 16 * n
 
 
-def apply_kernel_flops(n, nnz, real=True):
+def apply_kernel_flops(n, nnz, real=True, fixed=False):
     """FP64 flops of one Lanczos apply launch: 2 (real) or 4 (complex) FMAs per
-    non-zero, 14 per row for the recurrence term and the <v_j, w> partial."""
-    return nnz * (4 if real else 8) + 14 * n
+    non-zero (none in the fixed-point SpMV), 14 per row for the recurrence
+    term and the <v_j, w> partial."""
+    return (0 if fixed else nnz * (4 if real else 8)) + 14 * n
 
 
 KERNEL_KINDS = ["lanczos_apply", "lanczos_update", "krylov_step", "combine", "observables"]
@@ -204,6 +206,9 @@ def run_gb300(args):
     O = te.Matrix.from_coo(n, Oc)
     info = H.info()
     ev = te.Evolver(H, v, T_FINAL, SAMPLING, [("sparse", O)], tol=TOL, m=M_KRYLOV)
+    options = {te.OPT_FIXED_SPMV: 1 if args.spmv == "fixed" else 0}
+    for opt, val in options.items():
+        ev.set_option(opt, val)
     v_dev = torch.from_numpy(v.view(np.float64).copy()).cuda()
     for _ in range(args.warmup):
         ev.reset(None, device_ptr=v_dev.data_ptr())
@@ -239,7 +244,7 @@ def run_gb300(args):
     for _ in range(max(1, args.steps)):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        out = te.evolve(Hc, v, T_FINAL, SAMPLING, [("sparse", Oc)], tol=TOL, m=M_KRYLOV)
+        out = te.evolve(Hc, v, T_FINAL, SAMPLING, [("sparse", Oc)], tol=TOL, m=M_KRYLOV, options=options)
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t0)
     e2e_s = max_over_ranks(dist, float(np.mean(e2e_times)))
@@ -250,8 +255,9 @@ def run_gb300(args):
         return
     value = replica_seconds_per_solve(ms, args.steps, ws)
     peaks = load_peaks(te)
-    b_apply = apply_kernel_bytes(n, nnz, info["real"])
-    f_apply = apply_kernel_flops(n, nnz, info["real"])
+    fixed = args.spmv == "fixed" and info["real"]
+    b_apply = apply_kernel_bytes(n, nnz, info["real"], fixed)
+    f_apply = apply_kernel_flops(n, nnz, info["real"], fixed)
     avg_apply_s = apply_ms / 1000.0 / max(1, apply_n)
     achieved = b_apply / avg_apply_s / 1e9
     traffic = ncu_traffic()
@@ -260,12 +266,14 @@ def run_gb300(args):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "complex128 (FP64)", "data": "synthetic (Bose-Hubbard model, seeded state)",
         "config": {"workload": WORKLOAD, "n": n, "nnz": nnz, "krylov_steps_per_solve": steps_per_solve,
-                   "status": status, "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "status": status, "spmv": args.spmv, "parallelism": "replicas" if ws > 1 else "single GPU",
                    "l2": "inputs larger than L2 (H %.0f MB + Krylov basis %.0f MB)"
                          % (nnz * 12 / 1e6, (M_KRYLOV + 3) * 16 * n / 1e6)},
         "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": "lanczos_apply_kernel (SELL-32 SpMV + recurrence epilogue)",
+        "roofline": {"bound": "hbm",
+                     "kernel": ("lanczos_apply_fix_kernel (fixed-point SELL-32 SpMV + FP64 recurrence epilogue)"
+                                if fixed else "lanczos_apply_kernel (SELL-32 SpMV + recurrence epilogue)"),
                      "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
                      "traffic": traffic, "algorithmic_bytes_per_launch": b_apply,
@@ -528,8 +536,9 @@ def run_zipf(args):
         torch.cuda.synchronize()
         e2e.append(time.perf_counter() - t0)
     peaks = load_peaks(te)
-    b_apply = apply_kernel_bytes(n, nnz, info["real"])
-    f_apply = apply_kernel_flops(n, nnz, info["real"])
+    fixed = args.spmv == "fixed" and info["real"]
+    b_apply = apply_kernel_bytes(n, nnz, info["real"], fixed)
+    f_apply = apply_kernel_flops(n, nnz, info["real"], fixed)
     avg = apply_ms / 1e3 / max(1, apply_n)
     line = {"metric": ZIPF_METRIC, "value": value, "unit": "s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
@@ -576,7 +585,7 @@ def zipf_cpu_baseline(te, nnz_full, steps_full):
                       "(extrapolated)" % (len(coo[2]), ZIPF_CPU_T, r["n_steps"], el, per_step, steps_full)}
 
 
-def ncu_case(t_final, config="plain", zipf_n=2_000_000):
+def ncu_case(t_final, config="plain", zipf_n=2_000_000, spmv="fixed"):
     """A short solve of the same workload for ncu captures (t_final instead of
     the full time; the Zipf matrix at a smaller dimension)."""
     import timeevolver_gb300 as te
@@ -592,9 +601,10 @@ def ncu_case(t_final, config="plain", zipf_n=2_000_000):
               % (zipf_n, H.info()["nnz"], t_final, out["n_steps"], out["status"], out["launches"]))
         return
     n, Hc, Oc, v = build_problem()
-    out = te.evolve(Hc, v, t_final, t_final, [("sparse", Oc)], tol=TOL * t_final / T_FINAL, m=M_KRYLOV)
-    print("ncu case: t=%g, %d Krylov steps, status %d, %d launches" % (t_final, out["n_steps"], out["status"],
-                                                                      out["launches"]))
+    out = te.evolve(Hc, v, t_final, t_final, [("sparse", Oc)], tol=TOL * t_final / T_FINAL, m=M_KRYLOV,
+                    options={te.OPT_FIXED_SPMV: 1 if spmv == "fixed" else 0})
+    print("ncu case: t=%g, spmv %s, %d Krylov steps, status %d, %d launches"
+          % (t_final, spmv, out["n_steps"], out["status"], out["launches"]))
 
 
 def main():
@@ -609,11 +619,14 @@ def main():
                          "adjoint: gradients of <n_0(T)> for L=10; zipf: the dim-1e7 load-imbalanced matrix")
     ap.add_argument("--ncu-case", type=float, default=None, metavar="T",
                     help="run one short solve to time T (for ncu captures) and exit")
+    ap.add_argument("--spmv", default="fixed", choices=["fixed", "fp64"],
+                    help="SpMV arithmetic of the Lanczos passes for real H (plain config): exact fixed-point "
+                         "integer products (default) or FP64 FMAs")
     ap.add_argument("--zipf-n", type=int, default=2_000_000,
                     help="dimension of the Zipf matrix in --ncu-case runs of --config zipf")
     args = ap.parse_args()
     if args.ncu_case is not None:
-        ncu_case(args.ncu_case, args.config, args.zipf_n)
+        ncu_case(args.ncu_case, args.config, args.zipf_n, args.spmv)
         return
     if args.impl == "reference":
         run_reference(args)

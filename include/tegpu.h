@@ -291,6 +291,17 @@ int64_t te_evolver_launch_count(te_evolver ev);
  * at dim 6435, equal at dim 92378, slower from dim 352716); 2: always, where
  * a cooperative launch of the matrix's schedule is possible. */
 #define TE_OPT_FUSED_LANCZOS 1
+/* TE_OPT_FIXED_SPMV: the SpMV of the three-term Lanczos passes of a real H in
+ * integer arithmetic instead of FP64 FMAs (GB300 issues FP64 at 1/58 of its
+ * FP32 rate).  H's values are held as round(h 2^sh) with the largest row
+ * 1-norm R below 2^61, each Krylov vector as round(u 2^xs) with a bound U on
+ * max|u| below 2^61; a row sum is accumulated in int64 from int32 limb
+ * products and rounded to double once.  Error of a row of k entries below
+ * (1.25 k 2^-56 + (k + 1) 2^-61) R U + 2^-53 |y|, against FP64's
+ * k 2^-53 sum|h||u|.  The recurrence and all reductions stay FP64.
+ * 0: FP64 SpMV; 1 (default): fixed-point for real matrices with one lane per
+ * row in the per-iteration passes (at least 2048 32-row chunks). */
+#define TE_OPT_FIXED_SPMV 2
 int te_evolver_set_option(te_evolver ev, int option, int value);
 
 /* Prepare another run of the same evolution (same H, parameters and

@@ -174,6 +174,7 @@ def _as_u64(a):
 
 
 OPT_FUSED_LANCZOS = 1
+OPT_FIXED_SPMV = 2
 
 
 class TeTerm(ctypes.Structure):
@@ -409,7 +410,7 @@ class Evolver:
                "te_evolver_add_stop_condition")
 
     def set_option(self, option, value):
-        """te_evolver_set_option (e.g. OPT_FUSED_LANCZOS)."""
+        """te_evolver_set_option (OPT_FUSED_LANCZOS, OPT_FIXED_SPMV)."""
         _check(lib().te_evolver_set_option(self.handle, int(option), int(value)), "te_evolver_set_option")
 
     def kernel_time(self, kind):
@@ -578,11 +579,12 @@ class StopEvolution(Exception):
 
 
 def evolve(H_coo, v, t, sampling_step, observables=(), exp_factor=1.0, tol=1e-6, m=40, fast_integration=False,
-           trace=False, reorth=False):
+           trace=False, reorth=False, options=None):
     """One-call evolution with COO inputs, mirroring the oracle's signature.
 
     ``H_coo`` may also be a Matrix already on the device.  ``observables``:
-    ("sparse", (row, col, val)), ("vector", o) or ("callback", fn)."""
+    ("sparse", (row, col, val)), ("vector", o) or ("callback", fn).
+    ``options``: {OPT_*: value} for te_evolver_set_option."""
     n = len(v)
     H = H_coo if isinstance(H_coo, Matrix) else Matrix.from_coo(n, H_coo)
     obs = []
@@ -593,6 +595,8 @@ def evolve(H_coo, v, t, sampling_step, observables=(), exp_factor=1.0, tol=1e-6,
             obs.append((kind, data))
     ev = Evolver(H, v, t, sampling_step, obs, exp_factor, tol, m, fast_integration, reorth)
     try:
+        for opt, val in (options or {}).items():
+            ev.set_option(opt, val)
         return ev.time_evolve(trace=trace)
     finally:
         ev.close()

@@ -400,6 +400,7 @@ int set_theta(te_adjoint a, const double* theta) {
   double nrm;
   std::memcpy(&nrm, &bits, sizeof(nrm));
   H->norm1 = nrm;
+  if (int rc = te_sell_refresh_fixed(H)) return rc;
   a->theta_now.assign(theta, theta + a->K);
   a->launches += 3;
   return te_cuda_check(cudaGetLastError(), "theta refresh");

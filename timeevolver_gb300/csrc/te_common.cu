@@ -43,14 +43,6 @@ int te_grid_for(int64_t n_items, int threads, int blocks_per_sm) {
   return (int)(need < cap ? need : cap);
 }
 
-int te_grid_balanced(int64_t n_items, int threads, int blocks_per_sm) {
-  const int64_t cap = (int64_t)te_grid_for(n_items, threads, blocks_per_sm) * threads;
-  const int64_t per_thread = (n_items + cap - 1) / cap;  // items per thread in the capped grid
-  if (per_thread <= 1) return te_grid_for(n_items, threads, blocks_per_sm);
-  const int64_t threads_needed = (n_items + per_thread - 1) / per_thread;
-  return (int)((threads_needed + threads - 1) / threads);
-}
-
 int te_kernel_blocks_per_sm(const void* kernel, int threads, size_t dyn_smem) {
   static std::mutex mu;
   static std::map<std::tuple<const void*, int, size_t>, int> cache;

@@ -66,6 +66,8 @@ struct te_evolver_s {
   double* results = nullptr;  // n_obs x n_samples
   int max_batch = 1;
   int fused_lanczos = 1;  // TE_OPT_FUSED_LANCZOS: 0 never, 1 automatic, 2 always
+  int fixed_spmv = 1;     // TE_OPT_FIXED_SPMV: 0 FP64 SpMV, 1 fixed-point SpMV where it applies
+  int4* X = nullptr;      // fixed-point copy of the current Krylov vector (n rows)
   int batch_cap = 0;         // states the batch buffer holds
   size_t results_cap = 0;    // doubles the results buffer holds
   std::vector<HostObs> obs;
@@ -225,6 +227,7 @@ void free_evolver(te_evolver ev) {
   cudaFreeHost(ev->sum);
   cudaFreeHost(ev->host_state);
   cudaFree(ev->slab);
+  cudaFree(ev->X);
   cudaFree(ev->batch);
   cudaFree(ev->orig_tmp);
   cudaFree(ev->partials);
@@ -335,6 +338,14 @@ int run(te_evolver ev, te_result* out) {
   int m = ev->m;
   double err_prev = 0.0, t_prev = 0.0;
   int64_t guard = 0;
+  // fixed-point SpMV in the folded three-term passes (te_fixed.cuh): real H,
+  // one lane per row, matrices large enough for the per-iteration passes
+  const bool fix = ev->fixed_spmv != 0 && ev->p.reorth == 0 && ev->p.exp_factor != 0.0 && ev->H->is_real &&
+                   ev->H->sell.lanes == 1 && ev->H->sell.n_chunks >= 2048 && ev->fused_lanczos != 2;
+  if (fix) {
+    if ((rc = te_sell_build_fixed(ev->H)) != TE_OK) return rc;
+    if (!ev->X) TE_CUDA(cudaMalloc(&ev->X, sizeof(int4) * n));
+  }
   while (!S->done) {
     if (S->fatal) break;
     if (++guard > ((int64_t)1 << 40)) break;
@@ -353,17 +364,27 @@ int run(te_evolver ev, te_result* out) {
       fused = te_launch_lanczos_step(ev->H->sell, ev->H->is_real, ev->cols, m, ev->w, ev->ds, ev->partials, st);
       if (fused) ++ev->launches;
     }
+    const bool fix_step = fix && fold && !fused;
+    if (fix_step) {
+      ProfScope ps(ev, 3);
+      te_launch_fix_start(n, ev->cols[0], ev->X, ev->ds, ev->partials, st);
+      ev->launches += 2;
+    }
     for (int j = 0; j < m && !fused; ++j) {
       {
         ProfScope ps(ev, 0);
-        te_launch_lanczos_apply(ev->H->sell, ev->H->is_real, ev->cols[j],
-                                (j > 0 && !cgs2) ? ev->cols[j - 1] : nullptr, ev->w, ev->ds, ev->partials, j, fold,
-                                st);
+        if (fix_step)
+          te_launch_lanczos_apply_fix(ev->H->sell, ev->X, ev->cols[j], j > 0 ? ev->cols[j - 1] : nullptr, ev->w,
+                                      ev->ds, ev->partials, j, st);
+        else
+          te_launch_lanczos_apply(ev->H->sell, ev->H->is_real, ev->cols[j],
+                                  (j > 0 && !cgs2) ? ev->cols[j - 1] : nullptr, ev->w, ev->ds, ev->partials, j, fold,
+                                  st);
       }
       if (!cgs2) {
         ProfScope ps(ev, 1);
         te_launch_lanczos_update(n, ev->w, ev->cols[j], j + 1 < m ? ev->cols[j + 1] : nullptr, ev->ds, ev->partials,
-                                 j, fold, st);
+                                 j, fold, st, fix_step ? ev->X : nullptr);
         ev->launches += 2;
       } else {
         // classical Gram-Schmidt against u_0..u_j, then one reorthogonalisation pass
@@ -807,6 +828,13 @@ extern "C" int te_evolver_set_option(te_evolver ev, int option, int value) {
         return TE_ERR_INVALID_ARG;
       }
       ev->fused_lanczos = value;
+      return TE_OK;
+    case TE_OPT_FIXED_SPMV:
+      if (value < 0 || value > 1) {
+        te_set_error("te_evolver_set_option: TE_OPT_FIXED_SPMV takes 0 or 1");
+        return TE_ERR_INVALID_ARG;
+      }
+      ev->fixed_spmv = value;
       return TE_OK;
     default:
       te_set_error("te_evolver_set_option: unknown option %d", option);

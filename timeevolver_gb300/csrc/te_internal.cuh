@@ -89,6 +89,12 @@ struct TeDevState {
   double inv_exp_factor;
   // grid barrier of the persistent Lanczos kernel (arrivals, generation)
   unsigned int bar_count, bar_gen;
+  // fixed-point SpMV (te_fixed.cuh): u_j is encoded as round(u_j 2^fx_xs[j]);
+  // fx_umax[j] is the high word of max |u_j| (a bound), fx_wmax the running
+  // high word of max |w'| of the current apply pass
+  int fx_xs[TE_MMAX + 1];
+  unsigned int fx_umax[TE_MMAX + 1];
+  unsigned int fx_wmax, fx_pad;
 };
 
 // SELL-32 matrix in the sorted (permuted) basis.
@@ -119,6 +125,15 @@ struct TeSell {
   int64_t* long_ptr = nullptr;  // n_long + 1
   int32_t* long_col = nullptr;  // sorted-basis columns
   double* long_val = nullptr;   // real: 1, complex: 2 doubles per entry
+  // Fixed-point copy of the chunk values of a real matrix (te_fixed.cuh):
+  // slot value round(h 2^fix_sh) as int32 limbs {h0, h1}, built on first use
+  // by te_sell_build_fixed, with its own static schedule for the fixed-point
+  // apply kernel (whose resident blocks per SM differ).
+  int2* fix_val = nullptr;
+  int fix_sh = 0;
+  int32_t* fix_warp_chunk = nullptr;
+  int fix_grid = 0;
+  bool fix_saturated = false;
 };
 
 // The long rows of a SELL matrix, by value for kernels.
@@ -195,9 +210,6 @@ int te_cuda_check(cudaError_t e, const char* what);
 // launch shapes
 int te_num_sms();
 int te_grid_for(int64_t n_items, int threads, int blocks_per_sm);
-// Like te_grid_for, but shrinks the grid so that a grid-stride loop gives
-// every thread the same number of items (up to one).
-int te_grid_balanced(int64_t n_items, int threads, int blocks_per_sm);
 // Resident blocks per SM of a kernel at this block size (occupancy query, cached).
 int te_kernel_blocks_per_sm(const void* kernel, int threads, size_t dyn_smem);
 // One wave of a grid-stride kernel: at most every SM's resident blocks, and
@@ -220,8 +232,22 @@ void te_launch_permute(int64_t n, const int32_t* idx, const double2* in, double2
 // non-zero expFactor; the update kernel then takes the factor into s_{j+1}).
 void te_launch_lanczos_apply(const TeSell& A, bool is_real, const double2* u_j, const double2* u_jm1, double2* w,
                              TeDevState* ds, double* partials, int j, bool fold, cudaStream_t st);
+// X_out (optional): also write the fixed-point copy of u_{j+1} (te_fixed.cuh)
 void te_launch_lanczos_update(int64_t n, const double2* w, const double2* u_j, double2* u_jp1, TeDevState* ds,
-                              double* partials, int j, bool fold, cudaStream_t st);
+                              double* partials, int j, bool fold, cudaStream_t st, int4* X_out = nullptr);
+// Fixed-point path of the folded three-term iteration (real matrices, one lane
+// per row, te_sell_build_fixed done): te_launch_fix_start encodes u_0 at the
+// start of a Krylov step; the apply pass reads the fixed-point copy X of u_j.
+int te_sell_build_fixed(te_matrix_s* A);
+// Re-encode the fixed-point values after H's SELL values changed in place.
+int te_sell_refresh_fixed(te_matrix_s* A);
+void te_launch_fix_start(int64_t n, const double2* u_0, int4* X, TeDevState* ds, double* partials, cudaStream_t st);
+void te_launch_lanczos_apply_fix(const TeSell& A, const int4* X, const double2* u_j, const double2* u_jm1,
+                                 double2* w, TeDevState* ds, double* partials, int j, cudaStream_t st);
+// Static warp schedule of the SpMV passes over the chunk offsets (host): warp w
+// of grid blocks owns chunks [wc[w], wc[w + 1]) of equal estimated work.
+void te_sell_schedule(const std::vector<int64_t>& off, int64_t n_chunks, int blocks_per_sm,
+                      bool real, int& grid, bool& saturated, std::vector<int32_t>& wc);
 // All m three-term Lanczos iterations of one Krylov step in one cooperative
 // launch (te_lanczos.cu).  Returns false (nothing launched) when the matrix's
 // static schedule does not fit the persistent kernel's residency, or the

@@ -14,11 +14,13 @@
 // (fixed order), so the Krylov coefficients never leave the device.  Pass 1
 // runs on the SELL-32 layout: a warp owns 32 equal-length rows.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "te_internal.cuh"
 #include "te_reduce.cuh"
 #include "te_sell.cuh"
+#include "te_fixed.cuh"
 
 __device__ __forceinline__ bool te_step_inactive(const TeDevState* ds) {
   return ds->fatal != 0 || ds->done != 0 || ds->breakdown != 0;
@@ -27,7 +29,7 @@ __device__ __forceinline__ bool te_step_inactive(const TeDevState* ds) {
 // The recurrence epilogue of one row r (A u_j row sum y): writes w (or the
 // folded w') and accumulates conj(u_j) w.
 template <bool HAS_PREV, bool FOLD, bool CG = false>
-__device__ __forceinline__ void apply_row_epilogue(int64_t r, double2 y, double g, double cw,
+__device__ __forceinline__ double2 apply_row_epilogue(int64_t r, double2 y, double g, double cw,
                                                    const double2* __restrict__ u_j,
                                                    const double2* __restrict__ u_jm1, double2* __restrict__ w,
                                                    double (&acc)[2]) {
@@ -54,6 +56,7 @@ __device__ __forceinline__ void apply_row_epilogue(int64_t r, double2 y, double 
   // conj(u_j) * w
   acc[0] = fma(uj.x, wr.x, fma(uj.y, wr.y, acc[0]));
   acc[1] = fma(uj.x, wr.y, fma(-uj.y, wr.x, acc[1]));
+  return wr;
 }
 
 // 6 (real H: at most 40 registers) or 5 (complex H, or K > 1) resident blocks
@@ -120,6 +123,179 @@ __global__ void __launch_bounds__(TE_THREADS, (REAL && K == 1) ? 6 : 5) lanczos_
     const double f = FOLD ? sj * g : sj;
     if (threadIdx.x == 0) ds->alpha[j] = make_double2(f * tot[0], f * tot[1]);
   }
+}
+
+// Block maximum of a per-thread unsigned value, folded into *dst with one
+// atomicMax by thread 0.  Call between the warp loop and a block-wide
+// synchronisation that precedes thread 0's read (slots: one per warp).
+__device__ __forceinline__ void te_warp_max_to_smem(unsigned int v, unsigned int* slots) {
+  v = __reduce_max_sync(0xffffffffu, v);
+  if ((threadIdx.x & 31) == 0) slots[threadIdx.x >> 5] = v;
+}
+__device__ __forceinline__ unsigned int te_block_max_from_smem(const unsigned int* slots) {
+  unsigned int m = 0;
+  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) m = max(m, slots[i]);
+  return m;
+}
+
+// Folded three-term apply pass with the fixed-point SpMV (te_fixed.cuh):
+// w' = -i H u_j + (beta_j / e)^2 u_{j-1}, alpha_j = s_j g <u_j, w'> as in
+// lanczos_apply_kernel<REAL, HAS_PREV, FOLD = true, K = 1>, with H u_j of the
+// chunk rows from the integer pipes (X = round(u_j 2^xs_j)); long rows stay
+// FP64.  Also bounds the next vector: with W >= max|w'| (block maxima) and
+// U >= max|u_j|, u'_{j+1} = w' - (alpha_j / e) u_j has components below
+// B = W + (|Re| + |Im|)(alpha_j / e) U, which fixes xs_{j+1} for the update.
+// Resident blocks per SM of the fixed-point apply kernel (40 registers).
+// Measured on the L=12 Bose-Hubbard matrix (us per launch, with the slots per
+// lane in flight of te_sell_row_fix): 4 blocks 113 (4 slots) / 128 (2 slots);
+// 5 blocks 76; 6 blocks 72 (2 slots) / 117 (1 slot); 8 blocks 74.  The spill
+// of the 6-block build (a few words outside the slot loop) costs less than
+// the latency hiding it buys.
+#ifndef TE_FIX_MIN_BLOCKS
+#define TE_FIX_MIN_BLOCKS 6
+#endif
+template <bool HAS_PREV>
+__global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_fix_kernel(
+    int64_t n, const int32_t* __restrict__ warp_chunk, const int64_t* __restrict__ chunk_off,
+    const int32_t* __restrict__ col, const int2* __restrict__ hv, int sh, TeLongRows L, const int4* __restrict__ X,
+    const double2* __restrict__ u_j, const double2* __restrict__ u_jm1, double2* __restrict__ w, TeDevState* ds,
+    double* partials, int j) {
+  __shared__ double scratch[2 * 32];
+  __shared__ double wide[2 * TE_THREADS];
+  __shared__ unsigned int wmax_w[TE_THREADS / 32];
+  te_pdl_trigger();
+  te_pdl_wait();
+  if (te_step_inactive(ds)) return;
+  const int lane = threadIdx.x & 31;
+  const double sj = ds->s[j];
+  const double g = ds->exp_factor * sj;
+  const double ie = ds->inv_exp_factor;
+  double cw = 0.0;
+  if (HAS_PREV) {
+    const double bj = ds->beta[j];
+    cw = (bj * ie) * (bj * ie);
+  }
+  const int shift = sh + ds->fx_xs[j];
+  double acc[2] = {0.0, 0.0};
+  unsigned int wmax = 0;
+  const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t lr = wid; lr < L.n; lr += warps) {
+    const double2 y = te_long_row<true>(L, lr, u_j, lane);
+    if (lane == 0) {
+      const double2 wr = apply_row_epilogue<HAS_PREV, true>(lr, y, g, cw, u_j, u_jm1, w, acc);
+      wmax = max(wmax, max(te_fix_hiword(wr.x), te_fix_hiword(wr.y)));
+    }
+  }
+  // the warp's chunk offsets in one coalesced load (lane k holds the offset
+  // of chunk c_begin + k) when its range has at most 31 chunks
+  const int64_t c_begin = warp_chunk[wid], c_end = warp_chunk[wid + 1];
+  const bool offs_in_regs = c_end - c_begin <= 31;
+  const int64_t my_off = (offs_in_regs && c_begin + lane <= c_end) ? __ldg(chunk_off + c_begin + lane) : 0;
+  for (int64_t c = c_begin; c < c_end; ++c) {
+    const int k = (int)(c - c_begin);
+    int64_t s0, s1;
+    if (offs_in_regs) {
+      s0 = __shfl_sync(0xffffffffu, my_off, k);
+      s1 = __shfl_sync(0xffffffffu, my_off, k + 1);
+    } else {
+      s0 = __ldg(chunk_off + c);
+      s1 = __ldg(chunk_off + c + 1);
+    }
+    const int64_t r = c * 32 + lane;
+    const bool live = r < n && r >= L.n;
+    // the row's own vector entries, loaded ahead of the SpMV so that their
+    // latency overlaps the gathers
+    const double2 y = te_sell_row_fix(s0 + lane, s1, col, hv, X, shift);
+    if (live) {
+      const double2 wr = apply_row_epilogue<HAS_PREV, true>(r, y, g, cw, u_j, u_jm1, w, acc);
+      wmax = max(wmax, max(te_fix_hiword(wr.x), te_fix_hiword(wr.y)));
+    }
+  }
+  te_warp_max_to_smem(wmax, wmax_w);
+  te_block_sum_wide<2>(acc, wide);
+  if (threadIdx.x == 0) atomicMax(&ds->fx_wmax, te_block_max_from_smem(wmax_w));
+  if (te_publish_partials<2>(acc, partials, &ds->counter[0])) {
+    double tot[2];
+    te_final_sum<2>(tot, partials, &ds->counter[0], scratch);
+    if (threadIdx.x == 0) {
+      const double f = sj * g;
+      const double2 alpha = make_double2(f * tot[0], f * tot[1]);
+      ds->alpha[j] = alpha;
+      const double W = te_fix_upper(atomicExch(&ds->fx_wmax, 0u));
+      const double U = te_fix_upper(ds->fx_umax[j]);
+      const double B = (W + (fabs(alpha.x * ie) + fabs(alpha.y * ie)) * U) * (1.0 + 1e-12);
+      ds->fx_xs[j + 1] = te_fix_scale(B);
+      ds->fx_umax[j + 1] = 0u;
+    }
+  }
+}
+
+// Start of a Krylov step on the fixed-point path, two passes over u_0:
+// per-block maxima of |u_0| (high words) into partials, then every block of
+// the encode pass reduces those maxima itself (same value everywhere), sets
+// xs_0 and writes X = round(u_0 2^xs_0); block 0 records xs_0 and the bound.
+__global__ void __launch_bounds__(TE_THREADS) fix_start_max_kernel(int64_t n, const double2* __restrict__ u,
+                                                                   const TeDevState* ds, unsigned int* bmax) {
+  __shared__ unsigned int slots[TE_THREADS / 32];
+  if (ds->fatal != 0 || ds->done != 0) return;
+  unsigned int m = 0;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const double2 v = u[r];
+    m = max(m, max(te_fix_hiword(v.x), te_fix_hiword(v.y)));
+  }
+  te_warp_max_to_smem(m, slots);
+  __syncthreads();
+  if (threadIdx.x == 0) bmax[blockIdx.x] = te_block_max_from_smem(slots);
+}
+
+__global__ void __launch_bounds__(TE_THREADS) fix_start_encode_kernel(int64_t n, const double2* __restrict__ u,
+                                                                      int4* __restrict__ X, TeDevState* ds,
+                                                                      const unsigned int* __restrict__ bmax,
+                                                                      int n_bmax) {
+  __shared__ unsigned int slots[TE_THREADS / 32];
+  __shared__ int xs_s;
+  if (ds->fatal != 0 || ds->done != 0) return;
+  unsigned int m = 0;
+  for (int i = threadIdx.x; i < n_bmax; i += blockDim.x) m = max(m, bmax[i]);
+  te_warp_max_to_smem(m, slots);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned int um = te_block_max_from_smem(slots);
+    xs_s = te_fix_scale(te_fix_upper(um));
+    if (blockIdx.x == 0) {
+      ds->fx_xs[0] = xs_s;
+      ds->fx_umax[0] = um;
+      ds->fx_wmax = 0u;
+    }
+  }
+  __syncthreads();
+  const int xs = xs_s;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const double2 v = u[r];
+    const int2 a = te_fix_split(te_fix_encode(v.x, xs)), b = te_fix_split(te_fix_encode(v.y, xs));
+    X[r] = make_int4(a.x, a.y, b.x, b.y);
+  }
+}
+
+// Fixed-point chunk values: row 1-norms of the chunk rows (maximum as the bit
+// pattern of a non-negative double), then h~ = round(h 2^sh) as limbs.
+__global__ void __launch_bounds__(TE_THREADS) fix_rownorm_kernel(int64_t n_chunks, const int64_t* __restrict__ off,
+                                                                 const double* __restrict__ val,
+                                                                 unsigned long long* max_bits) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t c = t >> 5;
+  if (c >= n_chunks) return;
+  double s = 0.0;
+  for (int64_t q = off[c] + (t & 31); q < off[c + 1]; q += 32) s += fabs(val[q]);
+  for (int o = 16; o > 0; o >>= 1) s = fmax(s, __shfl_xor_sync(0xffffffffu, s, o));
+  if ((t & 31) == 0) atomicMax(max_bits, (unsigned long long)__double_as_longlong(s));
+}
+
+__global__ void __launch_bounds__(TE_THREADS) fix_encode_values_kernel(int64_t slots, const double* __restrict__ val,
+                                                                       int2* __restrict__ hv, int sh) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < slots; q += (int64_t)gridDim.x * blockDim.x)
+    hv[q] = te_fix_split(te_fix_encode(val[q], sh));
 }
 
 // ---------------------------------------------------------------------------
@@ -332,13 +508,17 @@ bool te_launch_lanczos_step(const TeSell& A, bool is_real, double2* const* cols,
 // u_{j+1} = w - alpha_j v_j and beta_{j+1} = ||u_{j+1}||.  With a folded w'
 // (fold != 0) the kernel forms u'_{j+1} = w' - (alpha_j s_j / g) u_j = u_{j+1} / g
 // and keeps the factor in the scale: beta_{j+1} = |g| ||u'||, s_{j+1} = g / beta_{j+1}.
-template <bool STORE>
+// FIX: also writes X = round(u'_{j+1} 2^xs_{j+1}) (the fixed-point copy read
+// by the next apply pass) and folds max |u'_{j+1}| into fx_umax[j + 1].
+template <bool STORE, bool FIX>
 __global__ void __launch_bounds__(TE_THREADS) lanczos_update_kernel(int64_t n, const double2* __restrict__ w,
                                                                     const double2* __restrict__ u_j,
                                                                     double2* __restrict__ u_jp1, TeDevState* ds,
-                                                                    double* partials, int j, int fold) {
+                                                                    double* partials, int j, int fold,
+                                                                    int4* __restrict__ X) {
   __shared__ double scratch[32];
   __shared__ double wide[TE_THREADS];
+  __shared__ unsigned int umax_w[TE_THREADS / 32];
   te_pdl_trigger();
   te_pdl_wait();
   if (te_step_inactive(ds)) return;
@@ -347,7 +527,9 @@ __global__ void __launch_bounds__(TE_THREADS) lanczos_update_kernel(int64_t n, c
   const double2 a = ds->alpha[j];
   const double q = fold ? ds->inv_exp_factor : sj;  // alpha_j s_j / g = alpha_j / expFactor
   const double gr = a.x * q, gi = a.y * q;
+  const int xs = FIX ? ds->fx_xs[j + 1] : 0;
   double acc[1] = {0.0};
+  unsigned int umax = 0;
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
     double2 wv = w[r];
     double2 u = u_j[r];
@@ -355,9 +537,16 @@ __global__ void __launch_bounds__(TE_THREADS) lanczos_update_kernel(int64_t n, c
     o.x = fma(-gr, u.x, fma(gi, u.y, wv.x));
     o.y = fma(-gr, u.y, fma(-gi, u.x, wv.y));
     if (STORE) u_jp1[r] = o;
+    if (FIX) {
+      const int2 p = te_fix_split(te_fix_encode(o.x, xs)), q2 = te_fix_split(te_fix_encode(o.y, xs));
+      X[r] = make_int4(p.x, p.y, q2.x, q2.y);
+      umax = max(umax, max(te_fix_hiword(o.x), te_fix_hiword(o.y)));
+    }
     acc[0] = fma(o.x, o.x, fma(o.y, o.y, acc[0]));
   }
+  if (FIX) te_warp_max_to_smem(umax, umax_w);
   te_block_sum_wide<1>(acc, wide);
+  if (FIX && threadIdx.x == 0) atomicMax(&ds->fx_umax[j + 1], te_block_max_from_smem(umax_w));
   if (te_publish_partials<1>(acc, partials, &ds->counter[1])) {
     double tot[1];
     te_final_sum<1>(tot, partials, &ds->counter[1], scratch);
@@ -697,9 +886,113 @@ int te_tune_sell_lanes(te_matrix_s* A) {
 }
 
 void te_launch_lanczos_update(int64_t n, const double2* w, const double2* u_j, double2* u_jp1, TeDevState* ds,
-                              double* partials, int j, bool fold, cudaStream_t st) {
-  const void* kk = (const void*)lanczos_update_kernel<true>;
+                              double* partials, int j, bool fold, cudaStream_t st, int4* X_out) {
+  const bool fix = u_jp1 && X_out;
+  const auto k = fix ? lanczos_update_kernel<true, true>
+                     : (u_jp1 ? lanczos_update_kernel<true, false> : lanczos_update_kernel<false, false>);
+  const void* kk = (const void*)k;
   const int grid = te_grid_fit(kk, n, TE_THREADS);
-  te_launch_pdl(te_grid_saturated(kk, n, TE_THREADS), u_jp1 ? lanczos_update_kernel<true> : lanczos_update_kernel<false>,
-                grid, TE_THREADS, st, n, w, u_j, u_jp1, ds, partials, j, (int)fold);
+  te_launch_pdl(te_grid_saturated(kk, n, TE_THREADS), k, grid, TE_THREADS, st, n, w, u_j, u_jp1, ds, partials, j,
+                (int)fold, fix ? X_out : nullptr);
 }
+
+void te_launch_fix_start(int64_t n, const double2* u_0, int4* X, TeDevState* ds, double* partials, cudaStream_t st) {
+  unsigned int* bmax = reinterpret_cast<unsigned int*>(partials);
+  const int g1 = te_grid_fit((const void*)fix_start_max_kernel, n, TE_THREADS);
+  fix_start_max_kernel<<<g1, TE_THREADS, 0, st>>>(n, u_0, ds, bmax);
+  const int g2 = te_grid_fit((const void*)fix_start_encode_kernel, n, TE_THREADS);
+  fix_start_encode_kernel<<<g2, TE_THREADS, 0, st>>>(n, u_0, X, ds, bmax, g1);
+}
+
+void te_launch_lanczos_apply_fix(const TeSell& A, const int4* X, const double2* u_j, const double2* u_jm1,
+                                 double2* w, TeDevState* ds, double* partials, int j, cudaStream_t st) {
+  if (u_jm1)
+    te_launch_pdl(A.fix_saturated, lanczos_apply_fix_kernel<true>, A.fix_grid, TE_THREADS, st, A.n,
+                  A.fix_warp_chunk, A.chunk_off, A.col, A.fix_val, A.fix_sh, te_long_rows(A), X, u_j, u_jm1, w, ds,
+                  partials, j);
+  else
+    te_launch_pdl(A.fix_saturated, lanczos_apply_fix_kernel<false>, A.fix_grid, TE_THREADS, st, A.n,
+                  A.fix_warp_chunk, A.chunk_off, A.col, A.fix_val, A.fix_sh, te_long_rows(A), X, u_j, u_jm1, w, ds,
+                  partials, j);
+}
+
+// Fixed-point chunk values (real matrices with one lane per row): sh puts the
+// largest chunk-row 1-norm below 2^61, then every slot value as limbs.
+static int fixed_values(TeSell& S) {
+  unsigned long long* d_max = nullptr;
+  TE_CUDA(cudaMalloc(&d_max, sizeof(unsigned long long)));
+  int rc = te_cuda_check(cudaMemset(d_max, 0, sizeof(unsigned long long)), "fixed values");
+  const int64_t threads = S.n_chunks * 32;
+  if (rc == TE_OK)
+    fix_rownorm_kernel<<<(unsigned)((threads + TE_THREADS - 1) / TE_THREADS), TE_THREADS>>>(S.n_chunks, S.chunk_off,
+                                                                                             S.val, d_max);
+  unsigned long long bits = 0;
+  if (rc == TE_OK) rc = te_cuda_check(cudaMemcpy(&bits, d_max, sizeof(bits), cudaMemcpyDeviceToHost), "fixed values");
+  cudaFree(d_max);
+  if (rc != TE_OK) return rc;
+  double rmax;
+  std::memcpy(&rmax, &bits, sizeof(rmax));
+  if (!(rmax < 1e300)) {
+    te_set_error("fixed-point SpMV: matrix row norm not finite");
+    return TE_ERR_INVALID_ARG;
+  }
+  int E = 0;
+  if (rmax > 0.0) std::frexp(rmax * (1.0 + 1e-12), &E);
+  S.fix_sh = 61 - E;
+  fix_encode_values_kernel<<<te_grid_fit((const void*)fix_encode_values_kernel, S.slots, TE_THREADS), TE_THREADS>>>(
+      S.slots, S.val, S.fix_val, S.fix_sh);
+  return te_cuda_check(cudaDeviceSynchronize(), "fixed values");
+}
+
+// The fixed-point values and the fixed-point apply kernel's own schedule,
+// once per matrix.
+static int build_fixed(te_matrix_s* A) {
+  TeSell& S = A->sell;
+  if (!A->is_real || S.lanes != 1 || S.n_chunks < 1) {
+    te_set_error("fixed-point SpMV needs a real matrix with one lane per row");
+    return TE_ERR_INVALID_ARG;
+  }
+  int rc;
+  if ((rc = te_cuda_check(cudaMalloc(&S.fix_val, sizeof(int2) * std::max<int64_t>(S.slots, 1)), "fixed values")) !=
+      TE_OK)
+    return rc;
+  if ((rc = fixed_values(S)) != TE_OK) return rc;
+  std::vector<int64_t> off(S.n_chunks + 1);
+  rc = te_cuda_check(cudaMemcpy(off.data(), S.chunk_off, sizeof(int64_t) * off.size(), cudaMemcpyDeviceToHost),
+                     "fixed values");
+  if (rc != TE_OK) return rc;
+  int bps = 8;
+  for (const void* k : {(const void*)lanczos_apply_fix_kernel<true>, (const void*)lanczos_apply_fix_kernel<false>})
+    bps = std::min(bps, te_kernel_blocks_per_sm(k, TE_THREADS, 0));
+  std::vector<int32_t> wc;
+  te_sell_schedule(off, S.n_chunks, bps, true, S.fix_grid, S.fix_saturated, wc);
+  int32_t* d_wc = nullptr;
+  if ((rc = te_cuda_check(cudaMalloc(&d_wc, sizeof(int32_t) * wc.size()), "fixed values")) != TE_OK) return rc;
+  rc = te_cuda_check(cudaMemcpy(d_wc, wc.data(), sizeof(int32_t) * wc.size(), cudaMemcpyHostToDevice),
+                     "fixed values");
+  if (rc != TE_OK) {
+    cudaFree(d_wc);
+    return rc;
+  }
+  S.fix_warp_chunk = d_wc;  // marks the fixed-point data complete
+  return TE_OK;
+}
+
+int te_sell_refresh_fixed(te_matrix_s* A) {
+  if (!A->sell.fix_warp_chunk) return TE_OK;
+  return fixed_values(A->sell);
+}
+
+int te_sell_build_fixed(te_matrix_s* A) {
+  TeSell& S = A->sell;
+  if (S.fix_warp_chunk) return TE_OK;
+  const int rc = build_fixed(A);
+  if (rc != TE_OK) {
+    cudaFree(S.fix_val);
+    S.fix_val = nullptr;
+    cudaFree(S.fix_warp_chunk);
+    S.fix_warp_chunk = nullptr;
+  }
+  return rc;
+}
+

@@ -252,6 +252,28 @@ __global__ void narrow_index_kernel(int64_t nnz, const uint64_t* __restrict__ in
 
 // ------------------------------------------------------------ host build
 
+// Static warp schedule of the SpMV passes (equal estimated work per warp:
+// 2 (real) or 4 (complex) FMAs per slot, about 8 per row for the epilogues).
+void te_sell_schedule(const std::vector<int64_t>& off, int64_t n_chunks, int blocks_per_sm,
+                      bool real, int& grid, bool& saturated, std::vector<int32_t>& wc) {
+  const int64_t need = (n_chunks * 32 + TE_THREADS - 1) / TE_THREADS;
+  const int64_t cap = (int64_t)te_num_sms() * std::max(blocks_per_sm, 1);
+  grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, cap));
+  saturated = need > cap;
+  const int64_t W = (int64_t)grid * (TE_THREADS / 32);
+  const double w_slot = real ? 2.0 : 4.0, w_chunk = 8.0 * 32;
+  auto cost = [&](int64_t c) { return w_slot * (double)off[c] + w_chunk * (double)c; };
+  const double total = cost(n_chunks);
+  wc.assign(W + 1, 0);
+  int64_t c = 0;
+  for (int64_t w = 0; w < W; ++w) {
+    const double target = total * (double)w / (double)W;
+    while (c < n_chunks && cost(c) < target) ++c;
+    wc[w] = (int32_t)c;
+  }
+  wc[W] = (int32_t)n_chunks;
+}
+
 namespace {
 
 void free_matrix(te_matrix_s* M) {
@@ -269,6 +291,8 @@ void free_matrix(te_matrix_s* M) {
   cudaFree(M->sell.long_ptr);
   cudaFree(M->sell.long_col);
   cudaFree(M->sell.long_val);
+  cudaFree(M->sell.fix_val);
+  cudaFree(M->sell.fix_warp_chunk);
   delete M;
 }
 
@@ -326,21 +350,8 @@ int sell_layout(te_matrix_s* M, const std::vector<int32_t>& rp, bool real, std::
                            te_kernel_blocks_per_sm(real ? (const void*)sell_spmv_kernel<true, 1>
                                                         : (const void*)sell_spmv_kernel<false, 1>,
                                                    TE_THREADS, 0));
-  const int64_t need = (S.n_chunks * 32 + TE_THREADS - 1) / TE_THREADS;
-  S.grid = (int)std::min<int64_t>(need, (int64_t)te_num_sms() * bps);
-  S.saturated = need > (int64_t)te_num_sms() * bps;
-  const int64_t W = (int64_t)S.grid * (TE_THREADS / 32);
-  const double w_slot = real ? 2.0 : 4.0, w_chunk = 8.0 * 32;
-  auto cost = [&](int64_t c) { return w_slot * (double)off[c] + w_chunk * (double)c; };
-  const double total = cost(S.n_chunks);
-  std::vector<int32_t> wc(W + 1);
-  int64_t c = 0;
-  for (int64_t w = 0; w < W; ++w) {
-    const double target = total * (double)w / (double)W;
-    while (c < S.n_chunks && cost(c) < target) ++c;
-    wc[w] = (int32_t)c;
-  }
-  wc[W] = (int32_t)S.n_chunks;
+  std::vector<int32_t> wc;
+  te_sell_schedule(off, S.n_chunks, bps, real, S.grid, S.saturated, wc);
   return upload(&S.warp_chunk, wc.data(), wc.size());
 }
 

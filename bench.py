@@ -160,13 +160,15 @@ def build_problem():
     return n, H, O, v
 
 
-def apply_kernel_bytes(n, nnz, real=True, fixed=False):
+def apply_kernel_bytes(n, nnz, real=True, fixed=False, packed=False):
     """Algorithmic bytes of one Lanczos apply launch: the matrix (values +
-    int32 columns), the SELL chunk offsets, x = u_j read once, u_{j-1} read,
-    w written.  The fixed-point apply reads the fixed-point copy of u_j (16
-    bytes per row, gathered) and u_j itself for <u_j, w'> (16 more)."""
+    int32 columns; with the value dictionary one 4-byte word per entry), the
+    SELL chunk offsets, x = u_j read once, u_{j-1} read, w written.  The
+    fixed-point apply reads the fixed-point copy of u_j (16 bytes per row,
+    gathered) and u_j itself for <u_j, w'> (16 more)."""
     chunks = (n + 31) // 32
-    return nnz * ((8 if real else 16) + 4) + 8 * (chunks + 1) + (4 if fixed else 3) * 16 * n
+    per_entry = 4 if packed else (8 if real else 16) + 4
+    return nnz * per_entry + 8 * (chunks + 1) + (4 if fixed else 3) * 16 * n
 
 
 def apply_kernel_flops(n, nnz, real=True, fixed=False):
@@ -236,6 +238,7 @@ def run_gb300(args):
     status = r.status
     apply_ms, apply_n, kernel_ms = profiled_solve(te, ev, v_dev)
     ev.close()
+    fixed_layout = H.fixed_layout()
 
     # ---- end to end through the C ABI with host buffers
     e2e_times = []
@@ -256,7 +259,7 @@ def run_gb300(args):
     value = replica_seconds_per_solve(ms, args.steps, ws)
     peaks = load_peaks(te)
     fixed = args.spmv == "fixed" and info["real"]
-    b_apply = apply_kernel_bytes(n, nnz, info["real"], fixed)
+    b_apply = apply_kernel_bytes(n, nnz, info["real"], fixed, fixed and fixed_layout["state"] == 2)
     f_apply = apply_kernel_flops(n, nnz, info["real"], fixed)
     avg_apply_s = apply_ms / 1000.0 / max(1, apply_n)
     achieved = b_apply / avg_apply_s / 1e9
@@ -272,7 +275,9 @@ def run_gb300(args):
         "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm",
-                     "kernel": ("lanczos_apply_fix_kernel (fixed-point SELL-32 SpMV + FP64 recurrence epilogue)"
+                     "kernel": ("lanczos_apply_fix_kernel (fixed-point SELL-32 SpMV%s + FP64 recurrence epilogue)"
+                                % (", value dictionary of %d values" % fixed_layout["n_values"]
+                                   if fixed_layout["state"] == 2 else "")
                                 if fixed else "lanczos_apply_kernel (SELL-32 SpMV + recurrence epilogue)"),
                      "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
@@ -537,7 +542,7 @@ def run_zipf(args):
         e2e.append(time.perf_counter() - t0)
     peaks = load_peaks(te)
     fixed = args.spmv == "fixed" and info["real"]
-    b_apply = apply_kernel_bytes(n, nnz, info["real"], fixed)
+    b_apply = apply_kernel_bytes(n, nnz, info["real"], fixed, fixed and H.fixed_layout()["state"] == 2)
     f_apply = apply_kernel_flops(n, nnz, info["real"], fixed)
     avg = apply_ms / 1e3 / max(1, apply_n)
     line = {"metric": ZIPF_METRIC, "value": value, "unit": "s", "n_gpus": 1, "steps": args.steps,

@@ -127,6 +127,13 @@ int te_matrix_layout(te_matrix A, int64_t* sell_slots, int64_t* long_rows, int64
  * the summation order of a row (results differ by rounding), so it is made
  * once per matrix.  Setting 1, 2 or 4 pins it. */
 int te_matrix_set_spmv_lanes(te_matrix A, int lanes);
+/* Fixed-point form of a real matrix for TE_OPT_FIXED_SPMV (no counterpart in
+ * the reference), built by the first evolver that uses it: *state 0 not built,
+ * 1 limbs of every slot value (8 bytes per slot plus the 4-byte column), 2 a
+ * value dictionary (one 4-byte word per slot: column and value index; at most
+ * 4096 distinct values and 2^(32 - column bits)); *n_values the dictionary
+ * size; *scale_shift the sh of round(h 2^sh). */
+int te_matrix_fixed_layout(te_matrix A, int* state, int* n_values, int* scale_shift);
 /* Current lanes per row (1, 2, 4), tuning first if tune_now != 0 and the
  * choice is still open; a negative value is an error code. */
 int te_matrix_spmv_lanes(te_matrix A, int tune_now);

@@ -55,8 +55,11 @@ def test_fixed_spmv_bose_hubbard(te_gpu, oracle_lib, L, U, t, same_steps):
     v = _fock(states, [L] + [0] * (L - 1))
     O = models.create_matrix([models.number_operator(0, 1.0)], states)
     M, Om = te_gpu.Matrix.from_coo(n, H), te_gpu.Matrix.from_coo(n, O)
+    assert M.fixed_layout()["state"] == 0
     a = _run(te_gpu, M, v, t, 0.5, [("sparse", Om)], 1)
     b = _run(te_gpu, M, v, t, 0.5, [("sparse", Om)], 0)
+    fl = M.fixed_layout()
+    assert fl["state"] == 2 and 0 < fl["n_values"] <= 4096  # few distinct values: dictionary
     assert a["launches"] == b["launches"] + 2 * a["n_steps"]
     assert a["n_steps"] == b["n_steps"] and a["status"] == b["status"]
     assert np.linalg.norm(a["state"] - b["state"]) < 2e-8
@@ -121,6 +124,7 @@ def test_fixed_spmv_long_rows(te_gpu, oracle_lib):
     d = (np.arange(n), np.arange(n), rng.uniform(-1, 1, n).astype(np.complex128))
     a = _run(te_gpu, M, v, 1.0, 0.25, [("sparse", d)], 1, m=30)
     b = _run(te_gpu, M, v, 1.0, 0.25, [("sparse", d)], 0, m=30)
+    assert M.fixed_layout()["state"] == 1  # Gaussian values: limbs per slot
     assert a["launches"] == b["launches"] + 2 * a["n_steps"]
     ref = oracle_lib.evolve((row, col, val), v, 1.0, 0.25, [("sparse", d)], tol=1e-8, m=30)
     for r in (a, b):
@@ -143,3 +147,25 @@ def test_fixed_spmv_not_for_complex(te_gpu):
     b = _run(te_gpu, M, v, 0.5, 0.25, [], 0, m=20)
     assert a["launches"] == b["launches"]
     assert np.array_equal(a["state"], b["state"])
+
+
+def test_fixed_spmv_dictionary_matches_limbs(te_gpu):
+    """The same BH matrix through the value dictionary and through per-slot
+    limbs (the dictionary ruled out by a value set too large for it: the
+    diagonal perturbed by up to 1e-13 of its largest entry, tens of thousands
+    of distinct doubles): the evolutions agree to the perturbation."""
+    states, H = models.bose_hubbard(10, 10, 1.0, 2.0)
+    n = len(states)
+    row, col, val = H
+    row, col, val = np.asarray(row), np.asarray(col), np.asarray(val, dtype=np.complex128)
+    rng = np.random.default_rng(2)
+    pert = val.copy()
+    diag = row == col
+    pert[diag] += rng.uniform(-1, 1, diag.sum()) * 1e-13 * np.abs(val[diag]).max()
+    v = _fock(states, [10] + [0] * 9)
+    Md, Ml = te_gpu.Matrix(n, row, col, val), te_gpu.Matrix(n, row, col, pert)
+    a = _run(te_gpu, Md, v, 1.0, 0.5, [], 1)
+    b = _run(te_gpu, Ml, v, 1.0, 0.5, [], 1)
+    assert Md.fixed_layout()["state"] == 2 and Ml.fixed_layout()["state"] == 1
+    assert a["n_steps"] == b["n_steps"]
+    assert np.linalg.norm(a["state"] - b["state"]) < 1e-10  # ||dH|| t <= 9e-12

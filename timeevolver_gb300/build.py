@@ -21,7 +21,8 @@ LIB_TEGPU = os.path.join(BUILD, "libtegpu.so")
 LIB_HOST = os.path.join(BUILD, "libtimeevolver.so")
 
 CUDA_SOURCES = ["te_common.cu", "te_matrix.cu", "te_lanczos.cu", "te_krylov.cu", "te_sample.cu", "te_evolver.cu",
-                "te_batch.cu", "te_adjoint.cu", "te_synth.cu", "te_model.cu", "te_probe.cu"]
+                "te_batch.cu", "te_adjoint.cu", "te_synth.cu", "te_model.cu", "te_probe.cu",
+                "te_fixed.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC"]
 HOST_SOURCES = ["matrixDataTypes.cpp", "krylovObservables.cpp", "krylovTimeEvolver.cpp", "krylovLogger.cpp",

@@ -119,3 +119,26 @@ __device__ __forceinline__ double2 te_sell_row_fix(int64_t s, int64_t e, const i
   }
   return make_double2(te_i64_to_double(sr, 62 - shift), te_i64_to_double(si, 62 - shift));
 }
+
+// te_sell_row_fix over packed slots: word = column | (value index << cbits),
+// the values' limbs in tab (shared memory).
+__device__ __forceinline__ double2 te_sell_row_fix_packed(int64_t s, int64_t e, const uint32_t* __restrict__ pk,
+                                                          const int2* tab, int cbits, const int4* __restrict__ X,
+                                                          int shift) {
+  const uint32_t cmask = (1u << cbits) - 1u;
+  int64_t sr = 0, si = 0;
+#pragma unroll(kTeFixUnroll)
+  for (; s < e; s += 32) {
+    const uint32_t wd = __ldcs(pk + s);
+    const int2 h = tab[wd >> cbits];
+    const int4 x = __ldg(X + (wd & cmask));
+    int tr, ti;
+    asm("mul.hi.s32 %0, %1, %2;" : "=r"(tr) : "r"(h.y), "r"(x.x));
+    asm("mad.hi.s32 %0, %1, %2, %0;" : "+r"(tr) : "r"(h.x), "r"(x.y));
+    asm("mul.hi.s32 %0, %1, %2;" : "=r"(ti) : "r"(h.y), "r"(x.z));
+    asm("mad.hi.s32 %0, %1, %2, %0;" : "+r"(ti) : "r"(h.x), "r"(x.w));
+    sr += (int64_t)h.y * x.y + 2 * (int64_t)tr;
+    si += (int64_t)h.y * x.w + 2 * (int64_t)ti;
+  }
+  return make_double2(te_i64_to_double(sr, 62 - shift), te_i64_to_double(si, 62 - shift));
+}

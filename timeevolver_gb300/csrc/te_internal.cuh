@@ -134,6 +134,14 @@ struct TeSell {
   int32_t* fix_warp_chunk = nullptr;
   int fix_grid = 0;
   bool fix_saturated = false;
+  // Value dictionary (matrices with few distinct values, e.g. lattice
+  // Hamiltonians): instead of fix_val and col, one word per slot,
+  // column | (value index << fix_cbits), and the fix_nvals distinct values
+  // (ascending) as fixed-point limbs in fix_table; the apply kernel keeps the
+  // table in shared memory.
+  uint32_t* fix_pk = nullptr;
+  int2* fix_table = nullptr;
+  int fix_nvals = 0, fix_cbits = 0;
 };
 
 // The long rows of a SELL matrix, by value for kernels.
@@ -178,12 +186,12 @@ __device__ __forceinline__ void te_pdl_trigger() { asm volatile("griddepcontrol.
 // 3% faster) and costs for smaller grids (dim 92 378: 10% slower), so callers
 // enable it only for saturated grids.
 template <typename... KArgs, typename... Args>
-cudaError_t te_launch_pdl(bool enable, void (*kernel)(KArgs...), int grid, int block, cudaStream_t st,
-                          Args... args) {
+cudaError_t te_launch_pdl_smem(bool enable, void (*kernel)(KArgs...), int grid, int block, size_t smem,
+                               cudaStream_t st, Args... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(block);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -196,6 +204,11 @@ cudaError_t te_launch_pdl(bool enable, void (*kernel)(KArgs...), int grid, int b
   cfg.numAttrs = enable ? 1 : 0;
 #endif
   return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+template <typename... KArgs, typename... Args>
+cudaError_t te_launch_pdl(bool enable, void (*kernel)(KArgs...), int grid, int block, cudaStream_t st,
+                          Args... args) {
+  return te_launch_pdl_smem(enable, kernel, grid, block, 0, st, args...);
 }
 
 // error reporting
@@ -239,6 +252,8 @@ void te_launch_lanczos_update(int64_t n, const double2* w, const double2* u_j, d
 // per row, te_sell_build_fixed done): te_launch_fix_start encodes u_0 at the
 // start of a Krylov step; the apply pass reads the fixed-point copy X of u_j.
 int te_sell_build_fixed(te_matrix_s* A);
+// Resident blocks per SM of the fixed-point apply kernel (te_lanczos.cu).
+int te_apply_fix_blocks_per_sm(bool packed, size_t dyn_smem);
 // Re-encode the fixed-point values after H's SELL values changed in place.
 int te_sell_refresh_fixed(te_matrix_s* A);
 void te_launch_fix_start(int64_t n, const double2* u_0, int4* X, TeDevState* ds, double* partials, cudaStream_t st);

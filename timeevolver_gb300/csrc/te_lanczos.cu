@@ -154,15 +154,29 @@ __device__ __forceinline__ unsigned int te_block_max_from_smem(const unsigned in
 #ifndef TE_FIX_MIN_BLOCKS
 #define TE_FIX_MIN_BLOCKS 6
 #endif
-template <bool HAS_PREV>
+// The matrix side of the fixed-point apply: limbs per slot (col, hv) or packed
+// slots with a value table (pk, table, nvals, cbits; PACKED).
+struct TeFixMatrix {
+  const int32_t* col;
+  const int2* hv;
+  const uint32_t* pk;
+  const int2* table;
+  int nvals, cbits, sh;
+};
+
+template <bool HAS_PREV, bool PACKED>
 __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_fix_kernel(
-    int64_t n, const int32_t* __restrict__ warp_chunk, const int64_t* __restrict__ chunk_off,
-    const int32_t* __restrict__ col, const int2* __restrict__ hv, int sh, TeLongRows L, const int4* __restrict__ X,
-    const double2* __restrict__ u_j, const double2* __restrict__ u_jm1, double2* __restrict__ w, TeDevState* ds,
-    double* partials, int j) {
+    int64_t n, const int32_t* __restrict__ warp_chunk, const int64_t* __restrict__ chunk_off, TeFixMatrix M,
+    TeLongRows L, const int4* __restrict__ X, const double2* __restrict__ u_j, const double2* __restrict__ u_jm1,
+    double2* __restrict__ w, TeDevState* ds, double* partials, int j) {
   __shared__ double scratch[2 * 32];
   __shared__ double wide[2 * TE_THREADS];
   __shared__ unsigned int wmax_w[TE_THREADS / 32];
+  extern __shared__ int2 tab[];  // PACKED: the value table (constant across launches)
+  if (PACKED) {
+    for (int i = threadIdx.x; i < M.nvals; i += blockDim.x) tab[i] = M.table[i];
+    __syncthreads();
+  }
   te_pdl_trigger();
   te_pdl_wait();
   if (te_step_inactive(ds)) return;
@@ -175,7 +189,7 @@ __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_f
     const double bj = ds->beta[j];
     cw = (bj * ie) * (bj * ie);
   }
-  const int shift = sh + ds->fx_xs[j];
+  const int shift = M.sh + ds->fx_xs[j];
   double acc[2] = {0.0, 0.0};
   unsigned int wmax = 0;
   const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -206,7 +220,8 @@ __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_f
     const bool live = r < n && r >= L.n;
     // the row's own vector entries, loaded ahead of the SpMV so that their
     // latency overlaps the gathers
-    const double2 y = te_sell_row_fix(s0 + lane, s1, col, hv, X, shift);
+    const double2 y = PACKED ? te_sell_row_fix_packed(s0 + lane, s1, M.pk, tab, M.cbits, X, shift)
+                             : te_sell_row_fix(s0 + lane, s1, M.col, M.hv, X, shift);
     if (live) {
       const double2 wr = apply_row_epilogue<HAS_PREV, true>(r, y, g, cw, u_j, u_jm1, w, acc);
       wmax = max(wmax, max(te_fix_hiword(wr.x), te_fix_hiword(wr.y)));
@@ -276,26 +291,6 @@ __global__ void __launch_bounds__(TE_THREADS) fix_start_encode_kernel(int64_t n,
     const int2 a = te_fix_split(te_fix_encode(v.x, xs)), b = te_fix_split(te_fix_encode(v.y, xs));
     X[r] = make_int4(a.x, a.y, b.x, b.y);
   }
-}
-
-// Fixed-point chunk values: row 1-norms of the chunk rows (maximum as the bit
-// pattern of a non-negative double), then h~ = round(h 2^sh) as limbs.
-__global__ void __launch_bounds__(TE_THREADS) fix_rownorm_kernel(int64_t n_chunks, const int64_t* __restrict__ off,
-                                                                 const double* __restrict__ val,
-                                                                 unsigned long long* max_bits) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const int64_t c = t >> 5;
-  if (c >= n_chunks) return;
-  double s = 0.0;
-  for (int64_t q = off[c] + (t & 31); q < off[c + 1]; q += 32) s += fabs(val[q]);
-  for (int o = 16; o > 0; o >>= 1) s = fmax(s, __shfl_xor_sync(0xffffffffu, s, o));
-  if ((t & 31) == 0) atomicMax(max_bits, (unsigned long long)__double_as_longlong(s));
-}
-
-__global__ void __launch_bounds__(TE_THREADS) fix_encode_values_kernel(int64_t slots, const double* __restrict__ val,
-                                                                       int2* __restrict__ hv, int sh) {
-  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < slots; q += (int64_t)gridDim.x * blockDim.x)
-    hv[q] = te_fix_split(te_fix_encode(val[q], sh));
 }
 
 // ---------------------------------------------------------------------------
@@ -904,95 +899,25 @@ void te_launch_fix_start(int64_t n, const double2* u_0, int4* X, TeDevState* ds,
   fix_start_encode_kernel<<<g2, TE_THREADS, 0, st>>>(n, u_0, X, ds, bmax, g1);
 }
 
+int te_apply_fix_blocks_per_sm(bool packed, size_t dyn_smem) {
+  const void* k[2] = {packed ? (const void*)lanczos_apply_fix_kernel<true, true>
+                             : (const void*)lanczos_apply_fix_kernel<true, false>,
+                      packed ? (const void*)lanczos_apply_fix_kernel<false, true>
+                             : (const void*)lanczos_apply_fix_kernel<false, false>};
+  return std::min(te_kernel_blocks_per_sm(k[0], TE_THREADS, dyn_smem),
+                  te_kernel_blocks_per_sm(k[1], TE_THREADS, dyn_smem));
+}
+
 void te_launch_lanczos_apply_fix(const TeSell& A, const int4* X, const double2* u_j, const double2* u_jm1,
                                  double2* w, TeDevState* ds, double* partials, int j, cudaStream_t st) {
-  if (u_jm1)
-    te_launch_pdl(A.fix_saturated, lanczos_apply_fix_kernel<true>, A.fix_grid, TE_THREADS, st, A.n,
-                  A.fix_warp_chunk, A.chunk_off, A.col, A.fix_val, A.fix_sh, te_long_rows(A), X, u_j, u_jm1, w, ds,
-                  partials, j);
-  else
-    te_launch_pdl(A.fix_saturated, lanczos_apply_fix_kernel<false>, A.fix_grid, TE_THREADS, st, A.n,
-                  A.fix_warp_chunk, A.chunk_off, A.col, A.fix_val, A.fix_sh, te_long_rows(A), X, u_j, u_jm1, w, ds,
-                  partials, j);
+  const bool packed = A.fix_pk != nullptr;
+  const TeFixMatrix M{A.col, A.fix_val, A.fix_pk, A.fix_table, A.fix_nvals, A.fix_cbits, A.fix_sh};
+  const size_t smem = packed ? sizeof(int2) * A.fix_nvals : 0;
+  auto k = packed ? (u_jm1 ? lanczos_apply_fix_kernel<true, true> : lanczos_apply_fix_kernel<false, true>)
+                  : (u_jm1 ? lanczos_apply_fix_kernel<true, false> : lanczos_apply_fix_kernel<false, false>);
+  te_launch_pdl_smem(A.fix_saturated, k, A.fix_grid, TE_THREADS, smem, st, A.n, A.fix_warp_chunk, A.chunk_off, M,
+                     te_long_rows(A), X, u_j, u_jm1, w, ds, partials, j);
 }
 
-// Fixed-point chunk values (real matrices with one lane per row): sh puts the
-// largest chunk-row 1-norm below 2^61, then every slot value as limbs.
-static int fixed_values(TeSell& S) {
-  unsigned long long* d_max = nullptr;
-  TE_CUDA(cudaMalloc(&d_max, sizeof(unsigned long long)));
-  int rc = te_cuda_check(cudaMemset(d_max, 0, sizeof(unsigned long long)), "fixed values");
-  const int64_t threads = S.n_chunks * 32;
-  if (rc == TE_OK)
-    fix_rownorm_kernel<<<(unsigned)((threads + TE_THREADS - 1) / TE_THREADS), TE_THREADS>>>(S.n_chunks, S.chunk_off,
-                                                                                             S.val, d_max);
-  unsigned long long bits = 0;
-  if (rc == TE_OK) rc = te_cuda_check(cudaMemcpy(&bits, d_max, sizeof(bits), cudaMemcpyDeviceToHost), "fixed values");
-  cudaFree(d_max);
-  if (rc != TE_OK) return rc;
-  double rmax;
-  std::memcpy(&rmax, &bits, sizeof(rmax));
-  if (!(rmax < 1e300)) {
-    te_set_error("fixed-point SpMV: matrix row norm not finite");
-    return TE_ERR_INVALID_ARG;
-  }
-  int E = 0;
-  if (rmax > 0.0) std::frexp(rmax * (1.0 + 1e-12), &E);
-  S.fix_sh = 61 - E;
-  fix_encode_values_kernel<<<te_grid_fit((const void*)fix_encode_values_kernel, S.slots, TE_THREADS), TE_THREADS>>>(
-      S.slots, S.val, S.fix_val, S.fix_sh);
-  return te_cuda_check(cudaDeviceSynchronize(), "fixed values");
-}
 
-// The fixed-point values and the fixed-point apply kernel's own schedule,
-// once per matrix.
-static int build_fixed(te_matrix_s* A) {
-  TeSell& S = A->sell;
-  if (!A->is_real || S.lanes != 1 || S.n_chunks < 1) {
-    te_set_error("fixed-point SpMV needs a real matrix with one lane per row");
-    return TE_ERR_INVALID_ARG;
-  }
-  int rc;
-  if ((rc = te_cuda_check(cudaMalloc(&S.fix_val, sizeof(int2) * std::max<int64_t>(S.slots, 1)), "fixed values")) !=
-      TE_OK)
-    return rc;
-  if ((rc = fixed_values(S)) != TE_OK) return rc;
-  std::vector<int64_t> off(S.n_chunks + 1);
-  rc = te_cuda_check(cudaMemcpy(off.data(), S.chunk_off, sizeof(int64_t) * off.size(), cudaMemcpyDeviceToHost),
-                     "fixed values");
-  if (rc != TE_OK) return rc;
-  int bps = 8;
-  for (const void* k : {(const void*)lanczos_apply_fix_kernel<true>, (const void*)lanczos_apply_fix_kernel<false>})
-    bps = std::min(bps, te_kernel_blocks_per_sm(k, TE_THREADS, 0));
-  std::vector<int32_t> wc;
-  te_sell_schedule(off, S.n_chunks, bps, true, S.fix_grid, S.fix_saturated, wc);
-  int32_t* d_wc = nullptr;
-  if ((rc = te_cuda_check(cudaMalloc(&d_wc, sizeof(int32_t) * wc.size()), "fixed values")) != TE_OK) return rc;
-  rc = te_cuda_check(cudaMemcpy(d_wc, wc.data(), sizeof(int32_t) * wc.size(), cudaMemcpyHostToDevice),
-                     "fixed values");
-  if (rc != TE_OK) {
-    cudaFree(d_wc);
-    return rc;
-  }
-  S.fix_warp_chunk = d_wc;  // marks the fixed-point data complete
-  return TE_OK;
-}
-
-int te_sell_refresh_fixed(te_matrix_s* A) {
-  if (!A->sell.fix_warp_chunk) return TE_OK;
-  return fixed_values(A->sell);
-}
-
-int te_sell_build_fixed(te_matrix_s* A) {
-  TeSell& S = A->sell;
-  if (S.fix_warp_chunk) return TE_OK;
-  const int rc = build_fixed(A);
-  if (rc != TE_OK) {
-    cudaFree(S.fix_val);
-    S.fix_val = nullptr;
-    cudaFree(S.fix_warp_chunk);
-    S.fix_warp_chunk = nullptr;
-  }
-  return rc;
-}
 

@@ -293,6 +293,8 @@ void free_matrix(te_matrix_s* M) {
   cudaFree(M->sell.long_val);
   cudaFree(M->sell.fix_val);
   cudaFree(M->sell.fix_warp_chunk);
+  cudaFree(M->sell.fix_pk);
+  cudaFree(M->sell.fix_table);
   delete M;
 }
 
@@ -908,6 +910,15 @@ extern "C" int te_matrix_layout(te_matrix A, int64_t* sell_slots, int64_t* long_
       TE_CUDA(cudaMemcpy(&e, A->sell.long_ptr + A->sell.n_long, sizeof(int64_t), cudaMemcpyDeviceToHost));
     *long_entries = e;
   }
+  return TE_OK;
+}
+
+extern "C" int te_matrix_fixed_layout(te_matrix A, int* state, int* n_values, int* scale_shift) {
+  if (!A) return TE_ERR_INVALID_ARG;
+  const TeSell& S = A->sell;
+  if (state) *state = !S.fix_warp_chunk ? 0 : (S.fix_pk ? 2 : 1);
+  if (n_values) *n_values = S.fix_nvals;
+  if (scale_shift) *scale_shift = S.fix_sh;
   return TE_OK;
 }
 

@@ -69,6 +69,14 @@ __device__ __forceinline__ double te_i64_to_double(int64_t v, int e2) {
   return __longlong_as_double((long long)(sign | ((uint64_t)(ex + 1023) << 52) | (mant & 0xfffffffffffffull)));
 }
 
+// v^2 / 2^62 for |v| < 2^61 from 31-bit limbs of |v| (a1^2 + 4 hi32(a1 a0),
+// the a0^2 term dropped): below the exact value by less than 5.
+__device__ __forceinline__ unsigned long long te_fix_sq(int64_t v) {
+  const uint64_t a = v < 0 ? 0ull - (uint64_t)v : (uint64_t)v;
+  const unsigned int a1 = (unsigned int)(a >> 31), a0 = (unsigned int)(a & 0x7fffffffull);
+  return (unsigned long long)a1 * a1 + 4ull * __umulhi(a1, a0);
+}
+
 // Upper bound of |v| from the high word of its bit pattern (sign cleared):
 // the double whose high word is one larger.
 __device__ __forceinline__ unsigned int te_fix_hiword(double v) {
@@ -91,6 +99,17 @@ __device__ __forceinline__ int te_fix_scale(double bound) {
 #endif
 constexpr int kTeFixUnroll = TE_FIX_UNROLL;  // slots per lane in flight
 
+// One slot: S += h~ X (see te_sell_row_fix).
+__device__ __forceinline__ void te_fix_mac(const int2 h, const int4 x, int64_t& sr, int64_t& si) {
+  int tr, ti;
+  asm("mul.hi.s32 %0, %1, %2;" : "=r"(tr) : "r"(h.y), "r"(x.x));
+  asm("mad.hi.s32 %0, %1, %2, %0;" : "+r"(tr) : "r"(h.x), "r"(x.y));
+  asm("mul.hi.s32 %0, %1, %2;" : "=r"(ti) : "r"(h.y), "r"(x.z));
+  asm("mad.hi.s32 %0, %1, %2, %0;" : "+r"(ti) : "r"(h.x), "r"(x.w));
+  sr += (int64_t)h.y * x.y + 2 * (int64_t)tr;
+  si += (int64_t)h.y * x.w + 2 * (int64_t)ti;
+}
+
 // One lane's row of a real SELL-32 matrix times the fixed-point vector X: the
 // lane's slots s, s + 32, ... below e of its chunk; returns the row sum as a
 // double, given the total scale shift = sh + xs (y = sum h~ X 2^-shift).
@@ -106,17 +125,7 @@ __device__ __forceinline__ double2 te_sell_row_fix(int64_t s, int64_t e, const i
                                                    int shift) {
   int64_t sr = 0, si = 0;
 #pragma unroll(kTeFixUnroll)
-  for (; s < e; s += 32) {
-    const int2 h = __ldcs(hv + s);              // {h0, h1}
-    const int4 x = __ldg(X + __ldcs(col + s));  // {re0, re1, im0, im1}
-    int tr, ti;
-    asm("mul.hi.s32 %0, %1, %2;" : "=r"(tr) : "r"(h.y), "r"(x.x));
-    asm("mad.hi.s32 %0, %1, %2, %0;" : "+r"(tr) : "r"(h.x), "r"(x.y));
-    asm("mul.hi.s32 %0, %1, %2;" : "=r"(ti) : "r"(h.y), "r"(x.z));
-    asm("mad.hi.s32 %0, %1, %2, %0;" : "+r"(ti) : "r"(h.x), "r"(x.w));
-    sr += (int64_t)h.y * x.y + 2 * (int64_t)tr;
-    si += (int64_t)h.y * x.w + 2 * (int64_t)ti;
-  }
+  for (; s < e; s += 32) te_fix_mac(__ldcs(hv + s), __ldg(X + __ldcs(col + s)), sr, si);  // {h0, h1}, {re0, re1, im0, im1}
   return make_double2(te_i64_to_double(sr, 62 - shift), te_i64_to_double(si, 62 - shift));
 }
 
@@ -130,15 +139,7 @@ __device__ __forceinline__ double2 te_sell_row_fix_packed(int64_t s, int64_t e, 
 #pragma unroll(kTeFixUnroll)
   for (; s < e; s += 32) {
     const uint32_t wd = __ldcs(pk + s);
-    const int2 h = tab[wd >> cbits];
-    const int4 x = __ldg(X + (wd & cmask));
-    int tr, ti;
-    asm("mul.hi.s32 %0, %1, %2;" : "=r"(tr) : "r"(h.y), "r"(x.x));
-    asm("mad.hi.s32 %0, %1, %2, %0;" : "+r"(tr) : "r"(h.x), "r"(x.y));
-    asm("mul.hi.s32 %0, %1, %2;" : "=r"(ti) : "r"(h.y), "r"(x.z));
-    asm("mad.hi.s32 %0, %1, %2, %0;" : "+r"(ti) : "r"(h.x), "r"(x.w));
-    sr += (int64_t)h.y * x.y + 2 * (int64_t)tr;
-    si += (int64_t)h.y * x.w + 2 * (int64_t)ti;
+    te_fix_mac(tab[wd >> cbits], __ldg(X + (wd & cmask)), sr, si);
   }
   return make_double2(te_i64_to_double(sr, 62 - shift), te_i64_to_double(si, 62 - shift));
 }

@@ -95,6 +95,9 @@ struct TeDevState {
   int fx_xs[TE_MMAX + 1];
   unsigned int fx_umax[TE_MMAX + 1];
   unsigned int fx_wmax, fx_pad;
+  // the update pass's coefficient alpha_j s_j / g (alpha_j / expFactor when
+  // folded), set with alpha_j by the apply pass
+  double upd_gr, upd_gi;
 };
 
 // SELL-32 matrix in the sorted (permuted) basis.

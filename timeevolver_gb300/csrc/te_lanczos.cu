@@ -121,7 +121,13 @@ __global__ void __launch_bounds__(TE_THREADS, (REAL && K == 1) ? 6 : 5) lanczos_
     double tot[2];
     te_final_sum<2>(tot, partials, &ds->counter[0], scratch);
     const double f = FOLD ? sj * g : sj;
-    if (threadIdx.x == 0) ds->alpha[j] = make_double2(f * tot[0], f * tot[1]);
+    if (threadIdx.x == 0) {
+      const double2 alpha = make_double2(f * tot[0], f * tot[1]);
+      ds->alpha[j] = alpha;
+      const double q = FOLD ? ds->inv_exp_factor : sj;  // alpha_j s_j / g = alpha_j / expFactor when folded
+      ds->upd_gr = alpha.x * q;
+      ds->upd_gi = alpha.y * q;
+    }
   }
 }
 
@@ -218,8 +224,6 @@ __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_f
     }
     const int64_t r = c * 32 + lane;
     const bool live = r < n && r >= L.n;
-    // the row's own vector entries, loaded ahead of the SpMV so that their
-    // latency overlaps the gathers
     const double2 y = PACKED ? te_sell_row_fix_packed(s0 + lane, s1, M.pk, tab, M.cbits, X, shift)
                              : te_sell_row_fix(s0 + lane, s1, M.col, M.hv, X, shift);
     if (live) {
@@ -237,6 +241,8 @@ __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_f
       const double f = sj * g;
       const double2 alpha = make_double2(f * tot[0], f * tot[1]);
       ds->alpha[j] = alpha;
+      ds->upd_gr = alpha.x * ie;
+      ds->upd_gi = alpha.y * ie;
       const double W = te_fix_upper(atomicExch(&ds->fx_wmax, 0u));
       const double U = te_fix_upper(ds->fx_umax[j]);
       const double B = (W + (fabs(alpha.x * ie) + fabs(alpha.y * ie)) * U) * (1.0 + 1e-12);
@@ -517,14 +523,11 @@ __global__ void __launch_bounds__(TE_THREADS) lanczos_update_kernel(int64_t n, c
   te_pdl_trigger();
   te_pdl_wait();
   if (te_step_inactive(ds)) return;
-  const double sj = ds->s[j];
-  const double g = fold ? ds->exp_factor * sj : 1.0;
-  const double2 a = ds->alpha[j];
-  const double q = fold ? ds->inv_exp_factor : sj;  // alpha_j s_j / g = alpha_j / expFactor
-  const double gr = a.x * q, gi = a.y * q;
+  const double gr = ds->upd_gr, gi = ds->upd_gi;  // alpha_j s_j / g
   const int xs = FIX ? ds->fx_xs[j + 1] : 0;
   double acc[1] = {0.0};
   unsigned int umax = 0;
+  unsigned long long sq_lo = 0, sq_hi = 0;  // FIX: sum |X|^2 / 2^62 in 128 bits
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
     double2 wv = w[r];
     double2 u = u_j[r];
@@ -533,19 +536,28 @@ __global__ void __launch_bounds__(TE_THREADS) lanczos_update_kernel(int64_t n, c
     o.y = fma(-gr, u.y, fma(-gi, u.x, wv.y));
     if (STORE) u_jp1[r] = o;
     if (FIX) {
-      const int2 p = te_fix_split(te_fix_encode(o.x, xs)), q2 = te_fix_split(te_fix_encode(o.y, xs));
+      const int64_t er = te_fix_encode(o.x, xs), ei = te_fix_encode(o.y, xs);
+      const int2 p = te_fix_split(er), q2 = te_fix_split(ei);
       X[r] = make_int4(p.x, p.y, q2.x, q2.y);
       umax = max(umax, max(te_fix_hiword(o.x), te_fix_hiword(o.y)));
+      // ||u'||^2 from the integer copy, off the FP64 pipe
+      const unsigned long long sq = te_fix_sq(er) + te_fix_sq(ei);
+      asm("add.cc.u64 %0, %0, %2;\n\taddc.u64 %1, %1, 0;" : "+l"(sq_lo), "+l"(sq_hi) : "l"(sq));
+    } else {
+      acc[0] = fma(o.x, o.x, fma(o.y, o.y, acc[0]));
     }
-    acc[0] = fma(o.x, o.x, fma(o.y, o.y, acc[0]));
   }
-  if (FIX) te_warp_max_to_smem(umax, umax_w);
+  if (FIX) {
+    acc[0] = ldexp(fma((double)sq_hi, 18446744073709551616.0, (double)sq_lo), 62 - 2 * xs);
+    te_warp_max_to_smem(umax, umax_w);
+  }
   te_block_sum_wide<1>(acc, wide);
   if (FIX && threadIdx.x == 0) atomicMax(&ds->fx_umax[j + 1], te_block_max_from_smem(umax_w));
   if (te_publish_partials<1>(acc, partials, &ds->counter[1])) {
     double tot[1];
     te_final_sum<1>(tot, partials, &ds->counter[1], scratch);
     if (threadIdx.x == 0) {
+      const double g = fold ? ds->exp_factor * ds->s[j] : 1.0;
       const double beta = fabs(g) * sqrt(tot[0]);
       const int m = ds->m_cur;
       if (beta < ds->tol_rate) {  // lucky breakdown (:551-555)

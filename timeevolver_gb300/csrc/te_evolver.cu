@@ -344,7 +344,7 @@ int run(te_evolver ev, te_result* out) {
                    ev->H->sell.lanes == 1 && ev->H->sell.n_chunks >= 2048 && ev->fused_lanczos != 2;
   if (fix) {
     if ((rc = te_sell_build_fixed(ev->H)) != TE_OK) return rc;
-    if (!ev->X) TE_CUDA(cudaMalloc(&ev->X, sizeof(int4) * n));
+    if (!ev->X) TE_CUDA(cudaMalloc(&ev->X, sizeof(int4) * n * ev->m));  // X_0 .. X_{m-1}
   }
   while (!S->done) {
     if (S->fatal) break;
@@ -374,8 +374,8 @@ int run(te_evolver ev, te_result* out) {
       {
         ProfScope ps(ev, 0);
         if (fix_step)
-          te_launch_lanczos_apply_fix(ev->H->sell, ev->X, ev->cols[j], j > 0 ? ev->cols[j - 1] : nullptr, ev->w,
-                                      ev->ds, ev->partials, j, st);
+          te_launch_lanczos_apply_fix(ev->H->sell, ev->X + (int64_t)j * n, ev->cols[j],
+                                      j > 0 ? ev->cols[j - 1] : nullptr, ev->w, ev->ds, ev->partials, j, st);
         else
           te_launch_lanczos_apply(ev->H->sell, ev->H->is_real, ev->cols[j],
                                   (j > 0 && !cgs2) ? ev->cols[j - 1] : nullptr, ev->w, ev->ds, ev->partials, j, fold,
@@ -384,7 +384,7 @@ int run(te_evolver ev, te_result* out) {
       if (!cgs2) {
         ProfScope ps(ev, 1);
         te_launch_lanczos_update(n, ev->w, ev->cols[j], j + 1 < m ? ev->cols[j + 1] : nullptr, ev->ds, ev->partials,
-                                 j, fold, st, fix_step ? ev->X : nullptr);
+                                 j, fold, st, fix_step && j + 1 < m ? ev->X + (int64_t)(j + 1) * n : nullptr);
         ev->launches += 2;
       } else {
         // classical Gram-Schmidt against u_0..u_j, then one reorthogonalisation pass
@@ -407,6 +407,7 @@ int run(te_evolver ev, te_result* out) {
     for (int j = 0; j < m; ++j) ca.cols[j] = ev->cols[j];
     ca.m = m;
     ca.w_out = ev->spare;
+    ca.fx = fix_step ? ev->X : nullptr;  // the basis's fixed-point copies, this step
     {
       ProfScope ps(ev, 3);
       te_launch_combine(ca, ev->ds, ev->sampled, st);

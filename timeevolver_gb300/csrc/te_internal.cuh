@@ -316,6 +316,9 @@ struct TeCombineArgs {
   int64_t n;
   double2* w_out;         // new start vector (when the step produced w)
   double2* sample_out;    // batch buffer: sample s at sample_out + s * n
+  // optional fixed-point copies of the basis (te_fixed.cuh): X_j at fx + j n,
+  // scale 2^fx_xs[j] in the state; the outputs are then formed in integers
+  const int4* fx;
 };
 void te_launch_combine(const TeCombineArgs& a, TeDevState* ds, double2* last_out, cudaStream_t st);
 struct TeFusedObs {

@@ -10,6 +10,7 @@
 // diagonal and vector observables are reduced in one further pass over the
 // batch.  All reductions finish in the last block to complete, in a fixed
 // order.
+#include "te_fixed.cuh"
 #include "te_internal.cuh"
 #include "te_reduce.cuh"
 #include "te_rowdot.cuh"
@@ -50,11 +51,60 @@ __device__ __forceinline__ void combine_rows(const TeCombineArgs& a, const doubl
   }
 }
 
+// The same outputs from the fixed-point copies X_j = round(u_j 2^xs_j) of the
+// basis (te_fixed.cuh), on the integer pipes: with c_oj = Y[slot_o][j] 2^-xs_j
+// (so that c_oj X_j = Y[slot_o][j] u_j) quantised per output as
+// C_oj = round(c_oj 2^sc_o), sc_o putting sum_j (|Re c_oj| + |Im c_oj|) below
+// 2^61, psi_o = 2^(62 - sc_o) sum_j C_oj X_j with the limb products of
+// te_fix_mac (complex: Re = Cr Xr - Ci Xi, Im = Cr Xi + Ci Xr).  Error per
+// component below 4 m 1.25 2^-56 + (m + 1) 2^-61 of sum_j |Y_oj| max|u_j|.
+__device__ __forceinline__ int64_t te_fix_prod(int c0, int c1, int x0, int x1) {
+  int t;
+  asm("mul.hi.s32 %0, %1, %2;" : "=r"(t) : "r"(c1), "r"(x0));
+  asm("mad.hi.s32 %0, %1, %2, %0;" : "+r"(t) : "r"(c0), "r"(x1));
+  return (int64_t)c1 * x1 + 2 * (int64_t)t;
+}
+
+template <int G>
+__device__ __forceinline__ void combine_rows_fix(const TeCombineArgs& a, int m, const int4 (*C)[TE_MMAX],
+                                                 const int* sc, const int* slot_s, int S, double2* last_out,
+                                                 double2* store, int64_t store_ld, int base) {
+  const int64_t n = a.n;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    int64_t sr[G], si[G];
+#pragma unroll
+    for (int o = 0; o < G; ++o) sr[o] = si[o] = 0;
+    for (int j = 0; j < m; ++j) {
+      const int4 x = __ldcs(a.fx + (int64_t)j * n + r);  // {re0, re1, im0, im1}
+#pragma unroll
+      for (int o = 0; o < G; ++o) {
+        const int4 c = C[o][j];  // {re0, re1, im0, im1}
+        sr[o] += te_fix_prod(c.x, c.y, x.x, x.y) - te_fix_prod(c.z, c.w, x.z, x.w);
+        si[o] += te_fix_prod(c.x, c.y, x.z, x.w) + te_fix_prod(c.z, c.w, x.x, x.y);
+      }
+    }
+#pragma unroll
+    for (int o = 0; o < G; ++o) {
+      const double2 v = make_double2(te_i64_to_double(sr[o], 62 - sc[o]), te_i64_to_double(si[o], 62 - sc[o]));
+      const int slot = slot_s[o];
+      if (slot == 0) {
+        a.w_out[r] = v;
+      } else {
+        a.sample_out[(int64_t)(slot - 1) * n + r] = v;
+        if (slot == S) last_out[r] = v;
+        if (store) store[(int64_t)(base + slot - 1) * store_ld + r] = v;
+      }
+    }
+  }
+}
+
 // psi_o = sum_j u_j Y[slot_o][j] for the outputs of this batch (the step's
 // next start vector w, then its samples), one pass over V per group of up to
 // four outputs.
 __global__ void __launch_bounds__(TE_THREADS) combine_kernel(TeCombineArgs a, TeDevState* ds, double2* last_out) {
   __shared__ double2 ys[TE_COMBINE_GROUP][TE_MMAX];
+  __shared__ int4 cfix[TE_COMBINE_GROUP][TE_MMAX];  // fixed-point coefficients (a.fx)
+  __shared__ int sc_s[TE_COMBINE_GROUP];
   __shared__ int slot_s[TE_COMBINE_GROUP];
   __shared__ const double2* cols[TE_MMAX];
   if (ds->fatal != 0) return;
@@ -79,6 +129,37 @@ __global__ void __launch_bounds__(TE_THREADS) combine_kernel(TeCombineArgs a, Te
     double2* store = ds->state_store;
     const int64_t sld = ds->store_ld;
     const int base = ds->sample_base;
+    if (a.fx) {
+      // coefficients c_oj = Y_oj 2^-xs_j in fixed point, per output scale
+      if (threadIdx.x < G) {
+        double b = 0.0;
+        for (int j = 0; j < m; ++j) {
+          const int xs = ds->fx_xs[j];
+          b += ldexp(fabs(ys[threadIdx.x][j].x), -xs) + ldexp(fabs(ys[threadIdx.x][j].y), -xs);
+        }
+        sc_s[threadIdx.x] = te_fix_scale(b * (1.0 + 1e-12));
+      }
+      __syncthreads();
+      for (int i = threadIdx.x; i < G * TE_MMAX; i += blockDim.x) {
+        const int o = i / TE_MMAX, j = i % TE_MMAX;
+        int4 c = make_int4(0, 0, 0, 0);
+        if (j < m) {
+          const int xs = ds->fx_xs[j];
+          const int2 cr = te_fix_split(te_fix_encode(ldexp(ys[o][j].x, -xs), sc_s[o]));
+          const int2 ci = te_fix_split(te_fix_encode(ldexp(ys[o][j].y, -xs), sc_s[o]));
+          c = make_int4(cr.x, cr.y, ci.x, ci.y);
+        }
+        cfix[o][j] = c;
+      }
+      __syncthreads();
+      switch (G) {
+        case 1: combine_rows_fix<1>(a, m, cfix, sc_s, slot_s, S, last_out, store, sld, base); break;
+        case 2: combine_rows_fix<2>(a, m, cfix, sc_s, slot_s, S, last_out, store, sld, base); break;
+        case 3: combine_rows_fix<3>(a, m, cfix, sc_s, slot_s, S, last_out, store, sld, base); break;
+        default: combine_rows_fix<4>(a, m, cfix, sc_s, slot_s, S, last_out, store, sld, base); break;
+      }
+      continue;
+    }
     switch (G) {
       case 1: combine_rows<1>(a, cols, m, ys, slot_s, S, last_out, store, sld, base); break;
       case 2: combine_rows<2>(a, cols, m, ys, slot_s, S, last_out, store, sld, base); break;

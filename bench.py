@@ -92,10 +92,10 @@ def load_peaks(te):
     return peaks
 
 
-def ncu_traffic():
-    """Per-launch DRAM traffic of the Lanczos apply kernel from the committed
-    ncu summary, if one exists."""
-    p = os.path.join(ROOT, "profiles", "lanczos_apply_bh12.json")
+def ncu_traffic(fixed=False):
+    """Per-launch DRAM traffic of the Lanczos apply kernel in use (fixed-point
+    or FP64 SpMV) from the committed ncu summary, if one exists."""
+    p = os.path.join(ROOT, "profiles", "lanczos_apply_fix_bh12.json" if fixed else "lanczos_apply_bh12.json")
     if os.path.exists(p):
         with open(p) as f:
             return json.load(f).get("dram_bytes_per_launch")
@@ -263,7 +263,7 @@ def run_gb300(args):
     f_apply = apply_kernel_flops(n, nnz, info["real"], fixed)
     avg_apply_s = apply_ms / 1000.0 / max(1, apply_n)
     achieved = b_apply / avg_apply_s / 1e9
-    traffic = ncu_traffic()
+    traffic = ncu_traffic(fixed)
     line = {
         "metric": METRIC, "value": value, "unit": "s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": False, "scaling": "weak",

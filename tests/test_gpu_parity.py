@@ -273,11 +273,18 @@ def test_spmv_lanes_variants(te_gpu, oracle_lib, lanes):
 
 
 def test_spmv_lanes_tuning(te_gpu):
+    """Complex matrices are tuned once; real ones keep one lane per row (the
+    fixed-point SpMV needs it)."""
     states, H = models.bose_hubbard(10, 10, 1.0, 2.0)
-    M = te_gpu.Matrix.from_coo(len(states), H)
+    row, col, val = (np.asarray(a) for a in H)
+    phase = np.where(row < col, np.exp(0.3j), np.where(row > col, np.exp(-0.3j), 1.0))
+    Hc = (row, col, np.asarray(val, dtype=np.complex128) * phase)  # Hermitian, complex hopping
+    M = te_gpu.Matrix.from_coo(len(states), Hc)
+    assert not M.info()["real"]
     k = M.spmv_lanes(tune=True)
     assert k in (1, 2, 4)
     assert M.spmv_lanes(tune=True) == k  # tuned once
+    assert te_gpu.Matrix.from_coo(len(states), H).spmv_lanes(tune=True) == 1
 
 
 @pytest.mark.parametrize("L,t,sampling", [(8, 10.0, 0.1), (11, 2.0, 0.5)])

@@ -814,8 +814,8 @@ void te_launch_lanczos_apply(const TeSell& A, bool is_real, const double2* u_j, 
                 A.col, A.val, te_long_rows(A), u_j, u_jm1, w, ds, partials, j);
 }
 
-// Autotuning of the lanes per row: time the three-term apply pass (the
-// dominant kernel) for K = 1, 2, 4 on the matrix itself, with scratch vectors
+// Autotuning of the lanes per row (complex matrices): time the three-term
+// apply pass (the dominant kernel) for K = 1, 2, 4 on the matrix itself, with scratch vectors
 // and a scratch state, and keep K > 1 only when it is clearly (> 10%) faster,
 // so that the choice -- which changes the rounding of the row sums -- is
 // stable from run to run.  Matrices that give every resident warp at least 8
@@ -826,7 +826,10 @@ int te_tune_sell_lanes(te_matrix_s* A) {
   if (S.lanes_fixed) return TE_OK;
   const int64_t resident_warps = (int64_t)te_num_sms() * te_sell_blocks_per_sm(A->is_real) * (TE_THREADS / 32);
   S.lanes = 1;
-  if (S.n_chunks >= 8 * resident_warps || S.n_chunks < 2048 || S.n_long > 0) {
+  // real matrices keep K = 1 for the fixed-point SpMV (the default for them,
+  // which needs one lane per row and beats the FP64 K = 1 pass by more than
+  // K > 1 ever did: 28% at L=12 against at most 8% for K = 2 at L=10)
+  if (S.n_chunks >= 8 * resident_warps || S.n_chunks < 2048 || S.n_long > 0 || A->is_real) {
     S.lanes_fixed = true;
     return TE_OK;
   }

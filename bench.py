@@ -160,6 +160,12 @@ def build_problem():
     return n, H, O, v
 
 
+def spmv_option(spmv):
+    """TE_OPT_FIXED_SPMV for --spmv: the product's default (fixed point for
+    real H only), fixed point for every H, or FP64."""
+    return {None: 1, "fixed": 2, "fp64": 0}[spmv]
+
+
 def apply_kernel_bytes(n, nnz, real=True, fixed=False, packed=False):
     """Algorithmic bytes of one Lanczos apply launch: the matrix (values +
     int32 columns; with the value dictionary one 4-byte word per entry), the
@@ -208,7 +214,7 @@ def run_gb300(args):
     O = te.Matrix.from_coo(n, Oc)
     info = H.info()
     ev = te.Evolver(H, v, T_FINAL, SAMPLING, [("sparse", O)], tol=TOL, m=M_KRYLOV)
-    options = {te.OPT_FIXED_SPMV: 1 if args.spmv == "fixed" else 0}
+    options = {te.OPT_FIXED_SPMV: spmv_option(args.spmv)}
     for opt, val in options.items():
         ev.set_option(opt, val)
     v_dev = torch.from_numpy(v.view(np.float64).copy()).cuda()
@@ -258,8 +264,8 @@ def run_gb300(args):
         return
     value = replica_seconds_per_solve(ms, args.steps, ws)
     peaks = load_peaks(te)
-    fixed = args.spmv == "fixed" and info["real"]
-    b_apply = apply_kernel_bytes(n, nnz, info["real"], fixed, fixed and fixed_layout["state"] == 2)
+    fixed = fixed_layout["state"] > 0
+    b_apply = apply_kernel_bytes(n, nnz, info["real"], fixed, fixed_layout["state"] == 2)
     f_apply = apply_kernel_flops(n, nnz, info["real"], fixed)
     avg_apply_s = apply_ms / 1000.0 / max(1, apply_n)
     achieved = b_apply / avg_apply_s / 1e9
@@ -269,7 +275,8 @@ def run_gb300(args):
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "complex128 (FP64)", "data": "synthetic (Bose-Hubbard model, seeded state)",
         "config": {"workload": WORKLOAD, "n": n, "nnz": nnz, "krylov_steps_per_solve": steps_per_solve,
-                   "status": status, "spmv": args.spmv, "parallelism": "replicas" if ws > 1 else "single GPU",
+                   "status": status, "spmv": "fixed" if fixed else "fp64",
+                   "parallelism": "replicas" if ws > 1 else "single GPU",
                    "l2": "inputs larger than L2 (H %.0f MB + Krylov basis %.0f MB)"
                          % (nnz * 12 / 1e6, (M_KRYLOV + 3) * 16 * n / 1e6)},
         "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -514,6 +521,9 @@ def run_zipf(args):
     v /= np.linalg.norm(v)
     v_dev = torch.from_numpy(v.view(np.float64).copy()).cuda()
     ev = te.Evolver(H, v, ZIPF_T, ZIPF_T, [], tol=TOL, m=M_KRYLOV)
+    options = {te.OPT_FIXED_SPMV: spmv_option(args.spmv)}
+    for opt, val in options.items():
+        ev.set_option(opt, val)
     for _ in range(args.warmup):
         ev.reset(None, device_ptr=v_dev.data_ptr())
         ev.run()
@@ -537,24 +547,28 @@ def run_zipf(args):
     for _ in range(max(1, args.steps)):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        out = te.evolve(H, v, ZIPF_T, ZIPF_T, [], tol=TOL, m=M_KRYLOV)
+        out = te.evolve(H, v, ZIPF_T, ZIPF_T, [], tol=TOL, m=M_KRYLOV, options=options)
         torch.cuda.synchronize()
         e2e.append(time.perf_counter() - t0)
     peaks = load_peaks(te)
-    fixed = args.spmv == "fixed" and info["real"]
-    b_apply = apply_kernel_bytes(n, nnz, info["real"], fixed, fixed and H.fixed_layout()["state"] == 2)
+    fl = H.fixed_layout()
+    fixed = fl["state"] > 0
+    b_apply = apply_kernel_bytes(n, nnz, info["real"], fixed, fixed and fl["state"] == 2)
     f_apply = apply_kernel_flops(n, nnz, info["real"], fixed)
     avg = apply_ms / 1e3 / max(1, apply_n)
     line = {"metric": ZIPF_METRIC, "value": value, "unit": "s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "complex128 (FP64)", "data": "synthetic (device generator, seeded)",
             "config": {"workload": ZIPF_WORKLOAD, "n": n, "nnz": nnz, "norm_estimate": est,
+                       "spmv": "fixed" if fixed else "fp64",
                        "generation_s": gen_s, "krylov_steps_per_solve": r.n_steps, "status": r.status,
                        "err": r.err, "l2": "inputs larger than L2 (H %.1f GB)" % (nnz * 20 / 1e9)},
             "e2e": {"value": float(np.mean(e2e)), "unit": "s", "h2d_bytes_per_step": 16 * n,
                     "d2h_bytes_per_step": 16 * n + 16},
             "gpu_launches": int(launches),
-            "roofline": {"bound": "hbm", "kernel": "lanczos_apply_kernel (SELL-32 SpMV, complex H)",
+            "roofline": {"bound": "hbm",
+                         "kernel": ("lanczos_apply_fix_kernel (fixed-point SELL-32 SpMV, complex H)" if fixed
+                                    else "lanczos_apply_kernel (SELL-32 SpMV, complex H)"),
                          "achieved": b_apply / avg / 1e9, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": b_apply / avg / 1e9 / peaks["hbm_gbs"], "peak_source": peaks["source"],
                          "traffic": None, "algorithmic_bytes_per_launch": b_apply, "avg_launch_us": avg * 1e6,
@@ -590,7 +604,7 @@ def zipf_cpu_baseline(te, nnz_full, steps_full):
                       "(extrapolated)" % (len(coo[2]), ZIPF_CPU_T, r["n_steps"], el, per_step, steps_full)}
 
 
-def ncu_case(t_final, config="plain", zipf_n=2_000_000, spmv="fixed"):
+def ncu_case(t_final, config="plain", zipf_n=2_000_000, spmv=None):
     """A short solve of the same workload for ncu captures (t_final instead of
     the full time; the Zipf matrix at a smaller dimension)."""
     import timeevolver_gb300 as te
@@ -607,7 +621,7 @@ def ncu_case(t_final, config="plain", zipf_n=2_000_000, spmv="fixed"):
         return
     n, Hc, Oc, v = build_problem()
     out = te.evolve(Hc, v, t_final, t_final, [("sparse", Oc)], tol=TOL * t_final / T_FINAL, m=M_KRYLOV,
-                    options={te.OPT_FIXED_SPMV: 1 if spmv == "fixed" else 0})
+                    options={te.OPT_FIXED_SPMV: spmv_option(spmv)})
     print("ncu case: t=%g, spmv %s, %d Krylov steps, status %d, %d launches"
           % (t_final, spmv, out["n_steps"], out["status"], out["launches"]))
 
@@ -624,9 +638,10 @@ def main():
                          "adjoint: gradients of <n_0(T)> for L=10; zipf: the dim-1e7 load-imbalanced matrix")
     ap.add_argument("--ncu-case", type=float, default=None, metavar="T",
                     help="run one short solve to time T (for ncu captures) and exit")
-    ap.add_argument("--spmv", default="fixed", choices=["fixed", "fp64"],
-                    help="SpMV arithmetic of the Lanczos passes for real H (plain config): exact fixed-point "
-                         "integer products (default) or FP64 FMAs")
+    ap.add_argument("--spmv", default=None, choices=["fixed", "fp64"],
+                    help="SpMV arithmetic of the Lanczos passes: fixed-point integer products or FP64 FMAs; "
+                         "default: the product's default (fixed for the real L=12 matrix, fp64 for the complex "
+                         "Zipf matrix)")
     ap.add_argument("--zipf-n", type=int, default=2_000_000,
                     help="dimension of the Zipf matrix in --ncu-case runs of --config zipf")
     args = ap.parse_args()

@@ -127,12 +127,13 @@ int te_matrix_layout(te_matrix A, int64_t* sell_slots, int64_t* long_rows, int64
  * the summation order of a row (results differ by rounding), so it is made
  * once per matrix.  Setting 1, 2 or 4 pins it. */
 int te_matrix_set_spmv_lanes(te_matrix A, int lanes);
-/* Fixed-point form of a real matrix for TE_OPT_FIXED_SPMV (no counterpart in
- * the reference), built by the first evolver that uses it: *state 0 not built,
- * 1 limbs of every slot value (8 bytes per slot plus the 4-byte column), 2 a
- * value dictionary (one 4-byte word per slot: column and value index; at most
- * 4096 distinct values and 2^(32 - column bits)); *n_values the dictionary
- * size; *scale_shift the sh of round(h 2^sh). */
+/* Fixed-point form of a matrix for TE_OPT_FIXED_SPMV (no counterpart in the
+ * reference), built by the first evolver that uses it: *state 0 not built,
+ * 1 limbs of every slot value (8 bytes per slot for real, 16 for complex
+ * values, plus the 4-byte column), 2 a value dictionary (real matrices: one
+ * 4-byte word per slot, column and value index; at most 4096 distinct values
+ * and 2^(32 - column bits)); *n_values the dictionary size; *scale_shift the
+ * sh of round(h 2^sh). */
 int te_matrix_fixed_layout(te_matrix A, int* state, int* n_values, int* scale_shift);
 /* Current lanes per row (1, 2, 4), tuning first if tune_now != 0 and the
  * choice is still open; a negative value is an error code. */
@@ -298,16 +299,21 @@ int64_t te_evolver_launch_count(te_evolver ev);
  * at dim 6435, equal at dim 92378, slower from dim 352716); 2: always, where
  * a cooperative launch of the matrix's schedule is possible. */
 #define TE_OPT_FUSED_LANCZOS 1
-/* TE_OPT_FIXED_SPMV: the SpMV of the three-term Lanczos passes of a real H in
- * integer arithmetic instead of FP64 FMAs (GB300 issues FP64 at 1/58 of its
- * FP32 rate).  H's values are held as round(h 2^sh) with the largest row
- * 1-norm R below 2^61, each Krylov vector as round(u 2^xs) with a bound U on
- * max|u| below 2^61; a row sum is accumulated in int64 from int32 limb
- * products and rounded to double once.  Error of a row of k entries below
- * (1.25 k 2^-56 + (k + 1) 2^-61) R U + 2^-53 |y|, against FP64's
- * k 2^-53 sum|h||u|.  The recurrence and all reductions stay FP64.
- * 0: FP64 SpMV; 1 (default): fixed-point for real matrices with one lane per
- * row in the per-iteration passes (at least 2048 32-row chunks). */
+/* TE_OPT_FIXED_SPMV: the SpMV of the three-term Lanczos passes in integer
+ * arithmetic instead of FP64 FMAs (GB300 issues FP64 at 1/58 of its FP32
+ * rate).  H's values are held as round(h 2^sh) with the largest row 1-norm R
+ * (complex: of |Re h| + |Im h|) below 2^61, each Krylov vector as
+ * round(u 2^xs) with a bound U on max|u| below 2^61; a row sum is accumulated
+ * in int64 from int32 limb products and rounded to double once.  Error of a
+ * row of k entries below (1.25 k 2^-56 + (k + 1) 2^-61) R U + 2^-53 |y| for
+ * real H, (5 k 2^-56 + (2 k + 1) 2^-61) R U + 2^-53 |y| for complex H, against
+ * FP64's k 2^-53 sum|h||u|.  The recurrence and all reductions stay FP64.
+ * Applies to the per-iteration passes of matrices of at least 2048 32-row
+ * chunks (smaller ones run the persistent FP64 kernel).  0: FP64 SpMV;
+ * 1 (default): fixed point for real H; 2: fixed point for real and complex H.
+ * Complex H stays FP64 by default: on the synthetic dim-1e7 Zipf matrix its
+ * SpMV is bound by the DRAM sectors of the gathered vector, which the integer
+ * format does not shrink (measured: equal time). */
 #define TE_OPT_FIXED_SPMV 2
 int te_evolver_set_option(te_evolver ev, int option, int value);
 

@@ -1,5 +1,5 @@
 """Fixed-point SpMV of the three-term Lanczos passes (te_fixed.cuh; needs a
-GB300).  The SpMV of a real H runs in exact integer arithmetic on values
+GB300).  The SpMV runs in integer arithmetic on values
 quantised at 2^-61 of the largest row 1-norm and of max|u|, with one rounding
 to double per row; the evolution must meet the same bounds against the oracle
 as the FP64 path (same steps, status and samples; states within 2 tol).
@@ -131,22 +131,36 @@ def test_fixed_spmv_long_rows(te_gpu, oracle_lib):
         _bounds(r, ref, 1e-8, 1.0)
 
 
-def test_fixed_spmv_not_for_complex(te_gpu):
-    """A complex H keeps the FP64 passes (same launches with the option on or off)."""
+def test_fixed_spmv_complex(te_gpu, oracle_lib):
+    """A complex Hermitian matrix of 70000 rows (2188 chunks, Gaussian values):
+    FP64 by default; with TE_OPT_FIXED_SPMV = 2 the complex fixed-point SpMV
+    (four limb products per entry) against the FP64 passes and the oracle."""
     rng = np.random.default_rng(8)
     n = 70000
     r = np.repeat(np.arange(n), 3)
     c = rng.integers(0, n, size=3 * n)
     z = rng.standard_normal(3 * n) + 1j * rng.standard_normal(3 * n)
     row, col, val = np.concatenate([r, c]), np.concatenate([c, r]), np.concatenate([z, z.conj()]) / 2
+    key = row * n + col
+    order = np.argsort(key, kind="stable")
+    uk, start = np.unique(key[order], return_index=True)
+    row, col, val = uk // n, uk % n, np.add.reduceat(val[order], start)
     M = te_gpu.Matrix(n, row, col, val)
     assert not M.info()["real"]
-    v = np.zeros(n, dtype=np.complex128)
-    v[0] = 1.0
-    a = _run(te_gpu, M, v, 0.5, 0.25, [], 1, m=20)
-    b = _run(te_gpu, M, v, 0.5, 0.25, [], 0, m=20)
-    assert a["launches"] == b["launches"]
-    assert np.array_equal(a["state"], b["state"])
+    v = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    v /= np.linalg.norm(v)
+    d = (np.arange(n), np.arange(n), rng.uniform(-1, 1, n).astype(np.complex128))
+    c = _run(te_gpu, M, v, 1.0, 0.25, [("sparse", d)], 1, m=30)  # default: complex H stays FP64
+    assert M.fixed_layout()["state"] == 0
+    a = _run(te_gpu, M, v, 1.0, 0.25, [("sparse", d)], 2, m=30)
+    b = _run(te_gpu, M, v, 1.0, 0.25, [("sparse", d)], 0, m=30)
+    assert M.fixed_layout()["state"] == 1
+    assert c["launches"] == b["launches"] and np.array_equal(c["state"], b["state"])
+    assert a["launches"] == b["launches"] + 2 * a["n_steps"]
+    assert a["n_steps"] == b["n_steps"] and a["status"] == b["status"]
+    ref = oracle_lib.evolve((row, col, val), v, 1.0, 0.25, [("sparse", d)], tol=1e-8, m=30)
+    for res in (a, b):
+        _bounds(res, ref, 1e-8, 1.0)
 
 
 def test_fixed_spmv_dictionary_matches_limbs(te_gpu):

@@ -66,7 +66,7 @@ struct te_evolver_s {
   double* results = nullptr;  // n_obs x n_samples
   int max_batch = 1;
   int fused_lanczos = 1;  // TE_OPT_FUSED_LANCZOS: 0 never, 1 automatic, 2 always
-  int fixed_spmv = 1;     // TE_OPT_FIXED_SPMV: 0 FP64 SpMV, 1 fixed-point SpMV where it applies
+  int fixed_spmv = 1;     // TE_OPT_FIXED_SPMV: 0 FP64, 1 fixed point for real H, 2 fixed point for all H
   int4* X = nullptr;      // fixed-point copy of the current Krylov vector (n rows)
   int batch_cap = 0;         // states the batch buffer holds
   size_t results_cap = 0;    // doubles the results buffer holds
@@ -338,10 +338,13 @@ int run(te_evolver ev, te_result* out) {
   int m = ev->m;
   double err_prev = 0.0, t_prev = 0.0;
   int64_t guard = 0;
-  // fixed-point SpMV in the folded three-term passes (te_fixed.cuh): real H,
-  // one lane per row, matrices large enough for the per-iteration passes
-  const bool fix = ev->fixed_spmv != 0 && ev->p.reorth == 0 && ev->p.exp_factor != 0.0 && ev->H->is_real &&
-                   ev->H->sell.lanes == 1 && ev->H->sell.n_chunks >= 2048 && ev->fused_lanczos != 2;
+  // fixed-point SpMV in the folded three-term passes (te_fixed.cuh) for
+  // matrices large enough for the per-iteration passes
+  // (its own schedule, one lane per row); otherwise the FP64 passes, whose
+  // lanes per row are tuned once per matrix on first use
+  const bool fix = (ev->fixed_spmv == 2 || (ev->fixed_spmv == 1 && ev->H->is_real)) && ev->p.reorth == 0 &&
+                   ev->p.exp_factor != 0.0 && ev->H->sell.n_chunks >= 2048 && ev->fused_lanczos != 2;
+  if (!fix && (rc = te_tune_sell_lanes(ev->H)) != TE_OK) return rc;
   if (fix) {
     if ((rc = te_sell_build_fixed(ev->H)) != TE_OK) return rc;
     if (!ev->X) TE_CUDA(cudaMalloc(&ev->X, sizeof(int4) * n * ev->m));  // X_0 .. X_{m-1}
@@ -557,8 +560,6 @@ extern "C" int te_evolver_create(te_matrix H, const double* v_host, const te_par
     return TE_ERR_UNSUPPORTED;
   }
   int rc = te_upload_quad_tables();
-  if (rc != TE_OK) return rc;
-  rc = te_tune_sell_lanes(H);  // once per matrix (lanes per row of the SpMV passes)
   if (rc != TE_OK) return rc;
   te_evolver ev = new te_evolver_s();
   ev->H = H;
@@ -831,8 +832,8 @@ extern "C" int te_evolver_set_option(te_evolver ev, int option, int value) {
       ev->fused_lanczos = value;
       return TE_OK;
     case TE_OPT_FIXED_SPMV:
-      if (value < 0 || value > 1) {
-        te_set_error("te_evolver_set_option: TE_OPT_FIXED_SPMV takes 0 or 1");
+      if (value < 0 || value > 2) {
+        te_set_error("te_evolver_set_option: TE_OPT_FIXED_SPMV takes 0, 1 or 2");
         return TE_ERR_INVALID_ARG;
       }
       ev->fixed_spmv = value;

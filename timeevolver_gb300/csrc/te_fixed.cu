@@ -1,8 +1,8 @@
-// te_fixed.cu -- the fixed-point data of a real SELL matrix (te_fixed.cuh):
-// the scale of its values, either a value dictionary with packed slots or the
-// limbs of every slot value, and the static schedule of the fixed-point apply
-// kernel.  Built once per matrix on first use; rebuilt when the values change
-// in place (te_sell_refresh_fixed).
+// te_fixed.cu -- the fixed-point data of a SELL matrix (te_fixed.cuh): the
+// scale of its values; a value dictionary with packed slots (real matrices
+// with few distinct values) or the limbs of every slot value; and the static
+// schedule of the fixed-point apply kernel.  Built once per matrix on first
+// use; rebuilt when the values change in place (te_sell_refresh_fixed).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -13,7 +13,9 @@
 
 namespace {
 
-// Largest chunk-row 1-norm, as the bit pattern of a non-negative double.
+// Largest chunk-row 1-norm (complex: sum of |Re| + |Im|), as the bit pattern
+// of a non-negative double.
+template <bool REAL>
 __global__ void __launch_bounds__(TE_THREADS) fix_rownorm_kernel(int64_t n_chunks, const int64_t* __restrict__ off,
                                                                  const double* __restrict__ val,
                                                                  unsigned long long* max_bits) {
@@ -21,7 +23,8 @@ __global__ void __launch_bounds__(TE_THREADS) fix_rownorm_kernel(int64_t n_chunk
   const int64_t c = t >> 5;
   if (c >= n_chunks) return;  // whole warps
   double s = 0.0;
-  for (int64_t q = off[c] + (t & 31); q < off[c + 1]; q += 32) s += fabs(val[q]);
+  for (int64_t q = off[c] + (t & 31); q < off[c + 1]; q += 32)
+    s += REAL ? fabs(val[q]) : fabs(val[2 * q]) + fabs(val[2 * q + 1]);
   for (int o = 16; o > 0; o >>= 1) s = fmax(s, __shfl_xor_sync(0xffffffffu, s, o));
   if ((t & 31) == 0) atomicMax(max_bits, (unsigned long long)__double_as_longlong(s));
 }
@@ -30,6 +33,16 @@ __global__ void __launch_bounds__(TE_THREADS) fix_encode_values_kernel(int64_t c
                                                                        int2* __restrict__ out, int sh) {
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < count; q += (int64_t)gridDim.x * blockDim.x)
     out[q] = te_fix_split(te_fix_encode(val[q], sh));
+}
+
+__global__ void __launch_bounds__(TE_THREADS) fix_encode_complex_kernel(int64_t count,
+                                                                        const double2* __restrict__ val,
+                                                                        int4* __restrict__ out, int sh) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < count; q += (int64_t)gridDim.x * blockDim.x) {
+    const double2 v = val[q];
+    const int2 re = te_fix_split(te_fix_encode(v.x, sh)), im = te_fix_split(te_fix_encode(v.y, sh));
+    out[q] = make_int4(re.x, re.y, im.x, im.y);
+  }
 }
 
 // Value dictionary: open addressing over the bit patterns of the slot values
@@ -104,6 +117,7 @@ void free_ptr(T*& p) {
 
 void free_fixed(TeSell& S) {
   free_ptr(S.fix_val);
+  free_ptr(S.fix_val4);
   free_ptr(S.fix_warp_chunk);
   free_ptr(S.fix_pk);
   free_ptr(S.fix_table);
@@ -112,14 +126,14 @@ void free_fixed(TeSell& S) {
 }
 
 // sh: the largest chunk-row 1-norm maps below 2^61.
-int fixed_scale(TeSell& S) {
+int fixed_scale(TeSell& S, bool real) {
   unsigned long long* d_max = nullptr;
   TE_CUDA(cudaMalloc(&d_max, sizeof(unsigned long long)));
   int rc = te_cuda_check(cudaMemset(d_max, 0, sizeof(unsigned long long)), "fixed values");
   const int64_t threads = S.n_chunks * 32;
-  if (rc == TE_OK)
-    fix_rownorm_kernel<<<(unsigned)((threads + TE_THREADS - 1) / TE_THREADS), TE_THREADS>>>(S.n_chunks, S.chunk_off,
-                                                                                             S.val, d_max);
+  const unsigned blocks = (unsigned)((threads + TE_THREADS - 1) / TE_THREADS);
+  if (rc == TE_OK && real) fix_rownorm_kernel<true><<<blocks, TE_THREADS>>>(S.n_chunks, S.chunk_off, S.val, d_max);
+  if (rc == TE_OK && !real) fix_rownorm_kernel<false><<<blocks, TE_THREADS>>>(S.n_chunks, S.chunk_off, S.val, d_max);
   unsigned long long bits = 0;
   if (rc == TE_OK) rc = te_cuda_check(cudaMemcpy(&bits, d_max, sizeof(bits), cudaMemcpyDeviceToHost), "fixed values");
   cudaFree(d_max);
@@ -223,12 +237,21 @@ int try_dictionary(TeSell& S, bool* packed) {
 }
 
 // Values (dictionary or limbs) at the current sh.
-int fixed_values(TeSell& S) {
+int fixed_values(TeSell& S, bool real) {
   int rc;
-  if ((rc = fixed_scale(S)) != TE_OK) return rc;
+  if ((rc = fixed_scale(S, real)) != TE_OK) return rc;
   free_ptr(S.fix_pk);
   free_ptr(S.fix_table);
   S.fix_nvals = 0;
+  if (!real) {  // complex: limbs of both parts per slot (no dictionary)
+    if (!S.fix_val4 &&
+        (rc = te_cuda_check(cudaMalloc(&S.fix_val4, sizeof(int4) * std::max<int64_t>(S.slots, 1)),
+                            "fixed values")) != TE_OK)
+      return rc;
+    fix_encode_complex_kernel<<<te_grid_fit((const void*)fix_encode_complex_kernel, S.slots, TE_THREADS),
+                                TE_THREADS>>>(S.slots, reinterpret_cast<const double2*>(S.val), S.fix_val4, S.fix_sh);
+    return te_cuda_check(cudaDeviceSynchronize(), "fixed values");
+  }
   bool packed = false;
   if ((rc = try_dictionary(S, &packed)) != TE_OK) return rc;
   if (packed) {
@@ -245,14 +268,14 @@ int fixed_values(TeSell& S) {
 }
 
 // The static schedule of the fixed-point apply kernel for the current layout.
-int fixed_schedule(TeSell& S) {
+int fixed_schedule(TeSell& S, bool real) {
   std::vector<int64_t> off(S.n_chunks + 1);
   int rc = te_cuda_check(cudaMemcpy(off.data(), S.chunk_off, sizeof(int64_t) * off.size(), cudaMemcpyDeviceToHost),
                          "fixed schedule");
   if (rc != TE_OK) return rc;
-  const int bps = te_apply_fix_blocks_per_sm(S.fix_pk != nullptr, sizeof(int2) * S.fix_nvals);
+  const int bps = te_apply_fix_blocks_per_sm(real ? (S.fix_pk ? 1 : 0) : 2, sizeof(int2) * S.fix_nvals);
   std::vector<int32_t> wc;
-  te_sell_schedule(off, S.n_chunks, bps, true, S.fix_grid, S.fix_saturated, wc);
+  te_sell_schedule(off, S.n_chunks, bps, real, S.fix_grid, S.fix_saturated, wc);
   int32_t* d_wc = nullptr;
   if ((rc = te_cuda_check(cudaMalloc(&d_wc, sizeof(int32_t) * wc.size()), "fixed schedule")) != TE_OK) return rc;
   rc = te_cuda_check(cudaMemcpy(d_wc, wc.data(), sizeof(int32_t) * wc.size(), cudaMemcpyHostToDevice),
@@ -271,12 +294,12 @@ int fixed_schedule(TeSell& S) {
 int te_sell_build_fixed(te_matrix_s* A) {
   TeSell& S = A->sell;
   if (S.fix_warp_chunk) return TE_OK;
-  if (!A->is_real || S.lanes != 1 || S.n_chunks < 1) {
-    te_set_error("fixed-point SpMV needs a real matrix with one lane per row");
+  if (S.n_chunks < 1) {
+    te_set_error("fixed-point SpMV: empty matrix");
     return TE_ERR_INVALID_ARG;
   }
-  int rc = fixed_values(S);
-  if (rc == TE_OK) rc = fixed_schedule(S);
+  int rc = fixed_values(S, A->is_real);
+  if (rc == TE_OK) rc = fixed_schedule(S, A->is_real);
   if (rc != TE_OK) free_fixed(S);
   return rc;
 }
@@ -286,9 +309,9 @@ int te_sell_refresh_fixed(te_matrix_s* A) {
   if (!S.fix_warp_chunk) return TE_OK;
   const bool was_packed = S.fix_pk != nullptr;
   const int nv = S.fix_nvals;
-  int rc = fixed_values(S);
+  int rc = fixed_values(S, A->is_real);
   // the schedule depends on the occupancy, which depends on the table size
-  if (rc == TE_OK && (was_packed != (S.fix_pk != nullptr) || nv != S.fix_nvals)) rc = fixed_schedule(S);
+  if (rc == TE_OK && (was_packed != (S.fix_pk != nullptr) || nv != S.fix_nvals)) rc = fixed_schedule(S, A->is_real);
   if (rc != TE_OK) free_fixed(S);
   return rc;
 }

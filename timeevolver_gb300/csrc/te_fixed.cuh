@@ -99,6 +99,16 @@ __device__ __forceinline__ int te_fix_scale(double bound) {
 #endif
 constexpr int kTeFixUnroll = TE_FIX_UNROLL;  // slots per lane in flight
 
+// hi-part product of two limb-split values c = c1 2^31 + c0, x = x1 2^31 + x0
+// in units of 2^62: c1 x1 + 2 (hi32(c1 x0) + hi32(c0 x1)), below c x / 2^62 by
+// less than 5.
+__device__ __forceinline__ int64_t te_fix_prod(int c0, int c1, int x0, int x1) {
+  int t;
+  asm("mul.hi.s32 %0, %1, %2;" : "=r"(t) : "r"(c1), "r"(x0));
+  asm("mad.hi.s32 %0, %1, %2, %0;" : "+r"(t) : "r"(c0), "r"(x1));
+  return (int64_t)c1 * x1 + 2 * (int64_t)t;
+}
+
 // One slot: S += h~ X (see te_sell_row_fix).
 __device__ __forceinline__ void te_fix_mac(const int2 h, const int4 x, int64_t& sr, int64_t& si) {
   int tr, ti;
@@ -140,6 +150,25 @@ __device__ __forceinline__ double2 te_sell_row_fix_packed(int64_t s, int64_t e, 
   for (; s < e; s += 32) {
     const uint32_t wd = __ldcs(pk + s);
     te_fix_mac(tab[wd >> cbits], __ldg(X + (wd & cmask)), sr, si);
+  }
+  return make_double2(te_i64_to_double(sr, 62 - shift), te_i64_to_double(si, 62 - shift));
+}
+
+// Complex H: slot value {Re h~ limbs, Im h~ limbs} as int4; R is then the
+// largest row sum of |Re h| + |Im h|.  Four limb products per slot
+// (Re = hr xr - hi xi, Im = hr xi + hi xr), so the per-slot term of the
+// error bound is four times the real one: below (5 k 2^-56 + (2 k + 1) 2^-61)
+// R U + 2^-53 |y|.
+__device__ __forceinline__ double2 te_sell_row_fix_c(int64_t s, int64_t e, const int32_t* __restrict__ col,
+                                                     const int4* __restrict__ hv, const int4* __restrict__ X,
+                                                     int shift) {
+  int64_t sr = 0, si = 0;
+#pragma unroll(kTeFixUnroll)
+  for (; s < e; s += 32) {
+    const int4 h = __ldcs(hv + s);
+    const int4 x = __ldg(X + __ldcs(col + s));
+    sr += te_fix_prod(h.x, h.y, x.x, x.y) - te_fix_prod(h.z, h.w, x.z, x.w);
+    si += te_fix_prod(h.x, h.y, x.z, x.w) + te_fix_prod(h.z, h.w, x.x, x.y);
   }
   return make_double2(te_i64_to_double(sr, 62 - shift), te_i64_to_double(si, 62 - shift));
 }

@@ -128,11 +128,12 @@ struct TeSell {
   int64_t* long_ptr = nullptr;  // n_long + 1
   int32_t* long_col = nullptr;  // sorted-basis columns
   double* long_val = nullptr;   // real: 1, complex: 2 doubles per entry
-  // Fixed-point copy of the chunk values of a real matrix (te_fixed.cuh):
+  // Fixed-point copy of the chunk values (te_fixed.cuh):
   // slot value round(h 2^fix_sh) as int32 limbs {h0, h1}, built on first use
   // by te_sell_build_fixed, with its own static schedule for the fixed-point
   // apply kernel (whose resident blocks per SM differ).
   int2* fix_val = nullptr;
+  int4* fix_val4 = nullptr;  // complex matrices: {Re limbs, Im limbs} per slot
   int fix_sh = 0;
   int32_t* fix_warp_chunk = nullptr;
   int fix_grid = 0;
@@ -256,7 +257,8 @@ void te_launch_lanczos_update(int64_t n, const double2* w, const double2* u_j, d
 // start of a Krylov step; the apply pass reads the fixed-point copy X of u_j.
 int te_sell_build_fixed(te_matrix_s* A);
 // Resident blocks per SM of the fixed-point apply kernel (te_lanczos.cu).
-int te_apply_fix_blocks_per_sm(bool packed, size_t dyn_smem);
+// fmt: 0 real limbs, 1 real value dictionary, 2 complex limbs.
+int te_apply_fix_blocks_per_sm(int fmt, size_t dyn_smem);
 // Re-encode the fixed-point values after H's SELL values changed in place.
 int te_sell_refresh_fixed(te_matrix_s* A);
 void te_launch_fix_start(int64_t n, const double2* u_0, int4* X, TeDevState* ds, double* partials, cudaStream_t st);

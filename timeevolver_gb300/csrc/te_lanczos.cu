@@ -160,17 +160,19 @@ __device__ __forceinline__ unsigned int te_block_max_from_smem(const unsigned in
 #ifndef TE_FIX_MIN_BLOCKS
 #define TE_FIX_MIN_BLOCKS 6
 #endif
-// The matrix side of the fixed-point apply: limbs per slot (col, hv) or packed
-// slots with a value table (pk, table, nvals, cbits; PACKED).
+// The matrix side of the fixed-point apply, by format FMT: 0 real limbs per
+// slot (col, hv), 1 real packed slots with a value table (pk, table, nvals,
+// cbits), 2 complex limbs per slot (col, hv4).
 struct TeFixMatrix {
   const int32_t* col;
   const int2* hv;
+  const int4* hv4;
   const uint32_t* pk;
   const int2* table;
   int nvals, cbits, sh;
 };
 
-template <bool HAS_PREV, bool PACKED>
+template <bool HAS_PREV, int FMT>
 __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_fix_kernel(
     int64_t n, const int32_t* __restrict__ warp_chunk, const int64_t* __restrict__ chunk_off, TeFixMatrix M,
     TeLongRows L, const int4* __restrict__ X, const double2* __restrict__ u_j, const double2* __restrict__ u_jm1,
@@ -178,8 +180,8 @@ __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_f
   __shared__ double scratch[2 * 32];
   __shared__ double wide[2 * TE_THREADS];
   __shared__ unsigned int wmax_w[TE_THREADS / 32];
-  extern __shared__ int2 tab[];  // PACKED: the value table (constant across launches)
-  if (PACKED) {
+  extern __shared__ int2 tab[];  // FMT 1: the value table (constant across launches)
+  if (FMT == 1) {
     for (int i = threadIdx.x; i < M.nvals; i += blockDim.x) tab[i] = M.table[i];
     __syncthreads();
   }
@@ -201,7 +203,7 @@ __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_f
   const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t lr = wid; lr < L.n; lr += warps) {
-    const double2 y = te_long_row<true>(L, lr, u_j, lane);
+    const double2 y = te_long_row<FMT != 2>(L, lr, u_j, lane);
     if (lane == 0) {
       const double2 wr = apply_row_epilogue<HAS_PREV, true>(lr, y, g, cw, u_j, u_jm1, w, acc);
       wmax = max(wmax, max(te_fix_hiword(wr.x), te_fix_hiword(wr.y)));
@@ -224,8 +226,9 @@ __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_f
     }
     const int64_t r = c * 32 + lane;
     const bool live = r < n && r >= L.n;
-    const double2 y = PACKED ? te_sell_row_fix_packed(s0 + lane, s1, M.pk, tab, M.cbits, X, shift)
-                             : te_sell_row_fix(s0 + lane, s1, M.col, M.hv, X, shift);
+    const double2 y = FMT == 1   ? te_sell_row_fix_packed(s0 + lane, s1, M.pk, tab, M.cbits, X, shift)
+                      : FMT == 2 ? te_sell_row_fix_c(s0 + lane, s1, M.col, M.hv4, X, shift)
+                                 : te_sell_row_fix(s0 + lane, s1, M.col, M.hv, X, shift);
     if (live) {
       const double2 wr = apply_row_epilogue<HAS_PREV, true>(r, y, g, cw, u_j, u_jm1, w, acc);
       wmax = max(wmax, max(te_fix_hiword(wr.x), te_fix_hiword(wr.y)));
@@ -814,8 +817,9 @@ void te_launch_lanczos_apply(const TeSell& A, bool is_real, const double2* u_j, 
                 A.col, A.val, te_long_rows(A), u_j, u_jm1, w, ds, partials, j);
 }
 
-// Autotuning of the lanes per row (complex matrices): time the three-term
-// apply pass (the dominant kernel) for K = 1, 2, 4 on the matrix itself, with scratch vectors
+// Autotuning of the lanes per row of the FP64 passes (the fixed-point passes
+// always use one lane per row): time the three-term apply pass (the dominant
+// kernel) for K = 1, 2, 4 on the matrix itself, with scratch vectors
 // and a scratch state, and keep K > 1 only when it is clearly (> 10%) faster,
 // so that the choice -- which changes the rounding of the row sums -- is
 // stable from run to run.  Matrices that give every resident warp at least 8
@@ -826,10 +830,7 @@ int te_tune_sell_lanes(te_matrix_s* A) {
   if (S.lanes_fixed) return TE_OK;
   const int64_t resident_warps = (int64_t)te_num_sms() * te_sell_blocks_per_sm(A->is_real) * (TE_THREADS / 32);
   S.lanes = 1;
-  // real matrices keep K = 1 for the fixed-point SpMV (the default for them,
-  // which needs one lane per row and beats the FP64 K = 1 pass by more than
-  // K > 1 ever did: 28% at L=12 against at most 8% for K = 2 at L=10)
-  if (S.n_chunks >= 8 * resident_warps || S.n_chunks < 2048 || S.n_long > 0 || A->is_real) {
+  if (S.n_chunks >= 8 * resident_warps || S.n_chunks < 2048 || S.n_long > 0) {
     S.lanes_fixed = true;
     return TE_OK;
   }
@@ -914,24 +915,33 @@ void te_launch_fix_start(int64_t n, const double2* u_0, int4* X, TeDevState* ds,
   fix_start_encode_kernel<<<g2, TE_THREADS, 0, st>>>(n, u_0, X, ds, bmax, g1);
 }
 
-int te_apply_fix_blocks_per_sm(bool packed, size_t dyn_smem) {
-  const void* k[2] = {packed ? (const void*)lanczos_apply_fix_kernel<true, true>
-                             : (const void*)lanczos_apply_fix_kernel<true, false>,
-                      packed ? (const void*)lanczos_apply_fix_kernel<false, true>
-                             : (const void*)lanczos_apply_fix_kernel<false, false>};
-  return std::min(te_kernel_blocks_per_sm(k[0], TE_THREADS, dyn_smem),
-                  te_kernel_blocks_per_sm(k[1], TE_THREADS, dyn_smem));
+namespace {
+
+using ApplyFixKernel = void (*)(int64_t, const int32_t*, const int64_t*, TeFixMatrix, TeLongRows, const int4*,
+                                const double2*, const double2*, double2*, TeDevState*, double*, int);
+
+ApplyFixKernel apply_fix_kernel(int fmt, bool has_prev) {
+  static const ApplyFixKernel table[3][2] = {
+      {lanczos_apply_fix_kernel<false, 0>, lanczos_apply_fix_kernel<true, 0>},
+      {lanczos_apply_fix_kernel<false, 1>, lanczos_apply_fix_kernel<true, 1>},
+      {lanczos_apply_fix_kernel<false, 2>, lanczos_apply_fix_kernel<true, 2>}};
+  return table[fmt][has_prev ? 1 : 0];
+}
+
+}  // namespace
+
+int te_apply_fix_blocks_per_sm(int fmt, size_t dyn_smem) {
+  return std::min(te_kernel_blocks_per_sm((const void*)apply_fix_kernel(fmt, true), TE_THREADS, dyn_smem),
+                  te_kernel_blocks_per_sm((const void*)apply_fix_kernel(fmt, false), TE_THREADS, dyn_smem));
 }
 
 void te_launch_lanczos_apply_fix(const TeSell& A, const int4* X, const double2* u_j, const double2* u_jm1,
                                  double2* w, TeDevState* ds, double* partials, int j, cudaStream_t st) {
-  const bool packed = A.fix_pk != nullptr;
-  const TeFixMatrix M{A.col, A.fix_val, A.fix_pk, A.fix_table, A.fix_nvals, A.fix_cbits, A.fix_sh};
-  const size_t smem = packed ? sizeof(int2) * A.fix_nvals : 0;
-  auto k = packed ? (u_jm1 ? lanczos_apply_fix_kernel<true, true> : lanczos_apply_fix_kernel<false, true>)
-                  : (u_jm1 ? lanczos_apply_fix_kernel<true, false> : lanczos_apply_fix_kernel<false, false>);
-  te_launch_pdl_smem(A.fix_saturated, k, A.fix_grid, TE_THREADS, smem, st, A.n, A.fix_warp_chunk, A.chunk_off, M,
-                     te_long_rows(A), X, u_j, u_jm1, w, ds, partials, j);
+  const int fmt = A.fix_val4 ? 2 : (A.fix_pk ? 1 : 0);
+  const TeFixMatrix M{A.col, A.fix_val, A.fix_val4, A.fix_pk, A.fix_table, A.fix_nvals, A.fix_cbits, A.fix_sh};
+  const size_t smem = fmt == 1 ? sizeof(int2) * A.fix_nvals : 0;
+  te_launch_pdl_smem(A.fix_saturated, apply_fix_kernel(fmt, u_jm1 != nullptr), A.fix_grid, TE_THREADS, smem, st, A.n,
+                     A.fix_warp_chunk, A.chunk_off, M, te_long_rows(A), X, u_j, u_jm1, w, ds, partials, j);
 }
 
 

@@ -292,6 +292,7 @@ void free_matrix(te_matrix_s* M) {
   cudaFree(M->sell.long_col);
   cudaFree(M->sell.long_val);
   cudaFree(M->sell.fix_val);
+  cudaFree(M->sell.fix_val4);
   cudaFree(M->sell.fix_warp_chunk);
   cudaFree(M->sell.fix_pk);
   cudaFree(M->sell.fix_table);

@@ -58,13 +58,6 @@ __device__ __forceinline__ void combine_rows(const TeCombineArgs& a, const doubl
 // 2^61, psi_o = 2^(62 - sc_o) sum_j C_oj X_j with the limb products of
 // te_fix_mac (complex: Re = Cr Xr - Ci Xi, Im = Cr Xi + Ci Xr).  Error per
 // component below 4 m 1.25 2^-56 + (m + 1) 2^-61 of sum_j |Y_oj| max|u_j|.
-__device__ __forceinline__ int64_t te_fix_prod(int c0, int c1, int x0, int x1) {
-  int t;
-  asm("mul.hi.s32 %0, %1, %2;" : "=r"(t) : "r"(c1), "r"(x0));
-  asm("mad.hi.s32 %0, %1, %2, %0;" : "+r"(t) : "r"(c0), "r"(x1));
-  return (int64_t)c1 * x1 + 2 * (int64_t)t;
-}
-
 template <int G>
 __device__ __forceinline__ void combine_rows_fix(const TeCombineArgs& a, int m, const int4 (*C)[TE_MMAX],
                                                  const int* sc, const int* slot_s, int S, double2* last_out,

@@ -114,3 +114,29 @@ def test_long_rows_layout_and_evolution(te_gpu, oracle_lib, n, complex_values):
     assert gpu["status"] == ref["status"] and gpu["n_steps"] == ref["n_steps"]
     assert np.linalg.norm(gpu["state"] - ref["state"]) < 2e-8
     assert np.max(np.abs(gpu["samples"] - ref["samples"])) < 4e-8
+
+
+def test_norm1_device_path_bit_identical(te_gpu):
+    """The reference's 1-norm (entry-order column sums) for a row-sorted COO
+    of 967 537 entries: computed on the device for a real matrix with
+    symmetric |H| (rows sorted, every entry mirrored), on host threads once
+    one entry breaks the symmetry -- bit-identical to the sequential sums
+    either way."""
+    from oracle import models
+    states, H = models.bose_hubbard(10, 10, 1.0, 2.0)
+    n = len(states)
+    row, col = np.asarray(H[0], np.int64), np.asarray(H[1], np.int64)
+    val = np.asarray(H[2], np.complex128)
+
+    def seq_norm1(c, v):
+        s = np.zeros(n)
+        np.add.at(s, c, np.abs(v))  # sequential in entry order
+        return s.max()
+
+    M = te_gpu.Matrix(n, row, col, val)
+    assert M.info()["norm1"] == seq_norm1(col, val)
+    asym = val.copy()
+    k = int(np.nonzero(row != col)[0][12345])
+    asym[k] *= 1.0 + 2.0 ** -40  # (r, c) no longer mirrors (c, r)
+    Ma = te_gpu.Matrix(n, row, col, asym)
+    assert Ma.info()["norm1"] == seq_norm1(col, asym)

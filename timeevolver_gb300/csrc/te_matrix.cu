@@ -12,9 +12,11 @@
 // all 32 lanes busy: rows are sorted by length, a warp owns 32 rows of equal
 // length, and a real-valued matrix stores real values.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <complex>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <numeric>
 #include <thread>
@@ -248,6 +250,43 @@ __global__ void row_count_kernel(int64_t nnz, const uint64_t* __restrict__ row, 
 __global__ void narrow_index_kernel(int64_t nnz, const uint64_t* __restrict__ in, int32_t* __restrict__ out) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nnz; i += (int64_t)gridDim.x * blockDim.x)
     out[i] = (int32_t)in[i];
+}
+
+// The reference's 1-norm on the device, for real matrices whose |H| is
+// symmetric: with every row sorted by column (no duplicates) and every entry
+// (r, c) mirrored by (c, r) of the same modulus, column c's entries in row
+// order have exactly the moduli of row c in column order, so each row's
+// sequential sum equals the entry-order column sum of the row-sorted COO input
+// bit for bit.  One thread per row checks the conditions (binary search for
+// the mirror entry); flags: 1 a complex value, 2 a row not strictly sorted,
+// 4 a missing or different mirror.  The maximum goes to *max_bits.
+__global__ void __launch_bounds__(TE_THREADS) mirror_norm1_kernel(int64_t n, const int32_t* __restrict__ rp,
+                                                                  const int32_t* __restrict__ ci,
+                                                                  const double2* __restrict__ v,
+                                                                  unsigned int* flags, unsigned long long* max_bits) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    int32_t prev = -1;
+    unsigned int f = 0;
+    for (int32_t k = rp[r]; k < rp[r + 1]; ++k) {
+      const int32_t c = ci[k];
+      const double2 a = v[k];
+      if (a.y != 0.0) f |= 1u;
+      if (c <= prev) f |= 2u;
+      prev = c;
+      const double m = fabs(a.x);
+      s += m;
+      int32_t lo = rp[c], hi = rp[c + 1];  // the mirror (c, r) by bisection
+      while (lo < hi) {
+        const int32_t mid = lo + (hi - lo) / 2;
+        if (ci[mid] < (int32_t)r) lo = mid + 1;
+        else hi = mid;
+      }
+      if (lo >= rp[c + 1] || ci[lo] != (int32_t)r || fabs(v[lo].x) != m) f |= 4u;
+    }
+    if (f) atomicOr(flags, f);
+    atomicMax(max_bits, (unsigned long long)__double_as_longlong(s));
+  }
 }
 
 // ------------------------------------------------------------ host build
@@ -645,21 +684,29 @@ namespace {
 // The reference's 1-norm (matrixDataTypes.cpp:67-79): column sums of |a| in the
 // order of the COO entries.  Threads own disjoint column ranges and each scans
 // all entries, so every column is summed in exactly that order.  Entries with
-// an out-of-range column are skipped (the caller rejects them).
-double coo_norm1(int64_t n_cols, int64_t nnz, const uint64_t* col, const double* val) {
-  const int T = (int)std::max<unsigned>(1u, std::min<unsigned>(8u, std::thread::hardware_concurrency()));
+// an out-of-range column are skipped (the caller rejects them).  |re + i 0| is
+// exactly |re| (hypot(x, +-0) = |x|), so real entries skip hypot.
+// A set cancel flag (checked every 2^16 entries) abandons the sums (NaN).
+double coo_norm1(int64_t n_cols, int64_t nnz, const uint64_t* col, const double* val,
+                 const std::atomic<bool>* cancel = nullptr) {
+  const int T = (int)std::max<unsigned>(1u, std::min<unsigned>(16u, std::thread::hardware_concurrency()));
   std::vector<double> colsum(n_cols, 0.0);
   auto work = [&](int t) {
     const uint64_t c0 = (uint64_t)(n_cols * t / T), c1 = (uint64_t)(n_cols * (t + 1) / T);
     for (int64_t i = 0; i < nnz; ++i) {
+      if (cancel && (i & 0xffff) == 0 && cancel->load(std::memory_order_relaxed)) return;
       const uint64_t c = col[i];
-      if (c >= c0 && c < c1) colsum[c] += std::abs(std::complex<double>(val[2 * i], val[2 * i + 1]));
+      if (c >= c0 && c < c1) {
+        const double re = val[2 * i], im = val[2 * i + 1];
+        colsum[c] += im == 0.0 ? std::fabs(re) : std::abs(std::complex<double>(re, im));
+      }
     }
   };
   std::vector<std::thread> pool;
   for (int t = 1; t < T; ++t) pool.emplace_back(work, t);
   work(0);
   for (auto& th : pool) th.join();
+  if (cancel && cancel->load()) return std::nan("");
   return n_cols > 0 ? *std::max_element(colsum.begin(), colsum.end()) : 0.0;
 }
 
@@ -690,7 +737,8 @@ int create_coo_host(int64_t n_rows, int64_t n_cols, int64_t nnz, const uint64_t*
 // from per-row counts, and the layout is built by kernels.  Returns
 // TE_ERR_UNSUPPORTED (nothing built, no error set) for unsorted input.
 int create_coo_device(int64_t n_rows, int64_t n_cols, int64_t nnz, const uint64_t* row_index, const uint64_t* columns,
-                      const double* values, double norm1, te_matrix* out) {
+                      const double* values, double* norm1_gpu, te_matrix* out) {
+  *norm1_gpu = std::nan("");
   uint64_t *d_row = nullptr, *d_col = nullptr;
   double2* d_v = nullptr;
   int32_t *d_cnt = nullptr, *d_rp = nullptr, *d_ci = nullptr;
@@ -751,9 +799,22 @@ int create_coo_device(int64_t n_rows, int64_t n_cols, int64_t nnz, const uint64_
     return fail(TE_ERR_CUDA);
   narrow_index_kernel<<<te_grid_fit((const void*)narrow_index_kernel, nnz, TE_THREADS), TE_THREADS>>>(nnz, d_col,
                                                                                                    d_ci);
+  if (n_rows == n_cols) {  // the reference's 1-norm on the device where |H| is symmetric and real
+    if (te_cuda_check(cudaMemset(d_flags, 0, sizeof(unsigned int)), "coo") != TE_OK ||
+        te_cuda_check(cudaMemset(d_bad, 0, sizeof(unsigned long long)), "coo") != TE_OK)
+      return fail(TE_ERR_CUDA);
+    mirror_norm1_kernel<<<te_grid_fit((const void*)mirror_norm1_kernel, n_rows, TE_THREADS), TE_THREADS>>>(
+        n_rows, d_rp, d_ci, d_v, d_flags, d_bad);
+    unsigned int mflags = 0;
+    unsigned long long mbits = 0;
+    if (te_cuda_check(cudaMemcpy(&mflags, d_flags, sizeof(mflags), cudaMemcpyDeviceToHost), "coo") != TE_OK ||
+        te_cuda_check(cudaMemcpy(&mbits, d_bad, sizeof(mbits), cudaMemcpyDeviceToHost), "coo") != TE_OK)
+      return fail(TE_ERR_CUDA);
+    if (mflags == 0) std::memcpy(norm1_gpu, &mbits, sizeof(double));
+  }
   if (te_cuda_check(cudaDeviceSynchronize(), "coo") != TE_OK) return fail(TE_ERR_CUDA);
   release();
-  return te_matrix_adopt_device_csr(n_rows, n_cols, rp, d_rp, d_ci, d_v, out, norm1);
+  return te_matrix_adopt_device_csr(n_rows, n_cols, rp, d_rp, d_ci, d_v, out, 0.0);
 }
 
 // Below this many entries the host conversion is as fast as the device one.
@@ -774,13 +835,17 @@ extern "C" int te_matrix_create_coo(int64_t n_rows, int64_t n_cols, int64_t nnz,
   if (nnz < kDeviceCooMinEntries)
     return create_coo_host(n_rows, n_cols, nnz, row_index, columns, values, coo_norm1(n_cols, nnz, columns, values),
                            out);
-  // the 1-norm on host threads while the device converts the layout
-  double norm1 = 0.0;
-  std::thread norm_thread([&]() { norm1 = coo_norm1(n_cols, nnz, columns, values); });
-  int rc = create_coo_device(n_rows, n_cols, nnz, row_index, columns, values, 0.0, out);
+  // the 1-norm on host threads while the device converts the layout; the
+  // device computes it itself where |H| is real and symmetric (then the host
+  // threads are called off)
+  double norm1 = 0.0, norm1_gpu = std::nan("");
+  std::atomic<bool> cancel(false);
+  std::thread norm_thread([&]() { norm1 = coo_norm1(n_cols, nnz, columns, values, &cancel); });
+  int rc = create_coo_device(n_rows, n_cols, nnz, row_index, columns, values, &norm1_gpu, out);
+  if (rc == TE_OK && !std::isnan(norm1_gpu)) cancel.store(true);
   norm_thread.join();
   if (rc == TE_OK) {
-    (*out)->norm1 = norm1;
+    (*out)->norm1 = std::isnan(norm1_gpu) ? norm1 : norm1_gpu;
     return TE_OK;
   }
   if (rc != TE_ERR_UNSUPPORTED) return rc;

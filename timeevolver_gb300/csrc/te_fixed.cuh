@@ -69,6 +69,34 @@ __device__ __forceinline__ double te_i64_to_double(int64_t v, int e2) {
   return __longlong_as_double((long long)(sign | ((uint64_t)(ex + 1023) << 52) | (mant & 0xfffffffffffffull)));
 }
 
+// (hi:lo) 2^e2 for an unsigned 128-bit value, rounded to the nearest double
+// (ties to even), integers only; results below the normal range flush to zero.
+__device__ __forceinline__ double te_u128_to_double(unsigned long long hi, unsigned long long lo, int e2) {
+  if ((hi | lo) == 0ull) return 0.0;
+  const int lz = hi ? __clzll((long long)hi) : 64 + __clzll((long long)lo);
+  uint64_t top, rest;
+  if (lz >= 64) {
+    top = lo << (lz - 64);
+    rest = 0;
+  } else if (lz == 0) {
+    top = hi;
+    rest = lo;
+  } else {
+    top = (hi << lz) | (lo >> (64 - lz));
+    rest = lo << lz;
+  }
+  uint64_t mant = top >> 11;
+  const uint64_t rb = top & 0x7ffull;
+  mant += (rb > 0x400ull || (rb == 0x400ull && (rest != 0ull || (mant & 1ull)))) ? 1ull : 0ull;
+  int ex = 127 - lz + e2;
+  if (mant >> 53) {
+    mant >>= 1;
+    ++ex;
+  }
+  if (ex < -1022) return 0.0;
+  return __longlong_as_double((long long)(((uint64_t)(ex + 1023) << 52) | (mant & 0xfffffffffffffull)));
+}
+
 // v^2 / 2^62 for |v| < 2^61 from 31-bit limbs of |v| (a1^2 + 4 hi32(a1 a0),
 // the a0^2 term dropped): below the exact value by less than 5.
 __device__ __forceinline__ unsigned long long te_fix_sq(int64_t v) {

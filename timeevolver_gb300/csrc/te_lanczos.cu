@@ -551,7 +551,7 @@ __global__ void __launch_bounds__(TE_THREADS) lanczos_update_kernel(int64_t n, c
     }
   }
   if (FIX) {
-    acc[0] = ldexp(fma((double)sq_hi, 18446744073709551616.0, (double)sq_lo), 62 - 2 * xs);
+    acc[0] = te_u128_to_double(sq_hi, sq_lo, 62 - 2 * xs);  // integers only
     te_warp_max_to_smem(umax, umax_w);
   }
   te_block_sum_wide<1>(acc, wide);

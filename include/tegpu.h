@@ -132,9 +132,18 @@ int te_matrix_set_spmv_lanes(te_matrix A, int lanes);
  * 1 limbs of every slot value (8 bytes per slot for real, 16 for complex
  * values, plus the 4-byte column), 2 a value dictionary (real matrices: one
  * 4-byte word per slot, column and value index; at most 4096 distinct values
- * and 2^(32 - column bits)); *n_values the dictionary size; *scale_shift the
- * sh of round(h 2^sh). */
+ * and 2^(32 - column bits)), 3 limbs split into column blocks (matrices
+ * whose fixed-point vector, 16 bytes per row, exceeds 96 MB: each block's
+ * slice of it stays in L2 during its pass); *n_values the dictionary size
+ * (state 2) or the number of blocks (state 3); *scale_shift the sh of
+ * round(h 2^sh). */
 int te_matrix_fixed_layout(te_matrix A, int* state, int* n_values, int* scale_shift);
+/* Column blocks of the fixed-point form (no counterpart in the reference):
+ * 0 (default) automatic (blocks of at most 56 MB of the fixed-point vector
+ * when it exceeds 96 MB), 1 none, 2..8 that many (matrices with a value
+ * dictionary or long rows are never blocked).  Drops an existing fixed-point
+ * form; the next evolver run that uses it builds it again. */
+int te_matrix_set_fixed_blocks(te_matrix A, int n_blocks);
 /* Current lanes per row (1, 2, 4), tuning first if tune_now != 0 and the
  * choice is still open; a negative value is an error code. */
 int te_matrix_spmv_lanes(te_matrix A, int tune_now);
@@ -309,11 +318,9 @@ int64_t te_evolver_launch_count(te_evolver ev);
  * real H, (5 k 2^-56 + (2 k + 1) 2^-61) R U + 2^-53 |y| for complex H, against
  * FP64's k 2^-53 sum|h||u|.  The recurrence and all reductions stay FP64.
  * Applies to the per-iteration passes of matrices of at least 2048 32-row
- * chunks (smaller ones run the persistent FP64 kernel).  0: FP64 SpMV;
- * 1 (default): fixed point for real H; 2: fixed point for real and complex H.
- * Complex H stays FP64 by default: on the synthetic dim-1e7 Zipf matrix its
- * SpMV is bound by the DRAM sectors of the gathered vector, which the integer
- * format does not shrink (measured: equal time). */
+ * chunks (smaller ones run the persistent FP64 kernel); see
+ * te_matrix_fixed_layout for the forms (value dictionary, column blocks).
+ * 0: FP64 SpMV; 1 (default): fixed point. */
 #define TE_OPT_FIXED_SPMV 2
 int te_evolver_set_option(te_evolver ev, int option, int value);
 

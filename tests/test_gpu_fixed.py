@@ -133,8 +133,8 @@ def test_fixed_spmv_long_rows(te_gpu, oracle_lib):
 
 def test_fixed_spmv_complex(te_gpu, oracle_lib):
     """A complex Hermitian matrix of 70000 rows (2188 chunks, Gaussian values):
-    FP64 by default; with TE_OPT_FIXED_SPMV = 2 the complex fixed-point SpMV
-    (four limb products per entry) against the FP64 passes and the oracle."""
+    the complex fixed-point SpMV (four limb products per entry) against the
+    FP64 passes and the oracle."""
     rng = np.random.default_rng(8)
     n = 70000
     r = np.repeat(np.arange(n), 3)
@@ -150,12 +150,9 @@ def test_fixed_spmv_complex(te_gpu, oracle_lib):
     v = rng.standard_normal(n) + 1j * rng.standard_normal(n)
     v /= np.linalg.norm(v)
     d = (np.arange(n), np.arange(n), rng.uniform(-1, 1, n).astype(np.complex128))
-    c = _run(te_gpu, M, v, 1.0, 0.25, [("sparse", d)], 1, m=30)  # default: complex H stays FP64
-    assert M.fixed_layout()["state"] == 0
-    a = _run(te_gpu, M, v, 1.0, 0.25, [("sparse", d)], 2, m=30)
+    a = _run(te_gpu, M, v, 1.0, 0.25, [("sparse", d)], 1, m=30)
     b = _run(te_gpu, M, v, 1.0, 0.25, [("sparse", d)], 0, m=30)
     assert M.fixed_layout()["state"] == 1
-    assert c["launches"] == b["launches"] and np.array_equal(c["state"], b["state"])
     assert a["launches"] == b["launches"] + 2 * a["n_steps"]
     assert a["n_steps"] == b["n_steps"] and a["status"] == b["status"]
     ref = oracle_lib.evolve((row, col, val), v, 1.0, 0.25, [("sparse", d)], tol=1e-8, m=30)
@@ -183,3 +180,42 @@ def test_fixed_spmv_dictionary_matches_limbs(te_gpu):
     assert Md.fixed_layout()["state"] == 2 and Ml.fixed_layout()["state"] == 1
     assert a["n_steps"] == b["n_steps"]
     assert np.linalg.norm(a["state"] - b["state"]) < 1e-10  # ||dH|| t <= 9e-12
+
+
+def _random_hermitian_70k(seed, complex_values):
+    rng = np.random.default_rng(seed)
+    n = 70000
+    r = np.repeat(np.arange(n), 3)
+    c = rng.integers(0, n, size=3 * n)
+    z = rng.standard_normal(3 * n) + (1j * rng.standard_normal(3 * n) if complex_values else 0)
+    row, col, val = np.concatenate([r, c]), np.concatenate([c, r]), np.concatenate([z, np.conj(z)]) / 2
+    key = row * n + col
+    order = np.argsort(key, kind="stable")
+    uk, start = np.unique(key[order], return_index=True)
+    return n, (uk // n, uk % n, np.add.reduceat(np.asarray(val, np.complex128)[order], start))
+
+
+@pytest.mark.parametrize("complex_values,blocks", [(False, 3), (True, 2), (True, 8)])
+def test_fixed_spmv_column_blocks(te_gpu, oracle_lib, complex_values, blocks):
+    """Column blocks of the fixed-point SpMV (forced on a 70000-row matrix;
+    automatic for fixed-point vectors above 96 MB): the block passes add exact
+    int64 row sums, so the products equal the unblocked ones; the evolutions
+    agree with the unblocked path and stay within the bounds of the oracle."""
+    n, coo = _random_hermitian_70k(21, complex_values)
+    rng = np.random.default_rng(5)
+    v = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    v /= np.linalg.norm(v)
+    d = (np.arange(n), np.arange(n), rng.uniform(-1, 1, n).astype(np.complex128))
+    Mb = te_gpu.Matrix(n, *coo)
+    Mb.set_fixed_blocks(blocks)
+    a = _run(te_gpu, Mb, v, 1.0, 0.25, [("sparse", d)], 1, m=30)
+    assert Mb.fixed_layout()["state"] == 3 and Mb.fixed_layout()["n_values"] == blocks
+    Mu = te_gpu.Matrix(n, *coo)
+    Mu.set_fixed_blocks(1)
+    b = _run(te_gpu, Mu, v, 1.0, 0.25, [("sparse", d)], 1, m=30)
+    assert Mu.fixed_layout()["state"] == 1
+    assert a["n_steps"] == b["n_steps"] and a["status"] == b["status"]
+    assert a["launches"] > b["launches"]  # the block passes
+    assert np.linalg.norm(a["state"] - b["state"]) < 1e-9
+    ref = oracle_lib.evolve(coo, v, 1.0, 0.25, [("sparse", d)], tol=1e-8, m=30)
+    _bounds(a, ref, 1e-8, 1.0)

@@ -74,6 +74,7 @@ SIGNATURES = {
     "te_model_state_index": (_I, [_I, _I, _I, _P, _P]),
     "te_matrix_spmv_lanes": (_I, [_P, _I]),
     "te_matrix_fixed_layout": (_I, [_P, _P, _P, _P]),
+    "te_matrix_set_fixed_blocks": (_I, [_P, _I]),
     "te_matrix_create_zipf": (_I, [_I64, _D, ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_int32, _P, _P]),
     "te_evolver_create": (_I, [_P, _P, _P, _P]),
     "te_evolver_destroy": (_I, [_P]),
@@ -267,11 +268,16 @@ class Matrix:
 
     def fixed_layout(self):
         """Fixed-point form for the integer SpMV (te_matrix_fixed_layout):
-        state 0 not built, 1 limbs per slot, 2 value dictionary."""
+        state 0 not built, 1 limbs per slot, 2 value dictionary, 3 limbs in column
+        blocks (n_values = number of blocks)."""
         st, nv, sh = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         _check(lib().te_matrix_fixed_layout(self.handle, ctypes.byref(st), ctypes.byref(nv), ctypes.byref(sh)),
                "te_matrix_fixed_layout")
         return dict(state=st.value, n_values=nv.value, scale_shift=sh.value)
+
+    def set_fixed_blocks(self, n_blocks):
+        """Column blocks of the fixed-point form: 0 automatic, 1 none, 2..8."""
+        _check(lib().te_matrix_set_fixed_blocks(self.handle, int(n_blocks)), "te_matrix_set_fixed_blocks")
 
     def spmv_lanes(self, tune=True):
         """Lanes per row of the SpMV passes (tuned on first use unless pinned)."""

@@ -66,8 +66,9 @@ struct te_evolver_s {
   double* results = nullptr;  // n_obs x n_samples
   int max_batch = 1;
   int fused_lanczos = 1;  // TE_OPT_FUSED_LANCZOS: 0 never, 1 automatic, 2 always
-  int fixed_spmv = 1;     // TE_OPT_FIXED_SPMV: 0 FP64, 1 fixed point for real H, 2 fixed point for all H
-  int4* X = nullptr;      // fixed-point copy of the current Krylov vector (n rows)
+  int fixed_spmv = 1;     // TE_OPT_FIXED_SPMV: 0 FP64 SpMV, 1 fixed-point SpMV
+  int4* X = nullptr;      // fixed-point copies of the Krylov vectors (m x n rows)
+  longlong2* fx_acc = nullptr;  // column-blocked fixed-point SpMV: exact row sums (n rows)
   int batch_cap = 0;         // states the batch buffer holds
   size_t results_cap = 0;    // doubles the results buffer holds
   std::vector<HostObs> obs;
@@ -228,6 +229,7 @@ void free_evolver(te_evolver ev) {
   cudaFreeHost(ev->host_state);
   cudaFree(ev->slab);
   cudaFree(ev->X);
+  cudaFree(ev->fx_acc);
   cudaFree(ev->batch);
   cudaFree(ev->orig_tmp);
   cudaFree(ev->partials);
@@ -342,12 +344,13 @@ int run(te_evolver ev, te_result* out) {
   // matrices large enough for the per-iteration passes
   // (its own schedule, one lane per row); otherwise the FP64 passes, whose
   // lanes per row are tuned once per matrix on first use
-  const bool fix = (ev->fixed_spmv == 2 || (ev->fixed_spmv == 1 && ev->H->is_real)) && ev->p.reorth == 0 &&
-                   ev->p.exp_factor != 0.0 && ev->H->sell.n_chunks >= 2048 && ev->fused_lanczos != 2;
+  const bool fix = ev->fixed_spmv != 0 && ev->p.reorth == 0 && ev->p.exp_factor != 0.0 &&
+                   ev->H->sell.n_chunks >= 2048 && ev->fused_lanczos != 2;
   if (!fix && (rc = te_tune_sell_lanes(ev->H)) != TE_OK) return rc;
   if (fix) {
     if ((rc = te_sell_build_fixed(ev->H)) != TE_OK) return rc;
     if (!ev->X) TE_CUDA(cudaMalloc(&ev->X, sizeof(int4) * n * ev->m));  // X_0 .. X_{m-1}
+    if (ev->H->sell.fix_nblk > 0 && !ev->fx_acc) TE_CUDA(cudaMalloc(&ev->fx_acc, sizeof(longlong2) * n));
   }
   while (!S->done) {
     if (S->fatal) break;
@@ -376,9 +379,15 @@ int run(te_evolver ev, te_result* out) {
     for (int j = 0; j < m && !fused; ++j) {
       {
         ProfScope ps(ev, 0);
-        if (fix_step)
+        if (fix_step && ev->H->sell.fix_nblk > 0) {
+          te_launch_lanczos_apply_fix_blocked(ev->H->sell, ev->H->is_real, ev->X + (int64_t)j * n, ev->fx_acc,
+                                              ev->cols[j], j > 0 ? ev->cols[j - 1] : nullptr, ev->w, ev->ds,
+                                              ev->partials, j, st);
+          ev->launches += ev->H->sell.fix_nblk;  // the block passes before the epilogue
+        } else if (fix_step) {
           te_launch_lanczos_apply_fix(ev->H->sell, ev->X + (int64_t)j * n, ev->cols[j],
                                       j > 0 ? ev->cols[j - 1] : nullptr, ev->w, ev->ds, ev->partials, j, st);
+        }
         else
           te_launch_lanczos_apply(ev->H->sell, ev->H->is_real, ev->cols[j],
                                   (j > 0 && !cgs2) ? ev->cols[j - 1] : nullptr, ev->w, ev->ds, ev->partials, j, fold,
@@ -832,8 +841,8 @@ extern "C" int te_evolver_set_option(te_evolver ev, int option, int value) {
       ev->fused_lanczos = value;
       return TE_OK;
     case TE_OPT_FIXED_SPMV:
-      if (value < 0 || value > 2) {
-        te_set_error("te_evolver_set_option: TE_OPT_FIXED_SPMV takes 0, 1 or 2");
+      if (value < 0 || value > 1) {
+        te_set_error("te_evolver_set_option: TE_OPT_FIXED_SPMV takes 0 or 1");
         return TE_ERR_INVALID_ARG;
       }
       ev->fixed_spmv = value;

@@ -109,13 +109,107 @@ __global__ void __launch_bounds__(TE_THREADS) dict_pack_kernel(int64_t slots, co
   }
 }
 
+// Column blocks: bounds lo[0] = 0 < lo[1] < ... < lo[nb] = n.
+struct BlockDesc {
+  int nb;
+  int64_t lo[TE_FIX_MAX_BLOCKS + 1];
+};
+
+__device__ __forceinline__ int block_of(const BlockDesc& d, int64_t c) {
+  int b = 0;
+  while (b + 1 < d.nb && c >= d.lo[b + 1]) ++b;
+  return b;
+}
+
+// The slots of the main layout that carry a value (padding and entries that
+// encode to zero contribute nothing and are left out of the blocks).
+template <bool REAL>
+__device__ __forceinline__ bool slot_has_value(const int2* hv, const int4* hv4, int64_t s) {
+  if (REAL) {
+    const int2 h = hv[s];
+    return (h.x | h.y) != 0;
+  }
+  const int4 h = hv4[s];
+  return (h.x | h.y | h.z | h.w) != 0;
+}
+
+// cnt[b n + r]: entries of main row r in column block b.
+template <bool REAL>
+__global__ void __launch_bounds__(TE_THREADS) block_count_kernel(int64_t n, const int64_t* __restrict__ off,
+                                                                 const int32_t* __restrict__ col,
+                                                                 const int2* __restrict__ hv,
+                                                                 const int4* __restrict__ hv4, BlockDesc d,
+                                                                 int32_t* __restrict__ cnt) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    int k[TE_FIX_MAX_BLOCKS] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const int64_t c = r >> 5;
+    for (int64_t s = off[c] + (r & 31); s < off[c + 1]; s += 32)
+      if (slot_has_value<REAL>(hv, hv4, s)) ++k[block_of(d, col[s])];
+    for (int b = 0; b < d.nb; ++b) cnt[(int64_t)b * n + r] = k[b];
+  }
+}
+
+struct BlockFill {
+  const int64_t* off[TE_FIX_MAX_BLOCKS];
+  int32_t* col[TE_FIX_MAX_BLOCKS];
+  int2* hv[TE_FIX_MAX_BLOCKS];
+  int4* hv4[TE_FIX_MAX_BLOCKS];
+};
+
+// Scatter every valued slot of main row r into its block: block row p =
+// pos[b n + r] (present: the row has entries in b), slot off_b[p / 32] +
+// p % 32 + 32 k for its k-th entry there (k < its count <= the chunk width).
+template <bool REAL>
+__global__ void __launch_bounds__(TE_THREADS) block_fill_kernel(int64_t n, const int64_t* __restrict__ off,
+                                                                const int32_t* __restrict__ col,
+                                                                const int2* __restrict__ hv,
+                                                                const int4* __restrict__ hv4, BlockDesc d,
+                                                                const int32_t* __restrict__ pos, BlockFill f) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    int k[TE_FIX_MAX_BLOCKS] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const int64_t c = r >> 5;
+    for (int64_t s = off[c] + (r & 31); s < off[c + 1]; s += 32) {
+      if (!slot_has_value<REAL>(hv, hv4, s)) continue;
+      const int32_t cl = col[s];
+      const int b = block_of(d, cl);
+      const int64_t p = pos[(int64_t)b * n + r];
+      const int64_t q = f.off[b][p >> 5] + (p & 31) + 32 * (int64_t)k[b]++;
+      f.col[b][q] = cl;
+      if (REAL)
+        f.hv[b][q] = hv[s];
+      else
+        f.hv4[b][q] = hv4[s];
+    }
+  }
+}
+
+__global__ void fill_i32_kernel(int64_t count, int32_t* __restrict__ out, int32_t v) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < count; q += (int64_t)gridDim.x * blockDim.x)
+    out[q] = v;
+}
+
 template <typename T>
 void free_ptr(T*& p) {
   cudaFree(p);
   p = nullptr;
 }
 
+void free_blocks(TeSell& S) {
+  for (int b = 0; b < TE_FIX_MAX_BLOCKS; ++b) {
+    TeSell::Block& B = S.fix_blk[b];
+    free_ptr(B.chunk_off);
+    free_ptr(B.row);
+    free_ptr(B.col);
+    free_ptr(B.hv);
+    free_ptr(B.hv4);
+    free_ptr(B.warp_chunk);
+    B = TeSell::Block();
+  }
+  S.fix_nblk = 0;
+}
+
 void free_fixed(TeSell& S) {
+  free_blocks(S);
   free_ptr(S.fix_val);
   free_ptr(S.fix_val4);
   free_ptr(S.fix_warp_chunk);
@@ -289,6 +383,114 @@ int fixed_schedule(TeSell& S, bool real) {
   return TE_OK;
 }
 
+// Column blocks when the fixed-point x (16 bytes per row) is larger than this:
+// slices of at most kBlockSliceBytes then stay in L2 (126 MB) during their pass.
+constexpr int64_t kBlockMinBytes = 96ll << 20;
+constexpr int64_t kBlockSliceBytes = 56ll << 20;
+
+int build_blocks(TeSell& S, bool real) {
+  const int64_t n = S.n;
+  if (S.fix_pk || S.n_long > 0 || S.fix_blocks_req == 1) return TE_OK;
+  if (S.fix_blocks_req == 0 && 16 * n <= kBlockMinBytes) return TE_OK;
+  const int nb = S.fix_blocks_req >= 2
+                     ? (int)std::min<int64_t>(S.fix_blocks_req, std::max<int64_t>(n / 32, 1))
+                     : (int)std::min<int64_t>(TE_FIX_MAX_BLOCKS, (16 * n + kBlockSliceBytes - 1) / kBlockSliceBytes);
+  if (nb < 2) return TE_OK;
+  BlockDesc d{};
+  d.nb = nb;
+  for (int b = 0; b <= nb; ++b) d.lo[b] = n * b / nb;
+  int32_t *d_cnt = nullptr, *d_pos = nullptr;
+  auto cleanup = [&]() {
+    cudaFree(d_cnt);
+    cudaFree(d_pos);
+  };
+  int rc;
+  if ((rc = te_cuda_check(cudaMalloc(&d_cnt, sizeof(int32_t) * nb * n), "column blocks")) != TE_OK) return rc;
+  if (real)
+    block_count_kernel<true><<<te_grid_fit((const void*)block_count_kernel<true>, n, TE_THREADS), TE_THREADS>>>(
+        n, S.chunk_off, S.col, S.fix_val, S.fix_val4, d, d_cnt);
+  else
+    block_count_kernel<false><<<te_grid_fit((const void*)block_count_kernel<false>, n, TE_THREADS), TE_THREADS>>>(
+        n, S.chunk_off, S.col, S.fix_val, S.fix_val4, d, d_cnt);
+  std::vector<int32_t> cnt((size_t)nb * n), pos((size_t)nb * n, -1);
+  if ((rc = te_cuda_check(cudaMemcpy(cnt.data(), d_cnt, sizeof(int32_t) * nb * n, cudaMemcpyDeviceToHost),
+                          "column blocks")) != TE_OK) {
+    cleanup();
+    return rc;
+  }
+  const int bps = te_fix_block_blocks_per_sm(real);
+  BlockFill fill{};
+  S.fix_nblk = nb;  // the arrays below are freed by free_blocks on failure
+  for (int b = 0; b < nb && rc == TE_OK; ++b) {
+    TeSell::Block& B = S.fix_blk[b];
+    const int32_t* cb = cnt.data() + (size_t)b * n;
+    // rows by count in the block, descending and stable; block 0 keeps every row
+    int32_t maxc = 0;
+    for (int64_t r = 0; r < n; ++r) maxc = std::max(maxc, cb[r]);
+    std::vector<int64_t> start((size_t)maxc + 2, 0);
+    for (int64_t r = 0; r < n; ++r) start[maxc - cb[r] + 1]++;
+    for (int32_t k = 0; k <= maxc; ++k) start[k + 1] += start[k];
+    const int64_t n_rows = b == 0 ? n : n - (start[maxc + 1] - start[maxc]);  // rows with entries (count 0 last)
+    std::vector<int32_t> row(std::max<int64_t>(n_rows, 1));
+    int32_t* pb = pos.data() + (size_t)b * n;
+    for (int64_t r = 0; r < n; ++r) {
+      const int64_t i = start[maxc - cb[r]]++;
+      if (i < n_rows) {
+        row[i] = (int32_t)r;
+        pb[r] = (int32_t)i;
+      }
+    }
+    B.n_rows = n_rows;
+    B.n_chunks = (n_rows + 31) / 32;
+    std::vector<int64_t> off(B.n_chunks + 1, 0);
+    for (int64_t c = 0; c < B.n_chunks; ++c) off[c + 1] = off[c] + 32 * (int64_t)cb[row[c * 32]];
+    B.slots = off[B.n_chunks];
+    std::vector<int32_t> wc;
+    te_sell_schedule(off, B.n_chunks, bps, real, B.grid, B.saturated, wc);
+    const int64_t slots = std::max<int64_t>(B.slots, 1);
+    if ((rc = te_cuda_check(cudaMalloc(&B.chunk_off, sizeof(int64_t) * off.size()), "column blocks")) != TE_OK ||
+        (rc = te_cuda_check(cudaMalloc(&B.row, sizeof(int32_t) * row.size()), "column blocks")) != TE_OK ||
+        (rc = te_cuda_check(cudaMalloc(&B.col, sizeof(int32_t) * slots), "column blocks")) != TE_OK ||
+        (rc = te_cuda_check(cudaMalloc(&B.warp_chunk, sizeof(int32_t) * wc.size()), "column blocks")) != TE_OK)
+      break;
+    if (real)
+      rc = te_cuda_check(cudaMalloc(&B.hv, sizeof(int2) * slots), "column blocks");
+    else
+      rc = te_cuda_check(cudaMalloc(&B.hv4, sizeof(int4) * slots), "column blocks");
+    if (rc != TE_OK) break;
+    cudaMemcpy(B.chunk_off, off.data(), sizeof(int64_t) * off.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(B.row, row.data(), sizeof(int32_t) * row.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(B.warp_chunk, wc.data(), sizeof(int32_t) * wc.size(), cudaMemcpyHostToDevice);
+    // padding slots: value 0 at the block's first column
+    fill_i32_kernel<<<te_grid_fit((const void*)fill_i32_kernel, slots, TE_THREADS), TE_THREADS>>>(
+        slots, B.col, (int32_t)d.lo[b]);
+    if (real)
+      cudaMemset(B.hv, 0, sizeof(int2) * slots);
+    else
+      cudaMemset(B.hv4, 0, sizeof(int4) * slots);
+    fill.off[b] = B.chunk_off;
+    fill.col[b] = B.col;
+    fill.hv[b] = B.hv;
+    fill.hv4[b] = B.hv4;
+  }
+  if (rc == TE_OK) rc = te_cuda_check(cudaMalloc(&d_pos, sizeof(int32_t) * nb * n), "column blocks");
+  if (rc == TE_OK)
+    rc = te_cuda_check(cudaMemcpy(d_pos, pos.data(), sizeof(int32_t) * nb * n, cudaMemcpyHostToDevice),
+                       "column blocks");
+  if (rc == TE_OK) {
+    if (real)
+      block_fill_kernel<true><<<te_grid_fit((const void*)block_fill_kernel<true>, n, TE_THREADS), TE_THREADS>>>(
+          n, S.chunk_off, S.col, S.fix_val, S.fix_val4, d, d_pos, fill);
+    else
+      block_fill_kernel<false><<<te_grid_fit((const void*)block_fill_kernel<false>, n, TE_THREADS), TE_THREADS>>>(
+          n, S.chunk_off, S.col, S.fix_val, S.fix_val4, d, d_pos, fill);
+    rc = te_cuda_check(cudaDeviceSynchronize(), "column blocks");
+  }
+  cleanup();
+  if (rc != TE_OK) free_blocks(S);
+  return rc;
+}
+
 }  // namespace
 
 int te_sell_build_fixed(te_matrix_s* A) {
@@ -300,6 +502,7 @@ int te_sell_build_fixed(te_matrix_s* A) {
   }
   int rc = fixed_values(S, A->is_real);
   if (rc == TE_OK) rc = fixed_schedule(S, A->is_real);
+  if (rc == TE_OK) rc = build_blocks(S, A->is_real);
   if (rc != TE_OK) free_fixed(S);
   return rc;
 }
@@ -312,6 +515,20 @@ int te_sell_refresh_fixed(te_matrix_s* A) {
   int rc = fixed_values(S, A->is_real);
   // the schedule depends on the occupancy, which depends on the table size
   if (rc == TE_OK && (was_packed != (S.fix_pk != nullptr) || nv != S.fix_nvals)) rc = fixed_schedule(S, A->is_real);
+  if (rc == TE_OK && S.fix_nblk > 0) {  // the blocks hold copies of the values
+    free_blocks(S);
+    rc = build_blocks(S, A->is_real);
+  }
   if (rc != TE_OK) free_fixed(S);
   return rc;
+}
+
+extern "C" int te_matrix_set_fixed_blocks(te_matrix A, int n_blocks) {
+  if (!A || n_blocks < 0 || n_blocks > TE_FIX_MAX_BLOCKS) {
+    te_set_error("te_matrix_set_fixed_blocks: 0 (automatic), 1 (none) or 2..%d column blocks", TE_FIX_MAX_BLOCKS);
+    return TE_ERR_INVALID_ARG;
+  }
+  A->sell.fix_blocks_req = n_blocks;
+  free_fixed(A->sell);  // rebuilt by the next evolver run that uses it
+  return TE_OK;
 }

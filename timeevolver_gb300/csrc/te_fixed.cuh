@@ -158,13 +158,20 @@ __device__ __forceinline__ void te_fix_mac(const int2 h, const int4 x, int64_t& 
 // is left out: at most 5 units of 2^62 per slot of a total below 2^122, so
 // the row error is below k 1.25 2^-56 R U + (k + 1) 2^-61 R U + 2^-53 |y|
 // for k slots, R the largest row 1-norm and U the bound on max|u|.
-__device__ __forceinline__ double2 te_sell_row_fix(int64_t s, int64_t e, const int32_t* __restrict__ col,
-                                                   const int2* __restrict__ hv, const int4* __restrict__ X,
-                                                   int shift) {
+__device__ __forceinline__ longlong2 te_sell_row_fix_sum(int64_t s, int64_t e, const int32_t* __restrict__ col,
+                                                         const int2* __restrict__ hv, const int4* __restrict__ X) {
   int64_t sr = 0, si = 0;
 #pragma unroll(kTeFixUnroll)
   for (; s < e; s += 32) te_fix_mac(__ldcs(hv + s), __ldg(X + __ldcs(col + s)), sr, si);  // {h0, h1}, {re0, re1, im0, im1}
-  return make_double2(te_i64_to_double(sr, 62 - shift), te_i64_to_double(si, 62 - shift));
+  return make_longlong2(sr, si);
+}
+__device__ __forceinline__ double2 te_fix_to_double(longlong2 S, int shift) {
+  return make_double2(te_i64_to_double(S.x, 62 - shift), te_i64_to_double(S.y, 62 - shift));
+}
+__device__ __forceinline__ double2 te_sell_row_fix(int64_t s, int64_t e, const int32_t* __restrict__ col,
+                                                   const int2* __restrict__ hv, const int4* __restrict__ X,
+                                                   int shift) {
+  return te_fix_to_double(te_sell_row_fix_sum(s, e, col, hv, X), shift);
 }
 
 // te_sell_row_fix over packed slots: word = column | (value index << cbits),
@@ -187,9 +194,8 @@ __device__ __forceinline__ double2 te_sell_row_fix_packed(int64_t s, int64_t e, 
 // (Re = hr xr - hi xi, Im = hr xi + hi xr), so the per-slot term of the
 // error bound is four times the real one: below (5 k 2^-56 + (2 k + 1) 2^-61)
 // R U + 2^-53 |y|.
-__device__ __forceinline__ double2 te_sell_row_fix_c(int64_t s, int64_t e, const int32_t* __restrict__ col,
-                                                     const int4* __restrict__ hv, const int4* __restrict__ X,
-                                                     int shift) {
+__device__ __forceinline__ longlong2 te_sell_row_fix_c_sum(int64_t s, int64_t e, const int32_t* __restrict__ col,
+                                                           const int4* __restrict__ hv, const int4* __restrict__ X) {
   int64_t sr = 0, si = 0;
 #pragma unroll(kTeFixUnroll)
   for (; s < e; s += 32) {
@@ -198,5 +204,10 @@ __device__ __forceinline__ double2 te_sell_row_fix_c(int64_t s, int64_t e, const
     sr += te_fix_prod(h.x, h.y, x.x, x.y) - te_fix_prod(h.z, h.w, x.z, x.w);
     si += te_fix_prod(h.x, h.y, x.z, x.w) + te_fix_prod(h.z, h.w, x.x, x.y);
   }
-  return make_double2(te_i64_to_double(sr, 62 - shift), te_i64_to_double(si, 62 - shift));
+  return make_longlong2(sr, si);
+}
+__device__ __forceinline__ double2 te_sell_row_fix_c(int64_t s, int64_t e, const int32_t* __restrict__ col,
+                                                     const int4* __restrict__ hv, const int4* __restrict__ X,
+                                                     int shift) {
+  return te_fix_to_double(te_sell_row_fix_c_sum(s, e, col, hv, X), shift);
 }

@@ -100,6 +100,8 @@ struct TeDevState {
   double upd_gr, upd_gi;
 };
 
+#define TE_FIX_MAX_BLOCKS 8  // column blocks of the fixed-point SpMV
+
 // SELL-32 matrix in the sorted (permuted) basis.
 struct TeSell {
   int64_t n = 0;          // rows = cols
@@ -146,6 +148,25 @@ struct TeSell {
   uint32_t* fix_pk = nullptr;
   int2* fix_table = nullptr;
   int fix_nvals = 0, fix_cbits = 0;
+  // Column blocks (the fixed-point x larger than a share of L2): block b holds
+  // the entries with columns in [b n / B, (b + 1) n / B), a slice of x that
+  // stays in L2 during its pass.  Each block is a SELL over the rows with
+  // entries there (block 0: all rows), sorted by their count in the block;
+  // row[i] maps block row i to the main row order.  The passes add their
+  // exact int64 row sums into an accumulator, one epilogue pass finishes.
+  int fix_nblk = 0;
+  int fix_blocks_req = 0;  // te_matrix_set_fixed_blocks: 0 automatic, 1 none, 2.. that many
+  struct Block {
+    int64_t n_rows = 0, n_chunks = 0, slots = 0;
+    int64_t* chunk_off = nullptr;
+    int32_t* row = nullptr;
+    int32_t* col = nullptr;
+    int2* hv = nullptr;   // real values
+    int4* hv4 = nullptr;  // complex values
+    int32_t* warp_chunk = nullptr;
+    int grid = 0;
+    bool saturated = false;
+  } fix_blk[TE_FIX_MAX_BLOCKS];
 };
 
 // The long rows of a SELL matrix, by value for kernels.
@@ -256,6 +277,12 @@ void te_launch_lanczos_update(int64_t n, const double2* w, const double2* u_j, d
 // per row, te_sell_build_fixed done): te_launch_fix_start encodes u_0 at the
 // start of a Krylov step; the apply pass reads the fixed-point copy X of u_j.
 int te_sell_build_fixed(te_matrix_s* A);
+// Column-blocked fixed-point apply (S.fix_nblk > 0): the block passes into
+// acc (n longlong2, exact row sums), then the epilogue pass.
+void te_launch_lanczos_apply_fix_blocked(const TeSell& A, bool is_real, const int4* X, longlong2* acc,
+                                         const double2* u_j, const double2* u_jm1, double2* w, TeDevState* ds,
+                                         double* partials, int j, cudaStream_t st);
+int te_fix_block_blocks_per_sm(bool is_real);
 // Resident blocks per SM of the fixed-point apply kernel (te_lanczos.cu).
 // fmt: 0 real limbs, 1 real value dictionary, 2 complex limbs.
 int te_apply_fix_blocks_per_sm(int fmt, size_t dyn_smem);

@@ -144,6 +144,33 @@ __device__ __forceinline__ unsigned int te_block_max_from_smem(const unsigned in
   return m;
 }
 
+// End of a fixed-point apply pass: block sums of <u_j, w'> and max|w'|, then
+// in the last block alpha_j = f <u_j, w'> (f = s_j g), the update's
+// coefficient alpha_j / e, and the scale xs_{j+1} of the next vector from
+// B = W + (|Re| + |Im|)(alpha_j / e) U (W >= max|w'|, U >= max|u_j|).
+__device__ __forceinline__ void fix_apply_finish(double (&acc)[2], unsigned int wmax, TeDevState* ds,
+                                                 double* partials, int j, double f, double ie, double* scratch,
+                                                 double* wide, unsigned int* wmax_w) {
+  te_warp_max_to_smem(wmax, wmax_w);
+  te_block_sum_wide<2>(acc, wide);
+  if (threadIdx.x == 0) atomicMax(&ds->fx_wmax, te_block_max_from_smem(wmax_w));
+  if (te_publish_partials<2>(acc, partials, &ds->counter[0])) {
+    double tot[2];
+    te_final_sum<2>(tot, partials, &ds->counter[0], scratch);
+    if (threadIdx.x == 0) {
+      const double2 alpha = make_double2(f * tot[0], f * tot[1]);
+      ds->alpha[j] = alpha;
+      ds->upd_gr = alpha.x * ie;
+      ds->upd_gi = alpha.y * ie;
+      const double W = te_fix_upper(atomicExch(&ds->fx_wmax, 0u));
+      const double U = te_fix_upper(ds->fx_umax[j]);
+      const double B = (W + (fabs(alpha.x * ie) + fabs(alpha.y * ie)) * U) * (1.0 + 1e-12);
+      ds->fx_xs[j + 1] = te_fix_scale(B);
+      ds->fx_umax[j + 1] = 0u;
+    }
+  }
+}
+
 // Folded three-term apply pass with the fixed-point SpMV (te_fixed.cuh):
 // w' = -i H u_j + (beta_j / e)^2 u_{j-1}, alpha_j = s_j g <u_j, w'> as in
 // lanczos_apply_kernel<REAL, HAS_PREV, FOLD = true, K = 1>, with H u_j of the
@@ -234,25 +261,71 @@ __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_f
       wmax = max(wmax, max(te_fix_hiword(wr.x), te_fix_hiword(wr.y)));
     }
   }
-  te_warp_max_to_smem(wmax, wmax_w);
-  te_block_sum_wide<2>(acc, wide);
-  if (threadIdx.x == 0) atomicMax(&ds->fx_wmax, te_block_max_from_smem(wmax_w));
-  if (te_publish_partials<2>(acc, partials, &ds->counter[0])) {
-    double tot[2];
-    te_final_sum<2>(tot, partials, &ds->counter[0], scratch);
-    if (threadIdx.x == 0) {
-      const double f = sj * g;
-      const double2 alpha = make_double2(f * tot[0], f * tot[1]);
-      ds->alpha[j] = alpha;
-      ds->upd_gr = alpha.x * ie;
-      ds->upd_gi = alpha.y * ie;
-      const double W = te_fix_upper(atomicExch(&ds->fx_wmax, 0u));
-      const double U = te_fix_upper(ds->fx_umax[j]);
-      const double B = (W + (fabs(alpha.x * ie) + fabs(alpha.y * ie)) * U) * (1.0 + 1e-12);
-      ds->fx_xs[j + 1] = te_fix_scale(B);
-      ds->fx_umax[j + 1] = 0u;
+  fix_apply_finish(acc, wmax, ds, partials, j, sj * g, ie, scratch, wide, wmax_w);
+}
+
+// One column block of the fixed-point SpMV: for block row i (main row
+// row[i]) the exact int64 sums S over the block's entries are added into
+// acc[row[i]] (written when first != 0; block 0 covers every row).
+template <bool REAL>
+__global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) fix_block_kernel(
+    int64_t n_rows, const int32_t* __restrict__ warp_chunk, const int64_t* __restrict__ chunk_off,
+    const int32_t* __restrict__ row, const int32_t* __restrict__ col, const int2* __restrict__ hv,
+    const int4* __restrict__ hv4, const int4* __restrict__ X, longlong2* __restrict__ acc, int first,
+    const TeDevState* ds) {
+  te_pdl_trigger();
+  te_pdl_wait();
+  if (te_step_inactive(ds)) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int64_t c_begin = warp_chunk[wid], c_end = warp_chunk[wid + 1];
+  for (int64_t c = c_begin; c < c_end; ++c) {
+    const int64_t s0 = __ldg(chunk_off + c), s1 = __ldg(chunk_off + c + 1);
+    longlong2 S = REAL ? te_sell_row_fix_sum(s0 + lane, s1, col, hv, X) : te_sell_row_fix_c_sum(s0 + lane, s1, col, hv4, X);
+    const int64_t i = c * 32 + lane;
+    if (i < n_rows) {
+      const int32_t r = __ldg(row + i);
+      if (!first) {
+        const longlong2 a = acc[r];
+        S.x += a.x;
+        S.y += a.y;
+      }
+      acc[r] = S;
     }
   }
+}
+
+// Epilogue pass of the column-blocked apply: y from the accumulated sums,
+// then as lanczos_apply_fix_kernel (w', <u_j, w'>, max|w'|, alpha_j, xs_{j+1}).
+template <bool HAS_PREV>
+__global__ void __launch_bounds__(TE_THREADS) fix_epilogue_kernel(int64_t n, const longlong2* __restrict__ acc_in,
+                                                                  int sh, const double2* __restrict__ u_j,
+                                                                  const double2* __restrict__ u_jm1,
+                                                                  double2* __restrict__ w, TeDevState* ds,
+                                                                  double* partials, int j) {
+  __shared__ double scratch[2 * 32];
+  __shared__ double wide[2 * TE_THREADS];
+  __shared__ unsigned int wmax_w[TE_THREADS / 32];
+  te_pdl_trigger();
+  te_pdl_wait();
+  if (te_step_inactive(ds)) return;
+  const double sj = ds->s[j];
+  const double g = ds->exp_factor * sj;
+  const double ie = ds->inv_exp_factor;
+  double cw = 0.0;
+  if (HAS_PREV) {
+    const double bj = ds->beta[j];
+    cw = (bj * ie) * (bj * ie);
+  }
+  const int shift = sh + ds->fx_xs[j];
+  double acc[2] = {0.0, 0.0};
+  unsigned int wmax = 0;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const double2 wr = apply_row_epilogue<HAS_PREV, true>(r, te_fix_to_double(acc_in[r], shift), g, cw, u_j, u_jm1, w,
+                                                          acc);
+    wmax = max(wmax, max(te_fix_hiword(wr.x), te_fix_hiword(wr.y)));
+  }
+  fix_apply_finish(acc, wmax, ds, partials, j, sj * g, ie, scratch, wide, wmax_w);
 }
 
 // Start of a Krylov step on the fixed-point path, two passes over u_0:
@@ -929,6 +1002,27 @@ ApplyFixKernel apply_fix_kernel(int fmt, bool has_prev) {
 }
 
 }  // namespace
+
+int te_fix_block_blocks_per_sm(bool is_real) {
+  return te_kernel_blocks_per_sm(is_real ? (const void*)fix_block_kernel<true> : (const void*)fix_block_kernel<false>,
+                                 TE_THREADS, 0);
+}
+
+void te_launch_lanczos_apply_fix_blocked(const TeSell& A, bool is_real, const int4* X, longlong2* acc,
+                                         const double2* u_j, const double2* u_jm1, double2* w, TeDevState* ds,
+                                         double* partials, int j, cudaStream_t st) {
+  for (int b = 0; b < A.fix_nblk; ++b) {
+    const TeSell::Block& B = A.fix_blk[b];
+    te_launch_pdl(B.saturated, is_real ? fix_block_kernel<true> : fix_block_kernel<false>, B.grid, TE_THREADS, st,
+                  B.n_rows, (const int32_t*)B.warp_chunk, (const int64_t*)B.chunk_off, (const int32_t*)B.row,
+                  (const int32_t*)B.col, (const int2*)B.hv, (const int4*)B.hv4, X, acc, b == 0 ? 1 : 0,
+                  (const TeDevState*)ds);
+  }
+  const auto k = u_jm1 ? fix_epilogue_kernel<true> : fix_epilogue_kernel<false>;
+  const void* kk = (const void*)k;
+  te_launch_pdl(te_grid_saturated(kk, A.n, TE_THREADS), k, te_grid_fit(kk, A.n, TE_THREADS), TE_THREADS, st, A.n,
+                (const longlong2*)acc, A.fix_sh, u_j, u_jm1, w, ds, partials, j);
+}
 
 int te_apply_fix_blocks_per_sm(int fmt, size_t dyn_smem) {
   return std::min(te_kernel_blocks_per_sm((const void*)apply_fix_kernel(fmt, true), TE_THREADS, dyn_smem),

@@ -982,8 +982,8 @@ extern "C" int te_matrix_layout(te_matrix A, int64_t* sell_slots, int64_t* long_
 extern "C" int te_matrix_fixed_layout(te_matrix A, int* state, int* n_values, int* scale_shift) {
   if (!A) return TE_ERR_INVALID_ARG;
   const TeSell& S = A->sell;
-  if (state) *state = !S.fix_warp_chunk ? 0 : (S.fix_pk ? 2 : 1);
-  if (n_values) *n_values = S.fix_nvals;
+  if (state) *state = !S.fix_warp_chunk ? 0 : (S.fix_pk ? 2 : (S.fix_nblk > 0 ? 3 : 1));
+  if (n_values) *n_values = S.fix_nblk > 0 ? S.fix_nblk : S.fix_nvals;
   if (scale_shift) *scale_shift = S.fix_sh;
   return TE_OK;
 }

@@ -607,7 +607,7 @@ def zipf_cpu_baseline(te, nnz_full, steps_full):
                       "(extrapolated)" % (len(coo[2]), ZIPF_CPU_T, r["n_steps"], el, per_step, steps_full)}
 
 
-def ncu_case(t_final, config="plain", zipf_n=2_000_000, spmv=None):
+def ncu_case(t_final, config="plain", zipf_n=2_000_000, spmv=None, fixed_blocks=None):
     """A short solve of the same workload for ncu captures (t_final instead of
     the full time; the Zipf matrix at a smaller dimension)."""
     import timeevolver_gb300 as te
@@ -615,10 +615,13 @@ def ncu_case(t_final, config="plain", zipf_n=2_000_000, spmv=None):
     te.lib().te_set_device(0)
     if config == "zipf":
         H, est = te.Matrix.zipf(zipf_n, 1.5, 2, 256, 1, 30)
+        if fixed_blocks is not None:
+            H.set_fixed_blocks(fixed_blocks)
         rng = np.random.default_rng(1)
         v = rng.standard_normal(zipf_n) + 1j * rng.standard_normal(zipf_n)
         v /= np.linalg.norm(v)
-        out = te.evolve(H, v, t_final, t_final, [], tol=TOL, m=M_KRYLOV)
+        out = te.evolve(H, v, t_final, t_final, [], tol=TOL, m=M_KRYLOV,
+                        options={te.OPT_FIXED_SPMV: spmv_option(spmv)})
         print("ncu case: zipf n=%d nnz=%d t=%g, %d Krylov steps, status %d, %d launches"
               % (zipf_n, H.info()["nnz"], t_final, out["n_steps"], out["status"], out["launches"]))
         return
@@ -644,11 +647,14 @@ def main():
     ap.add_argument("--spmv", default=None, choices=["fixed", "fp64"],
                     help="SpMV arithmetic of the Lanczos passes: fixed-point integer products (the default) or "
                          "FP64 FMAs")
+    ap.add_argument("--fixed-blocks", type=int, default=None,
+                    help="column blocks of the fixed-point form in --ncu-case runs of --config zipf "
+                         "(te_matrix_set_fixed_blocks: 0 automatic, 1 none, 2..8)")
     ap.add_argument("--zipf-n", type=int, default=2_000_000,
                     help="dimension of the Zipf matrix in --ncu-case runs of --config zipf")
     args = ap.parse_args()
     if args.ncu_case is not None:
-        ncu_case(args.ncu_case, args.config, args.zipf_n, args.spmv)
+        ncu_case(args.ncu_case, args.config, args.zipf_n, args.spmv, args.fixed_blocks)
         return
     if args.impl == "reference":
         run_reference(args)

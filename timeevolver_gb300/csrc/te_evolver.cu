@@ -344,14 +344,23 @@ int run(te_evolver ev, te_result* out) {
   // matrices large enough for the per-iteration passes
   // (its own schedule, one lane per row); otherwise the FP64 passes, whose
   // lanes per row are tuned once per matrix on first use
-  const bool fix = ev->fixed_spmv != 0 && ev->p.reorth == 0 && ev->p.exp_factor != 0.0 &&
-                   ev->H->sell.n_chunks >= 2048 && ev->fused_lanczos != 2;
-  if (!fix && (rc = te_tune_sell_lanes(ev->H)) != TE_OK) return rc;
+  bool fix = ev->fixed_spmv != 0 && ev->p.reorth == 0 && ev->p.exp_factor != 0.0 &&
+             ev->H->sell.n_chunks >= 2048 && ev->fused_lanczos != 2;
   if (fix) {
-    if ((rc = te_sell_build_fixed(ev->H)) != TE_OK) return rc;
-    if (!ev->X) TE_CUDA(cudaMalloc(&ev->X, sizeof(int4) * n * ev->m));  // X_0 .. X_{m-1}
-    if (ev->H->sell.fix_nblk > 0 && !ev->fx_acc) TE_CUDA(cudaMalloc(&ev->fx_acc, sizeof(longlong2) * n));
+    // the fixed-point form and its vectors; without memory for them the
+    // evolution runs the FP64 passes instead
+    rc = te_sell_build_fixed(ev->H);
+    if (rc == TE_OK && !ev->X) rc = te_cuda_check(cudaMalloc(&ev->X, sizeof(int4) * n * ev->m), "fixed-point basis");
+    if (rc == TE_OK && ev->H->sell.fix_nblk > 0 && !ev->fx_acc)
+      rc = te_cuda_check(cudaMalloc(&ev->fx_acc, sizeof(longlong2) * n), "fixed-point sums");
+    if (rc == TE_ERR_OUT_OF_MEMORY) {
+      cudaGetLastError();
+      fix = false;
+    } else if (rc != TE_OK) {
+      return rc;
+    }
   }
+  if (!fix && (rc = te_tune_sell_lanes(ev->H)) != TE_OK) return rc;
   while (!S->done) {
     if (S->fatal) break;
     if (++guard > ((int64_t)1 << 40)) break;

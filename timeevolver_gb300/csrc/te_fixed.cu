@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "te_fixed.cuh"
@@ -493,7 +494,11 @@ int build_blocks(TeSell& S, bool real) {
 
 }  // namespace
 
+// One build at a time: evolvers on other host threads may share the matrix.
+static std::mutex g_fixed_mutex;
+
 int te_sell_build_fixed(te_matrix_s* A) {
+  std::lock_guard<std::mutex> lock(g_fixed_mutex);
   TeSell& S = A->sell;
   if (S.fix_warp_chunk) return TE_OK;
   if (S.n_chunks < 1) {
@@ -508,6 +513,7 @@ int te_sell_build_fixed(te_matrix_s* A) {
 }
 
 int te_sell_refresh_fixed(te_matrix_s* A) {
+  std::lock_guard<std::mutex> lock(g_fixed_mutex);
   TeSell& S = A->sell;
   if (!S.fix_warp_chunk) return TE_OK;
   const bool was_packed = S.fix_pk != nullptr;
@@ -528,6 +534,7 @@ extern "C" int te_matrix_set_fixed_blocks(te_matrix A, int n_blocks) {
     te_set_error("te_matrix_set_fixed_blocks: 0 (automatic), 1 (none) or 2..%d column blocks", TE_FIX_MAX_BLOCKS);
     return TE_ERR_INVALID_ARG;
   }
+  std::lock_guard<std::mutex> lock(g_fixed_mutex);
   A->sell.fix_blocks_req = n_blocks;
   free_fixed(A->sell);  // rebuilt by the next evolver run that uses it
   return TE_OK;

@@ -140,3 +140,67 @@ def test_norm1_device_path_bit_identical(te_gpu):
     asym[k] *= 1.0 + 2.0 ** -40  # (r, c) no longer mirrors (c, r)
     Ma = te_gpu.Matrix(n, row, col, asym)
     assert Ma.info()["norm1"] == seq_norm1(col, asym)
+
+
+def _bh10():
+    from oracle import models
+    states, H = models.bose_hubbard(10, 10, 1.0, 2.0)
+    return len(states), np.asarray(H[0], np.int64), np.asarray(H[1], np.int64), np.asarray(H[2], np.complex128)
+
+
+@pytest.mark.parametrize("case", ["bh10", "hubs"])
+def test_device_layout_identical_to_host_layout(te_gpu, case):
+    """The SELL order built on the device (stable counting sort by length,
+    long rows ordered by length on the host) equals the host's stable sort:
+    the same matrix uploaded as a row-sorted COO (device build) and as a host
+    CSR (host build) has the same layout and evolves to bit-identical
+    results, whose reductions run in the permuted order."""
+    if case == "bh10":
+        n, row, col, val = _bh10()
+    else:
+        n = 40000
+        row, col, val = _hub_matrix(n, [17, n // 2, n - 1], 3000, 11, True)
+    assert len(val) >= 1 << 18  # the device conversion
+    rp = np.zeros(n + 1, dtype=np.int64)
+    np.add.at(rp, row + 1, 1)
+    rp = np.cumsum(rp)
+    Md = te_gpu.Matrix(n, row, col, val)
+    Mh = te_gpu.Matrix.from_csr(n, rp, col, val)
+    assert Md.layout() == Mh.layout()
+    if case == "hubs":
+        assert Md.layout()["long_rows"] == 3
+    assert Md.info()["norm1"] == Mh.info()["norm1"]
+    rng = np.random.default_rng(5)
+    v = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    v /= np.linalg.norm(v)
+    d = (np.arange(n), np.arange(n), rng.uniform(-1, 1, n).astype(np.complex128))
+    a = te_gpu.evolve(Md, v, 1.0, 0.25, [("sparse", d)], tol=1e-8, m=30)
+    b = te_gpu.evolve(Mh, v, 1.0, 0.25, [("sparse", d)], tol=1e-8, m=30)
+    assert a["n_steps"] == b["n_steps"] and a["status"] == b["status"]
+    assert np.array_equal(a["state"], b["state"])
+    assert np.array_equal(a["samples"], b["samples"])
+
+
+def test_destroy_frees_the_fixed_point_form(te_gpu):
+    """Destroying a matrix also frees its fixed-point form, column blocks
+    included (forced here): device memory returns to where it was.  The
+    hopping terms get Peierls phases (a complex Hermitian matrix, so int32
+    limbs per slot rather than the real value dictionary)."""
+    import torch
+    n, row, col, val = _bh10()
+    val = val * np.exp(0.3j * (row - col))
+    rng = np.random.default_rng(6)
+    v = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    v /= np.linalg.norm(v)
+    d = (np.arange(n), np.arange(n), np.ones(n, dtype=np.complex128))
+    free0 = None
+    for it in range(4):  # the first round also loads the kernels
+        M = te_gpu.Matrix(n, row, col, val)
+        M.set_fixed_blocks(3)
+        te_gpu.evolve(M, v, 0.5, 0.5, [("sparse", d)], tol=1e-8, m=30)
+        assert M.fixed_layout()["state"] == 3
+        M.close()
+        torch.cuda.synchronize()
+        if it == 0:
+            free0 = torch.cuda.mem_get_info()[0]
+    assert abs(torch.cuda.mem_get_info()[0] - free0) < 8 << 20

@@ -207,6 +207,18 @@ class Matrix:
         return M
 
     @classmethod
+    def from_csr(cls, n_rows, row_ptr, col, values, n_cols=None):
+        """From a host CSR (te_matrix_create_csr): row_ptr (n_rows + 1), col,
+        complex values; the layout is built on the host."""
+        rp = np.ascontiguousarray(row_ptr, dtype=np.int64)
+        ci = np.ascontiguousarray(col, dtype=np.int32)
+        val = np.ascontiguousarray(values, dtype=np.complex128)
+        h = ctypes.c_void_p()
+        _check(lib().te_matrix_create_csr(int(n_rows), int(n_cols or n_rows), len(ci), _ptr(rp), _ptr(ci), _ptr(val),
+                                          1, ctypes.byref(h)), "te_matrix_create_csr")
+        return cls._adopt(h)
+
+    @classmethod
     def from_device_csr(cls, n_rows, row_ptr, col, values, n_cols=None):
         """From a CSR already on the GPU (torch tensors: int32 row_ptr and
         col, complex128 or float64 values); the arrays are copied."""

@@ -634,16 +634,11 @@ extern "C" int te_evolver_add_sparse_observable(te_evolver ev, te_matrix O) {
     o.kind = 0;
     TE_CUDA(cudaMalloc(&o.diag_perm, sizeof(double) * ev->n));
     // permuted Re(diagonal): gather through the permutation of H
-    double2* dc = nullptr;
-    TE_CUDA(cudaMalloc(&dc, sizeof(double2) * ev->n));
-    te_launch_permute(ev->n, ev->H->sell.perm, O->diag_c, dc, ev->st);
-    std::vector<double2> h(ev->n);
-    TE_CUDA(cudaMemcpyAsync(h.data(), dc, sizeof(double2) * ev->n, cudaMemcpyDeviceToHost, ev->st));
-    TE_CUDA(cudaStreamSynchronize(ev->st));
-    cudaFree(dc);
-    std::vector<double> re(ev->n);
-    for (int64_t i = 0; i < ev->n; ++i) re[i] = h[i].x;
-    TE_CUDA(cudaMemcpy(o.diag_perm, re.data(), sizeof(double) * ev->n, cudaMemcpyHostToDevice));
+    te_launch_permute_real(ev->n, ev->H->sell.perm, O->diag_re, o.diag_perm, ev->st);
+    if (int rc = te_cuda_check(cudaStreamSynchronize(ev->st), "diagonal observable")) {
+      cudaFree(o.diag_perm);
+      return rc;
+    }
   } else {
     o.kind = 2;
     o.O = O;

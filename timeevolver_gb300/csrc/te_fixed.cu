@@ -529,6 +529,8 @@ int te_sell_refresh_fixed(te_matrix_s* A) {
   return rc;
 }
 
+void te_sell_free_fixed(TeSell& S) { free_fixed(S); }
+
 extern "C" int te_matrix_set_fixed_blocks(te_matrix A, int n_blocks) {
   if (!A || n_blocks < 0 || n_blocks > TE_FIX_MAX_BLOCKS) {
     te_set_error("te_matrix_set_fixed_blocks: 0 (automatic), 1 (none) or 2..%d column blocks", TE_FIX_MAX_BLOCKS);

@@ -193,11 +193,12 @@ struct te_matrix_s {
 };
 
 // Adopt a device CSR (int32 row pointers, columns, complex values; the matrix
-// frees them) -- the device-side build of te_matrix_create_csr_device.
+// frees them) -- the device-side build of te_matrix_create_csr_device; nnz =
+// d_rp[n_rows].
 // norm1: the 1-norm if the caller computed it, NAN to accumulate it on the
 // device in fixed point.
-int te_matrix_adopt_device_csr(int64_t n_rows, int64_t n_cols, const std::vector<int32_t>& rp_host, int32_t* d_rp,
-                               int32_t* d_ci, double2* d_v, te_matrix* out, double norm1);
+int te_matrix_adopt_device_csr(int64_t n_rows, int64_t n_cols, int64_t nnz, int32_t* d_rp, int32_t* d_ci,
+                               double2* d_v, te_matrix* out, double norm1);
 
 // Programmatic dependent launch: a kernel launched with te_launch_pdl may be
 // scheduled while its predecessor in the stream is still finishing (hiding the
@@ -265,6 +266,7 @@ void te_launch_sell_spmv(const TeSell& A, bool is_real, double2 alpha, const dou
                          cudaStream_t st);
 void te_launch_csr_spmv(const te_matrix_s& A, double2 alpha, const double2* x, double2* y, cudaStream_t st);
 void te_launch_permute(int64_t n, const int32_t* idx, const double2* in, double2* out, cudaStream_t st);
+void te_launch_permute_real(int64_t n, const int32_t* idx, const double* in, double* out, cudaStream_t st);
 // te_lanczos.cu
 // fold: store w / (expFactor s_j) instead of w (three-term mode with a
 // non-zero expFactor; the update kernel then takes the factor into s_{j+1}).
@@ -288,6 +290,8 @@ int te_fix_block_blocks_per_sm(bool is_real);
 int te_apply_fix_blocks_per_sm(int fmt, size_t dyn_smem);
 // Re-encode the fixed-point values after H's SELL values changed in place.
 int te_sell_refresh_fixed(te_matrix_s* A);
+// Frees the fixed-point form (values, dictionary, schedule, column blocks).
+void te_sell_free_fixed(TeSell& S);
 void te_launch_fix_start(int64_t n, const double2* u_0, int4* X, TeDevState* ds, double* partials, cudaStream_t st);
 void te_launch_lanczos_apply_fix(const TeSell& A, const int4* X, const double2* u_j, const double2* u_jm1,
                                  double2* w, TeDevState* ds, double* partials, int j, cudaStream_t st);

@@ -85,6 +85,12 @@ __global__ void permute_kernel(int64_t n, const int32_t* __restrict__ idx, const
     out[i] = __ldg(in + __ldg(idx + i));
 }
 
+__global__ void permute_real_kernel(int64_t n, const int32_t* __restrict__ idx, const double* __restrict__ in,
+                                    double* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = __ldg(in + __ldg(idx + i));
+}
+
 void te_launch_sell_spmv(const TeSell& A, bool is_real, double2 alpha, const double2* x_perm, double2* y_perm,
                          cudaStream_t st) {
   using K = void (*)(int64_t, int64_t, const int32_t*, const int64_t*, const int32_t*, const double*, TeLongRows,
@@ -112,6 +118,10 @@ void te_launch_csr_spmv(const te_matrix_s& A, double2 alpha, const double2* x, d
 
 void te_launch_permute(int64_t n, const int32_t* idx, const double2* in, double2* out, cudaStream_t st) {
   permute_kernel<<<te_grid_fit((const void*)permute_kernel, n, TE_THREADS), TE_THREADS, 0, st>>>(n, idx, in, out);
+}
+void te_launch_permute_real(int64_t n, const int32_t* idx, const double* in, double* out, cudaStream_t st) {
+  permute_real_kernel<<<te_grid_fit((const void*)permute_real_kernel, n, TE_THREADS), TE_THREADS, 0, st>>>(n, idx, in,
+                                                                                                           out);
 }
 
 // ------------------------------------------------- device build (kernels)
@@ -218,6 +228,208 @@ __global__ void fill_sell_kernel(int64_t n, int64_t n_long, int64_t n_chunks, co
         } else {
           reinterpret_cast<double2*>(sval)[sidx] = make_double2(0.0, 0.0);
         }
+      }
+    }
+  }
+}
+
+// ------------------------------------------ exclusive prefix sums (setup work)
+
+// Tiles of 2048 elements (256 threads x 8 consecutive): each tile's exclusive
+// scan and its total; the totals are scanned by one block, then added back.
+constexpr int kScanTile = 2048;
+
+template <typename T>
+__device__ __forceinline__ T scan_block_2048(T (&v)[8], T carry, T* warp_tot) {
+  T s = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) s += v[i];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T x = s;  // inclusive warp scan of the thread sums
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const T y = __shfl_up_sync(0xffffffffu, x, d);
+    if (lane >= d) x += y;
+  }
+  if (lane == 31) warp_tot[warp] = x;
+  __syncthreads();
+  T base = carry, total = carry;
+  for (int w = 0; w < 8; ++w) {
+    if (w < warp) base += warp_tot[w];
+    total += warp_tot[w];
+  }
+  T run = base + x - s;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const T e = v[i];
+    v[i] = run;
+    run += e;
+  }
+  __syncthreads();  // warp_tot is reused by the caller's next tile
+  return total;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) scan_tiles_kernel(int64_t count, const T* __restrict__ in, T* __restrict__ out,
+                                                         T* __restrict__ tile_sums) {
+  __shared__ T warp_tot[8];
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + threadIdx.x * 8;
+  T v[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) v[i] = base + i < count ? in[base + i] : (T)0;
+  const T total = scan_block_2048<T>(v, (T)0, warp_tot);
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+    if (base + i < count) out[base + i] = v[i];
+  if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) scan_sums_kernel(int64_t count, T* __restrict__ sums) {
+  __shared__ T warp_tot[8];
+  T carry = 0;
+  for (int64_t t0 = 0; t0 < count; t0 += kScanTile) {
+    const int64_t base = t0 + threadIdx.x * 8;
+    T v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = base + i < count ? sums[base + i] : (T)0;
+    const T total = scan_block_2048<T>(v, carry, warp_tot);
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      if (base + i < count) sums[base + i] = v[i];
+    carry = total;
+  }
+}
+
+template <typename T>
+__global__ void scan_add_kernel(int64_t count, T* __restrict__ out, const T* __restrict__ sums) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] += sums[i / kScanTile];
+}
+
+// out[i] = in[0] + ... + in[i - 1] for i < count (in == out allowed).
+template <typename T>
+int scan_exclusive(const T* in, T* out, int64_t count) {
+  if (count <= 0) return TE_OK;
+  const int64_t tiles = (count + kScanTile - 1) / kScanTile;
+  T* sums = nullptr;
+  int rc = te_cuda_check(cudaMalloc(&sums, sizeof(T) * tiles), "prefix sums");
+  if (rc != TE_OK) return rc;
+  scan_tiles_kernel<T><<<(unsigned)tiles, 256>>>(count, in, out, sums);
+  if (tiles > 1) {
+    scan_sums_kernel<T><<<1, 256>>>(tiles, sums);
+    scan_add_kernel<T><<<te_grid_fit((const void*)scan_add_kernel<T>, count, TE_THREADS), TE_THREADS>>>(count, out,
+                                                                                                       sums);
+  }
+  rc = te_cuda_check(cudaGetLastError(), "prefix sums");
+  cudaFree(sums);
+  return rc;
+}
+
+// ------------------------------------------ SELL order on the device
+
+// Sort key of a row for the length-sorted SELL order: 0 for long rows (longer
+// than long_min; ordered among themselves on the host), else 1 + long_min - len,
+// so longer rows come first.  Keys run from 0 to long_min + 1.
+__device__ __forceinline__ int layout_key(const int32_t* __restrict__ rp, int64_t r, int long_min) {
+  const int len = rp[r + 1] - rp[r];
+  return len > long_min ? 0 : 1 + long_min - len;
+}
+
+constexpr int kLayoutTile = 4096;  // rows per tile of the counting sort
+
+// Per-tile key counts, key-major: cnt[key * n_tiles + tile].
+__global__ void __launch_bounds__(256) layout_hist_kernel(int64_t n, const int32_t* __restrict__ rp, int long_min,
+                                                          int n_keys, int64_t n_tiles, int32_t* __restrict__ cnt) {
+  extern __shared__ int hist[];
+  for (int k = threadIdx.x; k < n_keys; k += blockDim.x) hist[k] = 0;
+  __syncthreads();
+  const int64_t r0 = (int64_t)blockIdx.x * kLayoutTile, r1 = min(n, r0 + kLayoutTile);
+  for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) atomicAdd(&hist[layout_key(rp, r, long_min)], 1);
+  __syncthreads();
+  for (int k = threadIdx.x; k < n_keys; k += blockDim.x) cnt[(int64_t)k * n_tiles + blockIdx.x] = hist[k];
+}
+
+// Stable scatter, one warp per tile: the tile's rows in order, 32 at a time.
+// Equal keys among the 32 are ranked by lane (match), and a running count per
+// key in shared memory carries the rank from one group of 32 to the next, so
+// rows of equal key keep their original order.  start = the exclusive scan of
+// the key-major counts.
+__global__ void __launch_bounds__(32) layout_scatter_kernel(int64_t n, const int32_t* __restrict__ rp, int long_min,
+                                                            int n_keys, int64_t n_tiles,
+                                                            const int32_t* __restrict__ start,
+                                                            int32_t* __restrict__ perm, int32_t* __restrict__ iperm) {
+  extern __shared__ int run[];
+  const int lane = threadIdx.x;
+  for (int k = lane; k < n_keys; k += 32) run[k] = 0;
+  __syncwarp();
+  const int64_t r0 = (int64_t)blockIdx.x * kLayoutTile, r1 = min(n, r0 + kLayoutTile);
+  for (int64_t rb = r0; rb < r1; rb += 32) {
+    const int64_t r = rb + lane;
+    const bool valid = r < r1;
+    const int key = valid ? layout_key(rp, r, long_min) : n_keys;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int leader = __ffs(peers) - 1;
+    int b = 0;
+    if (valid && lane == leader) {
+      b = run[key];
+      run[key] = b + __popc(peers);
+    }
+    b = __shfl_sync(0xffffffffu, b, leader);
+    if (valid) {
+      const int pos = start[(int64_t)key * n_tiles + blockIdx.x] + b + __popc(peers & ((1u << lane) - 1u));
+      perm[pos] = (int32_t)r;
+      iperm[r] = pos;
+    }
+    __syncwarp();
+  }
+}
+
+// 32 x the length of the first row of each chunk that is not long (rows are
+// sorted), and 0 at index n_chunks: scanned, the chunk offsets.
+__global__ void chunk_width_kernel(int64_t n, int64_t n_long, int64_t n_chunks, const int32_t* __restrict__ rp,
+                                   const int32_t* __restrict__ perm, int64_t* __restrict__ width) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c <= n_chunks;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    int64_t w = 0;
+    const int64_t i0 = max(c * 32, n_long);
+    if (c < n_chunks && i0 < min(n, c * 32 + 32)) {
+      const int32_t r = perm[i0];
+      w = 32 * (int64_t)(rp[r + 1] - rp[r]);
+    }
+    width[c] = w;
+  }
+}
+
+__global__ void long_len_kernel(int64_t n_long, const int32_t* __restrict__ perm, const int32_t* __restrict__ rp,
+                                int32_t* __restrict__ len) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_long; i += (int64_t)gridDim.x * blockDim.x)
+    len[i] = rp[perm[i] + 1] - rp[perm[i]];
+}
+
+__global__ void iperm_set_kernel(int64_t count, const int32_t* __restrict__ perm, int32_t* __restrict__ iperm) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+    iperm[perm[i]] = (int32_t)i;
+}
+
+// The long-row CSR in the sorted basis: block i copies long row i (columns
+// through iperm; values as 1 or 2 doubles per entry).
+template <bool REAL>
+__global__ void long_fill_kernel(int64_t n_long, const int32_t* __restrict__ perm, const int32_t* __restrict__ rp,
+                                 const int32_t* __restrict__ ci, const double2* __restrict__ v,
+                                 const int32_t* __restrict__ iperm, const int64_t* __restrict__ lp,
+                                 int32_t* __restrict__ lcol, double* __restrict__ lval) {
+  for (int64_t i = blockIdx.x; i < n_long; i += gridDim.x) {
+    const int32_t r = perm[i];
+    const int64_t p0 = rp[r], len = rp[r + 1] - p0, q0 = lp[i];
+    for (int64_t k = threadIdx.x; k < len; k += blockDim.x) {
+      lcol[q0 + k] = iperm[ci[p0 + k]];
+      const double2 x = v[p0 + k];
+      if (REAL) {
+        lval[q0 + k] = x.x;
+      } else {
+        lval[2 * (q0 + k)] = x.x;
+        lval[2 * (q0 + k) + 1] = x.y;
       }
     }
   }
@@ -330,11 +542,7 @@ void free_matrix(te_matrix_s* M) {
   cudaFree(M->sell.long_ptr);
   cudaFree(M->sell.long_col);
   cudaFree(M->sell.long_val);
-  cudaFree(M->sell.fix_val);
-  cudaFree(M->sell.fix_val4);
-  cudaFree(M->sell.fix_warp_chunk);
-  cudaFree(M->sell.fix_pk);
-  cudaFree(M->sell.fix_table);
+  te_sell_free_fixed(M->sell);
   delete M;
 }
 
@@ -351,6 +559,18 @@ int upload(T** dst, const T* src, size_t count) {
 // (real) or 4 (complex) FMAs per slot, the SpMV epilogues about 8 per row).
 // Uploads chunk_off, perm, iperm and warp_chunk; returns perm, iperm and the
 // offsets for filling col/val.
+// The static warp schedule of the FP64 SELL kernels from the host chunk
+// offsets; uploads warp_chunk.
+int sell_schedule(TeSell& S, const std::vector<int64_t>& off, bool real) {
+  const int bps = std::min(te_sell_blocks_per_sm(real),
+                           te_kernel_blocks_per_sm(real ? (const void*)sell_spmv_kernel<true, 1>
+                                                        : (const void*)sell_spmv_kernel<false, 1>,
+                                                   TE_THREADS, 0));
+  std::vector<int32_t> wc;
+  te_sell_schedule(off, S.n_chunks, bps, real, S.grid, S.saturated, wc);
+  return upload(&S.warp_chunk, wc.data(), wc.size());
+}
+
 int sell_layout(te_matrix_s* M, const std::vector<int32_t>& rp, bool real, std::vector<int32_t>& perm,
                 std::vector<int32_t>& iperm, std::vector<int64_t>& off) {
   const int64_t n = M->n_rows;
@@ -388,13 +608,105 @@ int sell_layout(te_matrix_s* M, const std::vector<int32_t>& rp, bool real, std::
   if ((rc = upload(&S.chunk_off, off.data(), off.size())) != TE_OK) return rc;
   if ((rc = upload(&S.perm, perm.data(), perm.size())) != TE_OK) return rc;
   if ((rc = upload(&S.iperm, iperm.data(), iperm.size())) != TE_OK) return rc;
-  const int bps = std::min(te_sell_blocks_per_sm(real),
-                           te_kernel_blocks_per_sm(real ? (const void*)sell_spmv_kernel<true, 1>
-                                                        : (const void*)sell_spmv_kernel<false, 1>,
-                                                   TE_THREADS, 0));
-  std::vector<int32_t> wc;
-  te_sell_schedule(off, S.n_chunks, bps, real, S.grid, S.saturated, wc);
-  return upload(&S.warp_chunk, wc.data(), wc.size());
+  return sell_schedule(S, off, real);
+}
+
+// The SELL order of a device CSR without a host copy of its row pointers:
+// the same order as sell_layout (stable by length, longest first, long rows
+// leading), from a counting sort on the device; the few long rows are
+// ordered on the host.  Sets perm, iperm, n_long, chunk_off, slots and the
+// schedule.  TE_ERR_UNSUPPORTED (nothing set) when the key range (the long-row
+// threshold) is too wide for the sort's shared-memory counters.
+int sell_layout_device(te_matrix_s* M, const int32_t* d_rp, bool real) {
+  const int64_t n = M->n_rows, nnz = M->nnz;
+  TeSell& S = M->sell;
+  const int64_t long_min = std::max<int64_t>(1024, 32 * ((nnz + n - 1) / std::max<int64_t>(n, 1)));
+  const int64_t n_tiles = (n + kLayoutTile - 1) / kLayoutTile;
+  if (long_min + 2 > 8192 || (long_min + 2) * n_tiles > ((int64_t)1 << 27)) return TE_ERR_UNSUPPORTED;
+  const int n_keys = (int)long_min + 2;
+  S.n = n;
+  S.n_chunks = (n + 31) / 32;
+  int32_t *cnt = nullptr, *d_len = nullptr;
+  auto done = [&](int rc) {
+    cudaFree(cnt);
+    cudaFree(d_len);
+    return rc;
+  };
+  int rc = te_cuda_check(cudaMalloc(&cnt, sizeof(int32_t) * n_keys * n_tiles), "layout");
+  if (rc == TE_OK) rc = te_cuda_check(cudaMalloc(&S.perm, sizeof(int32_t) * n), "layout");
+  if (rc == TE_OK) rc = te_cuda_check(cudaMalloc(&S.iperm, sizeof(int32_t) * n), "layout");
+  if (rc == TE_OK) rc = te_cuda_check(cudaMalloc(&S.chunk_off, sizeof(int64_t) * (S.n_chunks + 1)), "layout");
+  if (rc != TE_OK) return done(rc);
+  layout_hist_kernel<<<(unsigned)n_tiles, 256, sizeof(int) * n_keys>>>(n, d_rp, (int)long_min, n_keys, n_tiles, cnt);
+  if ((rc = scan_exclusive<int32_t>(cnt, cnt, n_keys * n_tiles)) != TE_OK) return done(rc);
+  layout_scatter_kernel<<<(unsigned)n_tiles, 32, sizeof(int) * n_keys>>>(n, d_rp, (int)long_min, n_keys, n_tiles,
+                                                                         cnt, S.perm, S.iperm);
+  int32_t n_long = 0;  // the rows of key 0: where key 1 starts
+  if ((rc = te_cuda_check(cudaMemcpy(&n_long, cnt + n_tiles, sizeof(int32_t), cudaMemcpyDeviceToHost), "layout")) !=
+      TE_OK)
+    return done(rc);
+  S.n_long = n_long;
+  if (n_long > 0) {  // long rows: by length, longest first, ties in row order
+    std::vector<int32_t> rows(n_long), len(n_long), sorted(n_long);
+    if ((rc = te_cuda_check(cudaMalloc(&d_len, sizeof(int32_t) * n_long), "layout")) != TE_OK) return done(rc);
+    long_len_kernel<<<te_grid_fit((const void*)long_len_kernel, n_long, TE_THREADS), TE_THREADS>>>(n_long, S.perm,
+                                                                                                   d_rp, d_len);
+    if ((rc = te_cuda_check(cudaMemcpy(rows.data(), S.perm, sizeof(int32_t) * n_long, cudaMemcpyDeviceToHost),
+                            "layout")) != TE_OK ||
+        (rc = te_cuda_check(cudaMemcpy(len.data(), d_len, sizeof(int32_t) * n_long, cudaMemcpyDeviceToHost),
+                            "layout")) != TE_OK)
+      return done(rc);
+    std::vector<int32_t> order(n_long);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return len[a] > len[b]; });
+    for (int32_t i = 0; i < n_long; ++i) sorted[i] = rows[order[i]];
+    if ((rc = te_cuda_check(cudaMemcpy(S.perm, sorted.data(), sizeof(int32_t) * n_long, cudaMemcpyHostToDevice),
+                            "layout")) != TE_OK)
+      return done(rc);
+    iperm_set_kernel<<<te_grid_fit((const void*)iperm_set_kernel, n_long, TE_THREADS), TE_THREADS>>>(n_long, S.perm,
+                                                                                                     S.iperm);
+  }
+  chunk_width_kernel<<<te_grid_fit((const void*)chunk_width_kernel, S.n_chunks + 1, TE_THREADS), TE_THREADS>>>(
+      n, S.n_long, S.n_chunks, d_rp, S.perm, S.chunk_off);
+  if ((rc = scan_exclusive<int64_t>(S.chunk_off, S.chunk_off, S.n_chunks + 1)) != TE_OK) return done(rc);
+  std::vector<int64_t> off(S.n_chunks + 1);
+  if ((rc = te_cuda_check(
+           cudaMemcpy(off.data(), S.chunk_off, sizeof(int64_t) * (S.n_chunks + 1), cudaMemcpyDeviceToHost),
+           "layout")) != TE_OK)
+    return done(rc);
+  S.slots = off[S.n_chunks];
+  return done(sell_schedule(S, off, real));
+}
+
+// The long-row CSR in the sorted basis from the device CSR (perm and iperm
+// final): one device pass after a host prefix over the long rows' lengths.
+int long_rows_device(te_matrix_s* M, const int32_t* d_rp, const int32_t* d_ci, const double2* d_v, bool real) {
+  TeSell& S = M->sell;
+  const int64_t nl = S.n_long;
+  if (nl == 0) return TE_OK;
+  int32_t* d_len = nullptr;
+  std::vector<int32_t> len(nl);
+  int rc = te_cuda_check(cudaMalloc(&d_len, sizeof(int32_t) * nl), "long rows");
+  if (rc != TE_OK) return rc;
+  long_len_kernel<<<te_grid_fit((const void*)long_len_kernel, nl, TE_THREADS), TE_THREADS>>>(nl, S.perm, d_rp, d_len);
+  rc = te_cuda_check(cudaMemcpy(len.data(), d_len, sizeof(int32_t) * nl, cudaMemcpyDeviceToHost), "long rows");
+  cudaFree(d_len);
+  if (rc != TE_OK) return rc;
+  std::vector<int64_t> lp(nl + 1, 0);
+  for (int64_t i = 0; i < nl; ++i) lp[i + 1] = lp[i] + len[i];
+  if ((rc = upload(&S.long_ptr, lp.data(), lp.size())) != TE_OK) return rc;
+  const int64_t ne = std::max<int64_t>(lp[nl], 1);
+  if ((rc = te_cuda_check(cudaMalloc(&S.long_col, sizeof(int32_t) * ne), "long rows")) != TE_OK ||
+      (rc = te_cuda_check(cudaMalloc(&S.long_val, sizeof(double) * (real ? 1 : 2) * ne), "long rows")) != TE_OK)
+    return rc;
+  const unsigned grid = (unsigned)std::min<int64_t>(nl, 4096);
+  if (real)
+    long_fill_kernel<true><<<grid, TE_THREADS>>>(nl, S.perm, d_rp, d_ci, d_v, S.iperm, S.long_ptr, S.long_col,
+                                                 S.long_val);
+  else
+    long_fill_kernel<false><<<grid, TE_THREADS>>>(nl, S.perm, d_rp, d_ci, d_v, S.iperm, S.long_ptr, S.long_col,
+                                                  S.long_val);
+  return te_cuda_check(cudaGetLastError(), "long rows");
 }
 
 // The long-row CSR (sorted basis) from host copies of the original CSR.
@@ -528,8 +840,7 @@ int finish_create(int64_t n_rows, int64_t n_cols, const std::vector<int32_t>& rp
 // The 1-norm is the maximum column sum of |a| accumulated in 64-bit fixed
 // point (relative resolution ~1e-12 of the largest entry), so it does not
 // depend on the order of the device atomics.
-int build_matrix_device(te_matrix_s* M, const std::vector<int32_t>& rp_host, int32_t* d_rp, int32_t* d_ci,
-                        double2* d_v, double norm1_given) {
+int build_matrix_device(te_matrix_s* M, int32_t* d_rp, int32_t* d_ci, double2* d_v, double norm1_given) {
   const int64_t n = M->n_rows, nnz = M->nnz;
   M->row_ptr = d_rp;
   M->col = d_ci;
@@ -604,10 +915,16 @@ int build_matrix_device(te_matrix_s* M, const std::vector<int32_t>& rp_host, int
   }
   int rc = TE_OK;
   if (M->n_rows == M->n_cols) {
-    std::vector<int32_t> perm, iperm;
-    std::vector<int64_t> off;
-    rc = sell_layout(M, rp_host, real, perm, iperm, off);
     TeSell& S = M->sell;
+    rc = sell_layout_device(M, d_rp, real);
+    if (rc == TE_ERR_UNSUPPORTED) {  // a wide key range: the host sort from a copy of the row pointers
+      std::vector<int32_t> rp_host(n + 1), perm, iperm;
+      std::vector<int64_t> off;
+      rc = te_cuda_check(cudaMemcpy(rp_host.data(), d_rp, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost),
+                         "layout");
+      if (rc == TE_OK) rc = sell_layout(M, rp_host, real, perm, iperm, off);
+    }
+    if (rc == TE_OK) rc = long_rows_device(M, d_rp, d_ci, d_v, real);
     if (rc == TE_OK) rc = te_cuda_check(cudaMalloc(&S.col, sizeof(int32_t) * std::max<int64_t>(S.slots, 1)), "sell");
     if (rc == TE_OK)
       rc = te_cuda_check(cudaMalloc(&S.val, sizeof(double) * (real ? 1 : 2) * std::max<int64_t>(S.slots, 1)), "sell");
@@ -623,35 +940,6 @@ int build_matrix_device(te_matrix_s* M, const std::vector<int32_t>& rp_host, int
     }
   }
   if (rc == TE_OK) rc = te_cuda_check(cudaDeviceSynchronize(), "device build");
-  if (rc == TE_OK && M->n_rows == M->n_cols && M->sell.n_long > 0) {
-    // the long rows are few: copy their entries to the host and build their CSR there
-    TeSell& S = M->sell;
-    std::vector<int32_t> perm(n), iperm(n);
-    rc = te_cuda_check(cudaMemcpy(perm.data(), S.perm, sizeof(int32_t) * n, cudaMemcpyDeviceToHost), "long rows");
-    if (rc == TE_OK)
-      rc = te_cuda_check(cudaMemcpy(iperm.data(), S.iperm, sizeof(int32_t) * n, cudaMemcpyDeviceToHost), "long rows");
-    std::vector<int64_t> lp(S.n_long + 1, 0);
-    std::vector<int32_t> lc;
-    std::vector<double> lv;
-    for (int64_t i = 0; i < S.n_long && rc == TE_OK; ++i) {
-      const int32_t r = perm[i];
-      const int64_t b = rp_host[r], len = rp_host[r + 1] - rp_host[r];
-      std::vector<int32_t> c(len);
-      std::vector<double2> v(len);
-      rc = te_cuda_check(cudaMemcpy(c.data(), d_ci + b, sizeof(int32_t) * len, cudaMemcpyDeviceToHost), "long rows");
-      if (rc == TE_OK)
-        rc = te_cuda_check(cudaMemcpy(v.data(), d_v + b, sizeof(double2) * len, cudaMemcpyDeviceToHost), "long rows");
-      for (int64_t k = 0; k < len && rc == TE_OK; ++k) {
-        lc.push_back(iperm[c[k]]);
-        lv.push_back(v[k].x);
-        if (!real) lv.push_back(v[k].y);
-      }
-      lp[i + 1] = (int64_t)lc.size();
-    }
-    if (rc == TE_OK) rc = upload(&S.long_ptr, lp.data(), lp.size());
-    if (rc == TE_OK) rc = upload(&S.long_col, lc.data(), lc.size());
-    if (rc == TE_OK) rc = upload(&S.long_val, lv.data(), lv.size());
-  }
   if (real) cudaFree(d_v);
   cleanup();
   return rc;
@@ -661,14 +949,14 @@ int build_matrix_device(te_matrix_s* M, const std::vector<int32_t>& rp_host, int
 
 // Adopt a device CSR (see build_matrix_device); used by the device-side
 // workload generators.  On failure the buffers are freed.
-int te_matrix_adopt_device_csr(int64_t n_rows, int64_t n_cols, const std::vector<int32_t>& rp_host, int32_t* d_rp,
-                               int32_t* d_ci, double2* d_v, te_matrix* out, double norm1) {
+int te_matrix_adopt_device_csr(int64_t n_rows, int64_t n_cols, int64_t nnz, int32_t* d_rp, int32_t* d_ci,
+                               double2* d_v, te_matrix* out, double norm1) {
   te_matrix_s* M = new te_matrix_s();
   cudaGetDevice(&M->device);
   M->n_rows = n_rows;
   M->n_cols = n_cols;
-  M->nnz = rp_host[n_rows];
-  int rc = build_matrix_device(M, rp_host, d_rp, d_ci, d_v, norm1);
+  M->nnz = nnz;
+  int rc = build_matrix_device(M, d_rp, d_ci, d_v, norm1);
   if (rc != TE_OK) {
     free_matrix(M);
     return rc;
@@ -788,14 +1076,11 @@ int create_coo_device(int64_t n_rows, int64_t n_cols, int64_t nnz, const uint64_
       te_cuda_check(cudaMemset(d_cnt, 0, sizeof(int32_t) * n_rows), "coo") != TE_OK)
     return fail(TE_ERR_CUDA);
   row_count_kernel<<<te_grid_fit((const void*)row_count_kernel, nnz, TE_THREADS), TE_THREADS>>>(nnz, d_row, d_cnt);
-  std::vector<int32_t> cnt(n_rows), rp(n_rows + 1, 0);
-  if (te_cuda_check(cudaMemcpy(cnt.data(), d_cnt, sizeof(int32_t) * n_rows, cudaMemcpyDeviceToHost), "coo") != TE_OK)
-    return fail(TE_ERR_CUDA);
-  for (int64_t r = 0; r < n_rows; ++r) rp[r + 1] = rp[r] + cnt[r];
+  const int32_t nnz32 = (int32_t)nnz;
   if (te_cuda_check(cudaMalloc(&d_rp, sizeof(int32_t) * (n_rows + 1)), "coo") != TE_OK ||
       te_cuda_check(cudaMalloc(&d_ci, sizeof(int32_t) * nnz), "coo") != TE_OK ||
-      te_cuda_check(cudaMemcpy(d_rp, rp.data(), sizeof(int32_t) * (n_rows + 1), cudaMemcpyHostToDevice), "coo") !=
-          TE_OK)
+      scan_exclusive<int32_t>(d_cnt, d_rp, n_rows) != TE_OK ||
+      te_cuda_check(cudaMemcpy(d_rp + n_rows, &nnz32, sizeof(int32_t), cudaMemcpyHostToDevice), "coo") != TE_OK)
     return fail(TE_ERR_CUDA);
   narrow_index_kernel<<<te_grid_fit((const void*)narrow_index_kernel, nnz, TE_THREADS), TE_THREADS>>>(nnz, d_col,
                                                                                                    d_ci);
@@ -814,7 +1099,7 @@ int create_coo_device(int64_t n_rows, int64_t n_cols, int64_t nnz, const uint64_
   }
   if (te_cuda_check(cudaDeviceSynchronize(), "coo") != TE_OK) return fail(TE_ERR_CUDA);
   release();
-  return te_matrix_adopt_device_csr(n_rows, n_cols, rp, d_rp, d_ci, d_v, out, 0.0);
+  return te_matrix_adopt_device_csr(n_rows, n_cols, nnz, d_rp, d_ci, d_v, out, 0.0);
 }
 
 // Below this many entries the host conversion is as fast as the device one.
@@ -938,7 +1223,7 @@ extern "C" int te_matrix_create_csr_device(int64_t n_rows, int64_t n_cols, int64
                                                                                                     d_v);
     }
   }
-  return te_matrix_adopt_device_csr(n_rows, n_cols, rp, d_rp, d_ci, d_v, out, NAN);
+  return te_matrix_adopt_device_csr(n_rows, n_cols, nnz, d_rp, d_ci, d_v, out, NAN);
 }
 
 extern "C" int te_matrix_download_csr(te_matrix A, int32_t* row_ptr, int32_t* col_idx, double* values) {

@@ -378,7 +378,7 @@ extern "C" int te_model_create_device(int n_particles, int n_modes, int quant, c
   d_terms = nullptr;
   d_cnt = nullptr;
   d_norm = nullptr;
-  rc = te_matrix_adopt_device_csr(n, n, rp, d_rp, d_col, d_val, out, norm1);
+  rc = te_matrix_adopt_device_csr(n, n, rp[n], d_rp, d_col, d_val, out, norm1);
   if (rc != TE_OK) return rc;  // the matrix freed the arrays
   if (dim_out) *dim_out = n;
   return TE_OK;

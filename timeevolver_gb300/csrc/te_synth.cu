@@ -352,7 +352,7 @@ extern "C" int te_matrix_create_zipf(int64_t n, double exponent, int32_t min_len
   cudaFree(d_sval.release());
   cudaFree(d_stag.release());
   te_matrix H = nullptr;
-  if ((rc = te_matrix_adopt_device_csr(n, n, rph, d_rph, d_hcol, d_hval, &H, NAN)) != TE_OK) return rc;
+  if ((rc = te_matrix_adopt_device_csr(n, n, rph[n], d_rph, d_hcol, d_hval, &H, NAN)) != TE_OK) return rc;
 
   // spectral-norm estimate by power iteration, then H /= estimate
   DevBuf<double2> x, y;

@@ -34,8 +34,13 @@ def _expected_csr(row, col, val):
     return np.cumsum(rp), col[order], val[order]
 
 
-@pytest.mark.parametrize("sort_rows", [True, False])
-def test_coo_upload(te_gpu, sort_rows):
+@pytest.mark.parametrize("sort_rows,copy_path", [(True, False), (True, True), (False, False)])
+def test_coo_upload(te_gpu, sort_rows, copy_path, monkeypatch):
+    """Row-sorted COO: read by a kernel straight from host memory where the
+    device accesses pageable memory (Grace), else (TE_COO_COPY=1 here) copied
+    first; unsorted COO: converted on the host."""
+    if copy_path:
+        monkeypatch.setenv("TE_COO_COPY", "1")
     row, col, val = _coo(1, sort_rows)
     M = te_gpu.Matrix(N, row, col, val)
     rp, ci, v = M.to_csr()
@@ -60,12 +65,37 @@ def test_coo_upload_real_and_diagonal(te_gpu):
     assert inf["diagonal"] and inf["real"] and inf["norm1"] == 2.0
 
 
-def test_coo_upload_rejects_out_of_range(te_gpu):
+@pytest.mark.parametrize("copy_path", [False, True])
+def test_coo_upload_rejects_out_of_range(te_gpu, copy_path, monkeypatch):
+    if copy_path:
+        monkeypatch.setenv("TE_COO_COPY", "1")
     row, col, val = _coo(4, True)
     col = col.copy()
     col[123_456] = N
     with pytest.raises(RuntimeError, match="entry 123456 out of range"):
         te_gpu.Matrix(N, row, col, val)
+    row = row.copy()
+    row[200_001] = N + 5
+    with pytest.raises(RuntimeError, match="entry 123456 out of range"):
+        te_gpu.Matrix(N, row, col, val)
+
+
+@pytest.mark.parametrize("copy_path", [False, True])
+def test_coo_upload_empty_rows(te_gpu, copy_path, monkeypatch):
+    """Row pointers across empty rows, before the first and after the last
+    stored row (the direct read derives them from the row boundaries)."""
+    if copy_path:
+        monkeypatch.setenv("TE_COO_COPY", "1")
+    rng = np.random.default_rng(8)
+    rows = np.sort(rng.choice(np.arange(5, N - 7), size=N // 3, replace=False))
+    row = np.repeat(rows, 5).astype(np.int64)
+    col = rng.integers(0, N, size=len(row)).astype(np.int64)
+    val = (rng.standard_normal(len(row)) + 1j * rng.standard_normal(len(row))).astype(np.complex128)
+    assert len(val) >= 1 << 18
+    M = te_gpu.Matrix(N, row, col, val)
+    rp, ci, v = M.to_csr()
+    rp0, ci0, v0 = _expected_csr(row, col, val)
+    assert np.array_equal(rp, rp0) and np.array_equal(ci, ci0) and np.array_equal(v, v0)
 
 
 def _hub_matrix(n, hubs, hub_len, seed, complex_values=True):

@@ -15,7 +15,9 @@
 #include <atomic>
 #include <cmath>
 #include <complex>
+#include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <mutex>
 #include <numeric>
@@ -450,6 +452,46 @@ __global__ void coo_scan_kernel(int64_t nnz, uint64_t n_rows, uint64_t n_cols, c
       atomicMin(first_bad, (unsigned long long)i);
     }
     if (i > 0 && row[i - 1] > r) f |= TE_COO_UNSORTED;
+  }
+  if (f) atomicOr(flags, f);
+}
+
+// Row-sorted COO read straight from host memory, on devices that access
+// pageable memory through the host's page tables (Grace): the checks of
+// coo_scan_kernel, the columns narrowed to int32, the values, and the row
+// pointers from the row boundaries (rp[q] = the first entry of a row >= q),
+// in one pass over the host arrays.  rp is valid when no flag is raised.
+__global__ void __launch_bounds__(TE_THREADS) coo_ingest_kernel(int64_t nnz, uint64_t n_rows, uint64_t n_cols,
+                                                                const uint64_t* __restrict__ row,
+                                                                const uint64_t* __restrict__ col,
+                                                                const double* __restrict__ val,
+                                                                int32_t* __restrict__ rp, int32_t* __restrict__ ci,
+                                                                double2* __restrict__ v, unsigned int* flags,
+                                                                unsigned long long* first_bad) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  unsigned int f = 0;
+  for (int64_t base = ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32; base < nnz;
+       base += warps * 32) {
+    const int64_t i = base + lane;
+    const bool live = i < nnz;
+    const uint64_t r = live ? row[i] : 0, c = live ? col[i] : 0;
+    uint64_t prev = __shfl_up_sync(0xffffffffu, r, 1);
+    if (lane == 0 && i > 0 && live) prev = row[i - 1];
+    if (!live) continue;
+    if (r >= n_rows || c >= n_cols) {
+      f |= TE_COO_BAD;
+      atomicMin(first_bad, (unsigned long long)i);
+      continue;
+    }
+    if (i > 0 && prev > r) f |= TE_COO_UNSORTED;
+    ci[i] = (int32_t)c;
+    v[i] = make_double2(val[2 * i], val[2 * i + 1]);
+    // rows (prev, r] start here (rows 0..r for the first entry)
+    const uint64_t q0 = i == 0 ? 0 : prev + 1;
+    for (uint64_t q = q0; q <= r; ++q) rp[q] = (int32_t)i;
+    if (i == nnz - 1)
+      for (uint64_t q = r + 1; q <= n_rows; ++q) rp[q] = (int32_t)nnz;
   }
   if (f) atomicOr(flags, f);
 }
@@ -1025,7 +1067,7 @@ int create_coo_host(int64_t n_rows, int64_t n_cols, int64_t nnz, const uint64_t*
 // from per-row counts, and the layout is built by kernels.  Returns
 // TE_ERR_UNSUPPORTED (nothing built, no error set) for unsorted input.
 int create_coo_device(int64_t n_rows, int64_t n_cols, int64_t nnz, const uint64_t* row_index, const uint64_t* columns,
-                      const double* values, double* norm1_gpu, te_matrix* out) {
+                      const double* values, double* norm1_gpu, te_matrix* out, const std::function<void()>& host_done) {
   *norm1_gpu = std::nan("");
   uint64_t *d_row = nullptr, *d_col = nullptr;
   double2* d_v = nullptr;
@@ -1046,44 +1088,60 @@ int create_coo_device(int64_t n_rows, int64_t n_cols, int64_t nnz, const uint64_
     cudaFree(d_ci);
     return rc;
   };
-  if (te_cuda_check(cudaMalloc(&d_row, sizeof(uint64_t) * nnz), "coo") != TE_OK ||
-      te_cuda_check(cudaMalloc(&d_col, sizeof(uint64_t) * nnz), "coo") != TE_OK ||
-      te_cuda_check(cudaMalloc(&d_v, sizeof(double2) * nnz), "coo") != TE_OK ||
+  int dev = 0, pageable = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) pageable = 0;
+  const char* copy_env = std::getenv("TE_COO_COPY");  // 1: the staging-copy path everywhere
+  if (copy_env && copy_env[0] == '1') pageable = 0;
+  if (te_cuda_check(cudaMalloc(&d_v, sizeof(double2) * nnz), "coo") != TE_OK ||
+      te_cuda_check(cudaMalloc(&d_rp, sizeof(int32_t) * (n_rows + 1)), "coo") != TE_OK ||
+      te_cuda_check(cudaMalloc(&d_ci, sizeof(int32_t) * nnz), "coo") != TE_OK ||
       te_cuda_check(cudaMalloc(&d_flags, sizeof(unsigned int)), "coo") != TE_OK ||
       te_cuda_check(cudaMalloc(&d_bad, sizeof(unsigned long long)), "coo") != TE_OK)
     return fail(TE_ERR_CUDA);
   const unsigned long long none = ~0ull;
-  if (te_cuda_check(cudaMemcpy(d_row, row_index, sizeof(uint64_t) * nnz, cudaMemcpyHostToDevice), "coo") != TE_OK ||
-      te_cuda_check(cudaMemcpy(d_col, columns, sizeof(uint64_t) * nnz, cudaMemcpyHostToDevice), "coo") != TE_OK ||
-      te_cuda_check(cudaMemcpy(d_v, values, sizeof(double2) * nnz, cudaMemcpyHostToDevice), "coo") != TE_OK ||
-      te_cuda_check(cudaMemset(d_flags, 0, sizeof(unsigned int)), "coo") != TE_OK ||
+  if (te_cuda_check(cudaMemset(d_flags, 0, sizeof(unsigned int)), "coo") != TE_OK ||
       te_cuda_check(cudaMemcpy(d_bad, &none, sizeof(none), cudaMemcpyHostToDevice), "coo") != TE_OK)
     return fail(TE_ERR_CUDA);
-  coo_scan_kernel<<<te_grid_fit((const void*)coo_scan_kernel, nnz, TE_THREADS), TE_THREADS>>>(
-      nnz, (uint64_t)n_rows, (uint64_t)n_cols, d_row, d_col, d_flags, d_bad);
+  if (pageable == 1) {
+    // the kernel reads the host arrays itself: one pass, no staging copies
+    coo_ingest_kernel<<<te_grid_fit((const void*)coo_ingest_kernel, nnz, TE_THREADS), TE_THREADS>>>(
+        nnz, (uint64_t)n_rows, (uint64_t)n_cols, row_index, columns, values, d_rp, d_ci, d_v, d_flags, d_bad);
+  } else {
+    if (te_cuda_check(cudaMalloc(&d_row, sizeof(uint64_t) * nnz), "coo") != TE_OK ||
+        te_cuda_check(cudaMalloc(&d_col, sizeof(uint64_t) * nnz), "coo") != TE_OK)
+      return fail(TE_ERR_CUDA);
+    if (te_cuda_check(cudaMemcpy(d_row, row_index, sizeof(uint64_t) * nnz, cudaMemcpyHostToDevice), "coo") != TE_OK ||
+        te_cuda_check(cudaMemcpy(d_col, columns, sizeof(uint64_t) * nnz, cudaMemcpyHostToDevice), "coo") != TE_OK ||
+        te_cuda_check(cudaMemcpy(d_v, values, sizeof(double2) * nnz, cudaMemcpyHostToDevice), "coo") != TE_OK)
+      return fail(TE_ERR_CUDA);
+    coo_scan_kernel<<<te_grid_fit((const void*)coo_scan_kernel, nnz, TE_THREADS), TE_THREADS>>>(
+        nnz, (uint64_t)n_rows, (uint64_t)n_cols, d_row, d_col, d_flags, d_bad);
+  }
   unsigned int flags = 0;
   unsigned long long bad = 0;
   if (te_cuda_check(cudaMemcpy(&flags, d_flags, sizeof(flags), cudaMemcpyDeviceToHost), "coo") != TE_OK ||
       te_cuda_check(cudaMemcpy(&bad, d_bad, sizeof(bad), cudaMemcpyDeviceToHost), "coo") != TE_OK)
     return fail(TE_ERR_CUDA);
+  host_done();  // the device is done with the host arrays
   if (flags & TE_COO_BAD) {
     te_set_error("te_matrix_create_coo: entry %lld out of range", (long long)bad);
     return fail(TE_ERR_INVALID_ARG);
   }
   if (flags & TE_COO_UNSORTED) return fail(TE_ERR_UNSUPPORTED);
-  // row pointers from the per-row counts (rows are sorted, so CSR order = input order)
-  if (te_cuda_check(cudaMalloc(&d_cnt, sizeof(int32_t) * n_rows), "coo") != TE_OK ||
-      te_cuda_check(cudaMemset(d_cnt, 0, sizeof(int32_t) * n_rows), "coo") != TE_OK)
-    return fail(TE_ERR_CUDA);
-  row_count_kernel<<<te_grid_fit((const void*)row_count_kernel, nnz, TE_THREADS), TE_THREADS>>>(nnz, d_row, d_cnt);
-  const int32_t nnz32 = (int32_t)nnz;
-  if (te_cuda_check(cudaMalloc(&d_rp, sizeof(int32_t) * (n_rows + 1)), "coo") != TE_OK ||
-      te_cuda_check(cudaMalloc(&d_ci, sizeof(int32_t) * nnz), "coo") != TE_OK ||
-      scan_exclusive<int32_t>(d_cnt, d_rp, n_rows) != TE_OK ||
-      te_cuda_check(cudaMemcpy(d_rp + n_rows, &nnz32, sizeof(int32_t), cudaMemcpyHostToDevice), "coo") != TE_OK)
-    return fail(TE_ERR_CUDA);
-  narrow_index_kernel<<<te_grid_fit((const void*)narrow_index_kernel, nnz, TE_THREADS), TE_THREADS>>>(nnz, d_col,
-                                                                                                   d_ci);
+  if (pageable != 1) {
+    // row pointers from the per-row counts (rows are sorted, so CSR order = input order)
+    const int32_t nnz32 = (int32_t)nnz;
+    if (te_cuda_check(cudaMalloc(&d_cnt, sizeof(int32_t) * n_rows), "coo") != TE_OK ||
+        te_cuda_check(cudaMemset(d_cnt, 0, sizeof(int32_t) * n_rows), "coo") != TE_OK)
+      return fail(TE_ERR_CUDA);
+    row_count_kernel<<<te_grid_fit((const void*)row_count_kernel, nnz, TE_THREADS), TE_THREADS>>>(nnz, d_row, d_cnt);
+    if (scan_exclusive<int32_t>(d_cnt, d_rp, n_rows) != TE_OK ||
+        te_cuda_check(cudaMemcpy(d_rp + n_rows, &nnz32, sizeof(int32_t), cudaMemcpyHostToDevice), "coo") != TE_OK)
+      return fail(TE_ERR_CUDA);
+    narrow_index_kernel<<<te_grid_fit((const void*)narrow_index_kernel, nnz, TE_THREADS), TE_THREADS>>>(nnz, d_col,
+                                                                                                     d_ci);
+  }
   if (n_rows == n_cols) {  // the reference's 1-norm on the device where |H| is symmetric and real
     if (te_cuda_check(cudaMemset(d_flags, 0, sizeof(unsigned int)), "coo") != TE_OK ||
         te_cuda_check(cudaMemset(d_bad, 0, sizeof(unsigned long long)), "coo") != TE_OK)
@@ -1120,15 +1178,23 @@ extern "C" int te_matrix_create_coo(int64_t n_rows, int64_t n_cols, int64_t nnz,
   if (nnz < kDeviceCooMinEntries)
     return create_coo_host(n_rows, n_cols, nnz, row_index, columns, values, coo_norm1(n_cols, nnz, columns, values),
                            out);
-  // the 1-norm on host threads while the device converts the layout; the
-  // device computes it itself where |H| is real and symmetric (then the host
-  // threads are called off)
+  // the 1-norm on host threads while the device builds the layout, started
+  // once the device has read the host arrays (the two would share host
+  // memory bandwidth); the device computes it itself where |H| is real and
+  // symmetric (then the host threads are called off)
   double norm1 = 0.0, norm1_gpu = std::nan("");
   std::atomic<bool> cancel(false);
-  std::thread norm_thread([&]() { norm1 = coo_norm1(n_cols, nnz, columns, values, &cancel); });
-  int rc = create_coo_device(n_rows, n_cols, nnz, row_index, columns, values, &norm1_gpu, out);
+  std::thread norm_thread;
+  auto start_norm = [&]() {
+    norm_thread = std::thread([&]() { norm1 = coo_norm1(n_cols, nnz, columns, values, &cancel); });
+  };
+  int rc = create_coo_device(n_rows, n_cols, nnz, row_index, columns, values, &norm1_gpu, out, start_norm);
   if (rc == TE_OK && !std::isnan(norm1_gpu)) cancel.store(true);
-  norm_thread.join();
+  if (norm_thread.joinable()) {
+    norm_thread.join();
+  } else if (rc == TE_ERR_UNSUPPORTED) {
+    norm1 = coo_norm1(n_cols, nnz, columns, values);
+  }
   if (rc == TE_OK) {
     (*out)->norm1 = std::isnan(norm1_gpu) ? norm1 : norm1_gpu;
     return TE_OK;

@@ -249,6 +249,8 @@ def run_gb300(args):
     e2e_times = []
     h2d = 32 * nnz + 32 * len(Oc[2]) + 16 * n
     d2h = 8 * (int(T_FINAL / SAMPLING) + 1) + 16 * n
+    if args.warmup > 0:  # one untimed call, as for the device-timed solves
+        te.evolve(Hc, v, T_FINAL, SAMPLING, [("sparse", Oc)], tol=TOL, m=M_KRYLOV, options=options)
     for _ in range(max(1, args.steps)):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -543,6 +545,8 @@ def run_zipf(args):
     ev.close()
     # end to end through the public call: start vector from the host, state back
     e2e = []
+    if args.warmup > 0:  # one untimed call, as for the device-timed solves
+        te.evolve(H, v, ZIPF_T, ZIPF_T, [], tol=TOL, m=M_KRYLOV, options=options)
     for _ in range(max(1, args.steps)):
         torch.cuda.synchronize()
         t0 = time.perf_counter()

@@ -79,7 +79,13 @@ int te_set_device(int device);
  * duplicates are kept (they add, as in the reference's COO loop).  A matrix
  * whose imaginary parts are all zero is stored with real values (same
  * results, half the value bytes and FP64 work).  Replaces smatrix(...) +
- * initialize() (matrixDataTypes.cpp:264-290, :352-396). */
+ * initialize() (matrixDataTypes.cpp:264-290, :352-396).
+ * A row-sorted COO of at least 2^18 entries (the order createMatrix produces)
+ * is converted on the device: where the device accesses pageable host memory
+ * (Grace hosts) one kernel reads the three arrays in place, elsewhere they are
+ * copied first (environment TE_COO_COPY=1 forces the copies everywhere).
+ * Other input is converted on the host.  The 1-norm is the reference's
+ * (column sums in entry order) either way. */
 int te_matrix_create_coo(int64_t n_rows, int64_t n_cols, int64_t nnz, const uint64_t* row_index,
                          const uint64_t* columns, const double* values, te_matrix* out);
 

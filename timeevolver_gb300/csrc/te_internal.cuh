@@ -197,6 +197,10 @@ struct te_matrix_s {
 // d_rp[n_rows].
 // norm1: the 1-norm if the caller computed it, NAN to accumulate it on the
 // device in fixed point.
+// out[i] = in[0] + ... + in[i - 1] for i < count, on the device (in == out
+// allowed); synchronous with the default stream.
+int te_scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t count);
+
 int te_matrix_adopt_device_csr(int64_t n_rows, int64_t n_cols, int64_t nnz, int32_t* d_rp, int32_t* d_ci,
                                double2* d_v, te_matrix* out, double norm1);
 

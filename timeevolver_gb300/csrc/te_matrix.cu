@@ -328,6 +328,10 @@ int scan_exclusive(const T* in, T* out, int64_t count) {
   return rc;
 }
 
+int te_scan_exclusive_i64(const int64_t* in, int64_t* out, int64_t count) {
+  return scan_exclusive<int64_t>(in, out, count);
+}
+
 // ------------------------------------------ SELL order on the device
 
 // Sort key of a row for the length-sorted SELL order: 0 for long rows (longer

@@ -182,6 +182,17 @@ __device__ int build_row(const Stages& st, const uint8_t* __restrict__ occ, int6
   return kept;
 }
 
+// counts (n) -> int64 (n + 1, last 0), for the row-pointer scan
+__global__ void widen_counts_kernel(int64_t n, const int32_t* __restrict__ cnt, int64_t* __restrict__ out) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j <= n; j += (int64_t)gridDim.x * blockDim.x)
+    out[j] = j < n ? cnt[j] : 0;
+}
+
+__global__ void narrow_rp_kernel(int64_t count, const int64_t* __restrict__ in, int32_t* __restrict__ out) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < count; j += (int64_t)gridDim.x * blockDim.x)
+    out[j] = (int32_t)in[j];
+}
+
 __global__ void row_count_model_kernel(Stages st, const uint8_t* __restrict__ occ, int64_t n,
                                        const DevTerm* __restrict__ terms, int n_terms, int32_t* __restrict__ count) {
   int32_t cols[TE_MODEL_MAX_TERMS];
@@ -348,23 +359,30 @@ extern "C" int te_model_create_device(int n_particles, int n_modes, int quant, c
   const Stages st = B.stages();
   const int g = te_grid_fit((const void*)row_count_model_kernel, n, 128);
   row_count_model_kernel<<<g, 128>>>(st, B.occ, n, d_terms, n_terms, d_cnt);
-  std::vector<int32_t> cnt(n), rp(n + 1, 0);
-  if (te_cuda_check(cudaMemcpy(cnt.data(), d_cnt, sizeof(int32_t) * n, cudaMemcpyDeviceToHost), "model") != TE_OK)
-    return fail(TE_ERR_CUDA);
+  // row pointers: a 64-bit scan of the counts on the device (the total must
+  // stay below 2^31), narrowed to int32
+  int64_t* d_rp64 = nullptr;
   int64_t nnz = 0;
-  for (int64_t j = 0; j < n; ++j) {
-    nnz += cnt[j];
-    if (nnz >= ((int64_t)1 << 31)) {
-      te_set_error("te_model_create_device: more than 2^31 entries");
-      return fail(TE_ERR_UNSUPPORTED);
-    }
-    rp[j + 1] = (int32_t)nnz;
+  if (te_cuda_check(cudaMalloc(&d_rp64, sizeof(int64_t) * (n + 1)), "model") != TE_OK) return fail(TE_ERR_CUDA);
+  widen_counts_kernel<<<te_grid_fit((const void*)widen_counts_kernel, n + 1, TE_THREADS), TE_THREADS>>>(n, d_cnt,
+                                                                                                      d_rp64);
+  rc = te_scan_exclusive_i64(d_rp64, d_rp64, n + 1);
+  if (rc == TE_OK)
+    rc = te_cuda_check(cudaMemcpy(&nnz, d_rp64 + n, sizeof(int64_t), cudaMemcpyDeviceToHost), "model");
+  if (rc == TE_OK && nnz >= ((int64_t)1 << 31)) {
+    te_set_error("te_model_create_device: more than 2^31 entries");
+    rc = TE_ERR_UNSUPPORTED;
   }
-  if (te_cuda_check(cudaMalloc(&d_rp, sizeof(int32_t) * (n + 1)), "model") != TE_OK ||
-      te_cuda_check(cudaMalloc(&d_col, sizeof(int32_t) * std::max<int64_t>(nnz, 1)), "model") != TE_OK ||
+  if (rc == TE_OK)
+    rc = te_cuda_check(cudaMalloc(&d_rp, sizeof(int32_t) * (n + 1)), "model");
+  if (rc == TE_OK)
+    narrow_rp_kernel<<<te_grid_fit((const void*)narrow_rp_kernel, n + 1, TE_THREADS), TE_THREADS>>>(n + 1, d_rp64,
+                                                                                                   d_rp);
+  cudaFree(d_rp64);
+  if (rc != TE_OK) return fail(rc);
+  if (te_cuda_check(cudaMalloc(&d_col, sizeof(int32_t) * std::max<int64_t>(nnz, 1)), "model") != TE_OK ||
       te_cuda_check(cudaMalloc(&d_val, sizeof(double2) * std::max<int64_t>(nnz, 1)), "model") != TE_OK)
     return fail(TE_ERR_CUDA);
-  cudaMemcpy(d_rp, rp.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice);
   row_write_model_kernel<<<te_grid_fit((const void*)row_write_model_kernel, n, 128), 128>>>(
       st, B.occ, n, d_terms, n_terms, d_rp, d_col, d_val, d_norm);
   unsigned long long bits = 0;
@@ -378,7 +396,7 @@ extern "C" int te_model_create_device(int n_particles, int n_modes, int quant, c
   d_terms = nullptr;
   d_cnt = nullptr;
   d_norm = nullptr;
-  rc = te_matrix_adopt_device_csr(n, n, rp[n], d_rp, d_col, d_val, out, norm1);
+  rc = te_matrix_adopt_device_csr(n, n, nnz, d_rp, d_col, d_val, out, norm1);
   if (rc != TE_OK) return rc;  // the matrix freed the arrays
   if (dim_out) *dim_out = n;
   return TE_OK;

@@ -62,9 +62,9 @@ int te_kernel_blocks_per_sm(const void* kernel, int threads, size_t dyn_smem) {
 int te_grid_fit(const void* kernel, int64_t n_items, int threads, size_t dyn_smem) {
   const int64_t cap = (int64_t)te_num_sms() * te_kernel_blocks_per_sm(kernel, threads, dyn_smem);
   const int64_t need = (n_items + threads - 1) / threads;
-  if (need <= cap) return (int)std::max<int64_t>(need, 1);
-  const int64_t per_thread = (n_items + cap * threads - 1) / (cap * threads);
-  return (int)((n_items + per_thread * threads - 1) / (per_thread * threads));
+  // more items than one wave of threads: exactly one wave, so that every SM
+  // holds the same number of blocks (threads differ by at most one item)
+  return (int)(need <= cap ? std::max<int64_t>(need, 1) : cap);
 }
 
 bool te_grid_saturated(const void* kernel, int64_t n_items, int threads, size_t dyn_smem) {

@@ -255,8 +255,9 @@ int te_num_sms();
 int te_grid_for(int64_t n_items, int threads, int blocks_per_sm);
 // Resident blocks per SM of a kernel at this block size (occupancy query, cached).
 int te_kernel_blocks_per_sm(const void* kernel, int threads, size_t dyn_smem);
-// One wave of a grid-stride kernel: at most every SM's resident blocks, and
-// shrunk so that every thread gets the same number of items (up to one).
+// Grid of a grid-stride kernel: one block per `threads` items up to one full
+// wave (every SM's resident blocks), so that every SM holds the same number
+// of blocks once the items exceed a wave.
 int te_grid_fit(const void* kernel, int64_t n_items, int threads, size_t dyn_smem = 0);
 // True when a grid-stride kernel over n_items would need more blocks than fit at once.
 bool te_grid_saturated(const void* kernel, int64_t n_items, int threads, size_t dyn_smem = 0);

@@ -219,3 +219,42 @@ def test_fixed_spmv_column_blocks(te_gpu, oracle_lib, complex_values, blocks):
     assert np.linalg.norm(a["state"] - b["state"]) < 1e-9
     ref = oracle_lib.evolve(coo, v, 1.0, 0.25, [("sparse", d)], tol=1e-8, m=30)
     _bounds(a, ref, 1e-8, 1.0)
+
+
+def test_fixed_spmv_without_memory_runs_fp64(te_gpu):
+    """An evolution that cannot get device memory for the fixed-point vectors
+    runs the FP64 passes instead of failing: the result equals, bit for bit,
+    the run with TE_OPT_FIXED_SPMV = 0.  The device is filled up to 24 MB
+    (the fixed-point copies of the basis need 59 MB) just for that run."""
+    import torch
+    states, H = models.bose_hubbard(10, 10, 1.0, 2.0)
+    n = len(states)
+    v = _fock(states, [10] + [0] * 9)
+    O = models.create_matrix([models.number_operator(0, 1.0)], states)
+    M, Om = te_gpu.Matrix.from_coo(n, H), te_gpu.Matrix.from_coo(n, O)
+    _run(te_gpu, M, v, 1.0, 0.5, [("sparse", Om)], 1)  # loads every kernel of both paths
+    ref = _run(te_gpu, M, v, 1.0, 0.5, [("sparse", Om)], 0)
+    M2 = te_gpu.Matrix.from_coo(n, H)
+    ev = te_gpu.Evolver(M2, v, 1.0, 0.5, [("sparse", Om)], tol=1e-8, m=40)
+    ev.set_option(te_gpu.OPT_FIXED_SPMV, 0)
+    ev.time_evolve()  # the evolver's own buffers, allocated on its first run
+    ev.reset(v)
+    ev.set_option(te_gpu.OPT_FIXED_SPMV, 1)
+    torch.cuda.synchronize()
+    blocker = None
+    for spare in (24, 32, 48):
+        try:
+            blocker = torch.empty(torch.cuda.mem_get_info()[0] - (spare << 20), dtype=torch.uint8, device="cuda")
+            break
+        except RuntimeError:
+            torch.cuda.empty_cache()
+    assert blocker is not None
+    try:
+        r = ev.time_evolve()
+    finally:
+        del blocker
+        torch.cuda.empty_cache()
+        ev.close()
+    assert r["n_steps"] == ref["n_steps"] and r["status"] == ref["status"]
+    assert np.array_equal(r["state"], ref["state"])
+    assert np.array_equal(r["samples"], ref["samples"])

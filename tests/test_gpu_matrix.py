@@ -178,7 +178,20 @@ def _bh10():
     return len(states), np.asarray(H[0], np.int64), np.asarray(H[1], np.int64), np.asarray(H[2], np.complex128)
 
 
-@pytest.mark.parametrize("case", ["bh10", "hubs"])
+def _wide_rows(n=1200, density=0.25, seed=9):
+    """A Hermitian matrix with ~300 entries per row: the long-row threshold
+    (32 x the mean) is too wide for the device sort's counters, so the device
+    build orders the rows on the host."""
+    rng = np.random.default_rng(seed)
+    mask = np.triu(rng.random((n, n)) < density)
+    mask = mask | mask.T
+    A = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) * mask
+    A = (A + A.conj().T) / 2
+    row, col = np.nonzero(A)
+    return n, row.astype(np.int64), col.astype(np.int64), A[row, col].astype(np.complex128)
+
+
+@pytest.mark.parametrize("case", ["bh10", "hubs", "wide"])
 def test_device_layout_identical_to_host_layout(te_gpu, case):
     """The SELL order built on the device (stable counting sort by length,
     long rows ordered by length on the host) equals the host's stable sort:
@@ -187,6 +200,8 @@ def test_device_layout_identical_to_host_layout(te_gpu, case):
     results, whose reductions run in the permuted order."""
     if case == "bh10":
         n, row, col, val = _bh10()
+    elif case == "wide":
+        n, row, col, val = _wide_rows()
     else:
         n = 40000
         row, col, val = _hub_matrix(n, [17, n // 2, n - 1], 3000, 11, True)

@@ -249,3 +249,26 @@ def test_destroy_frees_the_fixed_point_form(te_gpu):
         if it == 0:
             free0 = torch.cuda.mem_get_info()[0]
     assert abs(torch.cuda.mem_get_info()[0] - free0) < 8 << 20
+
+
+@pytest.mark.parametrize("copy_path", [False, True])
+def test_coo_upload_rectangular(te_gpu, copy_path, monkeypatch):
+    """A rectangular row-sorted COO (columns up to 2 N) through the device
+    conversion: exact CSR, no SELL layout (square matrices only)."""
+    if copy_path:
+        monkeypatch.setenv("TE_COO_COPY", "1")
+    rng = np.random.default_rng(10)
+    row = np.repeat(np.arange(N, dtype=np.int64), PER_ROW)
+    col = rng.integers(0, 2 * N, size=len(row)).astype(np.int64)
+    val = (rng.standard_normal(len(row)) + 1j * rng.standard_normal(len(row))).astype(np.complex128)
+    M = te_gpu.Matrix(N, row, col, val, n_cols=2 * N)
+    rp, ci, v = M.to_csr()
+    rp0, ci0, v0 = _expected_csr(row, col, val)
+    assert np.array_equal(rp, rp0) and np.array_equal(ci, ci0) and np.array_equal(v, v0)
+    inf = M.info()
+    assert inf["n_rows"] == N and inf["n_cols"] == 2 * N
+    colsum = np.zeros(2 * N)
+    np.add.at(colsum, col, np.abs(val))  # the reference's entry-order column sums
+    assert inf["norm1"] == colsum.max()
+    with pytest.raises(RuntimeError, match="square"):
+        M.layout()

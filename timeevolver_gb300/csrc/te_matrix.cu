@@ -522,10 +522,11 @@ __global__ void __launch_bounds__(TE_THREADS) mirror_norm1_kernel(int64_t n, con
                                                                   const int32_t* __restrict__ ci,
                                                                   const double2* __restrict__ v,
                                                                   unsigned int* flags, unsigned long long* max_bits) {
+  unsigned long long smax = 0;  // bit patterns (ordered as the non-negative sums); one atomic per thread
+  unsigned int f = 0;
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
     double s = 0.0;
     int32_t prev = -1;
-    unsigned int f = 0;
     for (int32_t k = rp[r]; k < rp[r + 1]; ++k) {
       const int32_t c = ci[k];
       const double2 a = v[k];
@@ -542,9 +543,10 @@ __global__ void __launch_bounds__(TE_THREADS) mirror_norm1_kernel(int64_t n, con
       }
       if (lo >= rp[c + 1] || ci[lo] != (int32_t)r || fabs(v[lo].x) != m) f |= 4u;
     }
-    if (f) atomicOr(flags, f);
-    atomicMax(max_bits, (unsigned long long)__double_as_longlong(s));
+    smax = max(smax, (unsigned long long)__double_as_longlong(s));
   }
+  if (f) atomicOr(flags, f);
+  atomicMax(max_bits, smax);
 }
 
 // ------------------------------------------------------------ host build

@@ -12,9 +12,9 @@
  * behaviour.
  *
  * Reference interfaces replaced (paths inside the TimeEvolver project):
- *   TE::smatrix + initialize()        core/matrixDataTypes.h:59-99, .cpp:264-290, :352-396
- *   smatrix::spMV                      core/matrixDataTypes.cpp:325-346
- *   smatrix::norm1                     core/matrixDataTypes.cpp:223-235
+ *   TE::smatrix + initialize()        core/matrixDataTypes.h:59-99, .cpp:108-134, :196-240
+ *   smatrix::spMV                      core/matrixDataTypes.cpp:169-190
+ *   smatrix::norm1                     core/matrixDataTypes.cpp:67-79
  *   krylovTimeEvolver(...) ctor        core/krylovTimeEvolver.h:59-60, .cpp:26-94
  *   krylovTimeEvolver::timeEvolve()    core/krylovTimeEvolver.h:61, .cpp:261-512
  *   krylovReturn                       core/krylovTimeEvolver.h:32-51, .cpp:662-676
@@ -43,7 +43,7 @@ extern "C" {
 #define TE_ERR_NOT_NORMALIZED (-4)  /* "Initial vector is not normalized" (krylovTimeEvolver.cpp:45-48) */
 #define TE_ERR_NO_STEP (-5)         /* 20 halvings did not meet the tolerance (krylovTimeEvolver.cpp:203-207) */
 #define TE_ERR_EIGEN (-6)           /* Krylov eigensolver did not converge (the LAPACK error of :365-370) */
-#define TE_ERR_DIM (-7)             /* "Incompatible dimensions" (krylovObservables.cpp:296-300) */
+#define TE_ERR_DIM (-7)             /* "Incompatible dimensions" (krylovObservables.cpp:180-184) */
 #define TE_ERR_OUT_OF_MEMORY (-8)
 #define TE_ERR_UNSUPPORTED (-9)     /* e.g. Krylov dimension above TE_MAX_KRYLOV */
 #define TE_ERR_DEVICE_TIMEOUT (-10) /* a bounded device-side wait gave up */
@@ -79,7 +79,7 @@ int te_set_device(int device);
  * duplicates are kept (they add, as in the reference's COO loop).  A matrix
  * whose imaginary parts are all zero is stored with real values (same
  * results, half the value bytes and FP64 work).  Replaces smatrix(...) +
- * initialize() (matrixDataTypes.cpp:264-290, :352-396).
+ * initialize() (matrixDataTypes.cpp:108-134, :196-240).
  * A row-sorted COO of at least 2^18 entries (the order createMatrix produces)
  * is converted on the device: where the device accesses pageable host memory
  * (Grace hosts) one kernel reads the three arrays in place, elsewhere they are
@@ -189,12 +189,12 @@ int te_matrix_download_csr(te_matrix A, int32_t* row_ptr, int32_t* col_idx, doub
 int te_matrix_destroy(te_matrix A);
 
 /* n_rows, n_cols, nnz, flags (bit0 real values, bit1 diagonal), and the
- * reference's 1-norm (max absolute column sum, matrixDataTypes.cpp:223-235). */
+ * reference's 1-norm (max absolute column sum, matrixDataTypes.cpp:67-79). */
 int te_matrix_info(te_matrix A, int64_t* n_rows, int64_t* n_cols, int64_t* nnz, int* flags, double* norm1);
 
 /* out = alpha * A * in on device buffers (complex n), on a CUDA stream
  * (NULL = the library's stream).  Replaces smatrix::spMV
- * (matrixDataTypes.cpp:325-346). */
+ * (matrixDataTypes.cpp:169-190). */
 int te_matrix_spmv(te_matrix A, double alpha_re, double alpha_im, const double* in_dev, double* out_dev,
                    void* cuda_stream);
 

@@ -196,7 +196,7 @@ struct CSR {
 
 // COO -> CSR, keeping the order of entries within each row so that the
 // row-parallel product equals the reference's serial COO loop
-// (core/matrixDataTypes.cpp:339-343) for row-sorted input.
+// (core/matrixDataTypes.cpp:183-188) for row-sorted input.
 CSR make_csr(int64_t n, int64_t nnz, const int64_t* row, const int64_t* col, const double* val) {
   CSR A;
   A.n = n;

@@ -72,11 +72,11 @@ int oracle_evolve(int64_t n, int64_t nnz, const int64_t* row, const int64_t* col
                   double* state_out, oracle_result* result, oracle_step* trace, int64_t max_trace,
                   int64_t* n_trace, int n_threads);
 
-/* out = alpha * H * in for a COO matrix (core/matrixDataTypes.cpp:338-344). */
+/* out = alpha * H * in for a COO matrix (core/matrixDataTypes.cpp:182-188). */
 int oracle_spmv(int64_t n, int64_t nnz, const int64_t* row, const int64_t* col, const double* val,
                 double alpha_re, double alpha_im, const double* in, double* out);
 
-/* Maximum absolute column sum (core/matrixDataTypes.cpp:223-235). */
+/* Maximum absolute column sum (core/matrixDataTypes.cpp:67-79). */
 double oracle_norm1(int64_t n, int64_t nnz, const int64_t* col, const double* val);
 
 /* One Lanczos pass (core/krylovTimeEvolver.cpp:523-571) from the normalised

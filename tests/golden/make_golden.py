@@ -16,7 +16,8 @@ Fixtures written next to this script:
 * ``simple_example.npy``  (2, 1001)   -- ``test/testSimpleExample.cpp`` golden
   (CSV only, 6 significant digits), two coupled oscillators, dim 201, tol 1e-6.
 
-Run from anywhere: ``python tests/golden/make_golden.py [reference_root]``.
+Run from anywhere: ``python tests/golden/make_golden.py [reference_root]`` (default:
+``$TE_REFERENCE_DIR``).
 """
 import os
 import sys
@@ -62,4 +63,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TE_REFERENCE_DIR")
+    if not root:
+        sys.exit("usage: make_golden.py REFERENCE_DIR (or set TE_REFERENCE_DIR)")
+    main(root)

@@ -1,8 +1,8 @@
 """The reference's own example programs compile and link unchanged against the
 drop-in C++ layer (timeevolver_gb300/host) and its libraries.
 
-Reads the reference tree where it exists (the development container); skipped
-elsewhere.  Running them needs a GPU; the runtime behaviour of the same API is
+Reads the reference tree named by the environment variable TE_REFERENCE_DIR;
+skipped where it is unset.  Running them needs a GPU; the runtime behaviour of the same API is
 covered by test_cpp_dropin.py.
 """
 import os
@@ -10,13 +10,15 @@ import subprocess
 
 import pytest
 
-REF_EXAMPLES = "/root/reference/example"
+REF_DIR = os.environ.get("TE_REFERENCE_DIR", "")
+REF_EXAMPLES = os.path.join(REF_DIR, "example") if REF_DIR else ""
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HOST = os.path.join(ROOT, "timeevolver_gb300", "host")
 INC = os.path.join(ROOT, "include")
 BUILD = os.path.join(ROOT, "timeevolver_gb300", "_build")
 
-pytestmark = pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference tree not present")
+pytestmark = pytest.mark.skipif(not REF_EXAMPLES or not os.path.isdir(REF_EXAMPLES),
+                                reason="TE_REFERENCE_DIR not set (reference tree absent)")
 
 
 def _cuda_include():

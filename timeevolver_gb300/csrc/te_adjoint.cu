@@ -99,7 +99,7 @@ __global__ void refresh_values_kernel(int64_t count, const int32_t* __restrict__
 
 __device__ __forceinline__ double2 operator*(const double2& a, double s) { return make_double2(a.x * s, a.y * s); }
 
-// 1-norm of H(theta) (maximum absolute column sum, matrixDataTypes.cpp:223-235):
+// 1-norm of H(theta) (maximum absolute column sum, matrixDataTypes.cpp:67-79):
 // one thread per column sums |theta_term| |a| over the column's entries in
 // ascending entry order; the maximum goes through the bit patterns of the
 // (non-negative) sums, so the result does not depend on the schedule.

@@ -1,7 +1,7 @@
 // te_matrix.cu -- sparse matrices on the device and the te_matrix C ABI.
 //
-// Replaces TE::smatrix with its MKL preparation (core/matrixDataTypes.cpp:264-290,
-// :352-396), smatrix::spMV (:325-346) and smatrix::norm1 (:223-235).
+// Replaces TE::smatrix with its MKL preparation (core/matrixDataTypes.cpp:108-134,
+// :196-240), smatrix::spMV (:169-190) and smatrix::norm1 (:67-79).
 //
 // Every matrix keeps its original-order CSR (int32 indices) for general
 // observables and the public product, and square matrices also get the
@@ -796,7 +796,7 @@ int build_matrix(te_matrix_s* M, const std::vector<int32_t>& rp, const std::vect
       }
   M->is_real = real;
   M->is_diag = diag;
-  // 1-norm as in matrixDataTypes.cpp:223-235 (max absolute column sum), unless
+  // 1-norm as in matrixDataTypes.cpp:67-79 (max absolute column sum), unless
   // the caller computed it in its own entry order
   if (std::isnan(norm1_given)) {
     std::vector<double> colsum(M->n_cols, 0.0);

@@ -1,5 +1,5 @@
 // krylovObservables.h -- observables of the GB300 TimeEvolver (same API as
-// core/krylovObservables.h:16-117).  During timeEvolve, sparse-matrix and
+// core/krylovObservables.h:16-116).  During timeEvolve, sparse-matrix and
 // vector observables are evaluated on the GPU (diagonal ones fused into the
 // sampling pass); any other subclass of krylovBasicObservable is called on
 // the host with the sampled state, exactly through its virtual expectation().

@@ -75,14 +75,14 @@ smatrix::~smatrix() {
   }
 }
 
-// maximum absolute column sum (core/matrixDataTypes.cpp:223-235)
+// maximum absolute column sum (core/matrixDataTypes.cpp:67-79)
 double smatrix::norm1() {
   std::vector<double> colVal(n, 0.0);
   for (size_t i = 0; i != numValues; i++) colVal[columns[i]] += std::abs(values[i]);
   return colVal.empty() ? 0.0 : *std::max_element(colVal.begin(), colVal.end());
 }
 
-// maximum absolute row sum (core/matrixDataTypes.cpp:241-253)
+// maximum absolute row sum (core/matrixDataTypes.cpp:85-97)
 double smatrix::normInf() {
   std::vector<double> rowVal(m, 0.0);
   for (size_t i = 0; i != numValues; i++) rowVal[rowIndex[i]] += std::abs(values[i]);
@@ -103,7 +103,7 @@ te_matrix smatrix::device() {
   return dev_;
 }
 
-// out = alpha * this * in on the GPU (core/matrixDataTypes.cpp:325-346)
+// out = alpha * this * in on the GPU (core/matrixDataTypes.cpp:169-190)
 int smatrix::spMV(std::complex<double> alpha, std::complex<double>* in, std::complex<double>* out) {
   te_matrix A = device();
   if (!A) return -1;
@@ -111,7 +111,7 @@ int smatrix::spMV(std::complex<double> alpha, std::complex<double>* in, std::com
                              reinterpret_cast<double*>(out));
 }
 
-// GPU preparation (core/matrixDataTypes.cpp:352-396): returns -1 when already
+// GPU preparation (core/matrixDataTypes.cpp:196-240): returns -1 when already
 // initialised, 0 on success.
 int smatrix::initialize() {
   if (initialized) return -1;

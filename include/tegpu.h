@@ -305,6 +305,17 @@ int te_evolver_trace(te_evolver ev, te_step_record* out, int64_t max_records, in
 /* Kernel launches issued by the last te_evolver_run (for launch accounting). */
 int64_t te_evolver_launch_count(te_evolver ev);
 
+/* The Krylov matrix of the last Krylov step, for tests and tracing (no
+ * counterpart in the reference, whose Hessenberg matrix H is internal,
+ * krylovTimeEvolver.cpp:523-571): the real symmetric tridiagonal T with
+ * H_k = D(-iT)D^-1 (diag: m doubles, offdiag: m - 1), *m_out = m, and
+ * *eig_used = 1 when that step evaluated exp(-ixT) through the eigen-
+ * decomposition of T (tridiagonal QR; arguments beyond the Chebyshev-Bessel
+ * series), whose m eigenvalues (unordered) are then written to eigenvalues.
+ * Buffers may be NULL; m <= TE_MAX_KRYLOV. */
+int te_evolver_krylov_matrix(te_evolver ev, double* diag, double* offdiag, double* eigenvalues, int32_t* m_out,
+                             int32_t* eig_used);
+
 /* Evolver options (no counterpart in the reference).
  * TE_OPT_FUSED_LANCZOS: run the three-term Lanczos iterations of a Krylov step
  * as one persistent cooperative kernel with grid barriers instead of two
@@ -328,6 +339,27 @@ int64_t te_evolver_launch_count(te_evolver ev);
  * te_matrix_fixed_layout for the forms (value dictionary, column blocks).
  * 0: FP64 SpMV; 1 (default): fixed point. */
 #define TE_OPT_FIXED_SPMV 2
+/* Options that bound or exercise the failure paths (no counterpart in the
+ * reference, which exits or keeps going where these return an error):
+ * TE_OPT_BARRIER_SPIN_LIMIT: polls (each a load and a short sleep) before a
+ * grid-barrier wait of the persistent Lanczos kernel gives up; the run then
+ * returns TE_ERR_DEVICE_TIMEOUT and the evolver can be reset and run again.
+ * Default 2^22 (seconds; a co-resident grid arrives in microseconds).
+ * TE_OPT_BARRIER_EXTRA_ARRIVALS: 1 makes every barrier of that kernel wait
+ * for one arrival more than the grid has, so every wait gives up after the
+ * spin limit: a test of the timeout path that faults nothing (default 0).
+ * TE_OPT_TS_MAX_LEVEL: the deepest tanh-sinh level of the error integral
+ * (2..8, default 8).  With fewer levels the quadrature misses its 1e-3
+ * relative accuracy, and a step whose integral matters for the bound gets
+ * code 20 (status TE_STATUS_INTEGRATION), the reference's response to a
+ * quadrature that did not converge (krylovTimeEvolver.cpp:584-618).
+ * TE_OPT_QR_SWEEP_LIMIT: sweeps of the tridiagonal QR eigensolve before it
+ * reports TE_ERR_EIGEN (the LAPACK failure of zhseqr, matrixDataTypes.h:135-156);
+ * 0 (default) 40 m + 40. */
+#define TE_OPT_BARRIER_SPIN_LIMIT 3
+#define TE_OPT_BARRIER_EXTRA_ARRIVALS 4
+#define TE_OPT_TS_MAX_LEVEL 5
+#define TE_OPT_QR_SWEEP_LIMIT 6
 int te_evolver_set_option(te_evolver ev, int option, int value);
 
 /* Prepare another run of the same evolution (same H, parameters and

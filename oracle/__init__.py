@@ -70,6 +70,8 @@ def lib():
         L.oracle_find_step.argtypes = [I, P, P, D, D, D, D, I, D, I, I, D, P, P, P, P]
         L.oracle_ts_test.argtypes = [I, D, D, D, D, P, P, P]
         L.oracle_ts_test.restype = D
+        L.oracle_set_ts_max_level.argtypes = [I]
+        L.oracle_set_ts_max_level.restype = None
         _lib = L
     return _lib
 
@@ -204,3 +206,9 @@ def ts_test(kind, p, a, b, tol):
     lv = ctypes.c_int(0)
     r = lib().oracle_ts_test(kind, p, a, b, tol, ctypes.byref(e), ctypes.byref(l1), ctypes.byref(lv))
     return r, e.value, l1.value, lv.value
+
+
+def set_ts_max_level(level):
+    """Last tanh-sinh level (2..8) of the oracle's later integrals (8 restores
+    the default)."""
+    lib().oracle_set_ts_max_level(int(level))

@@ -44,6 +44,7 @@ namespace {
 
 const int TS_KMIN = 2;   // always evaluate levels 0..2 before testing convergence
 const int TS_KMAX = 8;   // last refinement level
+int g_ts_kmax = TS_KMAX;  // oracle_set_ts_max_level: a lower last level makes the rule miss its tolerance
 const double TS_TMAX = 3.0;  // nodes t in [-3, 3]
 const int N_BLOCK = 1024;
 
@@ -147,7 +148,7 @@ TSResult tanh_sinh(F&& f, double a, double b, double tol) {
   const TanhSinhTable& T = ts_table();
   double c = 0.5 * (a + b), d = 0.5 * (b - a);
   double sum = 0, sum_abs = 0, prev = 0;
-  for (int k = 0; k <= TS_KMAX; ++k) {
+  for (int k = 0; k <= g_ts_kmax; ++k) {
     for (int j = T.level_begin[k]; j < T.level_begin[k + 1]; ++j) {
       double fv;
       if (T.t[j] == 0.0) {
@@ -827,4 +828,10 @@ extern "C" double oracle_ts_test(int kind, double p, double a, double b, double 
   if (l1) *l1 = r.l1;
   if (levels) *levels = r.levels;
   return r.value;
+}
+
+// Last tanh-sinh level (2..8) of every later integral; the failure-path tests
+// set it low so that the quadrature reports a miss (status 20).
+extern "C" void oracle_set_ts_max_level(int level) {
+  g_ts_kmax = level < TS_KMIN ? TS_KMIN : level > TS_KMAX ? TS_KMAX : level;
 }

@@ -108,6 +108,10 @@ int oracle_find_step(int m, const double* eigenvalues, const double* Z, double h
 double oracle_ts_test(int kind, double p, double a, double b, double tol, double* err, double* l1,
                       int* levels);
 
+/* Last tanh-sinh level (2..8, default 8) of every later integral; below 8 the
+ * rule gives up earlier, which the failure-path tests use to reach status 20. */
+void oracle_set_ts_max_level(int level);
+
 #ifdef __cplusplus
 }
 #endif

@@ -87,6 +87,7 @@ SIGNATURES = {
     "te_evolver_state_device": (_I, [_P, _P]),
     "te_evolver_trace": (_I, [_P, _P, _I64, _P]),
     "te_evolver_launch_count": (_I64, [_P]),
+    "te_evolver_krylov_matrix": (_I, [_P, _P, _P, _P, _P, _P]),
     "te_evolver_reset": (_I, [_P, _P, _I]),
     "te_evolver_stream": (_P, [_P]),
     "te_evolver_profile": (_I, [_P, _I]),
@@ -177,6 +178,10 @@ def _as_u64(a):
 
 OPT_FUSED_LANCZOS = 1
 OPT_FIXED_SPMV = 2
+OPT_BARRIER_SPIN_LIMIT = 3
+OPT_BARRIER_EXTRA_ARRIVALS = 4
+OPT_TS_MAX_LEVEL = 5
+OPT_QR_SWEEP_LIMIT = 6
 
 
 class TeTerm(ctypes.Structure):
@@ -436,8 +441,25 @@ class Evolver:
         _check(lib().te_evolver_add_stop_condition(self.handle, int(obs_index), float(threshold), int(direction)),
                "te_evolver_add_stop_condition")
 
+    def krylov_matrix(self):
+        """The last Krylov step's tridiagonal T (te_evolver_krylov_matrix):
+        dict with diag, offdiag, eig_used and, when the eigen path ran,
+        eigenvalues (unordered)."""
+        d = np.zeros(64)
+        e = np.zeros(64)
+        lam = np.zeros(64)
+        m, used = ctypes.c_int32(), ctypes.c_int32()
+        _check(lib().te_evolver_krylov_matrix(self.handle, _ptr(d), _ptr(e), _ptr(lam), ctypes.byref(m),
+                                              ctypes.byref(used)), "te_evolver_krylov_matrix")
+        k = m.value
+        out = dict(diag=d[:k].copy(), offdiag=e[:max(0, k - 1)].copy(), eig_used=bool(used.value))
+        if used.value:
+            out["eigenvalues"] = lam[:k].copy()
+        return out
+
     def set_option(self, option, value):
-        """te_evolver_set_option (OPT_FUSED_LANCZOS, OPT_FIXED_SPMV)."""
+        """te_evolver_set_option (OPT_FUSED_LANCZOS, OPT_FIXED_SPMV, OPT_BARRIER_SPIN_LIMIT,
+        OPT_BARRIER_EXTRA_ARRIVALS, OPT_TS_MAX_LEVEL, OPT_QR_SWEEP_LIMIT)."""
         _check(lib().te_evolver_set_option(self.handle, int(option), int(value)), "te_evolver_set_option")
 
     def kernel_time(self, kind):

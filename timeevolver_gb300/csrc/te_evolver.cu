@@ -67,6 +67,10 @@ struct te_evolver_s {
   int max_batch = 1;
   int fused_lanczos = 1;  // TE_OPT_FUSED_LANCZOS: 0 never, 1 automatic, 2 always
   int fixed_spmv = 1;     // TE_OPT_FIXED_SPMV: 0 FP64 SpMV, 1 fixed-point SpMV
+  unsigned int barrier_spins = 1u << 22;  // TE_OPT_BARRIER_SPIN_LIMIT (~seconds of polling)
+  unsigned int barrier_extra = 0;         // TE_OPT_BARRIER_EXTRA_ARRIVALS
+  int ts_max_level = 0;                   // TE_OPT_TS_MAX_LEVEL (0: 8)
+  int qr_sweeps = 0;                      // TE_OPT_QR_SWEEP_LIMIT (0: 40 m + 40)
   int4* X = nullptr;      // fixed-point copies of the Krylov vectors (m x n rows)
   longlong2* fx_acc = nullptr;  // column-blocked fixed-point SpMV: exact row sums (n rows)
   int batch_cap = 0;         // states the batch buffer holds
@@ -307,6 +311,8 @@ int run(te_evolver ev, te_result* out) {
   hs->sample_times = ev->sample_times;
   hs->state_store = ev->state_store;
   hs->store_ld = ev->store_ld;
+  hs->ts_kmax = ev->ts_max_level;
+  hs->qr_sweeps = ev->qr_sweeps;
   rc = te_cuda_check(cudaMemcpyAsync(ev->ds, hs, sizeof(TeDevState), cudaMemcpyHostToDevice, st), "state upload");
   TE_CUDA(cudaStreamSynchronize(st));
   delete hs;
@@ -376,7 +382,8 @@ int run(te_evolver ev, te_result* out) {
     const bool want_fused = ev->fused_lanczos == 2 || (ev->fused_lanczos == 1 && ev->H->sell.n_chunks < 2048);
     if (fold && want_fused) {
       ProfScope ps(ev, 0);
-      fused = te_launch_lanczos_step(ev->H->sell, ev->H->is_real, ev->cols, m, ev->w, ev->ds, ev->partials, st);
+      fused = te_launch_lanczos_step(ev->H->sell, ev->H->is_real, ev->cols, m, ev->w, ev->ds, ev->partials, st,
+                                     ev->barrier_spins, ev->barrier_extra);
       if (fused) ++ev->launches;
     }
     const bool fix_step = fix && fold && !fused;
@@ -489,9 +496,10 @@ int run(te_evolver ev, te_result* out) {
   }
   if (S->fatal) {
     te_set_error("device-side failure %d during the evolution (%s)", S->fatal,
-                 S->fatal == TE_ERR_NO_STEP ? "no small enough time step found to meet the tolerance"
-                                            : S->fatal == TE_ERR_EIGEN ? "Krylov eigensolver did not converge"
-                                                                       : "step search limit");
+                 S->fatal == TE_ERR_NO_STEP              ? "no small enough time step found to meet the tolerance"
+                 : S->fatal == TE_ERR_EIGEN              ? "Krylov eigensolver did not converge"
+                 : S->fatal == TE_ERR_DEVICE_TIMEOUT     ? "a grid-barrier wait of the persistent Lanczos kernel gave up"
+                                                         : "step search limit");
     return S->fatal;
   }
   // final checks (:445-504)
@@ -568,7 +576,7 @@ extern "C" int te_evolver_create(te_matrix H, const double* v_host, const te_par
   // normalisation check (:45-48), host-side on the caller's vector
   double nrm = 0.0;
   for (int64_t i = 0; i < 2 * n; ++i) nrm += v_host[i] * v_host[i];
-  if (std::fabs(std::sqrt(nrm) - 1.0) > p.tol) {
+  if (!(std::fabs(std::sqrt(nrm) - 1.0) <= p.tol)) {  // a NaN entry fails too
     te_set_error("Initial vector is not normalized");
     return TE_ERR_NOT_NORMALIZED;
   }
@@ -786,6 +794,26 @@ extern "C" int te_evolver_trace(te_evolver ev, te_step_record* out, int64_t max_
 
 extern "C" int64_t te_evolver_launch_count(te_evolver ev) { return ev ? ev->launches : 0; }
 
+extern "C" int te_evolver_krylov_matrix(te_evolver ev, double* diag, double* offdiag, double* eigenvalues,
+                                        int32_t* m_out, int32_t* eig_used) {
+  if (!ev || !ev->ds) {
+    te_set_error("te_evolver_krylov_matrix: null evolver");
+    return TE_ERR_INVALID_ARG;
+  }
+  TE_CUDA(cudaStreamSynchronize(ev->st));
+  int32_t m = 0, valid = 0;
+  TE_CUDA(cudaMemcpy(&m, (const char*)ev->ds + offsetof(TeDevState, m_eff), sizeof(int32_t), cudaMemcpyDeviceToHost));
+  TE_CUDA(cudaMemcpy(&valid, (const char*)ev->ds + offsetof(TeDevState, eig_valid), sizeof(int32_t),
+                     cudaMemcpyDeviceToHost));
+  m = std::max(0, std::min(m, (int32_t)TE_MMAX));
+  if (diag) TE_CUDA(cudaMemcpy(diag, ev->ds->d, sizeof(double) * m, cudaMemcpyDeviceToHost));
+  if (offdiag && m > 1) TE_CUDA(cudaMemcpy(offdiag, ev->ds->e, sizeof(double) * (m - 1), cudaMemcpyDeviceToHost));
+  if (eigenvalues && valid) TE_CUDA(cudaMemcpy(eigenvalues, ev->ds->eig_lam, sizeof(double) * m, cudaMemcpyDeviceToHost));
+  if (m_out) *m_out = m;
+  if (eig_used) *eig_used = valid;
+  return TE_OK;
+}
+
 // Sample at the given ascending times (times[0] = 0, times[count-1] <= t)
 // instead of multiples of sampling_step, and optionally store every sampled
 // state (evolver row order) at store_dev + k * store_ld.
@@ -819,7 +847,7 @@ extern "C" int te_evolver_reset(te_evolver ev, const double* v, int v_is_device)
   if (!v_is_device) {
     double nrm = 0.0;
     for (int64_t i = 0; i < 2 * n; ++i) nrm += v[i] * v[i];
-    if (std::fabs(std::sqrt(nrm) - 1.0) > ev->p.tol) {
+    if (!(std::fabs(std::sqrt(nrm) - 1.0) <= ev->p.tol)) {
       te_set_error("Initial vector is not normalized");
       return TE_ERR_NOT_NORMALIZED;
     }
@@ -850,6 +878,34 @@ extern "C" int te_evolver_set_option(te_evolver ev, int option, int value) {
         return TE_ERR_INVALID_ARG;
       }
       ev->fixed_spmv = value;
+      return TE_OK;
+    case TE_OPT_BARRIER_SPIN_LIMIT:
+      if (value < 1) {
+        te_set_error("te_evolver_set_option: TE_OPT_BARRIER_SPIN_LIMIT takes a positive poll count");
+        return TE_ERR_INVALID_ARG;
+      }
+      ev->barrier_spins = (unsigned int)value;
+      return TE_OK;
+    case TE_OPT_BARRIER_EXTRA_ARRIVALS:
+      if (value < 0 || value > 1) {
+        te_set_error("te_evolver_set_option: TE_OPT_BARRIER_EXTRA_ARRIVALS takes 0 or 1");
+        return TE_ERR_INVALID_ARG;
+      }
+      ev->barrier_extra = (unsigned int)value;
+      return TE_OK;
+    case TE_OPT_TS_MAX_LEVEL:
+      if (value < 2 || value > 8) {
+        te_set_error("te_evolver_set_option: TE_OPT_TS_MAX_LEVEL takes 2..8");
+        return TE_ERR_INVALID_ARG;
+      }
+      ev->ts_max_level = value == 8 ? 0 : value;
+      return TE_OK;
+    case TE_OPT_QR_SWEEP_LIMIT:
+      if (value < 0) {
+        te_set_error("te_evolver_set_option: TE_OPT_QR_SWEEP_LIMIT takes 0 (automatic) or a sweep count");
+        return TE_ERR_INVALID_ARG;
+      }
+      ev->qr_sweeps = value;
       return TE_OK;
     default:
       te_set_error("te_evolver_set_option: unknown option %d", option);

@@ -98,6 +98,10 @@ struct TeDevState {
   // the update pass's coefficient alpha_j s_j / g (alpha_j / expFactor when
   // folded), set with alpha_j by the apply pass
   double upd_gr, upd_gi;
+  // limits set by the evolver options that exercise the failure paths (0: the
+  // defaults): deepest tanh-sinh level (TE_OPT_TS_MAX_LEVEL), sweeps of the
+  // tridiagonal QR (TE_OPT_QR_SWEEP_LIMIT)
+  int ts_kmax, qr_sweeps;
 };
 
 #define TE_FIX_MAX_BLOCKS 8  // column blocks of the fixed-point SpMV
@@ -309,8 +313,11 @@ void te_sell_schedule(const std::vector<int64_t>& off, int64_t n_chunks, int blo
 // static schedule does not fit the persistent kernel's residency, or the
 // device has no cooperative launch; the caller then runs the per-iteration
 // passes.  cols[j]: the basis columns of the step.
+// spin_limit: polls before a grid-barrier wait gives up (TE_ERR_DEVICE_TIMEOUT);
+// extra_arrivals > 0 makes every barrier wait for arrivals that never come
+// (the failure-path test of TE_OPT_BARRIER_EXTRA_ARRIVALS).
 bool te_launch_lanczos_step(const TeSell& A, bool is_real, double2* const* cols, int m, double2* w, TeDevState* ds,
-                            double* partials, cudaStream_t st);
+                            double* partials, cudaStream_t st, unsigned int spin_limit, unsigned int extra_arrivals);
 // Device-side stop conditions: after a batch of samples, ds->stop_flag = k + 1
 // for the first sample k of the batch at which results[obs][sample] >= threshold
 // (direction > 0) or <= threshold (direction < 0) for any condition (te_sample.cu).

@@ -225,7 +225,7 @@ __device__ void bessel_table(double z, int K, double* out) {
 // Implicit symmetric tridiagonal QR with Wilkinson shifts, warp 0 only.
 // Q (col-major, ld TE_MMAX) must hold the identity on entry.  Returns 0 on
 // success, 1 if the sweep limit was reached.
-__device__ int tridiag_qr_warp(int m, double* d, double* e, double* Q, double* rc, double* rs) {
+__device__ int tridiag_qr_warp(int m, double* d, double* e, double* Q, double* rc, double* rs, int max_sweeps) {
   const int lane = threadIdx.x & 31;
   int q = m - 1;
   int sweeps = 0;
@@ -287,7 +287,7 @@ __device__ int tridiag_qr_warp(int m, double* d, double* e, double* Q, double* r
       Q[q * TE_MMAX + row] = a;
     }
     __syncwarp();
-    if (++sweeps > 40 * m + 40) return 1;
+    if (++sweeps > max_sweeps) return 1;
   }
   return 0;
 }
@@ -308,7 +308,8 @@ __device__ void ensure_eig(KCtx& C) {
   }
   __syncthreads();
   int fail = 0;
-  if (threadIdx.x < 32) fail = tridiag_qr_warp(m, dtmp, etmp, S->Q, S->rc, S->rs);
+  const int max_sweeps = C.ds->qr_sweeps > 0 ? C.ds->qr_sweeps : 40 * m + 40;
+  if (threadIdx.x < 32) fail = tridiag_qr_warp(m, dtmp, etmp, S->Q, S->rc, S->rs, max_sweeps);
   if (threadIdx.x == 0) S->ibc[0] = fail;
   __syncthreads();
   if (S->ibc[0] && threadIdx.x == 0) C.ds->fatal = TE_ERR_EIGEN;
@@ -378,7 +379,8 @@ __device__ IntResult ts_integrate(KCtx& C, double a, double b) {
   double sum = 0.0, sum_abs = 0.0, prev = 0.0;
   bool nonfinite = false;
   int evaluated = 4;
-  for (int k = 0; k <= TE_TS_KMAX; ++k) {
+  const int kmax = C.ds->ts_kmax >= TE_TS_KMIN && C.ds->ts_kmax < TE_TS_KMAX ? C.ds->ts_kmax : TE_TS_KMAX;
+  for (int k = 0; k <= kmax; ++k) {
     if (k > evaluated) {
       eval_ts_nodes(C, a, b, lb[k], lb[k + 1], use_eig, K);
       evaluated = k;

@@ -386,8 +386,6 @@ __global__ void __launch_bounds__(TE_THREADS) fix_start_encode_kernel(int64_t n,
 // This removes two launches, two block ramps and two serial last-block
 // reductions per iteration, which dominate small problems.
 
-#define TE_BARRIER_SPIN_LIMIT (1u << 22)  // ~ seconds of polling; a co-resident grid arrives in microseconds
-
 struct TeLanczosArgs {
   int64_t n;
   const int32_t* warp_chunk;
@@ -397,13 +395,17 @@ struct TeLanczosArgs {
   double2* w;
   double* partials;  // 3 * gridDim.x: alpha (re, im), beta
   int m;
+  unsigned int spin_limit;  // polls before a barrier wait gives up
+  unsigned int arrivals;    // arrivals that complete a barrier (gridDim.x; more only to test the timeout)
   double2* u[TE_MMAX];
 };
 
-// Grid barrier with a bounded wait.  Arrival after a fence; the last block
-// resets the count and bumps the generation.  A wait that gives up sets
-// fatal = TE_ERR_DEVICE_TIMEOUT and returns false (the kernel then exits).
-__device__ __forceinline__ bool te_grid_barrier(unsigned int* count, unsigned int* gen, int* fatal) {
+// Grid barrier with a bounded wait.  Arrival after a fence; the block that
+// brings the count to `arrivals` resets it and bumps the generation.  A wait
+// that gives up after spin_limit polls sets fatal = TE_ERR_DEVICE_TIMEOUT and
+// returns false (the kernel then exits).
+__device__ __forceinline__ bool te_grid_barrier(unsigned int* count, unsigned int* gen, int* fatal,
+                                                unsigned int spin_limit, unsigned int arrivals) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -411,7 +413,7 @@ __device__ __forceinline__ bool te_grid_barrier(unsigned int* count, unsigned in
     volatile unsigned int* vgen = gen;
     const unsigned int g0 = *vgen;
     __threadfence();
-    if (atomicAdd(count, 1u) == gridDim.x - 1) {
+    if (atomicAdd(count, 1u) == arrivals - 1) {
       atomicExch(count, 0u);
       __threadfence();
       atomicAdd(gen, 1u);
@@ -419,7 +421,7 @@ __device__ __forceinline__ bool te_grid_barrier(unsigned int* count, unsigned in
       unsigned int spins = 0;
       while (*vgen == g0) {
         __nanosleep(32);
-        if (++spins > TE_BARRIER_SPIN_LIMIT) {
+        if (++spins > spin_limit) {
           ok = 0;
           atomicExch(fatal, TE_ERR_DEVICE_TIMEOUT);
           break;
@@ -493,7 +495,7 @@ __global__ void __launch_bounds__(TE_THREADS, REAL ? 6 : 5) lanczos_step_kernel(
       a.partials[blockIdx.x] = acc[0];
       a.partials[G + blockIdx.x] = acc[1];
     }
-    if (!te_grid_barrier(&ds->bar_count, &ds->bar_gen, &ds->fatal)) return;
+    if (!te_grid_barrier(&ds->bar_count, &ds->bar_gen, &ds->fatal, a.spin_limit, a.arrivals)) return;
     double tot[2];
     te_grid_partials_sum<2>(tot, a.partials, scratch, bcast);
     const double f = sj * g;
@@ -517,7 +519,7 @@ __global__ void __launch_bounds__(TE_THREADS, REAL ? 6 : 5) lanczos_step_kernel(
     }
     te_block_sum_wide<1>(nrm, wide);
     if (threadIdx.x == 0) a.partials[2 * G + blockIdx.x] = nrm[0];
-    if (!te_grid_barrier(&ds->bar_count, &ds->bar_gen, &ds->fatal)) return;
+    if (!te_grid_barrier(&ds->bar_count, &ds->bar_gen, &ds->fatal, a.spin_limit, a.arrivals)) return;
     double t2[1];
     te_grid_partials_sum<1>(t2, a.partials + 2 * G, scratch, bcast);
     const double beta = fabs(g) * sqrt(t2[0]);
@@ -544,7 +546,7 @@ __global__ void __launch_bounds__(TE_THREADS, REAL ? 6 : 5) lanczos_step_kernel(
 }
 
 bool te_launch_lanczos_step(const TeSell& A, bool is_real, double2* const* cols, int m, double2* w, TeDevState* ds,
-                            double* partials, cudaStream_t st) {
+                            double* partials, cudaStream_t st, unsigned int spin_limit, unsigned int extra_arrivals) {
   if (A.lanes != 1 || A.n_long > 0 || m < 1 || m > TE_MMAX) return false;
   static int coop = -1;
   if (coop < 0) {
@@ -565,6 +567,8 @@ bool te_launch_lanczos_step(const TeSell& A, bool is_real, double2* const* cols,
   a.w = w;
   a.partials = partials;
   a.m = m;
+  a.spin_limit = spin_limit;
+  a.arrivals = (unsigned int)A.grid + extra_arrivals;
   for (int j = 0; j < TE_MMAX; ++j) a.u[j] = j < m ? cols[j] : nullptr;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(A.grid);

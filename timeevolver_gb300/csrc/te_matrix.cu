@@ -128,7 +128,7 @@ void te_launch_permute_real(int64_t n, const int32_t* idx, const double* in, dou
 
 // ------------------------------------------------- device build (kernels)
 
-enum { TE_CSR_BAD_COL = 1, TE_CSR_COMPLEX = 2, TE_CSR_OFFDIAG = 4 };
+enum { TE_CSR_BAD_COL = 1, TE_CSR_COMPLEX = 2, TE_CSR_OFFDIAG = 4, TE_CSR_NONFINITE = 8 };
 
 // One thread per row: column range, any imaginary part, any off-diagonal
 // entry (flag bits above) and the largest |value| (bit pattern of a
@@ -145,6 +145,7 @@ __global__ void csr_scan_kernel(int64_t n_rows, int64_t n_cols, const int32_t* _
       if (c < 0 || c >= n_cols) f |= TE_CSR_BAD_COL;
       if (x.y != 0.0) f |= TE_CSR_COMPLEX;
       if (c != r) f |= TE_CSR_OFFDIAG;
+      if (!isfinite(x.x) || !isfinite(x.y)) f |= TE_CSR_NONFINITE;
       vmax = fmax(vmax, hypot(x.x, x.y));
     }
   }
@@ -868,6 +869,11 @@ int build_matrix(te_matrix_s* M, const std::vector<int32_t>& rp, const std::vect
 
 int finish_create(int64_t n_rows, int64_t n_cols, const std::vector<int32_t>& rp, const std::vector<int32_t>& ci,
                   const std::vector<double>& vv, te_matrix* out, double norm1_given = NAN) {
+  for (size_t i = 0; i < vv.size(); ++i)
+    if (!std::isfinite(vv[i])) {
+      te_set_error("matrix creation: entry %lld is not finite (NaN or Inf)", (long long)(i / 2));
+      return TE_ERR_INVALID_ARG;
+    }
   te_matrix_s* M = new te_matrix_s();
   cudaGetDevice(&M->device);
   M->n_rows = n_rows;
@@ -917,6 +923,10 @@ int build_matrix_device(te_matrix_s* M, int32_t* d_rp, int32_t* d_ci, double2* d
     return fail(TE_ERR_CUDA);
   if (flags & TE_CSR_BAD_COL) {
     te_set_error("te_matrix_create_csr_device: a column index is out of range");
+    return fail(TE_ERR_INVALID_ARG);
+  }
+  if (flags & TE_CSR_NONFINITE) {
+    te_set_error("matrix creation: an entry is not finite (NaN or Inf)");
     return fail(TE_ERR_INVALID_ARG);
   }
   const bool real = !(flags & TE_CSR_COMPLEX);

@@ -41,7 +41,8 @@ OBS_SPARSE, OBS_VECTOR, OBS_STOP = 0, 1, 2
 def build(force=False):
     """Compile liboracle.so with g++ (OpenMP, no FP contraction)."""
     src = os.path.join(HERE, "te_oracle.cpp")
-    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src):
+    deps = [src, os.path.join(HERE, "te_oracle.h"), os.path.join(HERE, "te_quadrature.h")]
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= max(map(os.path.getmtime, deps)):
         return LIB_PATH
     os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
     cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
@@ -212,3 +213,74 @@ def set_ts_max_level(level):
     """Last tanh-sinh level (2..8) of the oracle's later integrals (8 restores
     the default)."""
     lib().oracle_set_ts_max_level(int(level))
+
+
+# ------------------------------------------------------------------------------
+# The reference itself, compiled by ref_recipe.py into _ref/libteref.so where the
+# reference tree is present (never on the GPU host): the restatement above is
+# checked against it.
+
+REF_LIB_PATH = os.path.join(HERE, "_ref", "libteref.so")
+_ref = None
+
+
+def build_ref(force=False):
+    """Compile the reference's own core into _ref/libteref.so (None where the
+    reference tree or numpy's OpenBLAS is missing)."""
+    from oracle import ref_recipe as recipe
+    return recipe.build_ref(force=force)
+
+
+def ref_available():
+    return os.path.exists(REF_LIB_PATH)
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        L = ctypes.CDLL(REF_LIB_PATH)
+        P, I64, D, I = ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, ctypes.c_int
+        L.teref_evolve.argtypes = [I64, I64, P, P, P, P, D, D, D, D, I, I, I, P, P, P, P, P, P, I64, P, P, P]
+        L.teref_evolve.restype = I
+        _ref = L
+    return _ref
+
+
+def ref_evolve(H, v, t, sampling_step, observables=(), exp_factor=1.0, tol=1e-6, m=40, fast_integration=False):
+    """The reference's own krylovTimeEvolver on the same inputs as evolve()
+    (observables: ("sparse", coo) or ("vector", o)); returns the same keys
+    (samples, state, err, evolved_time, num_samples, n_steps, krylov_dim,
+    status)."""
+    row, col, val = _coo(H)
+    n = int(len(v))
+    v = np.ascontiguousarray(v, dtype=np.complex128)
+    k = len(observables)
+    kinds = np.zeros(max(1, k), dtype=np.int32)
+    nnzs = np.zeros(max(1, k), dtype=np.int64)
+    rows, cols, vals = (ctypes.c_void_p * max(1, k))(), (ctypes.c_void_p * max(1, k))(), (ctypes.c_void_p * max(1, k))()
+    keep = []
+    for i, (kind, data) in enumerate(observables):
+        if kind == "sparse":
+            r, c, x = _coo(data)
+            keep += [r, c, x]
+            kinds[i], nnzs[i] = 0, len(x)
+            rows[i], cols[i], vals[i] = r.ctypes.data, c.ctypes.data, x.ctypes.data
+        elif kind == "vector":
+            x = np.ascontiguousarray(data, dtype=np.complex128)
+            keep.append(x)
+            kinds[i], vals[i] = 1, x.ctypes.data
+        else:
+            raise ValueError(kind)
+    cap = int(np.floor(t / sampling_step)) + 1
+    samples = np.zeros((max(1, k), cap))
+    state = np.zeros(n, dtype=np.complex128)
+    scalars = np.zeros(2)
+    counts = np.zeros(4, dtype=np.int64)
+    rc = ref_lib().teref_evolve(n, len(val), _p(row), _p(col), _p(val), _p(v), t, sampling_step, exp_factor, tol, m,
+                                int(fast_integration), k, _p(kinds), _p(nnzs), ctypes.addressof(rows),
+                                ctypes.addressof(cols), ctypes.addressof(vals), _p(samples), cap, _p(state),
+                                _p(scalars), _p(counts))
+    if rc != 0:
+        raise RuntimeError("teref_evolve failed with code %d" % rc)
+    return dict(samples=samples[:k], state=state, err=scalars[0], evolved_time=scalars[1],
+                num_samples=int(counts[0]), n_steps=int(counts[1]), krylov_dim=int(counts[2]), status=int(counts[3]))

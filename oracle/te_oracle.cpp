@@ -27,6 +27,7 @@
  * depend on the number of OpenMP threads.
  */
 #include "te_oracle.h"
+#include "te_quadrature.h"
 
 #include <algorithm>
 #include <cfloat>
@@ -42,150 +43,9 @@ typedef std::complex<double> cd;
 
 namespace {
 
-const int TS_KMIN = 2;   // always evaluate levels 0..2 before testing convergence
-const int TS_KMAX = 8;   // last refinement level
+using namespace te_quad;
 int g_ts_kmax = TS_KMAX;  // oracle_set_ts_max_level: a lower last level makes the rule miss its tolerance
-const double TS_TMAX = 3.0;  // nodes t in [-3, 3]
 const int N_BLOCK = 1024;
-
-/* ---------------------------------------------------------------- tables */
-
-struct TanhSinhTable {
-  // Nodes with t >= 0, grouped by level.  Level 0: t = 0,1,2,3; level k >= 1:
-  // t = (2i+1) 2^-k <= 3.  u = tanh(pi/2 sinh t), w = pi/2 cosh t / cosh^2(pi/2 sinh t).
-  std::vector<double> u, w, t;
-  std::vector<int> level_begin;  // size TS_KMAX + 2
-  TanhSinhTable() {
-    const double half_pi = 1.5707963267948966;
-    for (int k = 0; k <= TS_KMAX; ++k) {
-      level_begin.push_back((int)u.size());
-      if (k == 0) {
-        for (int i = 0; i <= 3; ++i) add(i, half_pi);
-      } else {
-        double h = std::ldexp(1.0, -k);
-        for (int i = 0;; ++i) {
-          double tt = (2 * i + 1) * h;
-          if (tt > TS_TMAX) break;
-          add(tt, half_pi);
-        }
-      }
-    }
-    level_begin.push_back((int)u.size());
-  }
-  void add(double tt, double half_pi) {
-    double s = half_pi * std::sinh(tt);
-    double cs = std::cosh(s);
-    t.push_back(tt);
-    u.push_back(std::tanh(s));
-    w.push_back(half_pi * std::cosh(tt) / (cs * cs));
-  }
-};
-
-struct GaussTable {
-  std::vector<double> x, w;  // full node set on [-1, 1]
-  explicit GaussTable(int n) {
-    // Newton iteration on P_n with the three-term Legendre recurrence,
-    // starting from the Chebyshev-like guess cos(pi (i + 3/4) / (n + 1/2)).
-    x.resize(n);
-    w.resize(n);
-    for (int i = 0; i < n; ++i) {
-      double z = std::cos(M_PI * (i + 0.75) / (n + 0.5));
-      double pp = 0;
-      for (int it = 0; it < 100; ++it) {
-        double p0 = 1.0, p1 = z;
-        for (int k = 2; k <= n; ++k) {
-          double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
-          p0 = p1;
-          p1 = p2;
-        }
-        pp = n * (z * p1 - p0) / (z * z - 1.0);
-        double dz = p1 / pp;
-        z -= dz;
-        if (std::fabs(dz) < 1e-17) break;
-      }
-      // recompute derivative at the converged root
-      double p0 = 1.0, p1 = z;
-      for (int k = 2; k <= n; ++k) {
-        double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
-        p0 = p1;
-        p1 = p2;
-      }
-      pp = n * (z * p1 - p0) / (z * z - 1.0);
-      x[i] = z;
-      w[i] = 2.0 / ((1.0 - z * z) * pp * pp);
-    }
-  }
-};
-
-const TanhSinhTable& ts_table() {
-  static TanhSinhTable t;
-  return t;
-}
-const GaussTable& gauss15() {
-  static GaussTable g(15);
-  return g;
-}
-const GaussTable& gauss7() {
-  static GaussTable g(7);
-  return g;
-}
-
-/* ------------------------------------------------------------ quadrature */
-
-struct TSResult {
-  double value, err, l1;
-  int levels;
-  bool nonfinite;
-};
-
-// Tanh-sinh on [a, b].  I_k = d h_k sum_{nodes of levels <= k} w f; the
-// error estimate at level k is |I_k - I_{k-1}|; stop at the first k >= KMIN
-// with err <= tol * L1_k, or at KMAX.
-template <class F>
-TSResult tanh_sinh(F&& f, double a, double b, double tol) {
-  TSResult r = {0, 0, 0, 0, false};
-  if (!(b > a)) return r;
-  const TanhSinhTable& T = ts_table();
-  double c = 0.5 * (a + b), d = 0.5 * (b - a);
-  double sum = 0, sum_abs = 0, prev = 0;
-  for (int k = 0; k <= g_ts_kmax; ++k) {
-    for (int j = T.level_begin[k]; j < T.level_begin[k + 1]; ++j) {
-      double fv;
-      if (T.t[j] == 0.0) {
-        fv = f(c);
-        sum += T.w[j] * fv;
-        sum_abs += T.w[j] * std::fabs(fv);
-      } else {
-        double fp = f(c + d * T.u[j]);
-        double fm = f(c - d * T.u[j]);
-        fv = fp + fm;
-        sum += T.w[j] * fv;
-        sum_abs += T.w[j] * (std::fabs(fp) + std::fabs(fm));
-      }
-      if (!std::isfinite(fv)) r.nonfinite = true;
-    }
-    double hk = std::ldexp(1.0, -k);
-    double I = d * hk * sum;
-    double L1 = d * hk * sum_abs;
-    r.levels = k;
-    r.value = I;
-    r.l1 = L1;
-    if (k >= 1) {
-      r.err = std::fabs(I - prev);
-      if (k >= TS_KMIN && r.err <= tol * L1) break;
-    }
-    prev = I;
-  }
-  return r;
-}
-
-template <class F>
-double gauss_rule(const GaussTable& g, F&& f, double a, double b) {
-  double c = 0.5 * (a + b), d = 0.5 * (b - a);
-  double s = 0;
-  for (size_t i = 0; i < g.x.size(); ++i) s += g.w[i] * f(c + d * g.x[i]);
-  return d * s;
-}
 
 /* --------------------------------------------------------------- BLAS-1 */
 
@@ -392,7 +252,7 @@ struct Evolver {
     } else if (method == 1) {
       ret = gauss_rule(gauss7(), f, a, b);
     } else {
-      TSResult r = tanh_sinh(f, a, b, termination);
+      TSResult r = tanh_sinh(f, a, b, termination, g_ts_kmax);
       if (r.nonfinite) {
         // the reference replaces a failed quadrature by 10*tol (:601-605)
         ret = tol * 10;
@@ -823,7 +683,7 @@ extern "C" double oracle_ts_test(int kind, double p, double a, double b, double 
     if (kind == 1) return std::cos(p * x);
     return std::exp(p * x);
   };
-  TSResult r = tanh_sinh(f, a, b, tol);
+  TSResult r = tanh_sinh(f, a, b, tol, g_ts_kmax);
   if (err) *err = r.err;
   if (l1) *l1 = r.l1;
   if (levels) *levels = r.levels;

@@ -9,7 +9,10 @@ value: seconds per solve with H, v and the observable resident in HBM (CUDA
 events on the evolver's stream).  e2e: the same solve through the C ABI with
 host buffers (COO upload, start vector, results back), wall clock.
 roofline: the Lanczos apply kernel (SELL-32 SpMV with the fused recurrence
-epilogue), algorithmic bytes per launch over its event-timed mean duration.
+epilogue): the algorithmic bytes of one complex128 CSR SpMV (20 nnz +
+4 (n + 1) + 32 n) over the kernel's event-timed mean duration; the bytes of
+the stored format (4 per entry with the value dictionary) and their fraction
+are given beside it, and `traffic` is the DRAM bytes ncu measured per launch.
 
 --impl reference: the CPU restatement of the reference algorithm (the oracle,
 OpenMP on all host cores), every step one whole solve of the same workload,
@@ -186,6 +189,14 @@ def spmv_option(spmv):
     return {None: 1, "fixed": 1, "fp64": 0}[spmv]
 
 
+def spmv_bytes(n, nnz):
+    """Algorithmic bytes of one SpMV of a complex128 CSR with int32 indices:
+    values and columns of every entry, the row pointers, x read once and y
+    written, B = 20 nnz + 4 (n + 1) + 32 n (the count the roofline is quoted
+    on, whatever the storage format)."""
+    return 20 * nnz + 4 * (n + 1) + 32 * n
+
+
 def apply_kernel_bytes(n, nnz, real=True, fixed=False, packed=False):
     """Algorithmic bytes of one Lanczos apply launch: the matrix (values +
     int32 columns; with the value dictionary one 4-byte word per entry), the
@@ -287,7 +298,8 @@ def run_gb300(args):
     value = replica_seconds_per_solve(ms, args.steps, ws)
     peaks = load_peaks(te)
     fixed = fixed_layout["state"] > 0
-    b_apply = apply_kernel_bytes(n, nnz, info["real"], fixed, fixed_layout["state"] == 2)
+    b_format = apply_kernel_bytes(n, nnz, info["real"], fixed, fixed_layout["state"] == 2)
+    b_apply = spmv_bytes(n, nnz)
     f_apply = apply_kernel_flops(n, nnz, info["real"], fixed)
     avg_apply_s = apply_ms / 1000.0 / max(1, apply_n)
     achieved = b_apply / avg_apply_s / 1e9
@@ -310,6 +322,9 @@ def run_gb300(args):
                      "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"],
                      "traffic": traffic, "algorithmic_bytes_per_launch": b_apply,
+                     "algorithmic_bytes": "complex128 CSR SpMV, 20 nnz + 4 (n + 1) + 32 n",
+                     "format_bytes_per_launch": b_format,
+                     "format_frac": b_format / avg_apply_s / 1e9 / peaks["hbm_gbs"],
                      "avg_launch_us": avg_apply_s * 1e6, "launches": apply_n,
                      "fp64": {"achieved_tflops": f_apply / avg_apply_s / 1e12, "peak_tflops": peaks["fp64_tflops"],
                               "peak_source": "measured (te_probe_fp64_tflops)",
@@ -584,9 +599,10 @@ def run_zipf(args):
     peaks = load_peaks(te)
     fl = H.fixed_layout()
     fixed = fl["state"] > 0
-    b_apply = apply_kernel_bytes(n, nnz, info["real"], fixed, fixed and fl["state"] == 2)
+    b_format = apply_kernel_bytes(n, nnz, info["real"], fixed, fixed and fl["state"] == 2)
     if fl["state"] == 3:  # column blocks: the int64 row sums written, re-read per block, read by the epilogue
-        b_apply += 2 * fl["n_values"] * 16 * n
+        b_format += 2 * fl["n_values"] * 16 * n
+    b_apply = spmv_bytes(n, nnz)
     f_apply = apply_kernel_flops(n, nnz, info["real"], fixed)
     avg = apply_ms / 1e3 / max(1, apply_n)
     line = {"metric": ZIPF_METRIC, "value": value, "unit": "s", "n_gpus": 1, "steps": args.steps,
@@ -606,7 +622,10 @@ def run_zipf(args):
                                     else "lanczos_apply_kernel (SELL-32 SpMV, complex H)"),
                          "achieved": b_apply / avg / 1e9, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": b_apply / avg / 1e9 / peaks["hbm_gbs"], "peak_source": peaks["source"],
-                         "traffic": None, "algorithmic_bytes_per_launch": b_apply, "avg_launch_us": avg * 1e6,
+                         "traffic": None, "algorithmic_bytes_per_launch": b_apply,
+                         "algorithmic_bytes": "complex128 CSR SpMV, 20 nnz + 4 (n + 1) + 32 n",
+                         "format_bytes_per_launch": b_format,
+                         "format_frac": b_format / avg / 1e9 / peaks["hbm_gbs"], "avg_launch_us": avg * 1e6,
                          "launches": apply_n,
                          "fp64": {"achieved_tflops": f_apply / avg / 1e12, "peak_tflops": peaks["fp64_tflops"],
                                   "frac": f_apply / avg / 1e12 / peaks["fp64_tflops"],

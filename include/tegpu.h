@@ -124,6 +124,17 @@ int te_matrix_create_zipf(int64_t n, double exponent, int32_t min_len, int32_t m
  * entries.  No counterpart in the reference. */
 int te_matrix_layout(te_matrix A, int64_t* sell_slots, int64_t* long_rows, int64_t* long_entries);
 
+/* Merge-path segments of the long rows (no counterpart in the reference,
+ * whose spMV is MKL's or a serial COO loop, matrixDataTypes.cpp:169-190): a
+ * long row of k entries is k + 1 merge items; segment_items (from the long
+ * rows' length histogram: at least 2048, about two segments per warp of a
+ * resident wave) bounds a segment.  Rows within it are multiplied
+ * warp-per-row; longer rows (split_rows of them) are split into segments of
+ * equal entry counts, one warp each, whose partial sums are added in segment
+ * order by the warp that finishes last (the sum does not depend on which
+ * warp ran which segment).  segments = all segments of all long rows. */
+int te_matrix_long_segments(te_matrix A, int64_t* segments, int64_t* split_rows, int64_t* segment_items);
+
 /* Lanes per row of the matrix's SELL-32 SpMV passes (no counterpart in the
  * reference).  1: one lane per row (the layout's native form); 2 or 4: each
  * row's entries are split over 2 or 4 lanes of a warp, which multiplies the

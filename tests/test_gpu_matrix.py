@@ -272,3 +272,68 @@ def test_coo_upload_rectangular(te_gpu, copy_path, monkeypatch):
     assert inf["norm1"] == colsum.max()
     with pytest.raises(RuntimeError, match="square"):
         M.layout()
+
+
+def _giant_matrix(n, hubs, hub_len, seed, complex_values):
+    """Random Hermitian rows of ~8 entries plus a few rows (and, mirrored,
+    columns) of hub_len entries, built with numpy (n up to a few 10^5)."""
+    rng = np.random.default_rng(seed)
+    r = np.repeat(np.arange(n), 4)
+    c = rng.integers(0, n, size=4 * n)
+    rows = [r] + [np.full(hub_len, h) for h in hubs]
+    cols = [c] + [rng.choice(n, size=hub_len, replace=False) for _ in hubs]
+    row, col = np.concatenate(rows), np.concatenate(cols)
+    val = rng.standard_normal(len(row)) + (1j * rng.standard_normal(len(row)) if complex_values else 0.0)
+    # H = (A + A^H) / 2, duplicates summed, row-sorted
+    R = np.concatenate([row, col])
+    C = np.concatenate([col, row])
+    V = np.concatenate([val, np.conj(val)]) / 2
+    key = R * n + C
+    uk, inv = np.unique(key, return_inverse=True)
+    acc = np.zeros(len(uk), dtype=np.complex128)
+    np.add.at(acc, inv, V)
+    return (uk // n).astype(np.int64), (uk % n).astype(np.int64), acc
+
+
+@pytest.mark.parametrize("complex_values", [False, True])
+def test_giant_rows_split_into_merge_path_segments(te_gpu, oracle_lib, complex_values):
+    """Rows of 120000 entries among rows of ~8 (dim 200000): each is split
+    into merge-path segments (one warp each, partial sums added in segment
+    order by the last warp), next to warp-per-row long rows.  The SpMV
+    (allocating and allocation-free entry points, repeated: the arrival counts
+    reset themselves) matches the COO product; evolutions on the fixed-point
+    and the FP64 passes match the oracle and repeat bit for bit."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+    n = 200_000
+    row, col, val = _giant_matrix(n, [5, n // 3, n - 2], 120_000, 21, complex_values)
+    M = te_gpu.Matrix(n, row, col, val)
+    seg = M.long_segments()
+    assert seg["segment_items"] >= 2048
+    assert seg["split_rows"] >= 3 and seg["segments"] > 3 * 50
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    y = np.zeros(n, dtype=np.complex128)
+    np.add.at(y, row, val * x[col])
+    scale = np.max(np.abs(y))
+    for _ in range(2):
+        assert np.max(np.abs(M.spmv(x) - y)) < 1e-12 * scale
+    xd = torch.from_numpy(x.view(np.float64).copy()).cuda()
+    for _ in range(2):
+        yd = torch.full_like(xd, float("nan"))
+        rc = te_gpu.lib().te_matrix_spmv_noalloc(M.handle, 1.0, 0.0, ctypes.c_void_p(xd.data_ptr()),
+                                                 ctypes.c_void_p(yd.data_ptr()), None)
+        assert rc == 0, te_gpu.lib().te_last_error()
+        torch.cuda.synchronize()
+        assert np.max(np.abs(yd.cpu().numpy().view(np.complex128) - y)) < 1e-12 * scale
+    v = x / np.linalg.norm(x)
+    d = (np.arange(n), np.arange(n), rng.uniform(-1, 1, n).astype(np.complex128))
+    ref = oracle_lib.evolve((row, col, val), v, 0.5, 0.25, [("sparse", d)], tol=1e-8, m=30)
+    for fixed in (1, 0):
+        runs = [te_gpu.evolve(M, v, 0.5, 0.25, [("sparse", d)], tol=1e-8, m=30,
+                              options={te_gpu.OPT_FIXED_SPMV: fixed}) for _ in range(2)]
+        assert np.array_equal(runs[0]["state"], runs[1]["state"])
+        gpu = runs[0]
+        assert gpu["status"] == ref["status"] and gpu["n_steps"] == ref["n_steps"]
+        assert np.linalg.norm(gpu["state"] - ref["state"]) < 2e-8
+        assert np.max(np.abs(gpu["samples"] - ref["samples"])) < 4e-8

@@ -70,6 +70,7 @@ SIGNATURES = {
     "te_matrix_download_csr": (_I, [_P, _P, _P, _P]),
     "te_matrix_set_spmv_lanes": (_I, [_P, _I]),
     "te_matrix_layout": (_I, [_P, _P, _P, _P]),
+    "te_matrix_long_segments": (_I, [_P, _P, _P, _P]),
     "te_model_create_device": (_I, [_I, _I, _I, _P, _I, _P, _P]),
     "te_model_state_index": (_I, [_I, _I, _I, _P, _P]),
     "te_matrix_spmv_lanes": (_I, [_P, _I]),
@@ -282,6 +283,13 @@ class Matrix:
         _check(lib().te_matrix_layout(self.handle, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
                "te_matrix_layout")
         return dict(sell_slots=a.value, long_rows=b.value, long_entries=c.value)
+
+    def long_segments(self):
+        """Merge-path segments of the long rows (te_matrix_long_segments)."""
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _check(lib().te_matrix_long_segments(self.handle, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)),
+               "te_matrix_long_segments")
+        return dict(segments=a.value, split_rows=b.value, segment_items=c.value)
 
     def fixed_layout(self):
         """Fixed-point form for the integer SpMV (te_matrix_fixed_layout):

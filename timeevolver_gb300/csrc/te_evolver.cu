@@ -73,6 +73,7 @@ struct te_evolver_s {
   int qr_sweeps = 0;                      // TE_OPT_QR_SWEEP_LIMIT (0: 40 m + 40)
   int4* X = nullptr;      // fixed-point copies of the Krylov vectors (m x n rows)
   longlong2* fx_acc = nullptr;  // column-blocked fixed-point SpMV: exact row sums (n rows)
+  TeSegCarry seg;               // carries of H's split long rows (this evolver's passes)
   int batch_cap = 0;         // states the batch buffer holds
   size_t results_cap = 0;    // doubles the results buffer holds
   std::vector<HostObs> obs;
@@ -233,6 +234,7 @@ void free_evolver(te_evolver ev) {
   cudaFreeHost(ev->host_state);
   cudaFree(ev->slab);
   cudaFree(ev->X);
+  te_seg_carry_free(&ev->seg);
   cudaFree(ev->fx_acc);
   cudaFree(ev->batch);
   cudaFree(ev->orig_tmp);
@@ -402,12 +404,12 @@ int run(te_evolver ev, te_result* out) {
           ev->launches += ev->H->sell.fix_nblk;  // the block passes before the epilogue
         } else if (fix_step) {
           te_launch_lanczos_apply_fix(ev->H->sell, ev->X + (int64_t)j * n, ev->cols[j],
-                                      j > 0 ? ev->cols[j - 1] : nullptr, ev->w, ev->ds, ev->partials, j, st);
+                                      j > 0 ? ev->cols[j - 1] : nullptr, ev->w, ev->ds, ev->partials, j, st, &ev->seg);
         }
         else
           te_launch_lanczos_apply(ev->H->sell, ev->H->is_real, ev->cols[j],
                                   (j > 0 && !cgs2) ? ev->cols[j - 1] : nullptr, ev->w, ev->ds, ev->partials, j, fold,
-                                  st);
+                                  st, &ev->seg);
       }
       if (!cgs2) {
         ProfScope ps(ev, 1);
@@ -603,6 +605,7 @@ extern "C" int te_evolver_create(te_matrix H, const double* v_host, const te_par
   if ((rc = te_cuda_check(cudaMalloc(&ev->ds, sizeof(TeDevState)), "state")) != TE_OK) return fail(rc);
   if ((rc = te_cuda_check(cudaMemset(ev->ds, 0, sizeof(TeDevState)), "state")) != TE_OK) return fail(rc);
   if ((rc = te_cuda_check(cudaMallocHost(&ev->sum, sizeof(Summary)), "pinned")) != TE_OK) return fail(rc);
+  if ((rc = te_seg_carry_alloc(H->sell, &ev->seg)) != TE_OK) return fail(rc);
   // basis columns, spare start vector, w, sampled state
   if ((rc = te_cuda_check(cudaMalloc(&ev->slab, sizeof(double2) * n * (m + 3)), "Krylov basis")) != TE_OK)
     return fail(rc);

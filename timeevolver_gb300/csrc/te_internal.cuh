@@ -134,6 +134,22 @@ struct TeSell {
   int64_t* long_ptr = nullptr;  // n_long + 1
   int32_t* long_col = nullptr;  // sorted-basis columns
   double* long_val = nullptr;   // real: 1, complex: 2 doubles per entry
+  // Merge-path segments of the long rows: a long row of k entries is k + 1
+  // merge items (its entries and its end); rows of at most seg_items items are
+  // one segment (multiplied warp-per-row), longer ones are split into
+  // ceil((k + 1) / seg_items) segments of equal entry counts, one warp each.
+  // seg_items comes from the long rows' length histogram (at least 2048, and
+  // about two segments per warp of a resident wave).  Segment s covers entries
+  // [seg_begin[s], seg_begin[s + 1]) of row seg_row[s]; row i owns segments
+  // [row_seg[i], row_seg[i + 1]).  n_split rows have more than one segment.
+  int64_t n_seg = 0, n_split = 0, seg_items = 0;
+  int32_t* seg_row = nullptr;
+  int64_t* seg_begin = nullptr;
+  int32_t* row_seg = nullptr;
+  // carries of the split rows owned by the matrix (te_matrix_spmv_noalloc;
+  // evolvers and te_matrix_spmv use their own)
+  double2* seg_part = nullptr;
+  unsigned int* seg_cnt = nullptr;
   // Fixed-point copy of the chunk values (te_fixed.cuh):
   // slot value round(h 2^fix_sh) as int32 limbs {h0, h1}, built on first use
   // by te_sell_build_fixed, with its own static schedule for the fixed-point
@@ -173,14 +189,35 @@ struct TeSell {
   } fix_blk[TE_FIX_MAX_BLOCKS];
 };
 
-// The long rows of a SELL matrix, by value for kernels.
+// Carries of the split long rows for one pass: the partial sum of every
+// segment and an arrival count per long row (zero between passes: the warp
+// that completes a row resets its count).  Passes that may overlap on the GPU
+// need their own.
+struct TeSegCarry {
+  double2* part = nullptr;    // n_seg
+  unsigned int* cnt = nullptr;  // n_long
+};
+// The long rows of a SELL matrix and their segments, by value for kernels.
 struct TeLongRows {
   int64_t n;
   const int64_t* ptr;
   const int32_t* col;
   const double* val;
+  int64_t n_seg;
+  const int32_t* seg_row;
+  const int64_t* seg_begin;
+  const int32_t* row_seg;
+  double2* part;
+  unsigned int* cnt;
 };
-inline TeLongRows te_long_rows(const TeSell& S) { return TeLongRows{S.n_long, S.long_ptr, S.long_col, S.long_val}; }
+inline TeLongRows te_long_rows(const TeSell& S, const TeSegCarry* carry = nullptr) {
+  return TeLongRows{S.n_long,   S.long_ptr, S.long_col, S.long_val, S.n_seg,
+                    S.seg_row,  S.seg_begin, S.row_seg,
+                    carry ? carry->part : S.seg_part, carry ? carry->cnt : S.seg_cnt};
+}
+// Allocate (zeroed) / free carries for the split rows of S (nothing when none).
+int te_seg_carry_alloc(const TeSell& S, TeSegCarry* c);
+void te_seg_carry_free(TeSegCarry* c);
 
 struct te_matrix_s {
   int64_t n_rows = 0, n_cols = 0, nnz = 0;
@@ -272,7 +309,7 @@ int te_sell_blocks_per_sm(bool is_real);
 // ---------------------------------------------------------------- launches
 // te_matrix.cu
 void te_launch_sell_spmv(const TeSell& A, bool is_real, double2 alpha, const double2* x_perm, double2* y_perm,
-                         cudaStream_t st);
+                         cudaStream_t st, const TeSegCarry* carry = nullptr);
 void te_launch_csr_spmv(const te_matrix_s& A, double2 alpha, const double2* x, double2* y, cudaStream_t st);
 void te_launch_permute(int64_t n, const int32_t* idx, const double2* in, double2* out, cudaStream_t st);
 void te_launch_permute_real(int64_t n, const int32_t* idx, const double* in, double* out, cudaStream_t st);
@@ -280,7 +317,8 @@ void te_launch_permute_real(int64_t n, const int32_t* idx, const double* in, dou
 // fold: store w / (expFactor s_j) instead of w (three-term mode with a
 // non-zero expFactor; the update kernel then takes the factor into s_{j+1}).
 void te_launch_lanczos_apply(const TeSell& A, bool is_real, const double2* u_j, const double2* u_jm1, double2* w,
-                             TeDevState* ds, double* partials, int j, bool fold, cudaStream_t st);
+                             TeDevState* ds, double* partials, int j, bool fold, cudaStream_t st,
+                             const TeSegCarry* carry = nullptr);
 // X_out (optional): also write the fixed-point copy of u_{j+1} (te_fixed.cuh)
 void te_launch_lanczos_update(int64_t n, const double2* w, const double2* u_j, double2* u_jp1, TeDevState* ds,
                               double* partials, int j, bool fold, cudaStream_t st, int4* X_out = nullptr);
@@ -303,7 +341,8 @@ int te_sell_refresh_fixed(te_matrix_s* A);
 void te_sell_free_fixed(TeSell& S);
 void te_launch_fix_start(int64_t n, const double2* u_0, int4* X, TeDevState* ds, double* partials, cudaStream_t st);
 void te_launch_lanczos_apply_fix(const TeSell& A, const int4* X, const double2* u_j, const double2* u_jm1,
-                                 double2* w, TeDevState* ds, double* partials, int j, cudaStream_t st);
+                                 double2* w, TeDevState* ds, double* partials, int j, cudaStream_t st,
+                                 const TeSegCarry* carry = nullptr);
 // Static warp schedule of the SpMV passes over the chunk offsets (host): warp w
 // of grid blocks owns chunks [wc[w], wc[w + 1]) of equal estimated work.
 void te_sell_schedule(const std::vector<int64_t>& off, int64_t n_chunks, int blocks_per_sm,

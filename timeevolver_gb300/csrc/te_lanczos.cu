@@ -96,9 +96,17 @@ __global__ void __launch_bounds__(TE_THREADS, (REAL && K == 1) ? 6 : 5) lanczos_
   const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (K == 1) {
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t lr = wid; lr < L.n; lr += warps) {  // long rows (sorted rows 0..L.n-1), warp-per-row
-      const double2 y = te_long_row<REAL>(L, lr, u_j, lane);
-      if (lane == 0) apply_row_epilogue<HAS_PREV, FOLD>(lr, y, g, cw, u_j, u_jm1, w, acc);
+    // long rows (sorted rows 0..L.n-1) by merge-path segments, one warp each
+    for (int64_t sg = wid; sg < L.n_seg; sg += warps) {
+      int64_t lr;
+      double2 y;
+      const int done = te_long_segment<REAL>(L, sg, u_j, lane, &lr, &y);
+      if (done == 1 && lane == 0) apply_row_epilogue<HAS_PREV, FOLD>(lr, y, g, cw, u_j, u_jm1, w, acc);
+      if (done == 2 && lane == 0) {  // a split row: its terms join the final sum in row order
+        double a2[2] = {0.0, 0.0};
+        apply_row_epilogue<HAS_PREV, FOLD>(lr, y, g, cw, u_j, u_jm1, w, a2);
+        te_split_row_publish(L, lr, a2);
+      }
     }
     const int64_t c_end = warp_chunk[wid + 1];
     for (int64_t c = warp_chunk[wid]; c < c_end; ++c) {
@@ -119,7 +127,7 @@ __global__ void __launch_bounds__(TE_THREADS, (REAL && K == 1) ? 6 : 5) lanczos_
   te_block_sum_wide<2>(acc, wide);
   if (te_publish_partials<2>(acc, partials, &ds->counter[0])) {
     double tot[2];
-    te_final_sum<2>(tot, partials, &ds->counter[0], scratch);
+    te_final_sum<2>(tot, partials, &ds->counter[0], scratch, [&](double (&o)[2]) { te_split_rows_add(o, L); });
     const double f = FOLD ? sj * g : sj;
     if (threadIdx.x == 0) {
       const double2 alpha = make_double2(f * tot[0], f * tot[1]);
@@ -148,15 +156,19 @@ __device__ __forceinline__ unsigned int te_block_max_from_smem(const unsigned in
 // in the last block alpha_j = f <u_j, w'> (f = s_j g), the update's
 // coefficient alpha_j / e, and the scale xs_{j+1} of the next vector from
 // B = W + (|Re| + |Im|)(alpha_j / e) U (W >= max|w'|, U >= max|u_j|).
+// L: the long rows whose split rows' terms are added in the final sum (none
+// for the column-blocked epilogue).
 __device__ __forceinline__ void fix_apply_finish(double (&acc)[2], unsigned int wmax, TeDevState* ds,
                                                  double* partials, int j, double f, double ie, double* scratch,
-                                                 double* wide, unsigned int* wmax_w) {
+                                                 double* wide, unsigned int* wmax_w, const TeLongRows* L) {
   te_warp_max_to_smem(wmax, wmax_w);
   te_block_sum_wide<2>(acc, wide);
   if (threadIdx.x == 0) atomicMax(&ds->fx_wmax, te_block_max_from_smem(wmax_w));
   if (te_publish_partials<2>(acc, partials, &ds->counter[0])) {
     double tot[2];
-    te_final_sum<2>(tot, partials, &ds->counter[0], scratch);
+    te_final_sum<2>(tot, partials, &ds->counter[0], scratch, [&](double (&o)[2]) {
+      if (L) te_split_rows_add(o, *L);
+    });
     if (threadIdx.x == 0) {
       const double2 alpha = make_double2(f * tot[0], f * tot[1]);
       ds->alpha[j] = alpha;
@@ -229,10 +241,14 @@ __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_f
   unsigned int wmax = 0;
   const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t lr = wid; lr < L.n; lr += warps) {
-    const double2 y = te_long_row<FMT != 2>(L, lr, u_j, lane);
-    if (lane == 0) {
-      const double2 wr = apply_row_epilogue<HAS_PREV, true>(lr, y, g, cw, u_j, u_jm1, w, acc);
+  for (int64_t sg = wid; sg < L.n_seg; sg += warps) {  // long rows: merge-path segments, FP64
+    int64_t lr;
+    double2 y;
+    const int done = te_long_segment<FMT != 2>(L, sg, u_j, lane, &lr, &y);
+    if (done && lane == 0) {
+      double a2[2] = {0.0, 0.0};  // a split row's terms join the final sum in row order
+      const double2 wr = apply_row_epilogue<HAS_PREV, true>(lr, y, g, cw, u_j, u_jm1, w, done == 1 ? acc : a2);
+      if (done == 2) te_split_row_publish(L, lr, a2);
       wmax = max(wmax, max(te_fix_hiword(wr.x), te_fix_hiword(wr.y)));
     }
   }
@@ -261,7 +277,7 @@ __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_f
       wmax = max(wmax, max(te_fix_hiword(wr.x), te_fix_hiword(wr.y)));
     }
   }
-  fix_apply_finish(acc, wmax, ds, partials, j, sj * g, ie, scratch, wide, wmax_w);
+  fix_apply_finish(acc, wmax, ds, partials, j, sj * g, ie, scratch, wide, wmax_w, &L);
 }
 
 // One column block of the fixed-point SpMV: for block row i (main row
@@ -325,7 +341,7 @@ __global__ void __launch_bounds__(TE_THREADS) fix_epilogue_kernel(int64_t n, con
                                                           acc);
     wmax = max(wmax, max(te_fix_hiword(wr.x), te_fix_hiword(wr.y)));
   }
-  fix_apply_finish(acc, wmax, ds, partials, j, sj * g, ie, scratch, wide, wmax_w);
+  fix_apply_finish(acc, wmax, ds, partials, j, sj * g, ie, scratch, wide, wmax_w, nullptr);
 }
 
 // Start of a Krylov step on the fixed-point path, two passes over u_0:
@@ -886,12 +902,13 @@ int te_sell_blocks_per_sm(bool is_real) {
 }
 
 void te_launch_lanczos_apply(const TeSell& A, bool is_real, const double2* u_j, const double2* u_jm1, double2* w,
-                             TeDevState* ds, double* partials, int j, bool fold, cudaStream_t st) {
+                             TeDevState* ds, double* partials, int j, bool fold, cudaStream_t st,
+                             const TeSegCarry* carry) {
   const int lanes = A.lanes;
   const ApplyKernel k = apply_kernel(lanes, is_real, u_jm1 != nullptr, fold);
   const int grid = lanes == 1 ? A.grid : apply_grid_k(A, lanes, k);
   te_launch_pdl(lanes == 1 && A.saturated, k, grid, TE_THREADS, st, A.n, A.n_chunks, A.warp_chunk, A.chunk_off,
-                A.col, A.val, te_long_rows(A), u_j, u_jm1, w, ds, partials, j);
+                A.col, A.val, te_long_rows(A, carry), u_j, u_jm1, w, ds, partials, j);
 }
 
 // Autotuning of the lanes per row of the FP64 passes (the fixed-point passes
@@ -1034,12 +1051,13 @@ int te_apply_fix_blocks_per_sm(int fmt, size_t dyn_smem) {
 }
 
 void te_launch_lanczos_apply_fix(const TeSell& A, const int4* X, const double2* u_j, const double2* u_jm1,
-                                 double2* w, TeDevState* ds, double* partials, int j, cudaStream_t st) {
+                                 double2* w, TeDevState* ds, double* partials, int j, cudaStream_t st,
+                                 const TeSegCarry* carry) {
   const int fmt = A.fix_val4 ? 2 : (A.fix_pk ? 1 : 0);
   const TeFixMatrix M{A.col, A.fix_val, A.fix_val4, A.fix_pk, A.fix_table, A.fix_nvals, A.fix_cbits, A.fix_sh};
   const size_t smem = fmt == 1 ? sizeof(int2) * A.fix_nvals : 0;
   te_launch_pdl_smem(A.fix_saturated, apply_fix_kernel(fmt, u_jm1 != nullptr), A.fix_grid, TE_THREADS, smem, st, A.n,
-                     A.fix_warp_chunk, A.chunk_off, M, te_long_rows(A), X, u_j, u_jm1, w, ds, partials, j);
+                     A.fix_warp_chunk, A.chunk_off, M, te_long_rows(A, carry), X, u_j, u_jm1, w, ds, partials, j);
 }
 
 

@@ -44,9 +44,11 @@ __global__ void __launch_bounds__(TE_THREADS) sell_spmv_kernel(int64_t n, int64_
   const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (K == 1) {
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t lr = wid; lr < L.n; lr += warps) {  // long rows, warp-per-row
-      const double2 acc = te_long_row<REAL>(L, lr, x, lane);
-      if (lane == 0) y[lr] = make_double2(alpha.x * acc.x - alpha.y * acc.y, alpha.x * acc.y + alpha.y * acc.x);
+    for (int64_t sg = wid; sg < L.n_seg; sg += warps) {  // long rows by merge-path segments
+      int64_t lr;
+      double2 acc;
+      if (te_long_segment<REAL>(L, sg, x, lane, &lr, &acc) != 0 && lane == 0)
+        y[lr] = make_double2(alpha.x * acc.x - alpha.y * acc.y, alpha.x * acc.y + alpha.y * acc.x);
     }
     const int64_t c_end = warp_chunk[wid + 1];
     for (int64_t c = warp_chunk[wid]; c < c_end; ++c) {
@@ -94,7 +96,7 @@ __global__ void permute_real_kernel(int64_t n, const int32_t* __restrict__ idx, 
 }
 
 void te_launch_sell_spmv(const TeSell& A, bool is_real, double2 alpha, const double2* x_perm, double2* y_perm,
-                         cudaStream_t st) {
+                         cudaStream_t st, const TeSegCarry* carry) {
   using K = void (*)(int64_t, int64_t, const int32_t*, const int64_t*, const int32_t*, const double*, TeLongRows,
                      double2, const double2*, double2*);
   static const K table[2][3] = {{sell_spmv_kernel<false, 1>, sell_spmv_kernel<false, 2>, sell_spmv_kernel<false, 4>},
@@ -106,8 +108,8 @@ void te_launch_sell_spmv(const TeSell& A, bool is_real, double2 alpha, const dou
     const int64_t cap = (int64_t)te_num_sms() * te_kernel_blocks_per_sm((const void*)k, TE_THREADS, 0);
     grid = (int)std::max<int64_t>(1, std::min<int64_t>((A.n_chunks * A.lanes + 7) / 8, cap));
   }
-  k<<<grid, TE_THREADS, 0, st>>>(A.n, A.n_chunks, A.warp_chunk, A.chunk_off, A.col, A.val, te_long_rows(A), alpha,
-                                 x_perm, y_perm);
+  k<<<grid, TE_THREADS, 0, st>>>(A.n, A.n_chunks, A.warp_chunk, A.chunk_off, A.col, A.val, te_long_rows(A, carry),
+                                 alpha, x_perm, y_perm);
 }
 
 void te_launch_csr_spmv(const te_matrix_s& A, double2 alpha, const double2* x, double2* y, cudaStream_t st) {
@@ -554,6 +556,22 @@ __global__ void __launch_bounds__(TE_THREADS) mirror_norm1_kernel(int64_t n, con
 
 // Static warp schedule of the SpMV passes (equal estimated work per warp:
 // 2 (real) or 4 (complex) FMAs per slot, about 8 per row for the epilogues).
+int te_seg_carry_alloc(const TeSell& S, TeSegCarry* c) {
+  *c = TeSegCarry{};
+  if (S.n_split == 0) return TE_OK;
+  TE_CUDA(cudaMalloc(&c->part, sizeof(double2) * S.n_seg));
+  int rc = te_cuda_check(cudaMalloc(&c->cnt, sizeof(unsigned int) * S.n_long), "segment carries");
+  if (rc == TE_OK) rc = te_cuda_check(cudaMemset(c->cnt, 0, sizeof(unsigned int) * S.n_long), "segment carries");
+  if (rc != TE_OK) te_seg_carry_free(c);
+  return rc;
+}
+
+void te_seg_carry_free(TeSegCarry* c) {
+  cudaFree(c->part);
+  cudaFree(c->cnt);
+  *c = TeSegCarry{};
+}
+
 void te_sell_schedule(const std::vector<int64_t>& off, int64_t n_chunks, int blocks_per_sm,
                       bool real, int& grid, bool& saturated, std::vector<int32_t>& wc) {
   const int64_t need = (n_chunks * 32 + TE_THREADS - 1) / TE_THREADS;
@@ -591,6 +609,11 @@ void free_matrix(te_matrix_s* M) {
   cudaFree(M->sell.long_ptr);
   cudaFree(M->sell.long_col);
   cudaFree(M->sell.long_val);
+  cudaFree(M->sell.seg_row);
+  cudaFree(M->sell.seg_begin);
+  cudaFree(M->sell.row_seg);
+  cudaFree(M->sell.seg_part);
+  cudaFree(M->sell.seg_cnt);
   te_sell_free_fixed(M->sell);
   delete M;
 }
@@ -727,6 +750,45 @@ int sell_layout_device(te_matrix_s* M, const int32_t* d_rp, bool real) {
   return done(sell_schedule(S, off, real));
 }
 
+// Merge-path segments of the long rows (lp: the long-row pointers, host).
+// A row of k entries is k + 1 merge items; seg_items is at least 2048 and
+// large enough for about two segments per warp of a resident wave over all
+// long rows' items, so a row is split only when it alone would hold up the
+// pass.  Rows split into equal entry counts per segment.  The matrix-owned
+// carries serve te_matrix_spmv_noalloc.
+int long_row_segments(TeSell& S, const std::vector<int64_t>& lp) {
+  const int64_t nl = S.n_long;
+  if (nl == 0) return TE_OK;
+  const int64_t items = lp[nl] + nl;
+  const int64_t wave_warps = (int64_t)te_num_sms() * 6 * (TE_THREADS / 32);
+  S.seg_items = std::max<int64_t>(2048, (items + 2 * wave_warps - 1) / (2 * wave_warps));
+  std::vector<int32_t> seg_row, row_seg(nl + 1, 0);
+  std::vector<int64_t> seg_begin;
+  S.n_split = 0;
+  for (int64_t i = 0; i < nl; ++i) {
+    const int64_t k = lp[i + 1] - lp[i];
+    const int64_t ns = std::max<int64_t>(1, (k + 1 + S.seg_items - 1) / S.seg_items);
+    if (ns > 1) ++S.n_split;
+    row_seg[i] = (int32_t)seg_row.size();
+    for (int64_t t = 0; t < ns; ++t) {
+      seg_row.push_back((int32_t)i);
+      seg_begin.push_back(lp[i] + k * t / ns);
+    }
+  }
+  row_seg[nl] = (int32_t)seg_row.size();
+  seg_begin.push_back(lp[nl]);
+  S.n_seg = (int64_t)seg_row.size();
+  int rc;
+  if ((rc = upload(&S.seg_row, seg_row.data(), seg_row.size())) != TE_OK) return rc;
+  if ((rc = upload(&S.seg_begin, seg_begin.data(), seg_begin.size())) != TE_OK) return rc;
+  if ((rc = upload(&S.row_seg, row_seg.data(), row_seg.size())) != TE_OK) return rc;
+  TeSegCarry c;
+  if ((rc = te_seg_carry_alloc(S, &c)) != TE_OK) return rc;
+  S.seg_part = c.part;
+  S.seg_cnt = c.cnt;
+  return TE_OK;
+}
+
 // The long-row CSR in the sorted basis from the device CSR (perm and iperm
 // final): one device pass after a host prefix over the long rows' lengths.
 int long_rows_device(te_matrix_s* M, const int32_t* d_rp, const int32_t* d_ci, const double2* d_v, bool real) {
@@ -744,6 +806,7 @@ int long_rows_device(te_matrix_s* M, const int32_t* d_rp, const int32_t* d_ci, c
   std::vector<int64_t> lp(nl + 1, 0);
   for (int64_t i = 0; i < nl; ++i) lp[i + 1] = lp[i] + len[i];
   if ((rc = upload(&S.long_ptr, lp.data(), lp.size())) != TE_OK) return rc;
+  if ((rc = long_row_segments(S, lp)) != TE_OK) return rc;
   const int64_t ne = std::max<int64_t>(lp[nl], 1);
   if ((rc = te_cuda_check(cudaMalloc(&S.long_col, sizeof(int32_t) * ne), "long rows")) != TE_OK ||
       (rc = te_cuda_check(cudaMalloc(&S.long_val, sizeof(double) * (real ? 1 : 2) * ne), "long rows")) != TE_OK)
@@ -779,7 +842,8 @@ int build_long_rows(te_matrix_s* M, const std::vector<int32_t>& rp, const std::v
   int rc;
   if ((rc = upload(&S.long_ptr, lp.data(), lp.size())) != TE_OK) return rc;
   if ((rc = upload(&S.long_col, lc.data(), lc.size())) != TE_OK) return rc;
-  return upload(&S.long_val, lv.data(), lv.size());
+  if ((rc = upload(&S.long_val, lv.data(), lv.size())) != TE_OK) return rc;
+  return long_row_segments(S, lp);
 }
 
 // rp/ci/vv: original-order CSR with interleaved complex values.
@@ -1330,6 +1394,17 @@ extern "C" int te_matrix_download_csr(te_matrix A, int32_t* row_ptr, int32_t* co
   return TE_OK;
 }
 
+extern "C" int te_matrix_long_segments(te_matrix A, int64_t* segments, int64_t* split_rows, int64_t* segment_items) {
+  if (!A || A->n_rows != A->n_cols) {
+    te_set_error("te_matrix_long_segments: square matrix required");
+    return TE_ERR_INVALID_ARG;
+  }
+  if (segments) *segments = A->sell.n_seg;
+  if (split_rows) *split_rows = A->sell.n_split;
+  if (segment_items) *segment_items = A->sell.seg_items;
+  return TE_OK;
+}
+
 extern "C" int te_matrix_layout(te_matrix A, int64_t* sell_slots, int64_t* long_rows, int64_t* long_entries) {
   if (!A || A->n_rows != A->n_cols) {
     te_set_error("te_matrix_layout: square matrix required");
@@ -1410,16 +1485,27 @@ extern "C" int te_matrix_spmv(te_matrix A, double alpha_re, double alpha_im, con
   const int64_t n = A->n_rows;
   // permute in, SELL product, permute out
   double2 *xp = nullptr, *yp = nullptr;
+  TeSegCarry carry;  // this call's carries of the split long rows (calls may overlap)
   TE_CUDA(cudaMallocAsync(&xp, sizeof(double2) * n, st));
   int rc = te_cuda_check(cudaMallocAsync(&yp, sizeof(double2) * n, st), "cudaMallocAsync");
+  if (rc == TE_OK && A->sell.n_split > 0) {
+    rc = te_cuda_check(cudaMallocAsync(&carry.part, sizeof(double2) * A->sell.n_seg, st), "cudaMallocAsync");
+    if (rc == TE_OK)
+      rc = te_cuda_check(cudaMallocAsync(&carry.cnt, sizeof(unsigned int) * A->sell.n_long, st), "cudaMallocAsync");
+    if (rc == TE_OK)
+      rc = te_cuda_check(cudaMemsetAsync(carry.cnt, 0, sizeof(unsigned int) * A->sell.n_long, st), "memset");
+  }
   if (rc == TE_OK) {
     te_launch_permute(n, A->sell.perm, reinterpret_cast<const double2*>(in_dev), xp, st);
-    te_launch_sell_spmv(A->sell, A->is_real, make_double2(alpha_re, alpha_im), xp, yp, st);
+    te_launch_sell_spmv(A->sell, A->is_real, make_double2(alpha_re, alpha_im), xp, yp, st,
+                        A->sell.n_split > 0 ? &carry : nullptr);
     te_launch_permute(n, A->sell.iperm, yp, reinterpret_cast<double2*>(out_dev), st);
     rc = te_cuda_check(cudaGetLastError(), "spmv launch");
   }
   cudaFreeAsync(xp, st);
   cudaFreeAsync(yp, st);
+  if (carry.part) cudaFreeAsync(carry.part, st);
+  if (carry.cnt) cudaFreeAsync(carry.cnt, st);
   return rc;
 }
 

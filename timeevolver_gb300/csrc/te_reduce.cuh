@@ -77,10 +77,12 @@ __device__ __forceinline__ bool te_publish_partials(const double (&v)[NV], doubl
 }
 
 // In the last block: sum the partials of NV values over all blocks in a fixed
-// order.  Result valid in thread 0; resets the counter.
-template <int NV>
+// order.  Result valid in thread 0; resets the counter.  extra(out) may add
+// further per-thread terms (in an order fixed by the thread index) before the
+// block tree.
+template <int NV, typename Extra>
 __device__ __forceinline__ void te_final_sum(double (&out)[NV], const double* partials, unsigned int* counter,
-                                             double* scratch) {
+                                             double* scratch, Extra extra) {
 #pragma unroll
   for (int k = 0; k < NV; ++k) out[k] = 0.0;
   // blocks ascending per thread for every value (the loads of consecutive
@@ -90,6 +92,13 @@ __device__ __forceinline__ void te_final_sum(double (&out)[NV], const double* pa
 #pragma unroll
     for (int k = 0; k < NV; ++k) out[k] += __ldcg(partials + k * gridDim.x + b);
   }
+  extra(out);
   te_block_sum<NV>(out, scratch);
   if (threadIdx.x == 0) *counter = 0u;
+}
+
+template <int NV>
+__device__ __forceinline__ void te_final_sum(double (&out)[NV], const double* partials, unsigned int* counter,
+                                             double* scratch) {
+  te_final_sum<NV>(out, partials, counter, scratch, [](double (&)[NV]) {});
 }

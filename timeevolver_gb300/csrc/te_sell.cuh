@@ -127,12 +127,11 @@ __device__ __forceinline__ double2 te_sell_row_k(const int64_t* __restrict__ chu
   return make_double2(re, im);
 }
 
-// One long row (row lr of the long-row CSR) by a whole warp: lanes stride over
-// its entries, then a warp sum; the result is returned to every lane.
+// Entries [b, e) of the long-row CSR times x by a whole warp: lanes stride
+// over the entries, then a warp sum (lane 0's value is the one used).
 template <bool REAL, bool XCG = false>
-__device__ __forceinline__ double2 te_long_row(const TeLongRows& L, int64_t lr, const double2* __restrict__ x,
-                                               int lane) {
-  const int64_t b = __ldg(L.ptr + lr), e = __ldg(L.ptr + lr + 1);
+__device__ __forceinline__ double2 te_long_range(const TeLongRows& L, int64_t b, int64_t e,
+                                                 const double2* __restrict__ x, int lane) {
   double re = 0.0, im = 0.0;
   if (REAL) {
     for (int64_t p = b + lane; p < e; p += 32) {
@@ -159,3 +158,75 @@ __device__ __forceinline__ double2 te_long_row(const TeLongRows& L, int64_t lr, 
   }
   return make_double2(re, im);
 }
+
+// Merge-path segment s of the long rows by one warp.  Returns non-zero when
+// this warp completes its row (then *row and *y hold the row and its sum,
+// lane 0's value being the one used): 1 at once for a row of one segment
+// (warp-per-row); 2 for a split row, where every warp publishes its segment's
+// partial sum and the warp that arrives last adds the row's partials in
+// segment order (lane k takes segments k, k + 32, ..., then a fixed shuffle
+// tree), so the sum does not depend on which warps ran which segments, and
+// resets the row's count.  Which warp completes a split row varies from run
+// to run, so a pass that reduces over rows must not fold a split row's terms
+// into that warp's sums: te_split_row_publish / te_split_rows_add move them
+// to a fixed place in the final reduction.
+template <bool REAL, bool XCG = false>
+__device__ __forceinline__ int te_long_segment(const TeLongRows& L, int64_t s, const double2* __restrict__ x,
+                                               int lane, int64_t* row, double2* y) {
+  const int32_t i = __ldg(L.seg_row + s);
+  const double2 part = te_long_range<REAL, XCG>(L, __ldg(L.seg_begin + s), __ldg(L.seg_begin + s + 1), x, lane);
+  *row = i;
+  const int32_t s0 = __ldg(L.row_seg + i), s1 = __ldg(L.row_seg + i + 1);
+  if (s1 - s0 == 1) {
+    *y = part;
+    return 1;
+  }
+  int last = 0;
+  if (lane == 0) {
+    __stcg(L.part + s, part);
+    __threadfence();
+    last = atomicAdd(L.cnt + i, 1u) == (unsigned int)(s1 - s0 - 1) ? 1 : 0;
+  }
+  last = __shfl_sync(0xffffffffu, last, 0);
+  if (!last) return 0;
+  __threadfence();
+  double re = 0.0, im = 0.0;
+  for (int32_t t = s0 + lane; t < s1; t += 32) {
+    const double2 p = __ldcg(L.part + t);
+    re += p.x;
+    im += p.y;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    re += __shfl_xor_sync(0xffffffffu, re, o);
+    im += __shfl_xor_sync(0xffffffffu, im, o);
+  }
+  if (lane == 0) L.cnt[i] = 0u;
+  *y = make_double2(re, im);
+  return 2;
+}
+
+// The reduction terms (v[0], v[1]) of split long row i, stored by the warp
+// that completed it (one lane) in the row's first carry slot, whose partial
+// sum that warp has consumed; the fence orders the store before the block's
+// publication of its own partials.
+__device__ __forceinline__ void te_split_row_publish(const TeLongRows& L, int64_t i, const double (&v)[2]) {
+  __stcg(L.part + __ldg(L.row_seg + i), make_double2(v[0], v[1]));
+  __threadfence();
+}
+
+// In the last block of a pass (after every block has published): add the
+// split long rows' terms to this thread's values, rows ascending per thread
+// (thread t takes rows t, t + blockDim.x, ...), a fixed order.
+__device__ __forceinline__ void te_split_rows_add(double (&out)[2], const TeLongRows& L) {
+  if (L.n_seg == L.n) return;  // no split rows
+  for (int64_t i = threadIdx.x; i < L.n; i += blockDim.x) {
+    const int32_t s0 = __ldg(L.row_seg + i), s1 = __ldg(L.row_seg + i + 1);
+    if (s1 - s0 > 1) {
+      const double2 p = __ldcg(L.part + s0);
+      out[0] += p.x;
+      out[1] += p.y;
+    }
+  }
+}
+

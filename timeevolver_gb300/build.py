@@ -26,7 +26,7 @@ CUDA_SOURCES = ["te_common.cu", "te_matrix.cu", "te_lanczos.cu", "te_krylov.cu",
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC"]
 HOST_SOURCES = ["matrixDataTypes.cpp", "krylovObservables.cpp", "krylovTimeEvolver.cpp", "krylovLogger.cpp",
-                "krylovHelper.cpp",
+                "krylovHelper.cpp", "h5min.cpp",
                 "Basis.cpp", "hamiltonian.cpp", "te_host_c.cpp"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off"]
 

@@ -335,9 +335,29 @@ def run_gb300(args):
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(Hc, Oc, v)
+    if ws == 1 and not args.no_other_workloads:
+        line["other_workloads"] = other_workloads(args)
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def other_workloads(args):
+    """The load-imbalanced, batched and adjoint workloads measured in the same
+    run (each its own full line: clocks sampled in its timed region, 1 warm-up
+    and 2 timed steps, no CPU leg), so that their numbers come from the same
+    box and record as the headline."""
+    sub = argparse.Namespace(**vars(args))
+    sub.steps, sub.warmup, sub.no_cpu_baseline = 2, 1, True
+    out = {}
+    for name, fn in (("zipf_1e7", run_zipf), ("batched_256", run_batched), ("adjoint_l10", run_adjoint)):
+        t0 = time.perf_counter()
+        try:
+            out[name] = fn(sub)
+        except Exception as exc:  # report, do not hide the headline
+            out[name] = {"error": "%s: %s" % (type(exc).__name__, exc)}
+        out[name]["wall_s"] = round(time.perf_counter() - t0, 1)
+    return out
 
 
 def oracle_solve(Hc, Oc, v, cores):
@@ -436,13 +456,31 @@ def run_batched(args):
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     launches = 0
+    with ClockSampler(0) as clk:
+        start.record(stream)
+        for _ in range(args.steps):
+            res = batch.run()
+            launches += batch.launch_count()
+        stop.record(stream)
+        stop.synchronize()
+    batch_ms = start.elapsed_time(stop) / args.steps
+    graph_samples = [batch.samples(i) for i in range(len(specs))]
+    # the same batch in one persistent launch per run
+    batch.set_option(te.BATCH_OPT_PERSISTENT, 1)
+    for _ in range(args.warmup):
+        batch.run()
+    torch.cuda.synchronize()
+    p_launches = 0
     start.record(stream)
     for _ in range(args.steps):
-        res = batch.run()
-        launches += batch.launch_count()
+        res_p = batch.run()
+        p_launches += batch.launch_count()
     stop.record(stream)
     stop.synchronize()
-    batch_ms = start.elapsed_time(stop) / args.steps
+    pers_ms = start.elapsed_time(stop) / args.steps
+    pers_diff = [i for i in range(len(specs))
+                 if res_p[i] != res[i] or not np.array_equal(batch.samples(i), graph_samples[i])]
+    batch.set_option(te.BATCH_OPT_PERSISTENT, 0)
     # per-instance loop of the plain evolver (evolvers created once, reset and run)
     evs = [te.Evolver(H, s["v"], s["t"], s["t"], [("sparse", O)], tol=1e-8, m=32) for s, (H, O) in zip(specs, mats)]
     for ev, s in zip(evs, specs):
@@ -465,11 +503,17 @@ def run_batched(args):
             "data": "synthetic (seeded Bose-Hubbard chains)",
             "config": {"workload": BATCH_WORKLOAD, "total_rows": int(sum(s["n"] for s in specs)),
                        "krylov_steps_min_mean_max": [int(min(steps)), float(np.mean(steps)), int(max(steps))]},
+            "clocks": clk.summary(),
+            "timing": "batch arms: CUDA events on the batch stream; per-instance loop: host wall clock between "
+                      "device synchronisations",
             "per_instance_loop": {"value": len(specs) / (loop_ms / 1e3), "unit": "solves/s", "ms": loop_ms,
                                   "gpu_launches": int(loop_launches),
                                   "instances_with_equal_step_count": same_steps},
-            "speedup_vs_loop": loop_ms / batch_ms, "gpu_launches": int(launches)}
-    print(json.dumps(line), flush=True)
+            "speedup_vs_loop": loop_ms / batch_ms, "gpu_launches": int(launches),
+            "persistent_launch": {"value": len(specs) / (pers_ms / 1e3), "unit": "solves/s", "ms": pers_ms,
+                                  "gpu_launches": int(p_launches), "same_results_as_graph_path": not pers_diff, "instances_differing": pers_diff[:8],
+                                  "speedup_vs_loop": loop_ms / pers_ms}}
+    return line
 
 
 ADJ_METRIC = "grads/s (adjoint d<n_0(T)>/d(J_1..J_9, U), Bose-Hubbard L=10 N=10, T=5, tol 1e-10, m=40)"
@@ -498,11 +542,12 @@ def run_adjoint(args, nodes=16):
         adj.run(theta)
         adj.forward(theta)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        loss, grad = adj.run(theta)
-    torch.cuda.synchronize()
-    t_grad = (time.perf_counter() - t0) / args.steps
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            loss, grad = adj.run(theta)
+        torch.cuda.synchronize()
+        t_grad = (time.perf_counter() - t0) / args.steps
     st = adj.stats()
     phases = adj.phase_times()
     t0 = time.perf_counter()
@@ -536,8 +581,9 @@ def run_adjoint(args, nodes=16):
             "phase_ms": {k: round(v, 3) for k, v in phases.items()},
             "fd_check": {"method": "central differences, Richardson over h and h/2", "step": h, "fd_tol": fd_tol,
                          "max_abs_diff_rel": rel, "target_rel": 1e-6, "grad": grad.tolist(), "fd": fd.tolist()},
-            "gpu_launches_per_gradient": int(st["launches"])}
-    print(json.dumps(line), flush=True)
+            "gpu_launches_per_gradient": int(st["launches"]), "clocks": clk.summary(),
+            "timing": "host wall clock between device synchronisations (gradient and forward alike)"}
+    return line
 
 
 ZIPF_N, ZIPF_T = 10_000_000, 100.0
@@ -634,7 +680,7 @@ def run_zipf(args):
             "clocks": clk.summary()}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = zipf_cpu_baseline(te, nnz, r.n_steps)
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def zipf_cpu_baseline(te, nnz_full, steps_full):
@@ -690,6 +736,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-other-workloads", action="store_true",
+                    help="plain config: skip the load-imbalanced, batched and adjoint workloads that the default run "
+                         "measures after the headline and attaches to its line")
     ap.add_argument("--config", default="plain", choices=["plain", "batched", "adjoint", "zipf"],
                     help="plain: the L=12 single evolution (headline); batched: 256 chains in one batch; "
                          "adjoint: gradients of <n_0(T)> for L=10; zipf: the dim-1e7 load-imbalanced matrix")
@@ -709,18 +758,11 @@ def main():
         return
     if args.impl == "reference":
         run_reference(args)
-    elif args.config == "batched":
+    elif args.config in ("batched", "adjoint", "zipf"):
         import timeevolver_gb300 as te
         te.build()
-        run_batched(args)
-    elif args.config == "adjoint":
-        import timeevolver_gb300 as te
-        te.build()
-        run_adjoint(args)
-    elif args.config == "zipf":
-        import timeevolver_gb300 as te
-        te.build()
-        run_zipf(args)
+        fn = {"batched": run_batched, "adjoint": run_adjoint, "zipf": run_zipf}[args.config]
+        print(json.dumps(fn(args)), flush=True)
     else:
         import timeevolver_gb300 as te
         te.build()

@@ -185,13 +185,34 @@ typedef struct te_term {
  * (helper/hamiltonian.cpp:318-402: terms applied per row in order, equal
  * columns merged in term order, columns ascending, |v| < DBL_EPSILON dropped),
  * so the result equals the host builder's entry for entry.  The 1-norm is the
- * reference's for Hermitian term lists.  Up to 64 modes, 255 particles, 64
+ * reference's for Hermitian term lists.  Up to 64 modes, 255 particles, 128
  * terms; *dim receives the dimension. */
 int te_model_create_device(int n_particles, int n_modes, int quant, const te_term* terms, int n_terms,
                            te_matrix* out, int64_t* dim);
 /* Index of an occupation vector (n_modes ints) in that basis, -1 if it is not
  * a basis state. */
 int te_model_state_index(int n_particles, int n_modes, int quant, const int32_t* occupation, int64_t* index);
+
+/* A basis for the device builder, given by the constructor arguments of the
+ * reference's bases:
+ *   n_modes2 == 0: basis(n_particles, n_modes, n_qudits, capacity, quant)
+ *     (helper/Basis.cpp:37-121): modes n_modes - n_qudits .. n_modes - 1 hold
+ *     at most `capacity` particles; when every mode is a qudit, states whose
+ *     mode 0 would exceed it are dropped;
+ *   n_modes2 > 0: tensorBasis(n_particles, n_modes, n_particles2, n_modes2,
+ *     capacity2) (helper/Basis.cpp:131-182): basis(n_particles, n_modes, 0, 0)
+ *     times basis(n_particles2, n_modes2, n_modes2, capacity2), the first set's
+ *     modes first, index i1 * dim2 + i2 (n_qudits 0 and quant 1 required). */
+typedef struct te_basis_desc {
+  int32_t n_particles, n_modes, n_qudits, capacity, quant;
+  int32_t n_particles2, n_modes2, capacity2;
+} te_basis_desc;
+/* te_model_create_device on any such basis (same rules, up to 64 modes in
+ * all); an empty second set of a tensor basis is rejected. */
+int te_model_create_device_basis(const te_basis_desc* basis, const te_term* terms, int n_terms, te_matrix* out,
+                                 int64_t* dim);
+/* Index of an occupation vector (all modes) in that basis, -1 if absent. */
+int te_model_basis_index(const te_basis_desc* basis, const int32_t* occupation, int64_t* index);
 
 /* Copy a matrix's original-order CSR to host buffers: row_ptr (n_rows + 1),
  * col_idx (nnz), values (nnz interleaved complex doubles). */
@@ -417,6 +438,26 @@ int te_batch_samples(te_batch b, int instance, int obs_index, double* out_host, 
 int te_batch_state(te_batch b, int instance, double* out_host);
 int64_t te_batch_launch_count(te_batch b);
 void* te_batch_stream(te_batch b);
+/* Global steps of the last te_batch_run (each: one Krylov step of every
+ * running instance).  No counterpart in the reference. */
+int64_t te_batch_global_steps(te_batch b);
+
+/* Batch options (no counterpart in the reference).
+ * TE_BATCH_OPT_PERSISTENT: 0 (default) replays the launches of one global step
+ *   as a CUDA graph and waits for each; 1 runs the whole batch in one
+ *   persistent cooperative launch (one 1024-thread block per SM, the passes
+ *   separated by grid barriers with bounded waits), which gives the same
+ *   results bit for bit and waits once per run.
+ * TE_BATCH_OPT_BARRIER_SPIN_LIMIT: polls before a grid-barrier wait of the
+ *   persistent kernel gives up (te_batch_run then returns
+ *   TE_ERR_DEVICE_TIMEOUT); default 2^22. */
+#define TE_BATCH_OPT_PERSISTENT 1
+#define TE_BATCH_OPT_BARRIER_SPIN_LIMIT 2
+/* TE_BATCH_OPT_BARRIER_EXTRA_ARRIVALS: 1 makes every grid barrier of the
+ *   persistent kernel wait for one block more than the grid has, so that the
+ *   first wait runs out (a test of the timeout path); default 0. */
+#define TE_BATCH_OPT_BARRIER_EXTRA_ARRIVALS 3
+int te_batch_set_option(te_batch b, int option, int value);
 
 /* ------------------------------------------------------------------ adjoint */
 

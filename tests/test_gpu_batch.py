@@ -70,3 +70,58 @@ def test_batch_rerun_is_deterministic(te_gpu):
     assert r1 == r2
     for a, b in zip(s1, s2):
         assert np.array_equal(a, b)
+
+
+def _batch(te, specs, persistent):
+    inst = [dict(H=te.Matrix.from_coo(s["n"], s["coo"]), v=s["v"], t=s["t"], sampling_step=s["sampling_step"],
+                 tol=s["tol"], m=s["m"], observables=[te.Matrix.from_coo(s["n"], s["n0"])]) for s in specs]
+    return te.Batch(inst, persistent=persistent)
+
+
+def test_persistent_launch_equals_graph_path(te_gpu, oracle_lib):
+    """The whole batch in one persistent cooperative launch runs the graph
+    path's passes over the same logical schedule: results, samples and final
+    states equal bit for bit, with one kernel launch per run (after the two of
+    the reset), and a second run repeats the first."""
+    specs = _instances(te_gpu, 3, 24)
+    graph = _batch(te_gpu, specs, False)
+    rg = graph.run()
+    pers = _batch(te_gpu, specs, True)
+    for rep in range(2):
+        rp = pers.run()
+        assert pers.launch_count() == 3
+        assert pers.global_steps() == graph.global_steps() > 0
+        assert rp == rg
+        for i in range(len(specs)):
+            assert np.array_equal(pers.samples(i), graph.samples(i)), i
+            assert np.array_equal(pers.state(i), graph.state(i)), i
+    s = specs[7]
+    ref = oracle_lib.evolve(s["coo"], s["v"], s["t"], s["sampling_step"], [("sparse", s["n0"])], tol=s["tol"],
+                            m=s["m"])
+    assert np.linalg.norm(pers.state(7) - ref["state"]) < 2 * s["tol"]
+    graph.close()
+    pers.close()
+
+
+def test_persistent_barrier_timeout_then_recovers(te_gpu):
+    """A grid barrier that waits for one block more than the grid has gives up
+    after the spin limit: te_batch_run returns TE_ERR_DEVICE_TIMEOUT (no hang,
+    the context stays usable), and the same batch then runs normally."""
+    specs = _instances(te_gpu, 5, 6)
+    ref = _batch(te_gpu, specs, False)
+    rr = ref.run()
+    b = _batch(te_gpu, specs, True)
+    b.set_option(te_gpu.BATCH_OPT_BARRIER_SPIN_LIMIT, 2000)
+    b.set_option(te_gpu.BATCH_OPT_BARRIER_EXTRA_ARRIVALS, 1)
+    with pytest.raises(te_gpu.TeError) as e:
+        b.run()
+    assert e.value.code == -10  # TE_ERR_DEVICE_TIMEOUT
+    b.set_option(te_gpu.BATCH_OPT_BARRIER_EXTRA_ARRIVALS, 0)
+    b.set_option(te_gpu.BATCH_OPT_BARRIER_SPIN_LIMIT, 1 << 22)
+    assert b.run() == rr
+    for i in range(len(specs)):
+        assert np.array_equal(b.samples(i), ref.samples(i))
+    with pytest.raises(te_gpu.TeError):
+        b.set_option(te_gpu.BATCH_OPT_PERSISTENT, 2)
+    ref.close()
+    b.close()

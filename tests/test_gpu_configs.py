@@ -129,6 +129,27 @@ def test_batched_instances_match_oracle(te_gpu, oracle_lib, batched_specs):
           "another step count on %s" % (worst_state, worst_obs, fixed_diff))
 
 
+def test_batched_persistent_launch_equals_graph_path(te_gpu, batched_specs):
+    """The benchmark's own instances (L 6..10, m=32) in one persistent launch
+    and through the per-step graph: same results, samples and states bit for
+    bit (the persistent kernel rereads what its blocks rewrite between grid
+    barriers through L2, so no SM uses a stale copy)."""
+    specs = batched_specs
+    mats = [(te_gpu.Matrix.from_coo(s["n"], s["coo"]), te_gpu.Matrix.from_coo(s["n"], s["n0"])) for s in specs]
+    inst = [dict(H=H, v=s["v"], t=s["t"], sampling_step=s["t"], tol=TOL, m=32, observables=[O])
+            for s, (H, O) in zip(specs, mats)]
+    graph, pers = te_gpu.Batch(inst), te_gpu.Batch(inst, persistent=True)
+    rg = graph.run()
+    for _ in range(2):
+        rp = pers.run()
+        bad = [i for i in range(len(specs)) if rp[i] != rg[i] or not np.array_equal(pers.samples(i), graph.samples(i))
+               or not np.array_equal(pers.state(i), graph.state(i))]
+        assert not bad, bad
+    assert pers.global_steps() == graph.global_steps()
+    graph.close()
+    pers.close()
+
+
 # ------------------------------------------------------------------- Zipf
 
 def test_zipf_1e6_matches_oracle(te_gpu, oracle_lib):

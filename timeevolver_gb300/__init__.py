@@ -73,6 +73,8 @@ SIGNATURES = {
     "te_matrix_long_segments": (_I, [_P, _P, _P, _P]),
     "te_model_create_device": (_I, [_I, _I, _I, _P, _I, _P, _P]),
     "te_model_state_index": (_I, [_I, _I, _I, _P, _P]),
+    "te_model_create_device_basis": (_I, [_P, _P, _I, _P, _P]),
+    "te_model_basis_index": (_I, [_P, _P, _P]),
     "te_matrix_spmv_lanes": (_I, [_P, _I]),
     "te_matrix_fixed_layout": (_I, [_P, _P, _P, _P]),
     "te_matrix_set_fixed_blocks": (_I, [_P, _I]),
@@ -102,6 +104,8 @@ SIGNATURES = {
     "te_batch_state": (_I, [_P, _I, _P]),
     "te_batch_launch_count": (_I64, [_P]),
     "te_batch_stream": (_P, [_P]),
+    "te_batch_global_steps": (_I64, [_P]),
+    "te_batch_set_option": (_I, [_P, _I, _I]),
     "te_evolver_set_option": (_I, [_P, _I, _I]),
     "te_evolver_add_dense_observable": (_I, [_P, _P, _I64]),
     "te_evolver_add_stop_condition": (_I, [_P, _I, _D, _I]),
@@ -183,6 +187,42 @@ OPT_BARRIER_SPIN_LIMIT = 3
 OPT_BARRIER_EXTRA_ARRIVALS = 4
 OPT_TS_MAX_LEVEL = 5
 OPT_QR_SWEEP_LIMIT = 6
+BATCH_OPT_PERSISTENT = 1
+BATCH_OPT_BARRIER_SPIN_LIMIT = 2
+BATCH_OPT_BARRIER_EXTRA_ARRIVALS = 3
+
+
+class TeBasisDesc(ctypes.Structure):
+    _fields_ = [("n_particles", ctypes.c_int32), ("n_modes", ctypes.c_int32), ("n_qudits", ctypes.c_int32),
+                ("capacity", ctypes.c_int32), ("quant", ctypes.c_int32), ("n_particles2", ctypes.c_int32),
+                ("n_modes2", ctypes.c_int32), ("capacity2", ctypes.c_int32)]
+
+
+def basis_desc(N, K, nb_qudits=0, capacity=0, quant=1, tensor=None):
+    """te_basis_desc of basis(N, K, nbQudits, capacity, quant), or with
+    tensor=(N1, K1, N2, K2, C2) of tensorBasis(N1, K1, N2, K2, C2)."""
+    if tensor is not None:
+        N1, K1, N2, K2, C2 = tensor
+        return TeBasisDesc(N1, K1, 0, 0, 1, N2, K2, C2)
+    return TeBasisDesc(N, K, nb_qudits, capacity, quant, 0, 0, 0)
+
+
+def basis_index_device(desc, occupation):
+    """Index of an occupation vector in the basis of a te_basis_desc (te_model_basis_index)."""
+    occ = np.ascontiguousarray(occupation, dtype=np.int32)
+    r = ctypes.c_int64()
+    _check(lib().te_model_basis_index(ctypes.byref(desc), _ptr(occ), ctypes.byref(r)), "te_model_basis_index")
+    return r.value
+
+
+def _term_array(terms):
+    arr = (TeTerm * len(terms))()
+    for t, (coef, ops, modes, caps) in zip(arr, terms):
+        c = complex(coef)
+        t.coef_re, t.coef_im, t.n_ops = c.real, c.imag, len(ops)
+        for k, (o, m_, cp) in enumerate(zip(ops, modes, caps)):
+            t.operation[k], t.mode[k], t.capacity[k] = o, m_, cp
+    return arr
 
 
 class TeTerm(ctypes.Structure):
@@ -266,6 +306,17 @@ class Matrix:
         dim = ctypes.c_int64()
         _check(lib().te_model_create_device(int(n_particles), int(n_modes), int(quant), arr, len(terms),
                                             ctypes.byref(h), ctypes.byref(dim)), "te_model_create_device")
+        return cls._adopt(h), dim.value
+
+    @classmethod
+    def from_terms_device_basis(cls, desc, terms):
+        """Operator matrix built on the GPU on the basis of a te_basis_desc
+        (basis_desc(): qudit capacities, tensor bases).  Returns (Matrix, dim)."""
+        arr = _term_array(terms)
+        h = ctypes.c_void_p()
+        dim = ctypes.c_int64()
+        _check(lib().te_model_create_device_basis(ctypes.byref(desc), arr, len(terms), ctypes.byref(h),
+                                                  ctypes.byref(dim)), "te_model_create_device_basis")
         return cls._adopt(h), dim.value
 
     def to_csr(self):
@@ -493,9 +544,11 @@ class Batch:
 
     ``instances``: list of dicts with keys H (Matrix), v, t, sampling_step and
     optional tol, m, exp_factor, fast_integration, observables (list of
-    diagonal Matrix objects)."""
+    diagonal Matrix objects).  ``persistent``: run the whole batch in one
+    persistent launch (TE_BATCH_OPT_PERSISTENT) instead of a graph replay per
+    global step."""
 
-    def __init__(self, instances):
+    def __init__(self, instances, persistent=False):
         B = len(instances)
         self._keep = []
         Hs = (ctypes.c_void_p * B)()
@@ -521,6 +574,14 @@ class Batch:
                 _check(lib().te_batch_add_observable(self.handle, i, O.handle), "te_batch_add_observable")
             self.n_obs.append(len(obs))
         self.B = B
+        if persistent:
+            self.set_option(BATCH_OPT_PERSISTENT, 1)
+
+    def set_option(self, option, value):
+        _check(lib().te_batch_set_option(self.handle, int(option), int(value)), "te_batch_set_option")
+
+    def global_steps(self):
+        return lib().te_batch_global_steps(self.handle)
 
     def run(self):
         res = (TeResult * self.B)()

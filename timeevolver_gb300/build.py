@@ -29,6 +29,13 @@ HOST_SOURCES = ["matrixDataTypes.cpp", "krylovObservables.cpp", "krylovTimeEvolv
                 "krylovHelper.cpp", "h5min.cpp",
                 "Basis.cpp", "hamiltonian.cpp", "te_host_c.cpp"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off"]
+# te_krylov.cu holds the persistent batched kernel, which rereads data that its
+# own blocks rewrite between grid barriers (instance states, schedule, active
+# list): global loads without an explicit cache operator bypass L1 there.  It
+# is compiled without implicit multiply-add contraction, so that the Krylov
+# step body, inlined into three kernels (single evolution, batched block per
+# instance, persistent batch), rounds the same way in each.
+NVCC_FILE_FLAGS = {"te_krylov.cu": ["-Xptxas", "-dlcm=cg", "-fmad=false"]}
 
 
 def _nvcc():
@@ -74,7 +81,9 @@ def build_tegpu(force=False, verbose=False):
         obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
         if force or _stale(obj, [src] + headers):
             extra = os.environ.get("TE_NVCC_FLAGS", "").split()  # e.g. -DTE_NO_PDL
-            out = _run([nvcc] + NVCC_FLAGS + extra + (["-Xptxas", "-v"] if verbose else []) + ["-c", src, "-o", obj])
+            per_file = NVCC_FILE_FLAGS.get(os.path.basename(src), [])
+            out = _run([nvcc] + NVCC_FLAGS + per_file + extra + (["-Xptxas", "-v"] if verbose else []) +
+                       ["-c", src, "-o", obj])
             if verbose:
                 print(out)
         return obj

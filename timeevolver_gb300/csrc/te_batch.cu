@@ -21,223 +21,26 @@
 #include <cstring>
 #include <vector>
 
+#include "te_batch.cuh"
 #include "te_internal.cuh"
-#include "te_reduce.cuh"
-#include "te_sell.cuh"
-
-#define TE_BATCH_MAX_OBS 4
 
 namespace {
 
-struct BatchGeom {
-  int64_t n_chunks;
-  const int32_t* chunk_inst;  // instance of every chunk
-  const int64_t* chunk_off;   // global SELL slot offsets (n_chunks + 1)
-  const int32_t* col;         // global row indices
-  const double* val;
-  const int64_t* inst_row;    // first global row of each instance
-  const int32_t* inst_n;      // dimension of each instance
-  const int64_t* inst_chunk;  // first chunk of each instance (n_inst + 1)
-  int64_t ld;                 // leading dimension of the basis (total padded rows)
-  // chunks of the instances still running at the start of the global step
-  // (null: every chunk); late global steps, when few instances are left, then
-  // cost no more than those instances' work
-  const int32_t* active;
-  const int* active_count;
-};
-
-// The i-th chunk of a pass and the number of chunks to visit.
-__device__ __forceinline__ int64_t batch_chunk_count(const BatchGeom& g) {
-  return g.active ? (int64_t)*g.active_count : g.n_chunks;
-}
-__device__ __forceinline__ int64_t batch_chunk(const BatchGeom& g, int64_t i) {
-  return g.active ? (int64_t)__ldg(g.active + i) : i;
-}
-
-// Compact the chunks of the running instances (one thread per chunk, one
-// atomic per warp) for the once-per-step passes (new start vector, combine).
-// The order of the list does not matter: those passes write rows, not sums.
+// Per-pass kernels of the graph path: one hardware warp per schedule warp.
 __global__ void batch_active_kernel(int64_t n_chunks, const int32_t* __restrict__ chunk_inst,
                                     const TeDevState* states, int32_t* active, int* count) {
-  const int lane = threadIdx.x & 31;
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n_chunks; base += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t c = base + threadIdx.x;
-    bool keep = false;
-    if (c < n_chunks) {
-      const TeDevState* ds = states + chunk_inst[c];
-      keep = !ds->done && !ds->fatal;
-    }
-    const unsigned mask = __ballot_sync(0xffffffffu, keep);
-    int pos = 0;
-    if (lane == 0 && mask) pos = atomicAdd(count, __popc(mask));
-    pos = __shfl_sync(0xffffffffu, pos, 0);
-    if (keep) active[pos + __popc(mask & ((1u << lane) - 1u))] = (int32_t)c;
-  }
+  batch_active_body(n_chunks, chunk_inst, states, active, count, (int64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                    (int64_t)gridDim.x * blockDim.x);
 }
 
-__device__ __forceinline__ bool lanczos_skip(const TeDevState* ds, int j) {
-  return ds->fatal != 0 || ds->done != 0 || ds->breakdown != 0 || j >= ds->m_cur;
-}
-
-// ---------------------------------------------------------------------------
-// Lanczos passes over the segmented layout.
-//
-// A schedule, recomputed on the device at the start of every global step,
-// gives warp w the contiguous chunk range [warp_begin[w], warp_begin[w + 1])
-// of equal FP64 cost over the running instances (finished instances inside a
-// range are skipped whole).  A warp accumulates per lane across the chunks of
-// one instance and reduces once per (warp, instance) segment; segment s of
-// instance i goes to slot seg_base[i] + (w - inst_w0[i]), so the per-instance
-// sum runs over consecutive slots in a fixed order (deterministic).  The
-// recurrence is folded as in the single-instance passes: the apply pass
-// stores w' = w / (e s_j), the update forms u'_{j+1} = w' - (alpha_j / e) u_j
-// and sets s_{j+1} = e s_j / beta_{j+1}.
-
-struct BatchSched {
-  const int32_t* warp_begin;  // W + 1 global chunk indices
-  const int32_t* inst_w0;     // first warp covering each instance
-  const int32_t* inst_nseg;   // segments (warps) covering each running instance, 0 otherwise
-  const int32_t* seg_base;    // first segment slot of each instance
-  const int32_t* next_run;    // the next running instance after each instance (n_inst: none)
-  const int32_t* inst_nwrite; // segments of each instance that are written (non-empty warps)
-  unsigned int* arrivals;     // per instance: segments written so far (apply pass, update pass)
-};
-
-// Where a warp continues after the chunks of instance inst that it must skip:
-// past every finished instance at once, or past this instance only.
-__device__ __forceinline__ int64_t batch_skip_to(const BatchGeom& g, const BatchSched& sc, const TeDevState* ds,
-                                                 int inst, int64_t cend) {
-  const int64_t nxt = (ds->done || ds->fatal) ? (int64_t)g.inst_chunk[sc.next_run[inst]]
-                                              : (int64_t)g.inst_chunk[inst + 1];
-  return min(nxt, cend);
-}
-
-// One block: per-instance costs, warp boundaries by binary search, segment bases.
 __global__ void __launch_bounds__(1024) batch_schedule_kernel(BatchGeom g, const TeDevState* states, int n_inst,
                                                               int n_warps, double w_slot, double* inst_cost,
                                                               int32_t* warp_begin, int32_t* inst_w0,
                                                               int32_t* inst_nseg, int32_t* seg_base,
                                                               int32_t* next_run, int32_t* inst_nwrite) {
-  const double w_chunk = 8.0 * 32.0;
   __shared__ double total;
-  for (int i = threadIdx.x; i < n_inst; i += blockDim.x) {
-    const TeDevState& d = states[i];
-    const int64_t c0 = g.inst_chunk[i], c1 = g.inst_chunk[i + 1];
-    const bool run = !d.done && !d.fatal;
-    inst_cost[i + 1] = run ? w_slot * (double)(g.chunk_off[c1] - g.chunk_off[c0]) + w_chunk * (double)(c1 - c0) : 0.0;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {  // exclusive prefix over instances (n_inst is small)
-    inst_cost[0] = 0.0;
-    for (int i = 0; i < n_inst; ++i) inst_cost[i + 1] += inst_cost[i];
-    total = inst_cost[n_inst];
-  }
-  __syncthreads();
-  for (int w = threadIdx.x; w <= n_warps; w += blockDim.x) {
-    int32_t c;
-    const double target = total * (double)w / (double)n_warps;
-    if (w == n_warps || !(total > 0.0)) {
-      c = (int32_t)g.n_chunks;
-    } else {
-      int lo = 0, hi = n_inst - 1;  // instance k: inst_cost[k] <= target < inst_cost[k + 1]
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (inst_cost[mid] <= target)
-          lo = mid;
-        else
-          hi = mid - 1;
-      }
-      int k = lo;
-      while (k < n_inst - 1 && !(inst_cost[k + 1] > target)) ++k;  // step over empty (finished) instances
-      const double rem = target - inst_cost[k];
-      const int64_t c0 = g.inst_chunk[k], c1 = g.inst_chunk[k + 1];
-      int64_t a = c0, b = c1;  // first chunk whose cost prefix within the instance reaches rem
-      while (a < b) {
-        const int64_t mid = (a + b) >> 1;
-        const double cm = w_slot * (double)(g.chunk_off[mid] - g.chunk_off[c0]) + w_chunk * (double)(mid - c0);
-        if (cm < rem)
-          a = mid + 1;
-        else
-          b = mid;
-      }
-      c = (int32_t)a;
-    }
-    warp_begin[w] = c;
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < n_inst; i += blockDim.x) {
-    const TeDevState& d = states[i];
-    const int64_t c0 = g.inst_chunk[i], c1 = g.inst_chunk[i + 1];
-    int nseg = 0, w0 = 0;
-    if (!d.done && !d.fatal && c1 > c0) {
-      auto last_warp_at_or_before = [&](int64_t c) {  // last w with warp_begin[w] <= c
-        int lo = 0, hi = n_warps;
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (warp_begin[mid] <= c)
-            lo = mid;
-          else
-            hi = mid - 1;
-        }
-        return lo;
-      };
-      w0 = last_warp_at_or_before(c0);
-      nseg = last_warp_at_or_before(c1 - 1) - w0 + 1;
-    }
-    inst_w0[i] = w0;
-    inst_nseg[i] = nseg;
-    int nw = 0;
-    for (int s = 0; s < nseg; ++s) nw += warp_begin[w0 + s] < warp_begin[w0 + s + 1];
-    inst_nwrite[i] = nw;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int32_t base = 0;
-    for (int i = 0; i < n_inst; ++i) {
-      seg_base[i] = base;
-      base += inst_nseg[i];
-    }
-  } else if (threadIdx.x == 32) {
-    int32_t nxt = n_inst;  // next running instance after i
-    for (int i = n_inst - 1; i >= 0; --i) {
-      next_run[i] = nxt;
-      if (!states[i].done && !states[i].fatal) nxt = i;
-    }
-  }
-}
-
-// Lane 0 has written this warp's segment partial(s) of instance inst; the warp
-// that completes the instance's count sums its written segments in slot order
-// (the same order whichever warp comes last) and returns true with the sums in
-// every lane.  NV values per segment at seg_partials[NV * slot + k].
-template <int NV>
-__device__ __forceinline__ bool batch_segment_done(const BatchSched& sc, int inst, int which,
-                                                   const double* seg_partials, double (&tot)[NV]) {
-  const int lane = threadIdx.x & 31;
-  unsigned int prev = 0;
-  if (lane == 0) {
-    __threadfence();
-    prev = atomicAdd(&sc.arrivals[2 * inst + which], 1u);
-  }
-  prev = __shfl_sync(0xffffffffu, prev, 0);
-  if (prev + 1 != (unsigned int)sc.inst_nwrite[inst]) return false;
-  __threadfence();
-  const int64_t s0 = sc.seg_base[inst];
-  const int w0 = sc.inst_w0[inst], ns = sc.inst_nseg[inst];
-#pragma unroll
-  for (int k = 0; k < NV; ++k) tot[k] = 0.0;
-  for (int s = lane; s < ns; s += 32) {
-    if (!(sc.warp_begin[w0 + s] < sc.warp_begin[w0 + s + 1])) continue;  // an empty warp wrote nothing
-#pragma unroll
-    for (int k = 0; k < NV; ++k) tot[k] += __ldcg(seg_partials + NV * (s0 + s) + k);
-  }
-#pragma unroll
-  for (int k = 0; k < NV; ++k) {
-    tot[k] = te_warp_sum(tot[k]);
-    tot[k] = __shfl_sync(0xffffffffu, tot[k], 0);
-  }
-  if (lane == 0) sc.arrivals[2 * inst + which] = 0u;  // ready for the next pass
-  return true;
+  batch_schedule_body(g, states, n_inst, n_warps, w_slot, inst_cost, warp_begin, inst_w0, inst_nseg, seg_base,
+                      next_run, inst_nwrite, &total);
 }
 
 template <bool REAL, bool HAS_PREV>
@@ -245,138 +48,22 @@ __global__ void __launch_bounds__(TE_THREADS, REAL ? 6 : 5) batch_apply_kernel(B
                                                                  const double2* __restrict__ V,
                                                                  double2* __restrict__ w, TeDevState* states,
                                                                  double* seg_partials, int j) {
-  const int lane = threadIdx.x & 31;
-  const int wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const double2* __restrict__ u_j = V + (int64_t)j * g.ld;
-  const double2* __restrict__ u_jm1 = HAS_PREV ? V + (int64_t)(j - 1) * g.ld : nullptr;
-  int64_t c = sc.warp_begin[wid];
-  const int64_t cend = sc.warp_begin[wid + 1];
-  while (c < cend) {
-    const int inst = __ldg(g.chunk_inst + c);
-    const TeDevState* ds = states + inst;
-    const int64_t c1 = min((int64_t)__ldg(g.inst_chunk + inst + 1), cend);
-    if (lanczos_skip(ds, j)) {
-      c = batch_skip_to(g, sc, ds, inst, cend);
-      continue;
-    }
-    const double sj = ds->s[j];
-    const double gg = ds->exp_factor * sj;
-    double cw = 0.0;
-    if (HAS_PREV) {
-      const double bie = ds->beta[j] * ds->inv_exp_factor;
-      cw = bie * bie;
-    }
-    const int64_t row0 = __ldg(g.inst_row + inst);
-    const int n_i = __ldg(g.inst_n + inst);
-    double a0 = 0.0, a1 = 0.0;
-    for (; c < c1; ++c) {
-      const double2 y = te_sell_row<REAL>(g.chunk_off, g.col, g.val, u_j, c, lane);
-      const int64_t r = c * 32 + lane;
-      double2 wr = make_double2(0.0, 0.0);
-      if (r - row0 < n_i) {
-        if (HAS_PREV) {
-          const double2 up = u_jm1[r];
-          wr.x = fma(cw, up.x, y.y);
-          wr.y = fma(cw, up.y, -y.x);
-        } else {
-          wr.x = y.y;
-          wr.y = -y.x;
-        }
-        const double2 uj = u_j[r];
-        a0 = fma(uj.x, wr.x, fma(uj.y, wr.y, a0));
-        a1 = fma(uj.x, wr.y, fma(-uj.y, wr.x, a1));
-      }
-      w[r] = wr;
-    }
-    a0 = te_warp_sum(a0);
-    a1 = te_warp_sum(a1);
-    if (lane == 0) {
-      const int64_t seg = sc.seg_base[inst] + (wid - sc.inst_w0[inst]);
-      seg_partials[2 * seg] = a0;
-      seg_partials[2 * seg + 1] = a1;
-    }
-    double tot[2];
-    if (batch_segment_done<2>(sc, inst, 0, seg_partials, tot) && lane == 0) {
-      const double f = sj * gg;  // alpha_j = s_j g <u_j, w'>
-      states[inst].alpha[j] = make_double2(f * tot[0], f * tot[1]);
-    }
-  }
+  batch_apply_warp<REAL, HAS_PREV, false>(g, sc, V, w, states, seg_partials, j,
+                                          blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5));
 }
 
 __global__ void __launch_bounds__(TE_THREADS) batch_update_kernel(BatchGeom g, BatchSched sc,
                                                                   double2* __restrict__ V,
                                                                   const double2* __restrict__ w, TeDevState* states,
                                                                   double* seg_partials, int j) {
-  const int lane = threadIdx.x & 31;
-  const int wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const double2* __restrict__ u_j = V + (int64_t)j * g.ld;
-  double2* __restrict__ u_jp1 = V + (int64_t)(j + 1) * g.ld;
-  int64_t c = sc.warp_begin[wid];
-  const int64_t cend = sc.warp_begin[wid + 1];
-  while (c < cend) {
-    const int inst = __ldg(g.chunk_inst + c);
-    const TeDevState* ds = states + inst;
-    const int64_t c1 = min((int64_t)__ldg(g.inst_chunk + inst + 1), cend);
-    if (lanczos_skip(ds, j)) {
-      c = batch_skip_to(g, sc, ds, inst, cend);
-      continue;
-    }
-    const double2 al = ds->alpha[j];
-    const double q = ds->inv_exp_factor;  // alpha_j s_j / (e s_j)
-    const double gr = al.x * q, gi = al.y * q;
-    const bool store = j + 1 < ds->m_cur;
-    const int64_t row0 = __ldg(g.inst_row + inst);
-    const int n_i = __ldg(g.inst_n + inst);
-    double nrm = 0.0;
-    for (; c < c1; ++c) {
-      const int64_t r = c * 32 + lane;
-      double2 o = make_double2(0.0, 0.0);
-      if (r - row0 < n_i) {
-        const double2 wv = w[r], u = u_j[r];
-        o.x = fma(-gr, u.x, fma(gi, u.y, wv.x));
-        o.y = fma(-gr, u.y, fma(-gi, u.x, wv.y));
-        nrm = fma(o.x, o.x, fma(o.y, o.y, nrm));
-      }
-      if (store) u_jp1[r] = o;
-    }
-    nrm = te_warp_sum(nrm);
-    if (lane == 0) seg_partials[sc.seg_base[inst] + (wid - sc.inst_w0[inst])] = nrm;
-    double tot[1];
-    if (batch_segment_done<1>(sc, inst, 1, seg_partials, tot) && lane == 0) {
-      TeDevState* dw = states + inst;
-      const double g = dw->exp_factor * dw->s[j];
-      const double beta = fabs(g) * sqrt(tot[0]);
-      const int m = dw->m_cur;
-      if (beta < dw->tol_rate) {  // lucky breakdown (:551-555)
-        dw->breakdown = 1;
-        dw->m_eff = j + 1;
-        dw->h = beta;
-      } else if (j + 1 != m) {
-        dw->beta[j + 1] = beta;
-        dw->s[j + 1] = g / beta;
-      } else {
-        dw->h = beta;
-        dw->m_eff = m;
-      }
-    }
-  }
+  batch_update_warp<false>(g, sc, V, w, states, seg_partials, j, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5));
 }
 
-// Start vector of the next step: u_0 = the w of the previous step.
 __global__ void __launch_bounds__(TE_THREADS) batch_new_start_kernel(BatchGeom g, double2* __restrict__ V,
                                                                      const double2* __restrict__ spare,
                                                                      const TeDevState* states) {
-  const int lane = threadIdx.x & 31;
-  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  const int64_t n_visit = batch_chunk_count(g);
-  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n_visit; i += warps) {
-    const int64_t c = batch_chunk(g, i);
-    const int inst = __ldg(g.chunk_inst + c);
-    const TeDevState* ds = states + inst;
-    if (!ds->new_start || ds->fatal || ds->done) continue;
-    const int64_t r = c * 32 + lane;
-    V[r] = spare[r];
-  }
+  batch_new_start_body<false>(g, V, spare, states, (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5),
+                       (int64_t)gridDim.x * (blockDim.x >> 5));
 }
 
 // Clear the new-start flags once the copies are done (one thread per instance).
@@ -385,107 +72,38 @@ __global__ void batch_clear_start_kernel(TeDevState* states, int n_inst) {
     states[i].new_start = 0;
 }
 
-// psi = sum_j u_j Y[slot][j] for each instance's outputs of this batch:
-// slot 0 (w) -> spare, slot 1 (the sample; batches hold one sample) -> sampled.
-template <int G>
-__device__ __forceinline__ void batch_combine_rows(const double2* __restrict__ V, int64_t ld, int64_t r, int m,
-                                                   const double2* Y, const int* slots, double2* spare,
-                                                   double2* sampled) {
-  double2 acc[G];
-#pragma unroll
-  for (int o = 0; o < G; ++o) acc[o] = make_double2(0.0, 0.0);
-  for (int j = 0; j < m; ++j) {
-    const double2 u = V[(int64_t)j * ld + r];
-#pragma unroll
-    for (int o = 0; o < G; ++o) {
-      const double2 y = Y[slots[o] * TE_MMAX + j];
-      acc[o].x = fma(u.x, y.x, fma(-u.y, y.y, acc[o].x));
-      acc[o].y = fma(u.x, y.y, fma(u.y, y.x, acc[o].y));
-    }
-  }
-#pragma unroll
-  for (int o = 0; o < G; ++o) {
-    if (slots[o] == 0)
-      spare[r] = acc[o];
-    else
-      sampled[r] = acc[o];
-  }
-}
-
 __global__ void __launch_bounds__(TE_THREADS) batch_combine_kernel(BatchGeom g, const double2* __restrict__ V,
                                                                    double2* spare, double2* sampled,
                                                                    const TeDevState* states, int m_override) {
-  const int lane = threadIdx.x & 31;
-  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  const int64_t n_visit = batch_chunk_count(g);
-  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n_visit; i += warps) {
-    const int64_t c = batch_chunk(g, i);
-    const int inst = __ldg(g.chunk_inst + c);
-    const TeDevState* ds = states + inst;
-    if (ds->fatal) continue;
-    const int want_w = ds->want_w, S = ds->samples_in_batch;
-    const int nout = want_w + S;
-    if (nout == 0) continue;
-    const int m = m_override > 0 ? m_override : ds->m_eff;
-    const int64_t r = c * 32 + lane;
-    int slots[2];
-    slots[0] = want_w ? 0 : 1;
-    slots[1] = 1;
-    if (nout == 1)
-      batch_combine_rows<1>(V, g.ld, r, m, ds->Y, slots, spare, sampled);
-    else
-      batch_combine_rows<2>(V, g.ld, r, m, ds->Y, slots, spare, sampled);
-  }
+  batch_combine_body<false>(g, V, spare, sampled, states, m_override,
+                     (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5),
+                     (int64_t)gridDim.x * (blockDim.x >> 5));
 }
 
-// Diagonal observables of every instance with a sample in this batch
-// (one block per instance): Re sum_i O_ii |psi_i|^2.
+struct BlockSync {
+  __device__ void operator()() const { __syncthreads(); }
+};
+
+// Diagonal observables, one block per instance.
 __global__ void __launch_bounds__(TE_THREADS) batch_obs_kernel(BatchGeom g, const double2* __restrict__ sampled,
                                                                const double* __restrict__ diag, const int* n_obs,
                                                                const int64_t* result_off, double* results,
                                                                TeDevState* states) {
   __shared__ double scratch[TE_BATCH_MAX_OBS * 32];
-  const int inst = blockIdx.x;
-  TeDevState* ds = states + inst;
-  const int no = n_obs[inst];
-  if (ds->fatal || ds->samples_in_batch == 0 || no == 0) return;
-  const int64_t r0 = g.inst_row[inst];
-  const int n = g.inst_n[inst];
-  double acc[TE_BATCH_MAX_OBS] = {0.0, 0.0, 0.0, 0.0};
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const double2 p = sampled[r0 + i];
-    const double p2 = fma(p.x, p.x, p.y * p.y);
-    for (int k = 0; k < no; ++k) acc[k] = fma(diag[(int64_t)k * g.ld + r0 + i], p2, acc[k]);
-  }
-  te_block_sum<TE_BATCH_MAX_OBS>(acc, scratch);
-  if (threadIdx.x == 0) {
-    const int s = ds->sample_base;
-    for (int k = 0; k < no; ++k) results[result_off[inst] + (int64_t)k * ds->n_samples + s] = acc[k];
-  }
+  batch_obs_inst<false>(g, sampled, diag, n_obs, result_off, results, states, blockIdx.x, threadIdx.x, blockDim.x, scratch,
+                 BlockSync());
 }
 
-// ||sampled||^2 of every instance (final norm check of :446).
+// ||sampled||^2 of every instance, one block per instance.
 __global__ void __launch_bounds__(TE_THREADS) batch_norm_kernel(BatchGeom g, const double2* __restrict__ sampled,
                                                                 TeDevState* states) {
   __shared__ double scratch[32];
-  const int inst = blockIdx.x;
-  const int64_t r0 = g.inst_row[inst];
-  const int n = g.inst_n[inst];
-  double acc[1] = {0.0};
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const double2 p = sampled[r0 + i];
-    acc[0] = fma(p.x, p.x, fma(p.y, p.y, acc[0]));
-  }
-  te_block_sum<1>(acc, scratch);
-  if (threadIdx.x == 0) states[inst].norm2_final = acc[0];
+  batch_norm_inst<false>(g, sampled, states, blockIdx.x, threadIdx.x, blockDim.x, scratch, BlockSync());
 }
 
-// One flag word per instance: bit0 done, bit1 samples pending, bit2 fatal.
 __global__ void batch_flags_kernel(const TeDevState* states, int n_inst, int* flags) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_inst; i += gridDim.x * blockDim.x) {
-    const TeDevState& d = states[i];
-    flags[i] = (d.done ? 1 : 0) | (d.samples_pending && !d.done ? 2 : 0) | (d.fatal ? 4 : 0);
-  }
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_inst; i += gridDim.x * blockDim.x)
+    flags[i] = batch_flag(states[i]);
 }
 
 // global = local + offset (columns of one instance into the concatenated rows)
@@ -562,6 +180,14 @@ struct te_batch_s {
   cudaGraphExec_t g_step = nullptr, g_batch = nullptr;
   int64_t launches = 0;
   bool ran = false;
+  // TE_BATCH_OPT_PERSISTENT: 0 graph replay per global step, 1 one persistent launch
+  int persistent = 0;
+  unsigned int spin_limit = 1u << 22;  // TE_BATCH_OPT_BARRIER_SPIN_LIMIT
+  unsigned int extra_arrivals = 0;     // TE_BATCH_OPT_BARRIER_EXTRA_ARRIVALS
+  unsigned int* d_bar = nullptr;       // grid barrier: count, generation
+  int* d_err = nullptr;                // error raised on the device by the persistent kernel
+  int64_t* d_steps = nullptr;          // global steps the persistent kernel completed
+  int64_t global_steps = 0;
 };
 
 namespace {
@@ -618,6 +244,9 @@ void free_batch(te_batch b) {
   cudaFree(b->d_inst_w0);
   cudaFree(b->d_inst_nseg);
   cudaFree(b->d_seg_base);
+  cudaFree(b->d_bar);
+  cudaFree(b->d_err);
+  cudaFree(b->d_steps);
   cudaFree(b->d_next_run);
   cudaFree(b->d_inst_nwrite);
   cudaFree(b->d_arrivals);
@@ -635,7 +264,10 @@ int grid_chunks(const te_batch_s* b) {
   return (int)std::min<int64_t>((b->n_chunks * 32 + TE_THREADS - 1) / TE_THREADS, (int64_t)te_num_sms() * bps);
 }
 
-// Warps of the Lanczos passes: one resident wave of the apply/update kernels.
+// Logical warps of the Lanczos schedule: one resident wave of the apply/update
+// kernels.  The graph path launches one hardware warp for each; the persistent
+// kernel's warps loop over them, so both sum the same segments in the same
+// order.
 int lanczos_warps(const te_batch_s* b) {
   const void* k[] = {(const void*)batch_apply_kernel<true, true>,  (const void*)batch_apply_kernel<true, false>,
                      (const void*)batch_apply_kernel<false, true>, (const void*)batch_apply_kernel<false, false>,
@@ -723,6 +355,59 @@ int capture(te_batch b, bool full_step, cudaGraphExec_t* exec) {
   rc = te_cuda_check(cudaGraphInstantiate(exec, graph, 0), "graph instantiate");
   cudaGraphDestroy(graph);
   return rc;
+}
+
+// The whole run in one persistent launch (after reset_states).
+int run_persistent(te_batch b, int grid) {
+  TeBatchPersist a;
+  a.g = geom(b);
+  a.sc = sched(b);
+  a.inst_cost = b->d_inst_cost;
+  a.warp_begin = b->d_warp_begin;
+  a.inst_w0 = b->d_inst_w0;
+  a.inst_nseg = b->d_inst_nseg;
+  a.seg_base = b->d_seg_base;
+  a.next_run = b->d_next_run;
+  a.inst_nwrite = b->d_inst_nwrite;
+  a.active = b->d_active;
+  a.active_count = b->d_active_count;
+  a.V = b->V;
+  a.w = b->w;
+  a.spare = b->spare;
+  a.sampled = b->sampled;
+  a.states = b->ds;
+  a.seg_partials = b->seg_partials;
+  a.diag = b->diag;
+  a.n_obs = b->d_nobs;
+  a.result_off = b->d_result_off;
+  a.results = b->results;
+  a.n_inst = b->B;
+  a.m_max = b->m_max;
+  a.n_warps = b->n_warps;
+  a.is_real = b->is_real;
+  a.w_slot = b->is_real ? 2.0 : 4.0;
+  a.bar_count = b->d_bar;
+  a.bar_gen = b->d_bar + 1;
+  a.err = b->d_err;
+  a.spin_limit = b->spin_limit;
+  a.arrivals = (unsigned int)grid + b->extra_arrivals;
+  a.max_global_steps = (int64_t)1 << 40;
+  a.steps_done = b->d_steps;
+  TE_CUDA(cudaMemsetAsync(b->d_bar, 0, 2 * sizeof(unsigned int), b->st));
+  TE_CUDA(cudaMemsetAsync(b->d_err, 0, sizeof(int), b->st));
+  TE_CUDA(cudaMemsetAsync(b->d_steps, 0, sizeof(int64_t), b->st));
+  int rc = te_launch_batch_persistent(a, grid, b->st);
+  if (rc != TE_OK) return rc;
+  b->launches += 1;
+  int err = 0;
+  TE_CUDA(cudaMemcpyAsync(&err, b->d_err, sizeof(int), cudaMemcpyDeviceToHost, b->st));
+  TE_CUDA(cudaMemcpyAsync(&b->global_steps, b->d_steps, sizeof(int64_t), cudaMemcpyDeviceToHost, b->st));
+  TE_CUDA(cudaStreamSynchronize(b->st));
+  if (err) {
+    te_set_error("te_batch_run: a grid-barrier wait of the persistent batched kernel gave up");
+    return err;
+  }
+  return TE_OK;
 }
 
 int reset_states(te_batch b) {
@@ -907,6 +592,9 @@ extern "C" int te_batch_create(int n_instances, const te_matrix* H, const double
   if ((rc = alloc((void**)&b->d_inst_nwrite, sizeof(int32_t) * n_instances)) != TE_OK) return fail(rc);
   if ((rc = alloc((void**)&b->d_arrivals, sizeof(unsigned int) * 2 * n_instances)) != TE_OK) return fail(rc);
   if ((rc = alloc((void**)&b->d_inst_cost, sizeof(double) * (n_instances + 1))) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_bar, 2 * sizeof(unsigned int))) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_err, sizeof(int))) != TE_OK) return fail(rc);
+  if ((rc = alloc((void**)&b->d_steps, sizeof(int64_t))) != TE_OK) return fail(rc);
   // segments: every warp has at most one per instance it touches
   if ((rc = alloc((void**)&b->seg_partials, sizeof(double) * 2 * ((int64_t)b->n_warps + n_instances + 1))) != TE_OK)
     return fail(rc);
@@ -976,6 +664,15 @@ extern "C" int te_batch_run(te_batch b, te_result* results) {
   }
   int rc = reset_states(b);
   if (rc != TE_OK) return rc;
+  b->global_steps = 0;
+  if (b->persistent) {
+    const int grid = te_batch_persistent_grid(b->is_real);
+    if (grid <= 0) {
+      te_set_error("te_batch_run: the persistent batched kernel cannot be co-resident on this device");
+      return TE_ERR_UNSUPPORTED;
+    }
+    if ((rc = run_persistent(b, grid)) != TE_OK) return rc;
+  } else {
   if (!b->g_step) {
     if ((rc = capture(b, true, &b->g_step)) != TE_OK) return rc;
     if ((rc = capture(b, false, &b->g_batch)) != TE_OK) return rc;
@@ -1003,10 +700,12 @@ extern "C" int te_batch_run(te_batch b, te_result* results) {
         fatal |= (b->h_flags[i] & 4) != 0;
       }
     }
+    ++b->global_steps;
     if (fatal || all_done) break;
   }
   batch_norm_kernel<<<b->B, TE_THREADS, 0, b->st>>>(geom(b), b->sampled, b->ds);
   b->launches += 1;
+  }
   std::vector<TeDevState> hs(b->B);
   TE_CUDA(cudaMemcpyAsync(hs.data(), b->ds, sizeof(TeDevState) * b->B, cudaMemcpyDeviceToHost, b->st));
   TE_CUDA(cudaStreamSynchronize(b->st));
@@ -1089,6 +788,34 @@ extern "C" int te_batch_state(te_batch b, int instance, double* out_host) {
 }
 
 extern "C" int64_t te_batch_launch_count(te_batch b) { return b ? b->launches : 0; }
+
+extern "C" int64_t te_batch_global_steps(te_batch b) { return b ? b->global_steps : 0; }
+
+extern "C" int te_batch_set_option(te_batch b, int option, int value) {
+  if (!b) {
+    te_set_error("te_batch_set_option: null batch");
+    return TE_ERR_INVALID_ARG;
+  }
+  switch (option) {
+    case TE_BATCH_OPT_PERSISTENT:
+      if (value != 0 && value != 1) break;
+      b->persistent = value;
+      return TE_OK;
+    case TE_BATCH_OPT_BARRIER_SPIN_LIMIT:
+      if (value < 1) break;
+      b->spin_limit = (unsigned int)value;
+      return TE_OK;
+    case TE_BATCH_OPT_BARRIER_EXTRA_ARRIVALS:
+      if (value != 0 && value != 1) break;
+      b->extra_arrivals = (unsigned int)value;
+      return TE_OK;
+    default:
+      te_set_error("te_batch_set_option: unknown option %d", option);
+      return TE_ERR_INVALID_ARG;
+  }
+  te_set_error("te_batch_set_option: value %d out of range for option %d", value, option);
+  return TE_ERR_INVALID_ARG;
+}
 
 extern "C" void* te_batch_stream(te_batch b) { return b ? (void*)b->st : nullptr; }
 

@@ -38,6 +38,7 @@
 #include <cmath>
 #include <vector>
 
+#include "te_batch.cuh"
 #include "te_internal.cuh"
 
 __constant__ TeQuadTables c_quad;
@@ -852,6 +853,91 @@ __global__ void __launch_bounds__(TE_THREADS) krylov_batch_kernel(TeDevState* st
   krylov_step_body(states + blockIdx.x, mode, reinterpret_cast<KSmem*>(smem_raw));
 }
 
+// ---------------------------------------------------------------------------
+// Batched evolutions in one persistent launch: the whole run of a batch (every
+// global step: active list, new start vectors, schedule, the m Lanczos
+// iterations, the Krylov-space step of every instance, combine, observables,
+// extra sample batches, and the final norms) in one cooperative kernel of one
+// 1024-thread block per SM, the passes separated by bounded grid barriers.
+// The passes are the device bodies of te_batch.cuh, called with the same
+// logical schedule warps as the per-pass kernels (hardware warps loop over
+// them) and with 256-thread groups for the per-instance reductions, so the
+// results equal the graph path's bit for bit; the host waits once per run
+// instead of once per global step.
+__device__ __forceinline__ void batch_flags_all(const TeDevState* states, int n_inst, int& pending, int& all_done,
+                                                int& fatal) {
+  int p = 0, d = 1, f = 0;
+  for (int i = threadIdx.x; i < n_inst; i += blockDim.x) {
+    const int fl = batch_flag(states[i]);
+    p |= (fl & 2) != 0;
+    d &= (fl & 1) != 0;
+    f |= (fl & 4) != 0;
+  }
+  pending = __syncthreads_or(p);
+  all_done = __syncthreads_and(d);
+  fatal = __syncthreads_or(f);
+}
+
+template <bool REAL>
+__global__ void __launch_bounds__(TE_BATCH_PTHREADS, 1) batch_persistent_kernel(TeBatchPersist a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  KSmem* S = reinterpret_cast<KSmem*>(smem_raw);
+  // outside the Krylov phase the start of the shared memory serves the group
+  // reductions and the schedule's total
+  const int ngrp = blockDim.x / TE_THREADS, grp = threadIdx.x / TE_THREADS, gtid = threadIdx.x % TE_THREADS;
+  double* gscratch = reinterpret_cast<double*>(smem_raw) + grp * (TE_BATCH_MAX_OBS * 32);
+  double* total = reinterpret_cast<double*>(smem_raw) + ngrp * (TE_BATCH_MAX_OBS * 32);
+  auto gsync = [grp]() { asm volatile("bar.sync %0, %1;" ::"r"(grp + 1), "r"(TE_THREADS) : "memory"); };
+  const int G = gridDim.x;
+  auto bar = [&]() { return te_grid_barrier(a.bar_count, a.bar_gen, a.err, a.spin_limit, a.arrivals); };
+  const int64_t wpb = blockDim.x >> 5;
+  const int64_t pw = (int64_t)blockIdx.x * wpb + (threadIdx.x >> 5), PW = (int64_t)G * wpb;
+  const int64_t tg = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, TG = (int64_t)G * blockDim.x;
+  const int n_inst = a.n_inst;
+  for (int64_t step = 0; step < a.max_global_steps; ++step) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.active_count = 0;
+    if (!bar()) return;
+    batch_active_body(a.g.n_chunks, a.g.chunk_inst, a.states, a.active, a.active_count, tg, TG);
+    if (!bar()) return;
+    batch_new_start_body<true>(a.g, a.V, a.spare, a.states, pw, PW);
+    if (!bar()) return;
+    for (int64_t i = tg; i < n_inst; i += TG) a.states[i].new_start = 0;
+    if (blockIdx.x == 0)
+      batch_schedule_body(a.g, a.states, n_inst, a.n_warps, a.w_slot, a.inst_cost, a.warp_begin, a.inst_w0,
+                          a.inst_nseg, a.seg_base, a.next_run, a.inst_nwrite, total);
+    if (!bar()) return;
+    for (int j = 0; j < a.m_max; ++j) {
+      for (int64_t vw = pw; vw < a.n_warps; vw += PW) {
+        if (j > 0)
+          batch_apply_warp<REAL, true, true>(a.g, a.sc, a.V, a.w, a.states, a.seg_partials, j, (int)vw);
+        else
+          batch_apply_warp<REAL, false, true>(a.g, a.sc, a.V, a.w, a.states, a.seg_partials, j, (int)vw);
+      }
+      if (!bar()) return;
+      for (int64_t vw = pw; vw < a.n_warps; vw += PW)
+        batch_update_warp<true>(a.g, a.sc, a.V, a.w, a.states, a.seg_partials, j, (int)vw);
+      if (!bar()) return;
+    }
+    int pending, all_done, fatal;
+    for (int mode = 0;; mode = 1) {
+      for (int i = blockIdx.x; i < n_inst; i += G) krylov_step_body(a.states + i, mode, S);
+      if (!bar()) return;
+      batch_combine_body<true>(a.g, a.V, a.spare, a.sampled, a.states, 0, pw, PW);
+      if (!bar()) return;
+      for (int i = blockIdx.x * ngrp + grp; i < n_inst; i += G * ngrp)
+        batch_obs_inst<true>(a.g, a.sampled, a.diag, a.n_obs, a.result_off, a.results, a.states, i, gtid,
+                             TE_THREADS, gscratch, gsync);
+      if (!bar()) return;
+      batch_flags_all(a.states, n_inst, pending, all_done, fatal);
+      if (!pending || fatal) break;
+    }
+    if (threadIdx.x == 0 && blockIdx.x == 0) *a.steps_done = step + 1;
+    if (fatal || all_done) break;
+  }
+  for (int i = blockIdx.x * ngrp + grp; i < n_inst; i += G * ngrp)
+    batch_norm_inst<true>(a.g, a.sampled, a.states, i, gtid, TE_THREADS, gscratch, gsync);
+}
+
 // ---------------------------------------------------------------- host side
 
 static bool g_tables_uploaded = false;
@@ -932,4 +1018,29 @@ void te_launch_schedule_samples(TeDevState* ds, cudaStream_t st) {
 
 void te_launch_krylov_batch(TeDevState* states, int n_instances, int mode, cudaStream_t st) {
   krylov_batch_kernel<<<n_instances, TE_THREADS, sizeof(KSmem), st>>>(states, mode);
+}
+
+int te_batch_persistent_grid(bool is_real) {
+  const void* k = is_real ? (const void*)batch_persistent_kernel<true> : (const void*)batch_persistent_kernel<false>;
+  int dev = 0, coop = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return 0;
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(KSmem)) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, TE_BATCH_PTHREADS, sizeof(KSmem)) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return per_sm >= 1 ? te_num_sms() : 0;  // one block per SM
+}
+
+int te_launch_batch_persistent(const TeBatchPersist& a, int grid, cudaStream_t st) {
+  void* k = a.is_real ? (void*)batch_persistent_kernel<true> : (void*)batch_persistent_kernel<false>;
+  TeBatchPersist arg = a;
+  void* params[] = {&arg};
+  return te_cuda_check(cudaLaunchCooperativeKernel(k, dim3(grid), dim3(TE_BATCH_PTHREADS), params, sizeof(KSmem), st),
+                       "persistent batch launch");
 }

@@ -416,40 +416,6 @@ struct TeLanczosArgs {
   double2* u[TE_MMAX];
 };
 
-// Grid barrier with a bounded wait.  Arrival after a fence; the block that
-// brings the count to `arrivals` resets it and bumps the generation.  A wait
-// that gives up after spin_limit polls sets fatal = TE_ERR_DEVICE_TIMEOUT and
-// returns false (the kernel then exits).
-__device__ __forceinline__ bool te_grid_barrier(unsigned int* count, unsigned int* gen, int* fatal,
-                                                unsigned int spin_limit, unsigned int arrivals) {
-  __shared__ int ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    ok = 1;
-    volatile unsigned int* vgen = gen;
-    const unsigned int g0 = *vgen;
-    __threadfence();
-    if (atomicAdd(count, 1u) == arrivals - 1) {
-      atomicExch(count, 0u);
-      __threadfence();
-      atomicAdd(gen, 1u);
-    } else {
-      unsigned int spins = 0;
-      while (*vgen == g0) {
-        __nanosleep(32);
-        if (++spins > spin_limit) {
-          ok = 0;
-          atomicExch(fatal, TE_ERR_DEVICE_TIMEOUT);
-          break;
-        }
-      }
-    }
-    __threadfence();
-  }
-  __syncthreads();
-  return ok != 0;
-}
-
 // Sum of NV partial arrays (stride gridDim.x) in the order of te_final_sum;
 // the result is returned to every thread of the block.
 template <int NV>

@@ -8,17 +8,19 @@
 #pragma once
 #include "te_internal.cuh"
 
-// Loads of x: through the read-only (non-coherent) cache by default; XCG
-// selects ordinary cached loads (ld.global.ca) for x written earlier in the
-// same kernel by other SMs (the persistent Lanczos kernel), which are coherent
-// after that kernel's grid barrier (release/acquire fences) where the
-// read-only path is not.
-template <bool XCG>
+// Loads of x (XCG): 0 through the read-only (non-coherent) cache; 1 ordinary
+// cached loads (ld.global.ca) for x written earlier in the same kernel by
+// other SMs and read after a grid barrier, with no copy of it in this SM's L1
+// from before the write (the persistent Lanczos kernel: each basis vector is
+// written once per launch, then read); 2 L2-only loads (ld.global.cg) for
+// vectors rewritten again and again within one launch (the persistent batched
+// kernel), where this SM's L1 could still hold an earlier copy.
+template <int XCG>
 __device__ __forceinline__ double2 te_load_x(const double2* __restrict__ x, int32_t c) {
-  return XCG ? __ldca(x + c) : __ldg(x + c);
+  return XCG == 2 ? __ldcg(x + c) : (XCG == 1 ? __ldca(x + c) : __ldg(x + c));
 }
 
-template <bool REAL, bool XCG = false>
+template <bool REAL, int XCG = 0>
 __device__ __forceinline__ double2 te_sell_row(const int64_t* __restrict__ chunk_off,
                                                const int32_t* __restrict__ col, const double* __restrict__ val,
                                                const double2* __restrict__ x, int64_t chunk, int lane) {
@@ -129,7 +131,7 @@ __device__ __forceinline__ double2 te_sell_row_k(const int64_t* __restrict__ chu
 
 // Entries [b, e) of the long-row CSR times x by a whole warp: lanes stride
 // over the entries, then a warp sum (lane 0's value is the one used).
-template <bool REAL, bool XCG = false>
+template <bool REAL, int XCG = 0>
 __device__ __forceinline__ double2 te_long_range(const TeLongRows& L, int64_t b, int64_t e,
                                                  const double2* __restrict__ x, int lane) {
   double re = 0.0, im = 0.0;
@@ -170,7 +172,7 @@ __device__ __forceinline__ double2 te_long_range(const TeLongRows& L, int64_t b,
 // to run, so a pass that reduces over rows must not fold a split row's terms
 // into that warp's sums: te_split_row_publish / te_split_rows_add move them
 // to a fixed place in the final reduction.
-template <bool REAL, bool XCG = false>
+template <bool REAL, int XCG = 0>
 __device__ __forceinline__ int te_long_segment(const TeLongRows& L, int64_t s, const double2* __restrict__ x,
                                                int lane, int64_t* row, double2* y) {
   const int32_t i = __ldg(L.seg_row + s);

@@ -79,3 +79,75 @@ def test_device_built_evolution(te_gpu):
     b = te_gpu.evolve(coo, v, 5.0, 0.5, [("sparse", n0)], tol=1e-8, m=40)
     assert a["n_steps"] == b["n_steps"] and a["status"] == b["status"]
     assert np.array_equal(a["samples"], b["samples"]) and np.array_equal(a["state"], b["state"])
+
+
+def _device_equals_host(te_gpu, desc, host_basis, terms):
+    from timeevolver_gb300 import models
+    coo = models.operator_matrix(terms, host_basis)
+    Hd, dim = te_gpu.Matrix.from_terms_device_basis(desc, terms)
+    assert dim == host_basis.size
+    rp, ci, val = Hd.to_csr()
+    rp0, ci0, val0 = _csr_of_coo(dim, coo)
+    assert np.array_equal(rp, rp0) and np.array_equal(ci, ci0)
+    assert np.array_equal(val, val0)  # bit for bit
+    assert Hd.info()["norm1"] == te_gpu.Matrix.from_coo(dim, coo).info()["norm1"]
+    el = host_basis.elements()
+    rng = np.random.default_rng(7)
+    for i in rng.integers(0, dim, size=25):
+        assert te_gpu.basis_index_device(desc, el[i]) == i
+    return Hd, dim, coo
+
+
+@pytest.mark.parametrize("N,K,nq,cap,quant", [(6, 5, 2, 2, 1), (8, 4, 4, 3, 1), (5, 5, 5, 1, 1), (7, 6, 3, 1, 1),
+                                              (9, 5, 2, 4, 2), (10, 3, 3, 4, 2)])
+def test_qudit_basis_device_equals_host(te_gpu, N, K, nq, cap, quant):
+    """basis(N, K, nbQudits, capacity, quant) on the GPU: the last nbQudits
+    modes capped, and with every mode a qudit the states whose mode 0 would
+    exceed the capacity dropped; hopping terms with capacities on the
+    creation operators, on-site terms.  Entries, 1-norm and indices equal the
+    host builder's."""
+    from timeevolver_gb300 import models
+    terms = []
+    for b in range(K - 1):
+        terms.append((complex(-0.7 - 0.1 * b), [-1, 1], [b + 1, b], [0, cap if b >= K - nq else 0]))
+        terms.append((complex(-0.7 - 0.1 * b), [-1, 1], [b, b + 1], [0, cap if b + 1 >= K - nq else 0]))
+    for i in range(K):
+        terms.append(models.four_point_a(i, i, i, i, 0, 0, 0, 0, 0.8))
+        terms.append(models.number_operator(i, 0.3 * i - 0.8))
+    B = models.Basis(N, K, nq, cap, quant)
+    _device_equals_host(te_gpu, te_gpu.basis_desc(N, K, nq, cap, quant), B, terms)
+    # states outside the capacity are not basis states
+    occ = [0] * K
+    occ[K - 1] = cap + 1
+    occ[0] = N - cap - 1
+    if occ[0] >= 0:
+        assert te_gpu.basis_index_device(te_gpu.basis_desc(N, K, nq, cap, quant), occ) == -1
+
+
+def test_tensor_basis_black_hole_device_golden(te_gpu, oracle_lib):
+    """The black-hole model of the reference's example on tensorBasis(20, 2,
+    2, 8, 1) (dim 588, 74 terms) built on the GPU: the matrix equals the host
+    builder's bit for bit, and its evolution reproduces the reference's golden
+    trajectories (output/ResultBlackHole_N20_...h5)."""
+    import os
+    from oracle import models as omodels
+    from timeevolver_gb300 import models
+    terms = omodels.black_hole_terms(20, 2, 12.0, 4)
+    assert len(terms) > 64
+    B = models.Basis.tensor(20, 2, 2, 8, 1)
+    desc = te_gpu.basis_desc(0, 0, tensor=(20, 2, 2, 8, 1))
+    Hd, dim, coo = _device_equals_host(te_gpu, desc, B, terms)
+    assert dim == 588
+    init = [20, 0, 1, 1] + [0] * 6
+    v = np.zeros(dim, dtype=np.complex128)
+    v[te_gpu.basis_index_device(desc, init)] = 1.0
+    obs = [("sparse", o) for o in models.number_operator_observables(B)]
+    r = te_gpu.evolve(Hd, v, 10.0, 0.01, obs, tol=1e-8, m=40)
+    gold = np.load(os.path.join(os.path.dirname(__file__), "golden", "blackhole_N20.npy"))
+    assert r["num_samples"] == 1001 and r["err"] <= 1e-8
+    assert np.max(np.abs(r["samples"] - gold)) < 1e-8
+    # an empty second set is rejected, as are inconsistent descriptors
+    with pytest.raises(te_gpu.TeError):
+        te_gpu.Matrix.from_terms_device_basis(te_gpu.basis_desc(0, 0, tensor=(2, 2, 5, 2, 1)), terms[:4])
+    with pytest.raises(te_gpu.TeError):
+        te_gpu.Matrix.from_terms_device_basis(te_gpu.basis_desc(4, 3, 4, 1, 1), terms[:2])

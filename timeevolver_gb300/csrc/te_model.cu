@@ -38,7 +38,7 @@ namespace {
 
 #define TE_MODEL_MAX_MODES 64
 #define TE_MODEL_MAX_OPS 8
-#define TE_MODEL_MAX_TERMS 64  // per-thread row buffers (a row has at most one entry per term)
+#define TE_MODEL_MAX_TERMS 128  // per-thread row buffers (a row has at most one entry per term)
 
 struct DevTerm {
   double2 coef;
@@ -48,19 +48,37 @@ struct DevTerm {
   int capacity[TE_MODEL_MAX_OPS];
 };
 
+// One basis on the device: the stage lists' sizes and prefix sums, the
+// capacity of the qudit modes, and (when every mode is a qudit) the map from
+// the staged list to the final list, from which the states whose mode 0
+// would exceed the capacity are dropped (Basis.cpp:97-110).
 struct Stages {
   int K, N, quant;
-  const int64_t* n_s;  // K entries: list sizes before each stage (n_s[0] = 1)
+  int nq, cap;               // modes K - nq .. K - 1 hold at most cap particles
+  const int64_t* n_s;        // K entries: list sizes before each stage (n_s[0] = 1)
   const int64_t* const* ps;  // K - 1 prefix arrays (device pointers)
+  const int64_t* keep;       // all modes qudits: final index of each staged state, -1 if dropped; else null
+  const uint8_t* occ;        // final list, K occupations per state
+  int64_t dim;
 };
 
-// children counts of list L_s (stage of mode m)
-__global__ void stage_count_kernel(int64_t n, const uint8_t* __restrict__ occ, int K, int N, int quant,
+// A model basis: one basis, or the tensor product of two (tensorBasis,
+// Basis.cpp:131-182: index i1 * dim2 + i2, the first set's modes first).
+struct ModelBasis {
+  Stages a, b;
+  int tensor;
+  int K;  // modes in all
+  int64_t dim;
+};
+
+// children counts of list L_s (stage of mode m); qudit stages stop at the capacity
+__global__ void stage_count_kernel(int64_t n, const uint8_t* __restrict__ occ, int K, int N, int quant, int cap,
                                    int64_t* __restrict__ cnt) {
   for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x) {
     int tot = 0;
     for (int a = 1; a < K; ++a) tot += occ[l * K + a];
-    cnt[l] = (N - tot) / quant;
+    const int upper = cap >= 0 ? min(N - tot, cap) : N - tot;
+    cnt[l] = upper / quant;
   }
 }
 
@@ -76,15 +94,36 @@ __global__ void stage_expand_kernel(int64_t n, uint8_t* occ, int K, int m, int q
   }
 }
 
-__global__ void finish_basis_kernel(int64_t n, uint8_t* occ, int K, int N) {
+// mode 0 takes the missing particles; keep (all-qudit bases) marks the states
+// whose mode 0 stays within the capacity
+__global__ void finish_basis_kernel(int64_t n, uint8_t* occ, int K, int N, int cap, int64_t* keep) {
   for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x) {
     int tot = 0;
     for (int a = 1; a < K; ++a) tot += occ[l * K + a];
     occ[l * K] = (uint8_t)(N - tot);
+    if (keep) keep[l] = (N - tot <= cap) ? 1 : 0;
   }
 }
 
-// Index of an occupation vector in the basis, or -1 if it is not a basis state.
+// keep flags -> exclusive prefix (in place, scanned on the host side) ->
+// final index or -1, and the kept states copied into the final list
+__global__ void compact_basis_kernel(int64_t n, const uint8_t* __restrict__ occ, int K, const uint8_t* __restrict__ kept,
+                                     int64_t* __restrict__ keep, uint8_t* __restrict__ out) {
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x) {
+    if (kept[l]) {
+      for (int a = 0; a < K; ++a) out[keep[l] * K + a] = occ[l * K + a];
+    } else {
+      keep[l] = -1;
+    }
+  }
+}
+
+__global__ void keep_flags_kernel(int64_t n, const int64_t* __restrict__ keep, uint8_t* __restrict__ kept) {
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < n; l += (int64_t)gridDim.x * blockDim.x)
+    kept[l] = (uint8_t)keep[l];
+}
+
+// Index of an occupation vector in one basis, or -1 if it is not a basis state.
 __device__ int64_t state_index(const Stages& st, const int* e) {
   int tot = 0;
   for (int a = 0; a < st.K; ++a) {
@@ -92,6 +131,8 @@ __device__ int64_t state_index(const Stages& st, const int* e) {
     tot += e[a];
   }
   if (tot != st.N) return -1;
+  for (int a = st.K - st.nq; a < st.K; ++a)
+    if (a >= 0 && e[a] > st.cap) return -1;
   int64_t r = 0;
   for (int s = 0; s < st.K - 1; ++s) {
     const int m = st.K - 1 - s;
@@ -100,7 +141,25 @@ __device__ int64_t state_index(const Stages& st, const int* e) {
     if (o % st.quant) return -1;
     r = st.n_s[s] + st.ps[s][r] + o / st.quant - 1;
   }
-  return r;
+  return st.keep ? st.keep[r] : r;
+}
+
+__device__ int64_t model_index(const ModelBasis& M, const int* e) {
+  if (!M.tensor) return state_index(M.a, e);
+  const int64_t i1 = state_index(M.a, e);
+  if (i1 < 0) return -1;
+  const int64_t i2 = state_index(M.b, e + M.a.K);
+  return i2 < 0 ? -1 : i1 * M.b.dim + i2;
+}
+
+__device__ void model_occupation(const ModelBasis& M, int64_t j, int* e) {
+  if (!M.tensor) {
+    for (int a = 0; a < M.K; ++a) e[a] = M.a.occ[j * M.K + a];
+    return;
+  }
+  const int64_t j1 = j / M.b.dim, j2 = j - j1 * M.b.dim;
+  for (int a = 0; a < M.a.K; ++a) e[a] = M.a.occ[j1 * M.a.K + a];
+  for (int a = 0; a < M.b.K; ++a) e[M.a.K + a] = M.b.occ[j2 * M.b.K + a];
 }
 
 // Apply one term to the occupations (apply_term of hamiltonian.cpp): false if
@@ -127,21 +186,20 @@ __device__ bool apply_term_dev(const DevTerm& t, int* occ, int K, double2& coef)
 
 // One row: the merged, column-sorted, filtered entries (count returned; with
 // out_col != null they are also written).
-__device__ int build_row(const Stages& st, const uint8_t* __restrict__ occ, int64_t j, const DevTerm* __restrict__ terms,
-                         int n_terms, int32_t* cols, double2* vals, int32_t* out_col, double2* out_val,
-                         double* abs_sum) {
+__device__ int build_row(const ModelBasis& M, int64_t j, const DevTerm* __restrict__ terms, int n_terms,
+                         int32_t* cols, double2* vals, int32_t* out_col, double2* out_val, double* abs_sum) {
   int e[TE_MODEL_MAX_MODES];
   int cnt = 0;
   for (int ti = 0; ti < n_terms; ++ti) {
     const DevTerm& t = terms[ti];
-    for (int a = 0; a < st.K; ++a) e[a] = occ[j * st.K + a];
+    model_occupation(M, j, e);
     double2 c = make_double2(1.0, 0.0);
-    if (!apply_term_dev(t, e, st.K, c)) continue;
+    if (!apply_term_dev(t, e, M.K, c)) continue;
     // coef = coef * t.coef: the complex product rounded term by term, without
     // contraction into FMAs (as the host build)
     c = make_double2(__dsub_rn(__dmul_rn(c.x, t.coef.x), __dmul_rn(c.y, t.coef.y)),
                      __dadd_rn(__dmul_rn(c.x, t.coef.y), __dmul_rn(c.y, t.coef.x)));
-    const int64_t col = state_index(st, e);
+    const int64_t col = model_index(M, e);
     if (col < 0) continue;
     int k = 0;
     while (k < cnt && cols[k] != (int32_t)col) ++k;
@@ -193,24 +251,23 @@ __global__ void narrow_rp_kernel(int64_t count, const int64_t* __restrict__ in, 
     out[j] = (int32_t)in[j];
 }
 
-__global__ void row_count_model_kernel(Stages st, const uint8_t* __restrict__ occ, int64_t n,
-                                       const DevTerm* __restrict__ terms, int n_terms, int32_t* __restrict__ count) {
+__global__ void row_count_model_kernel(ModelBasis M, int64_t n, const DevTerm* __restrict__ terms, int n_terms,
+                                       int32_t* __restrict__ count) {
   int32_t cols[TE_MODEL_MAX_TERMS];
   double2 vals[TE_MODEL_MAX_TERMS];
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x)
-    count[j] = build_row(st, occ, j, terms, n_terms, cols, vals, nullptr, nullptr, nullptr);
+    count[j] = build_row(M, j, terms, n_terms, cols, vals, nullptr, nullptr, nullptr);
 }
 
-__global__ void row_write_model_kernel(Stages st, const uint8_t* __restrict__ occ, int64_t n,
-                                       const DevTerm* __restrict__ terms, int n_terms, const int32_t* __restrict__ rp,
-                                       int32_t* __restrict__ col, double2* __restrict__ val,
-                                       unsigned long long* norm_bits) {
+__global__ void row_write_model_kernel(ModelBasis M, int64_t n, const DevTerm* __restrict__ terms, int n_terms,
+                                       const int32_t* __restrict__ rp, int32_t* __restrict__ col,
+                                       double2* __restrict__ val, unsigned long long* norm_bits) {
   int32_t cols[TE_MODEL_MAX_TERMS];
   double2 vals[TE_MODEL_MAX_TERMS];
   double mx = 0.0;
   for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
     double s = 0.0;
-    build_row(st, occ, j, terms, n_terms, cols, vals, col + rp[j], val + rp[j], &s);
+    build_row(M, j, terms, n_terms, cols, vals, col + rp[j], val + rp[j], &s);
     mx = fmax(mx, s);
   }
   atomicMax(norm_bits, (unsigned long long)__double_as_longlong(mx));
@@ -227,49 +284,63 @@ int exclusive_scan(const int64_t* d_in, int64_t n, int64_t* d_out, int64_t* tota
 }
 
 struct DeviceBasis {
-  int K = 0, N = 0, quant = 1;
+  int K = 0, N = 0, quant = 1, nq = 0, cap = 0;
   int64_t dim = 0;
-  uint8_t* occ = nullptr;
+  uint8_t* occ = nullptr;   // final list
+  int64_t* keep = nullptr;  // all-qudit bases: staged index -> final index or -1
   std::vector<int64_t> n_s;
   std::vector<int64_t*> ps;
   int64_t* d_n_s = nullptr;
   int64_t** d_ps = nullptr;
   ~DeviceBasis() {
     cudaFree(occ);
+    cudaFree(keep);
     for (int64_t* p : ps) cudaFree(p);
     cudaFree(d_n_s);
     cudaFree(d_ps);
   }
-  Stages stages() const { return Stages{K, N, quant, d_n_s, d_ps}; }
+  Stages stages() const { return Stages{K, N, quant, nq, cap, d_n_s, d_ps, keep, occ, dim}; }
 };
 
-int build_basis(int N, int K, int quant, DeviceBasis& B) {
+// basis(N, K, nq, cap, quant) of helper/Basis.cpp:37-121 on the device.
+int build_basis(int N, int K, int nq, int cap, int quant, DeviceBasis& B) {
   B.K = K;
   B.N = N;
   B.quant = quant;
-  // final size: number of states of modes 1..K-1 with multiples of quant summing to <= N
-  // = compositions; computed by running the stage counts on the host in closed form
-  // (the list sizes grow stage by stage, so the device list is reallocated once at its final size)
-  std::vector<double> ways(N / quant + 1, 0.0);  // ways[q]: states using q quanta over the modes so far
+  B.nq = nq;
+  B.cap = cap;
+  // size of the staged list: states of modes 1..K-1 (multiples of quant, the
+  // qudit modes at most cap) with at most N particles, counted per number of
+  // quanta used; the final list drops, when every mode is a qudit, the states
+  // whose mode 0 would exceed cap
+  const int Q = N / quant;
+  std::vector<double> ways(Q + 1, 0.0);
   ways[0] = 1.0;
   for (int s = 0; s < K - 1; ++s) {
+    const int m = K - 1 - s;
+    const int tmax = m >= K - nq ? cap / quant : Q;
     std::vector<double> nw(ways.size(), 0.0);
-    for (size_t q = 0; q < ways.size(); ++q)
-      for (size_t r = q; r < ways.size(); ++r) nw[r] += ways[q];
+    for (int q = 0; q <= Q; ++q)
+      for (int r = q; r <= Q && r - q <= tmax; ++r) nw[r] += ways[q];
     ways.swap(nw);
   }
-  double total = 0.0;
-  for (double w : ways) total += w;
+  double total = 0.0, kept = 0.0;
+  for (int q = 0; q <= Q; ++q) {
+    total += ways[q];
+    if (K != nq || N - q * quant <= cap) kept += ways[q];
+  }
   if (!(total < 2147483647.0)) {
     te_set_error("te_model: basis dimension %.0f exceeds the int32 index range", total);
     return TE_ERR_UNSUPPORTED;
   }
-  const int64_t dim = (int64_t)total;
-  TE_CUDA(cudaMalloc(&B.occ, (size_t)dim * K));
-  TE_CUDA(cudaMemset(B.occ, 0, (size_t)dim * K));
+  const int64_t n_full = (int64_t)total;
+  uint8_t* occ = nullptr;
+  TE_CUDA(cudaMalloc(&occ, (size_t)std::max<int64_t>(n_full, 1) * K));
+  TE_CUDA(cudaMemset(occ, 0, (size_t)std::max<int64_t>(n_full, 1) * K));
+  B.occ = occ;
   int64_t n = 1;
   int64_t* cnt = nullptr;
-  TE_CUDA(cudaMalloc(&cnt, sizeof(int64_t) * std::max<int64_t>(dim, 1)));
+  TE_CUDA(cudaMalloc(&cnt, sizeof(int64_t) * std::max<int64_t>(n_full, 1)));
   int rc = TE_OK;
   for (int s = 0; s < K - 1 && rc == TE_OK; ++s) {
     const int m = K - 1 - s;
@@ -278,22 +349,51 @@ int build_basis(int N, int K, int quant, DeviceBasis& B) {
     if ((rc = te_cuda_check(cudaMalloc(&ps, sizeof(int64_t) * (n + 1)), "basis")) != TE_OK) break;
     B.ps.push_back(ps);
     const int g = te_grid_for(n, 256, 4);
-    stage_count_kernel<<<g, 256>>>(n, B.occ, K, N, quant, cnt);
+    stage_count_kernel<<<g, 256>>>(n, occ, K, N, quant, m >= K - nq ? cap : -1, cnt);
     int64_t added = 0;
     if ((rc = exclusive_scan(cnt, n, ps, &added)) != TE_OK) break;
-    if (n + added > dim) {
+    if (n + added > n_full) {
       te_set_error("te_model: basis enumeration inconsistent");
       rc = TE_ERR_INVALID_ARG;
       break;
     }
-    stage_expand_kernel<<<g, 256>>>(n, B.occ, K, m, quant, ps);
+    stage_expand_kernel<<<g, 256>>>(n, occ, K, m, quant, ps);
     n += added;
   }
   cudaFree(cnt);
   if (rc != TE_OK) return rc;
+  if (n != n_full) {
+    te_set_error("te_model: basis enumeration inconsistent");
+    return TE_ERR_INVALID_ARG;
+  }
   B.n_s.push_back(n);
+  const bool filter = K == nq;
+  if (filter) TE_CUDA(cudaMalloc(&B.keep, sizeof(int64_t) * (n + 1)));
+  finish_basis_kernel<<<te_grid_for(n, 256, 4), 256>>>(n, occ, K, N, cap, B.keep);
   B.dim = n;
-  finish_basis_kernel<<<te_grid_for(n, 256, 4), 256>>>(n, B.occ, K, N);
+  if (filter) {
+    uint8_t* flags = nullptr;
+    uint8_t* out = nullptr;
+    int64_t count = 0;
+    TE_CUDA(cudaMalloc(&flags, n));
+    keep_flags_kernel<<<te_grid_for(n, 256, 4), 256>>>(n, B.keep, flags);
+    rc = exclusive_scan(B.keep, n, B.keep, &count);
+    if (rc == TE_OK && count != (int64_t)kept) {
+      te_set_error("te_model: basis filter inconsistent");
+      rc = TE_ERR_INVALID_ARG;
+    }
+    if (rc == TE_OK) rc = te_cuda_check(cudaMalloc(&out, (size_t)std::max<int64_t>(count, 1) * K), "basis");
+    if (rc == TE_OK) compact_basis_kernel<<<te_grid_for(n, 256, 4), 256>>>(n, occ, K, flags, B.keep, out);
+    cudaFree(flags);
+    if (rc != TE_OK) {
+      cudaFree(out);
+      return rc;
+    }
+    TE_CUDA(cudaDeviceSynchronize());
+    cudaFree(occ);
+    B.occ = out;
+    B.dim = count;
+  }
   TE_CUDA(cudaMalloc(&B.d_n_s, sizeof(int64_t) * B.n_s.size()));
   TE_CUDA(cudaMemcpy(B.d_n_s, B.n_s.data(), sizeof(int64_t) * B.n_s.size(), cudaMemcpyHostToDevice));
   TE_CUDA(cudaMalloc(&B.d_ps, sizeof(int64_t*) * std::max<size_t>(B.ps.size(), 1)));
@@ -302,16 +402,67 @@ int build_basis(int N, int K, int quant, DeviceBasis& B) {
   return te_cuda_check(cudaDeviceSynchronize(), "basis");
 }
 
-}  // namespace
+// The basis of a descriptor: one basis, or the tensor product of basis(N1, K1,
+// 0, 0) and basis(N2, K2, K2, C2) (Basis.cpp:131-182).
+struct DeviceModelBasis {
+  DeviceBasis a, b;
+  ModelBasis view;
+};
 
-extern "C" int te_model_create_device(int n_particles, int n_modes, int quant, const te_term* terms, int n_terms,
-                                      te_matrix* out, int64_t* dim_out) {
-  if (!out || !terms || n_terms < 1 || n_terms > TE_MODEL_MAX_TERMS || n_modes < 1 ||
-      n_modes > TE_MODEL_MAX_MODES || n_particles < 0 || n_particles > 255 || quant < 1) {
-    te_set_error("te_model_create_device: invalid arguments (1..%d modes, 0..255 particles, 1..%d terms, quant >= 1)",
-                 TE_MODEL_MAX_MODES, TE_MODEL_MAX_TERMS);
+int check_desc(const te_basis_desc* d, const char* who) {
+  if (!d || d->n_modes < 1 || d->n_particles < 0 || d->n_particles > 255 || d->quant < 1 || d->n_qudits < 0 ||
+      d->n_qudits > d->n_modes || d->capacity < 0 || d->n_modes2 < 0 ||
+      d->n_modes + d->n_modes2 > TE_MODEL_MAX_MODES) {
+    te_set_error("%s: invalid basis (1..%d modes in all, 0..255 particles, 0 <= qudit modes <= modes, "
+                 "capacity >= 0, quant >= 1)", who, TE_MODEL_MAX_MODES);
     return TE_ERR_INVALID_ARG;
   }
+  if (d->n_modes2 > 0 && (d->n_qudits != 0 || d->quant != 1 || d->n_particles2 < 0 || d->n_particles2 > 255 ||
+                          d->capacity2 < 0)) {
+    te_set_error("%s: a tensor basis takes a first set without qudit modes and quant 1, and 0..255 particles "
+                 "and capacity >= 0 in the second set", who);
+    return TE_ERR_INVALID_ARG;
+  }
+  return TE_OK;
+}
+
+int build_model_basis(const te_basis_desc* d, DeviceModelBasis& M) {
+  int rc = build_basis(d->n_particles, d->n_modes, d->n_qudits, d->capacity, d->quant, M.a);
+  if (rc != TE_OK) return rc;
+  M.view.a = M.a.stages();
+  M.view.tensor = d->n_modes2 > 0 ? 1 : 0;
+  M.view.K = d->n_modes;
+  M.view.dim = M.a.dim;
+  if (M.view.tensor) {
+    if ((rc = build_basis(d->n_particles2, d->n_modes2, d->n_modes2, d->capacity2, 1, M.b)) != TE_OK) return rc;
+    if (M.b.dim == 0) {
+      te_set_error("te_model: the second set of the tensor basis is empty");
+      return TE_ERR_UNSUPPORTED;
+    }
+    if (!((double)M.a.dim * (double)M.b.dim < 2147483647.0)) {
+      te_set_error("te_model: basis dimension exceeds the int32 index range");
+      return TE_ERR_UNSUPPORTED;
+    }
+    M.view.b = M.b.stages();
+    M.view.K += d->n_modes2;
+    M.view.dim = M.a.dim * M.b.dim;
+  } else {
+    M.view.b = M.view.a;
+  }
+  return TE_OK;
+}
+
+}  // namespace
+
+extern "C" int te_model_create_device_basis(const te_basis_desc* basis, const te_term* terms, int n_terms,
+                                            te_matrix* out, int64_t* dim_out) {
+  int rc = check_desc(basis, "te_model_create_device_basis");
+  if (rc != TE_OK) return rc;
+  if (!out || !terms || n_terms < 1 || n_terms > TE_MODEL_MAX_TERMS) {
+    te_set_error("te_model_create_device_basis: invalid arguments (1..%d terms)", TE_MODEL_MAX_TERMS);
+    return TE_ERR_INVALID_ARG;
+  }
+  const int n_modes = basis->n_modes + basis->n_modes2;
   std::vector<DevTerm> dt(n_terms);
   for (int i = 0; i < n_terms; ++i) {
     const te_term& t = terms[i];
@@ -333,10 +484,13 @@ extern "C" int te_model_create_device(int n_particles, int n_modes, int quant, c
       d.capacity[k] = t.capacity[k];
     }
   }
-  DeviceBasis B;
-  int rc = build_basis(n_particles, n_modes, quant, B);
-  if (rc != TE_OK) return rc;
-  const int64_t n = B.dim;
+  DeviceModelBasis MB;
+  if ((rc = build_model_basis(basis, MB)) != TE_OK) return rc;
+  const int64_t n = MB.view.dim;
+  if (n == 0) {
+    te_set_error("te_model_create_device_basis: the basis is empty");
+    return TE_ERR_DIM;
+  }
   DevTerm* d_terms = nullptr;
   int32_t *d_cnt = nullptr, *d_rp = nullptr, *d_col = nullptr;
   double2* d_val = nullptr;
@@ -356,9 +510,9 @@ extern "C" int te_model_create_device(int n_particles, int n_modes, int quant, c
     return fail(TE_ERR_CUDA);
   cudaMemcpy(d_terms, dt.data(), sizeof(DevTerm) * n_terms, cudaMemcpyHostToDevice);
   cudaMemset(d_norm, 0, sizeof(unsigned long long));
-  const Stages st = B.stages();
+  const ModelBasis st = MB.view;
   const int g = te_grid_fit((const void*)row_count_model_kernel, n, 128);
-  row_count_model_kernel<<<g, 128>>>(st, B.occ, n, d_terms, n_terms, d_cnt);
+  row_count_model_kernel<<<g, 128>>>(st, n, d_terms, n_terms, d_cnt);
   // row pointers: a 64-bit scan of the counts on the device (the total must
   // stay below 2^31), narrowed to int32
   int64_t* d_rp64 = nullptr;
@@ -384,7 +538,7 @@ extern "C" int te_model_create_device(int n_particles, int n_modes, int quant, c
       te_cuda_check(cudaMalloc(&d_val, sizeof(double2) * std::max<int64_t>(nnz, 1)), "model") != TE_OK)
     return fail(TE_ERR_CUDA);
   row_write_model_kernel<<<te_grid_fit((const void*)row_write_model_kernel, n, 128), 128>>>(
-      st, B.occ, n, d_terms, n_terms, d_rp, d_col, d_val, d_norm);
+      st, n, d_terms, n_terms, d_rp, d_col, d_val, d_norm);
   unsigned long long bits = 0;
   if (te_cuda_check(cudaMemcpy(&bits, d_norm, sizeof(bits), cudaMemcpyDeviceToHost), "model") != TE_OK)
     return fail(TE_ERR_CUDA);
@@ -402,24 +556,34 @@ extern "C" int te_model_create_device(int n_particles, int n_modes, int quant, c
   return TE_OK;
 }
 
+extern "C" int te_model_create_device(int n_particles, int n_modes, int quant, const te_term* terms, int n_terms,
+                                      te_matrix* out, int64_t* dim_out) {
+  te_basis_desc d;
+  std::memset(&d, 0, sizeof(d));
+  d.n_particles = n_particles;
+  d.n_modes = n_modes;
+  d.quant = quant;
+  return te_model_create_device_basis(&d, terms, n_terms, out, dim_out);
+}
+
 namespace {
 
-__global__ void state_index_kernel(Stages st, const int* e, int64_t* out) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) *out = state_index(st, e);
+__global__ void state_index_kernel(ModelBasis M, const int* e, int64_t* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *out = model_index(M, e);
 }
 
 }  // namespace
 
-extern "C" int te_model_state_index(int n_particles, int n_modes, int quant, const int32_t* occupation,
-                                    int64_t* index) {
-  if (!occupation || !index || n_modes < 1 || n_modes > TE_MODEL_MAX_MODES || quant < 1 || n_particles < 0 ||
-      n_particles > 255) {
-    te_set_error("te_model_state_index: invalid arguments");
+extern "C" int te_model_basis_index(const te_basis_desc* basis, const int32_t* occupation, int64_t* index) {
+  int rc = check_desc(basis, "te_model_basis_index");
+  if (rc != TE_OK) return rc;
+  if (!occupation || !index) {
+    te_set_error("te_model_basis_index: invalid arguments");
     return TE_ERR_INVALID_ARG;
   }
-  DeviceBasis B;
-  int rc = build_basis(n_particles, n_modes, quant, B);
-  if (rc != TE_OK) return rc;
+  const int n_modes = basis->n_modes + basis->n_modes2;
+  DeviceModelBasis MB;
+  if ((rc = build_model_basis(basis, MB)) != TE_OK) return rc;
   int* d_e = nullptr;
   int64_t* d_r = nullptr;
   if (te_cuda_check(cudaMalloc(&d_e, sizeof(int) * n_modes), "index") != TE_OK ||
@@ -429,9 +593,19 @@ extern "C" int te_model_state_index(int n_particles, int n_modes, int quant, con
     return TE_ERR_CUDA;
   }
   cudaMemcpy(d_e, occupation, sizeof(int) * n_modes, cudaMemcpyHostToDevice);
-  state_index_kernel<<<1, 32>>>(B.stages(), d_e, d_r);
+  state_index_kernel<<<1, 32>>>(MB.view, d_e, d_r);
   rc = te_cuda_check(cudaMemcpy(index, d_r, sizeof(int64_t), cudaMemcpyDeviceToHost), "index");
   cudaFree(d_e);
   cudaFree(d_r);
   return rc;
+}
+
+extern "C" int te_model_state_index(int n_particles, int n_modes, int quant, const int32_t* occupation,
+                                    int64_t* index) {
+  te_basis_desc d;
+  std::memset(&d, 0, sizeof(d));
+  d.n_particles = n_particles;
+  d.n_modes = n_modes;
+  d.quant = quant;
+  return te_model_basis_index(&d, occupation, index);
 }

@@ -704,17 +704,25 @@ def evolve(H_coo, v, t, sampling_step, observables=(), exp_factor=1.0, tol=1e-6,
     ("sparse", (row, col, val)), ("vector", o) or ("callback", fn).
     ``options``: {OPT_*: value} for te_evolver_set_option."""
     n = len(v)
+    created = []  # matrices made here are released before returning, not whenever Python collects them
     H = H_coo if isinstance(H_coo, Matrix) else Matrix.from_coo(n, H_coo)
+    if H is not H_coo:
+        created.append(H)
     obs = []
-    for kind, data in observables:
-        if kind == "sparse":
-            obs.append(("sparse", Matrix.from_coo(n, data)))
-        else:
-            obs.append((kind, data))
-    ev = Evolver(H, v, t, sampling_step, obs, exp_factor, tol, m, fast_integration, reorth)
+    ev = None
     try:
+        for kind, data in observables:
+            if kind == "sparse" and not isinstance(data, Matrix):
+                created.append(Matrix.from_coo(n, data))
+                obs.append(("sparse", created[-1]))
+            else:
+                obs.append((kind, data))
+        ev = Evolver(H, v, t, sampling_step, obs, exp_factor, tol, m, fast_integration, reorth)
         for opt, val in (options or {}).items():
             ev.set_option(opt, val)
         return ev.time_evolve(trace=trace)
     finally:
-        ev.close()
+        if ev is not None:
+            ev.close()
+        for M in created:
+            M.close()

@@ -414,7 +414,8 @@ int run(te_evolver ev, te_result* out) {
       if (!cgs2) {
         ProfScope ps(ev, 1);
         te_launch_lanczos_update(n, ev->w, ev->cols[j], j + 1 < m ? ev->cols[j + 1] : nullptr, ev->ds, ev->partials,
-                                 j, fold, st, fix_step && j + 1 < m ? ev->X + (int64_t)(j + 1) * n : nullptr);
+                                 j, fold, st, fix_step && j + 1 < m ? ev->X + (int64_t)(j + 1) * n : nullptr,
+                                 fix_step);
         ev->launches += 2;
       } else {
         // classical Gram-Schmidt against u_0..u_j, then one reorthogonalisation pass

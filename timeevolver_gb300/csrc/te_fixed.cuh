@@ -44,6 +44,36 @@ __device__ __forceinline__ int64_t te_fix_encode(double v, int xs) {
   return (b >> 63) ? -(int64_t)mag : (int64_t)mag;
 }
 
+// x 2^k rounded to the nearest integer (half away from zero) as a signed
+// 128-bit two's complement {lo, hi}; zeros and subnormals give 0.  The caller
+// keeps |x| 2^k below 2^126.  Integer instructions only.
+__device__ __forceinline__ void te_fix_encode128(double x, int k, unsigned long long& lo, unsigned long long& hi) {
+  const uint64_t b = (uint64_t)__double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ff);
+  lo = hi = 0ull;
+  if (e == 0) return;
+  const uint64_t m = (b & 0xfffffffffffffull) | (1ull << 52);
+  const int sft = e - 1075 + k;  // |x| 2^k = m 2^sft
+  if (sft >= 64) {
+    hi = m << min(sft - 64, 63);
+  } else if (sft > 0) {
+    lo = m << sft;
+    hi = m >> (64 - sft);
+  } else if (sft == 0) {
+    lo = m;
+  } else if (sft > -64) {
+    const int r = -sft;
+    lo = (m >> r) + ((m >> (r - 1)) & 1ull);
+  }
+  if (b >> 63) {  // negate
+    lo = ~lo + 1ull;
+    hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+  }
+}
+
+// Signed 128-bit {lo, hi} times 2^e2, rounded to the nearest double.
+__device__ __forceinline__ double te_i128_to_double(unsigned long long lo, unsigned long long hi, int e2);
+
 // Limb split v = v1 2^31 + v0, 0 <= v0 < 2^31 (|v| < 2^61 keeps |v1| < 2^30).
 __device__ __forceinline__ int2 te_fix_split(int64_t v) {
   return make_int2((int)(v & 0x7fffffffll), (int)(v >> 31));
@@ -95,6 +125,21 @@ __device__ __forceinline__ double te_u128_to_double(unsigned long long hi, unsig
   }
   if (ex < -1022) return 0.0;
   return __longlong_as_double((long long)(((uint64_t)(ex + 1023) << 52) | (mant & 0xfffffffffffffull)));
+}
+
+__device__ __forceinline__ double te_i128_to_double(unsigned long long lo, unsigned long long hi, int e2) {
+  if (hi >> 63) {
+    const unsigned long long nlo = ~lo + 1ull, nhi = ~hi + (nlo == 0ull ? 1ull : 0ull);
+    return -te_u128_to_double(nhi, nlo, e2);
+  }
+  return te_u128_to_double(hi, lo, e2);
+}
+
+// {lo, hi} added to the 128-bit integer at p (two atomics, the carry of the
+// low word into the high word; any order of additions gives the same total).
+__device__ __forceinline__ void te_atomic_add128(unsigned long long* p, unsigned long long lo, unsigned long long hi) {
+  const unsigned long long old = atomicAdd(p, lo);
+  atomicAdd(p + 1, hi + (old + lo < old ? 1ull : 0ull));
 }
 
 // v^2 / 2^62 for |v| < 2^61 from 31-bit limbs of |v| (a1^2 + 4 hi32(a1 a0),

@@ -95,6 +95,18 @@ struct TeDevState {
   int fx_xs[TE_MMAX + 1];
   unsigned int fx_umax[TE_MMAX + 1];
   unsigned int fx_wmax, fx_pad;
+  // ||u'_j||^2 of the fixed-point copy, exactly: the sum over all rows of the
+  // components' squares in units of 2^(2 fx_xs[j] - 62), as a 128-bit integer
+  // {low, high} that the update pass's blocks add atomically (the order does
+  // not matter) and the next apply pass reads
+  unsigned long long fx_nrm[TE_MMAX + 1][2];
+  // <u_j, w'> of the fixed-point apply pass j, exactly: each block's FP64 sum
+  // (re, im) rounded to a signed 128-bit integer in units of 2^-fx_ak[j] (from
+  // an a-priori bound of the sum, so the units are the same in every block)
+  // and added atomically {re low, re high, im low, im high}; max|w'| per pass
+  unsigned long long fx_alpha[TE_MMAX][4];
+  int fx_ak[TE_MMAX];
+  unsigned int fx_wmaxj[TE_MMAX];
   // the update pass's coefficient alpha_j s_j / g (alpha_j / expFactor when
   // folded), set with alpha_j by the apply pass
   double upd_gr, upd_gi;
@@ -320,8 +332,11 @@ void te_launch_lanczos_apply(const TeSell& A, bool is_real, const double2* u_j, 
                              TeDevState* ds, double* partials, int j, bool fold, cudaStream_t st,
                              const TeSegCarry* carry = nullptr);
 // X_out (optional): also write the fixed-point copy of u_{j+1} (te_fixed.cuh)
+// alpha_acc: alpha_j from the fixed-point apply pass's exact accumulator (the
+// fixed-point path; X_out non-null implies it)
 void te_launch_lanczos_update(int64_t n, const double2* w, const double2* u_j, double2* u_jp1, TeDevState* ds,
-                              double* partials, int j, bool fold, cudaStream_t st, int4* X_out = nullptr);
+                              double* partials, int j, bool fold, cudaStream_t st, int4* X_out = nullptr,
+                              bool alpha_acc = false);
 // Fixed-point path of the folded three-term iteration (real matrices, one lane
 // per row, te_sell_build_fixed done): te_launch_fix_start encodes u_0 at the
 // start of a Krylov step; the apply pass reads the fixed-point copy X of u_j.

@@ -152,34 +152,87 @@ __device__ __forceinline__ unsigned int te_block_max_from_smem(const unsigned in
   return m;
 }
 
-// End of a fixed-point apply pass: block sums of <u_j, w'> and max|w'|, then
-// in the last block alpha_j = f <u_j, w'> (f = s_j g), the update's
-// coefficient alpha_j / e, and the scale xs_{j+1} of the next vector from
-// B = W + (|Re| + |Im|)(alpha_j / e) U (W >= max|w'|, U >= max|u_j|).
-// L: the long rows whose split rows' terms are added in the final sum (none
-// for the column-blocked epilogue).
-__device__ __forceinline__ void fix_apply_finish(double (&acc)[2], unsigned int wmax, TeDevState* ds,
-                                                 double* partials, int j, double f, double ie, double* scratch,
-                                                 double* wide, unsigned int* wmax_w, const TeLongRows* L) {
+// Start of a fixed-point apply pass j, by thread 0 of every block (a square
+// root and divisions are long FP64 sequences on GB300), shared through sh[3]:
+// for j > 0, beta_j = |e s_{j-1}| ||u'_j|| from the exact norm that update
+// pass j - 1 accumulated, s_j = e s_{j-1} / beta_j, or the lucky breakdown
+// (:551-555; false is returned and the pass does nothing); then the units
+// 2^-k of the exact <u_j, w'> sum, from the bound
+// |<u_j, w'>| <= ||u_j|| (R ||u_j|| + c_w ||u_{j-1}||) with ||u_i|| = 1/|s_i|,
+// R < 2^(61 - sh) the matrix's row-norm bound, doubled for rounding, below
+// 2^(124 - k).  Block 0 records beta_j, s_j and k.
+template <bool HAS_PREV>
+__device__ __forceinline__ bool fix_apply_prologue(TeDevState* ds, int j, int msh, double* sh, double& sj, double& bj,
+                                                   int& k) {
+  if (threadIdx.x == 0) {
+    double s0 = ds->s[j], b = 0.0;
+    bool ok = true;
+    if (HAS_PREV) {
+      const unsigned long long lo = ds->fx_nrm[j][0], hi = ds->fx_nrm[j][1];
+      const double gp = ds->exp_factor * ds->s[j - 1];
+      b = fabs(gp) * sqrt(te_u128_to_double(hi, lo, 62 - 2 * ds->fx_xs[j]));
+      if (b < ds->tol_rate) {
+        ok = false;
+        if (blockIdx.x == 0) {
+          ds->breakdown = 1;
+          ds->m_eff = j;
+          ds->h = b;
+        }
+      } else {
+        s0 = gp / b;
+      }
+    }
+    int kk = 0;
+    if (ok) {
+      const double ie = ds->inv_exp_factor;
+      const double nu = 1.0 / fabs(s0);
+      const double cw = HAS_PREV ? (b * ie) * (b * ie) : 0.0;
+      const double nprev = HAS_PREV ? 1.0 / fabs(ds->s[j - 1]) : 0.0;
+      const double B = 2.0 * nu * (ldexp(1.0, 61 - msh) * nu + cw * nprev);
+      if (B > 0.0 && B < 1e300) {
+        int E;
+        frexp(B, &E);  // B < 2^E
+        kk = 124 - E;
+      }
+      if (blockIdx.x == 0) {
+        if (HAS_PREV) {
+          ds->beta[j] = b;
+          ds->s[j] = s0;
+        }
+        ds->fx_ak[j] = kk;
+      }
+    }
+    sh[0] = b;
+    sh[1] = ok ? s0 : 0.0;
+    sh[2] = (double)kk;
+  }
+  __syncthreads();
+  bj = sh[0];
+  sj = sh[1];
+  k = (int)sh[2];
+  return sj != 0.0;
+}
+
+// <u_j, w'> terms (re, im) added exactly to the pass's accumulator in units
+// of 2^-k (one thread).
+__device__ __forceinline__ void fix_alpha_add(TeDevState* ds, int j, int k, double re, double im) {
+  unsigned long long lo, hi;
+  te_fix_encode128(re, k, lo, hi);
+  te_atomic_add128(&ds->fx_alpha[j][0], lo, hi);
+  te_fix_encode128(im, k, lo, hi);
+  te_atomic_add128(&ds->fx_alpha[j][2], lo, hi);
+}
+
+// End of a fixed-point apply pass: the block's <u_j, w'> sums into the exact
+// accumulator and its max|w'| into fx_wmaxj[j].  No last-block reduction: the
+// update pass finishes alpha_j, its coefficient and xs_{j+1} from them.
+__device__ __forceinline__ void fix_apply_publish(double (&acc)[2], unsigned int wmax, TeDevState* ds, int j, int k,
+                                                  double* wide, unsigned int* wmax_w) {
   te_warp_max_to_smem(wmax, wmax_w);
   te_block_sum_wide<2>(acc, wide);
-  if (threadIdx.x == 0) atomicMax(&ds->fx_wmax, te_block_max_from_smem(wmax_w));
-  if (te_publish_partials<2>(acc, partials, &ds->counter[0])) {
-    double tot[2];
-    te_final_sum<2>(tot, partials, &ds->counter[0], scratch, [&](double (&o)[2]) {
-      if (L) te_split_rows_add(o, *L);
-    });
-    if (threadIdx.x == 0) {
-      const double2 alpha = make_double2(f * tot[0], f * tot[1]);
-      ds->alpha[j] = alpha;
-      ds->upd_gr = alpha.x * ie;
-      ds->upd_gi = alpha.y * ie;
-      const double W = te_fix_upper(atomicExch(&ds->fx_wmax, 0u));
-      const double U = te_fix_upper(ds->fx_umax[j]);
-      const double B = (W + (fabs(alpha.x * ie) + fabs(alpha.y * ie)) * U) * (1.0 + 1e-12);
-      ds->fx_xs[j + 1] = te_fix_scale(B);
-      ds->fx_umax[j + 1] = 0u;
-    }
+  if (threadIdx.x == 0) {
+    atomicMax(&ds->fx_wmaxj[j], te_block_max_from_smem(wmax_w));
+    fix_alpha_add(ds, j, k, acc[0], acc[1]);
   }
 }
 
@@ -228,14 +281,13 @@ __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_f
   te_pdl_wait();
   if (te_step_inactive(ds)) return;
   const int lane = threadIdx.x & 31;
-  const double sj = ds->s[j];
+  double sj, bj;
+  int ak;
+  if (!fix_apply_prologue<HAS_PREV>(ds, j, M.sh, scratch, sj, bj, ak)) return;
   const double g = ds->exp_factor * sj;
   const double ie = ds->inv_exp_factor;
   double cw = 0.0;
-  if (HAS_PREV) {
-    const double bj = ds->beta[j];
-    cw = (bj * ie) * (bj * ie);
-  }
+  if (HAS_PREV) cw = (bj * ie) * (bj * ie);
   const int shift = M.sh + ds->fx_xs[j];
   double acc[2] = {0.0, 0.0};
   unsigned int wmax = 0;
@@ -246,9 +298,11 @@ __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_f
     double2 y;
     const int done = te_long_segment<FMT != 2>(L, sg, u_j, lane, &lr, &y);
     if (done && lane == 0) {
-      double a2[2] = {0.0, 0.0};  // a split row's terms join the final sum in row order
+      // a split row's terms go to the exact accumulator on their own, so that
+      // no block's FP64 sum depends on which warp completed the row
+      double a2[2] = {0.0, 0.0};
       const double2 wr = apply_row_epilogue<HAS_PREV, true>(lr, y, g, cw, u_j, u_jm1, w, done == 1 ? acc : a2);
-      if (done == 2) te_split_row_publish(L, lr, a2);
+      if (done == 2) fix_alpha_add(ds, j, ak, a2[0], a2[1]);
       wmax = max(wmax, max(te_fix_hiword(wr.x), te_fix_hiword(wr.y)));
     }
   }
@@ -277,7 +331,7 @@ __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_f
       wmax = max(wmax, max(te_fix_hiword(wr.x), te_fix_hiword(wr.y)));
     }
   }
-  fix_apply_finish(acc, wmax, ds, partials, j, sj * g, ie, scratch, wide, wmax_w, &L);
+  fix_apply_publish(acc, wmax, ds, j, ak, wide, wmax_w);
 }
 
 // One column block of the fixed-point SpMV: for block row i (main row
@@ -325,14 +379,13 @@ __global__ void __launch_bounds__(TE_THREADS) fix_epilogue_kernel(int64_t n, con
   te_pdl_trigger();
   te_pdl_wait();
   if (te_step_inactive(ds)) return;
-  const double sj = ds->s[j];
+  double sj, bj;
+  int ak;
+  if (!fix_apply_prologue<HAS_PREV>(ds, j, sh, scratch, sj, bj, ak)) return;
   const double g = ds->exp_factor * sj;
   const double ie = ds->inv_exp_factor;
   double cw = 0.0;
-  if (HAS_PREV) {
-    const double bj = ds->beta[j];
-    cw = (bj * ie) * (bj * ie);
-  }
+  if (HAS_PREV) cw = (bj * ie) * (bj * ie);
   const int shift = sh + ds->fx_xs[j];
   double acc[2] = {0.0, 0.0};
   unsigned int wmax = 0;
@@ -341,7 +394,7 @@ __global__ void __launch_bounds__(TE_THREADS) fix_epilogue_kernel(int64_t n, con
                                                           acc);
     wmax = max(wmax, max(te_fix_hiword(wr.x), te_fix_hiword(wr.y)));
   }
-  fix_apply_finish(acc, wmax, ds, partials, j, sj * g, ie, scratch, wide, wmax_w, nullptr);
+  fix_apply_publish(acc, wmax, ds, j, ak, wide, wmax_w);
 }
 
 // Start of a Krylov step on the fixed-point path, two passes over u_0:
@@ -380,6 +433,14 @@ __global__ void __launch_bounds__(TE_THREADS) fix_start_encode_kernel(int64_t n,
       ds->fx_xs[0] = xs_s;
       ds->fx_umax[0] = um;
       ds->fx_wmax = 0u;
+    }
+  }
+  if (blockIdx.x == 0) {  // the exact accumulators of this Krylov step's passes
+    for (int i = threadIdx.x; i < TE_MMAX; i += blockDim.x) {
+      ds->fx_alpha[i][0] = ds->fx_alpha[i][1] = ds->fx_alpha[i][2] = ds->fx_alpha[i][3] = 0ull;
+      ds->fx_wmaxj[i] = 0u;
+      ds->fx_nrm[i + 1][0] = ds->fx_nrm[i + 1][1] = 0ull;
+      ds->fx_umax[i + 1] = 0u;
     }
   }
   __syncthreads();
@@ -573,7 +634,11 @@ bool te_launch_lanczos_step(const TeSell& A, bool is_real, double2* const* cols,
 // and keeps the factor in the scale: beta_{j+1} = |g| ||u'||, s_{j+1} = g / beta_{j+1}.
 // FIX: also writes X = round(u'_{j+1} 2^xs_{j+1}) (the fixed-point copy read
 // by the next apply pass) and folds max |u'_{j+1}| into fx_umax[j + 1].
-template <bool STORE, bool FIX>
+// ACC (fixed-point path): alpha_j = s_j g <u_j, w'> from the apply pass's
+// exact accumulator, its coefficient alpha_j / e and xs_{j+1} from
+// B = (W + (|Re| + |Im|)(alpha_j / e) U)(1 + 1e-12) (W >= max|w'|, U >=
+// max|u_j|), computed by thread 0 of every block; block 0 records them.
+template <bool STORE, bool FIX, bool ACC>
 __global__ void __launch_bounds__(TE_THREADS) lanczos_update_kernel(int64_t n, const double2* __restrict__ w,
                                                                     const double2* __restrict__ u_j,
                                                                     double2* __restrict__ u_jp1, TeDevState* ds,
@@ -585,8 +650,41 @@ __global__ void __launch_bounds__(TE_THREADS) lanczos_update_kernel(int64_t n, c
   te_pdl_trigger();
   te_pdl_wait();
   if (te_step_inactive(ds)) return;
-  const double gr = ds->upd_gr, gi = ds->upd_gi;  // alpha_j s_j / g
-  const int xs = FIX ? ds->fx_xs[j + 1] : 0;
+  double gr, gi;  // alpha_j s_j / g
+  int xs;
+  if (ACC) {
+    if (threadIdx.x == 0) {
+      const int k = ds->fx_ak[j];
+      const double re = te_i128_to_double(ds->fx_alpha[j][0], ds->fx_alpha[j][1], -k);
+      const double im = te_i128_to_double(ds->fx_alpha[j][2], ds->fx_alpha[j][3], -k);
+      const double sj = ds->s[j];
+      const double f = sj * (ds->exp_factor * sj);
+      const double ie = ds->inv_exp_factor;
+      const double2 alpha = make_double2(f * re, f * im);
+      const double W = te_fix_upper(ds->fx_wmaxj[j]);
+      const double U = te_fix_upper(ds->fx_umax[j]);
+      const double B = (W + (fabs(alpha.x * ie) + fabs(alpha.y * ie)) * U) * (1.0 + 1e-12);
+      const int x = te_fix_scale(B);
+      scratch[0] = alpha.x * ie;
+      scratch[1] = alpha.y * ie;
+      scratch[2] = (double)x;
+      if (blockIdx.x == 0) {
+        ds->alpha[j] = alpha;
+        ds->upd_gr = alpha.x * ie;
+        ds->upd_gi = alpha.y * ie;
+        ds->fx_xs[j + 1] = x;
+      }
+    }
+    __syncthreads();
+    gr = scratch[0];
+    gi = scratch[1];
+    xs = FIX ? (int)scratch[2] : 0;
+    __syncthreads();
+  } else {
+    gr = ds->upd_gr;
+    gi = ds->upd_gi;
+    xs = FIX ? ds->fx_xs[j + 1] : 0;
+  }
   double acc[1] = {0.0};
   unsigned int umax = 0;
   unsigned long long sq_lo = 0, sq_hi = 0;  // FIX: sum |X|^2 / 2^62 in 128 bits
@@ -610,11 +708,35 @@ __global__ void __launch_bounds__(TE_THREADS) lanczos_update_kernel(int64_t n, c
     }
   }
   if (FIX) {
-    acc[0] = te_u128_to_double(sq_hi, sq_lo, 62 - 2 * xs);  // integers only
+    // ||u'||^2 exactly: 128-bit sums per warp and block, then two atomics into
+    // fx_nrm[j + 1]; the next apply pass takes beta_{j+1} from it (no
+    // last-block reduction, and the total does not depend on the order)
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long l2 = __shfl_xor_sync(0xffffffffu, sq_lo, o);
+      const unsigned long long h2 = __shfl_xor_sync(0xffffffffu, sq_hi, o);
+      sq_lo += l2;
+      sq_hi += h2 + (sq_lo < l2 ? 1ull : 0ull);
+    }
     te_warp_max_to_smem(umax, umax_w);
+    unsigned long long* wsum = reinterpret_cast<unsigned long long*>(wide);  // 2 words per warp
+    if ((threadIdx.x & 31) == 0) {
+      wsum[2 * (threadIdx.x >> 5)] = sq_lo;
+      wsum[2 * (threadIdx.x >> 5) + 1] = sq_hi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long lo = 0, hi = 0;
+      for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+        lo += wsum[2 * k];
+        hi += wsum[2 * k + 1] + (lo < wsum[2 * k] ? 1ull : 0ull);
+      }
+      const unsigned long long old = atomicAdd(&ds->fx_nrm[j + 1][0], lo);
+      atomicAdd(&ds->fx_nrm[j + 1][1], hi + (old + lo < old ? 1ull : 0ull));
+      atomicMax(&ds->fx_umax[j + 1], te_block_max_from_smem(umax_w));
+    }
+    return;
   }
   te_block_sum_wide<1>(acc, wide);
-  if (FIX && threadIdx.x == 0) atomicMax(&ds->fx_umax[j + 1], te_block_max_from_smem(umax_w));
   if (te_publish_partials<1>(acc, partials, &ds->counter[1])) {
     double tot[1];
     te_final_sum<1>(tot, partials, &ds->counter[1], scratch);
@@ -957,10 +1079,12 @@ int te_tune_sell_lanes(te_matrix_s* A) {
 }
 
 void te_launch_lanczos_update(int64_t n, const double2* w, const double2* u_j, double2* u_jp1, TeDevState* ds,
-                              double* partials, int j, bool fold, cudaStream_t st, int4* X_out) {
+                              double* partials, int j, bool fold, cudaStream_t st, int4* X_out, bool alpha_acc) {
   const bool fix = u_jp1 && X_out;
-  const auto k = fix ? lanczos_update_kernel<true, true>
-                     : (u_jp1 ? lanczos_update_kernel<true, false> : lanczos_update_kernel<false, false>);
+  const auto k = fix ? lanczos_update_kernel<true, true, true>
+                     : (alpha_acc ? lanczos_update_kernel<false, false, true>
+                                  : (u_jp1 ? lanczos_update_kernel<true, false, false>
+                                           : lanczos_update_kernel<false, false, false>));
   const void* kk = (const void*)k;
   const int grid = te_grid_fit(kk, n, TE_THREADS);
   te_launch_pdl(te_grid_saturated(kk, n, TE_THREADS), k, grid, TE_THREADS, st, n, w, u_j, u_jp1, ds, partials, j,

@@ -10,9 +10,13 @@
 //                    beta_{j+1} = ||u_{j+1}||          (:548)
 //                    lucky breakdown if beta_{j+1} < tolRate (:551-555)
 // The 1/beta scaling of :558-565 is deferred into s_{j+1}, so no pass rewrites
-// a vector.  Each pass finishes its reduction in the last block to complete
-// (fixed order), so the Krylov coefficients never leave the device.  Pass 1
-// runs on the SELL-32 layout: a warp owns 32 equal-length rows.
+// a vector.  The Krylov coefficients never leave the device.  On the FP64
+// path each pass finishes its reduction in the last block to complete (fixed
+// order).  On the fixed-point path alpha_j and ||u_{j+1}||^2 are summed exactly
+// as 128-bit integers with per-block atomics, and the pass after each sum
+// finishes it (no block waits for the others; the total does not depend on
+// the order of the atomics).  Pass 1 runs on the SELL-32 layout: a warp owns
+// 32 equal-length rows.
 #include <algorithm>
 #include <cmath>
 #include <cstring>

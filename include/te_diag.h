@@ -13,6 +13,14 @@ extern "C" {
  * CUDA events.  Returns 0 or a negative TE_ERR_* code. */
 int te_probe_fp64_tflops(double* tflops);
 
+/* FP64 FMA issue with `warps` warps per block on `blocks` blocks (1..32 warps;
+ * at most one block per SM for a per-SM figure): cycles_indep = SM clock
+ * cycles per warp FMA per block when each thread runs 8 independent chains,
+ * cycles_chain = cycles per FMA of one dependent chain per thread.  The clock
+ * is the device's nominal clock (cudaDevAttrClockRate).  Returns 0 or a
+ * negative TE_ERR_* code. */
+int te_probe_fp64_issue(int warps, int blocks, double* cycles_indep, double* cycles_chain);
+
 #ifdef __cplusplus
 }
 #endif

@@ -96,6 +96,7 @@ SIGNATURES = {
     "te_evolver_profile": (_I, [_P, _I]),
     "te_evolver_kernel_time": (_I, [_P, _I, _P, _P]),
     "te_probe_fp64_tflops": (_I, [_P]),
+    "te_probe_fp64_issue": (_I, [_I, _I, _P, _P]),
     "te_batch_create": (_I, [_I, _P, _P, _P, _P]),
     "te_batch_destroy": (_I, [_P]),
     "te_batch_add_observable": (_I, [_P, _I, _P]),
@@ -161,6 +162,16 @@ def probe_fp64_tflops():
     x = ctypes.c_double()
     _check(lib().te_probe_fp64_tflops(ctypes.byref(x)), "te_probe_fp64_tflops")
     return x.value
+
+
+def probe_fp64_issue(warps, blocks=1):
+    """FP64 FMA issue with ``warps`` warps per block on ``blocks`` blocks:
+    (cycles per warp FMA per block with 8 independent chains per thread,
+    cycles per FMA of one dependent chain)."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    _check(lib().te_probe_fp64_issue(int(warps), int(blocks), ctypes.byref(a), ctypes.byref(b)),
+           "te_probe_fp64_issue")
+    return a.value, b.value
 
 
 def _check(rc, where):

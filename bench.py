@@ -197,6 +197,14 @@ def spmv_bytes(n, nnz):
     return 20 * nnz + 4 * (n + 1) + 32 * n
 
 
+def whole_solve_bytes(n, nnz, iterations, vw_products, m):
+    """Algorithmic bytes of a whole solve: per Lanczos iteration one SpMV plus
+    the recurrence's vector traffic (u_j and w read, u_{j+1} written, u_{j-1}
+    read: 64 n), per V.w product the basis read and the result written
+    (16 n m + 16 n)."""
+    return iterations * (spmv_bytes(n, nnz) + 64 * n) + vw_products * (16 * n * m + 16 * n)
+
+
 def apply_kernel_bytes(n, nnz, real=True, fixed=False, packed=False):
     """Algorithmic bytes of one Lanczos apply launch: the matrix (values +
     int32 columns; with the value dictionary one 4-byte word per entry), the
@@ -304,6 +312,9 @@ def run_gb300(args):
     avg_apply_s = apply_ms / 1000.0 / max(1, apply_n)
     achieved = b_apply / avg_apply_s / 1e9
     traffic = ncu_traffic(fixed)
+    iters = kernel_ms["lanczos_update"][1]  # one update pass per Lanczos iteration
+    vw = steps_per_solve + int(T_FINAL / SAMPLING)  # V.w per step and per sample after t=0
+    b_whole = whole_solve_bytes(n, nnz, iters, vw, M_KRYLOV)
     line = {
         "metric": METRIC, "value": value, "unit": "s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": False, "scaling": "weak",
@@ -330,6 +341,11 @@ def run_gb300(args):
                               "peak_source": "measured (te_probe_fp64_tflops)",
                               "frac": f_apply / avg_apply_s / 1e12 / peaks["fp64_tflops"],
                               "flops_per_launch": f_apply}},
+        "whole_solve": {"algorithmic_bytes": b_whole, "achieved_gbs": b_whole / value / 1e9,
+                        "frac": b_whole / value / 1e9 / peaks["hbm_gbs"], "lanczos_iterations": int(iters),
+                        "v_w_products": vw,
+                        "accounting": "per Lanczos iteration 20 nnz + 4 (n + 1) + 32 n + 64 n; "
+                                      "per V.w product 16 n m + 16 n"},
         "kernel_ms_per_solve": {k: round(v_[0], 3) for k, v_ in kernel_ms.items()},
         "clocks": clk.summary(),
     }

@@ -484,8 +484,7 @@ extern "C" int te_batch_create(int n_instances, const te_matrix* H, const double
       return fail(TE_ERR_UNSUPPORTED);
     }
     const int64_t n = H[i]->n_rows;
-    double nrm = 0.0;
-    for (int64_t k = 0; k < 2 * n; ++k) nrm += v_host[i][k] * v_host[i][k];
+    const double nrm = te_host_sumsq(v_host[i], 2 * n);
     if (!(std::fabs(std::sqrt(nrm) - 1.0) <= p.tol)) {
       te_set_error("te_batch_create: instance %d: Initial vector is not normalized", i);
       return fail(TE_ERR_NOT_NORMALIZED);

@@ -577,8 +577,7 @@ extern "C" int te_evolver_create(te_matrix H, const double* v_host, const te_par
     return TE_ERR_UNSUPPORTED;
   }
   // normalisation check (:45-48), host-side on the caller's vector
-  double nrm = 0.0;
-  for (int64_t i = 0; i < 2 * n; ++i) nrm += v_host[i] * v_host[i];
+  const double nrm = te_host_sumsq(v_host, 2 * n);
   if (!(std::fabs(std::sqrt(nrm) - 1.0) <= p.tol)) {  // a NaN entry fails too
     te_set_error("Initial vector is not normalized");
     return TE_ERR_NOT_NORMALIZED;
@@ -849,8 +848,7 @@ extern "C" int te_evolver_reset(te_evolver ev, const double* v, int v_is_device)
   }
   const int64_t n = ev->n;
   if (!v_is_device) {
-    double nrm = 0.0;
-    for (int64_t i = 0; i < 2 * n; ++i) nrm += v[i] * v[i];
+    const double nrm = te_host_sumsq(v, 2 * n);
     if (!(std::fabs(std::sqrt(nrm) - 1.0) <= ev->p.tol)) {
       te_set_error("Initial vector is not normalized");
       return TE_ERR_NOT_NORMALIZED;

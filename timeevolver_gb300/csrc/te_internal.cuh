@@ -305,6 +305,7 @@ int te_cuda_check(cudaError_t e, const char* what);
 
 // launch shapes
 int te_num_sms();
+double te_host_sumsq(const double* x, int64_t len);
 int te_grid_for(int64_t n_items, int threads, int blocks_per_sm);
 // Resident blocks per SM of a kernel at this block size (occupancy query, cached).
 int te_kernel_blocks_per_sm(const void* kernel, int threads, size_t dyn_smem);

@@ -4,6 +4,7 @@
  */
 #ifndef TE_DIAG_H
 #define TE_DIAG_H
+#include "tegpu.h"
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -20,6 +21,22 @@ int te_probe_fp64_tflops(double* tflops);
  * is the device's nominal clock (cudaDevAttrClockRate).  Returns 0 or a
  * negative TE_ERR_* code. */
 int te_probe_fp64_issue(int warps, int blocks, double* cycles_indep, double* cycles_chain);
+
+/* Gather throughput: 16-byte rows of a table fetched by index, the access
+ * pattern of the SpMV passes' gathers of the fixed-point vector.  With a
+ * matrix M the indices are its SELL slot columns in chunk order (what one
+ * SpMV pass gathers, padding included) and the table has its dimension;
+ * with M = NULL, n_gathers uniform random indices into n_rows rows.  Every
+ * warp walks its own run of 32-index rows.  mode 0: ordinary loads with depth
+ * (1, 2 or 4) rows in flight per lane; mode 1: TMA tile::gather4 copies into
+ * shared memory with depth (4, 8 or 16) stages per warp, completion on
+ * mbarriers with bounded waits (TE_ERR_DEVICE_TIMEOUT if one gives up).
+ * blocks_per_sm 1..8 blocks of 256 threads per SM (TE_ERR_UNSUPPORTED when
+ * they do not fit).  Returns the best of 4 timed launches in *rows_per_s and
+ * a checksum of the gathered rows that is the same for both modes at the same
+ * blocks_per_sm (which fixes the indices every warp walks). */
+int te_probe_gather(te_matrix M, int64_t n_rows, int64_t n_gathers, int mode, int depth, int blocks_per_sm,
+                    double* rows_per_s, unsigned long long* checksum);
 
 #ifdef __cplusplus
 }

@@ -97,6 +97,7 @@ SIGNATURES = {
     "te_evolver_kernel_time": (_I, [_P, _I, _P, _P]),
     "te_probe_fp64_tflops": (_I, [_P]),
     "te_probe_fp64_issue": (_I, [_I, _I, _P, _P]),
+    "te_probe_gather": (_I, [_P, _I64, _I64, _I, _I, _I, _P, _P]),
     "te_batch_create": (_I, [_I, _P, _P, _P, _P]),
     "te_batch_destroy": (_I, [_P]),
     "te_batch_add_observable": (_I, [_P, _I, _P]),
@@ -172,6 +173,18 @@ def probe_fp64_issue(warps, blocks=1):
     _check(lib().te_probe_fp64_issue(int(warps), int(blocks), ctypes.byref(a), ctypes.byref(b)),
            "te_probe_fp64_issue")
     return a.value, b.value
+
+
+def probe_gather(mode, depth, blocks_per_sm=6, matrix=None, n_rows=1352078, n_gathers=16871581):
+    """Gathers of 16-byte rows per second (include/te_diag.h): mode 0 ordinary
+    loads (depth rows in flight per lane), mode 1 TMA tile::gather4 (depth
+    stages per warp); the indices are the SELL slot columns of ``matrix`` or
+    uniform random.  Returns (rows_per_s, checksum)."""
+    rate, csum = ctypes.c_double(), ctypes.c_ulonglong()
+    _check(lib().te_probe_gather(matrix.handle if matrix is not None else None, int(n_rows), int(n_gathers),
+                                 int(mode), int(depth), int(blocks_per_sm), ctypes.byref(rate), ctypes.byref(csum)),
+           "te_probe_gather")
+    return rate.value, csum.value
 
 
 def _check(rc, where):

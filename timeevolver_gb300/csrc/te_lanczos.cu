@@ -311,12 +311,15 @@ __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_f
     }
   }
   // the warp's chunk offsets in one coalesced load (lane k holds the offset
-  // of chunk c_begin + k) when its range has at most 31 chunks
-  const int64_t c_begin = warp_chunk[wid], c_end = warp_chunk[wid + 1];
+  // of chunk c_begin + k) when its range has at most 31 chunks.  Chunk and
+  // row counters are 32-bit (rows < 2^31), and a row is live when r - L.n is
+  // below n - L.n as unsigned: fewer registers across the slot loop
+  const int c_begin = warp_chunk[wid], c_end = warp_chunk[wid + 1];
   const bool offs_in_regs = c_end - c_begin <= 31;
   const int64_t my_off = (offs_in_regs && c_begin + lane <= c_end) ? __ldg(chunk_off + c_begin + lane) : 0;
-  for (int64_t c = c_begin; c < c_end; ++c) {
-    const int k = (int)(c - c_begin);
+  const uint32_t live_lo = (uint32_t)L.n, live_cnt = (uint32_t)(n - L.n);
+  for (int c = c_begin; c < c_end; ++c) {
+    const int k = c - c_begin;
     int64_t s0, s1;
     if (offs_in_regs) {
       s0 = __shfl_sync(0xffffffffu, my_off, k);
@@ -325,8 +328,8 @@ __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_f
       s0 = __ldg(chunk_off + c);
       s1 = __ldg(chunk_off + c + 1);
     }
-    const int64_t r = c * 32 + lane;
-    const bool live = r < n && r >= L.n;
+    const int64_t r = (int64_t)c * 32 + lane;
+    const bool live = (uint32_t)r - live_lo < live_cnt;
     const double2 y = FMT == 1   ? te_sell_row_fix_packed(s0 + lane, s1, M.pk, tab, M.cbits, X, shift)
                       : FMT == 2 ? te_sell_row_fix_c(s0 + lane, s1, M.col, M.hv4, X, shift)
                                  : te_sell_row_fix(s0 + lane, s1, M.col, M.hv, X, shift);
@@ -335,7 +338,7 @@ __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_f
       wmax = max(wmax, max(te_fix_hiword(wr.x), te_fix_hiword(wr.y)));
     }
   }
-  fix_apply_publish(acc, wmax, ds, j, ak, wide, wmax_w);
+  fix_apply_publish(acc, wmax, ds, j, (int)scratch[2], wide, wmax_w);  // k from the prologue's broadcast
 }
 
 // One column block of the fixed-point SpMV: for block row i (main row

@@ -71,6 +71,19 @@ int te_abi_version(void);
 /* Select the CUDA device used by subsequently created objects. */
 int te_set_device(int device);
 
+/* Buffer cache.  Device buffers of at least 1 MiB (and small pinned host
+ * buffers) that the library releases are kept and reused by a later request
+ * of exactly the same size on the same device, so that repeated evolutions
+ * of one dimension skip the driver's allocation and release.  A block is
+ * cached only once the device is idle.  te_set_buffer_cache_limit caps the
+ * cached device bytes (default 8 GiB; 0 disables the cache and frees what it
+ * holds), te_release_buffers frees every cached block, te_buffer_cache_bytes
+ * reports the cached device bytes.  A failed allocation releases the cache
+ * and tries again. */
+int te_set_buffer_cache_limit(int64_t device_bytes);
+int te_release_buffers(void);
+int64_t te_buffer_cache_bytes(void);
+
 /* --------------------------------------------------------------- matrices */
 
 /* Upload a COO matrix (the storage of TE::smatrix: values, columns and

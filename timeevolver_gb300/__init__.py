@@ -59,6 +59,9 @@ SIGNATURES = {
     "te_last_error": (ctypes.c_char_p, []),
     "te_abi_version": (_I, []),
     "te_set_device": (_I, [_I]),
+    "te_set_buffer_cache_limit": (_I, [_I64]),
+    "te_release_buffers": (_I, []),
+    "te_buffer_cache_bytes": (_I64, []),
     "te_matrix_create_coo": (_I, [_I64, _I64, _I64, _P, _P, _P, _P]),
     "te_matrix_create_csr": (_I, [_I64, _I64, _I64, _P, _P, _P, _I, _P]),
     "te_matrix_destroy": (_I, [_P]),
@@ -156,6 +159,22 @@ def state_index_device(n_particles, occupation, quant=1):
     _check(lib().te_model_state_index(int(n_particles), len(occ), int(quant), _ptr(occ), ctypes.byref(r)),
            "te_model_state_index")
     return r.value
+
+
+def set_buffer_cache_limit(device_bytes):
+    """Cap the device bytes the library keeps for reuse after releasing
+    buffers (0 disables the cache and frees what it holds)."""
+    _check(lib().te_set_buffer_cache_limit(int(device_bytes)), "te_set_buffer_cache_limit")
+
+
+def release_buffers():
+    """Free every buffer the library keeps for reuse."""
+    _check(lib().te_release_buffers(), "te_release_buffers")
+
+
+def buffer_cache_bytes():
+    """Device bytes currently kept for reuse."""
+    return int(lib().te_buffer_cache_bytes())
 
 
 def probe_fp64_tflops():

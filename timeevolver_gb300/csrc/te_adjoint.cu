@@ -247,7 +247,7 @@ void free_adjoint(te_adjoint a) {
                     (void*)a->d_term_ptr, (void*)a->d_term_slots, (void*)a->store_psi, (void*)a->store_lam,
                     (void*)a->lam0, (void*)a->contrib, (void*)a->red, (void*)a->counter, (void*)a->d_scalar,
                     (void*)a->d_weights, (void*)a->d_fwd, (void*)a->d_bwd, (void*)a->d_grad})
-    cudaFree(ptr);
+    te_free(ptr);
   delete a;
 }
 
@@ -277,7 +277,7 @@ int download_term(te_matrix H, HostTerm& t) {
 
 template <class T>
 int upload_vec(T** dst, const std::vector<T>& src) {
-  TE_CUDA(cudaMalloc(dst, sizeof(T) * std::max<size_t>(src.size(), 1)));
+  TE_CUDA(te_malloc(dst, sizeof(T) * std::max<size_t>(src.size(), 1)));
   if (!src.empty()) TE_CUDA(cudaMemcpy(*dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice));
   return TE_OK;
 }
@@ -364,9 +364,9 @@ int build_pattern(te_adjoint a, const std::vector<HostTerm>& terms) {
   if ((rc = upload_vec(&a->d_abs, absval)) != TE_OK) return rc;
   if ((rc = upload_vec(&a->d_term_ptr, tptr)) != TE_OK) return rc;
   if ((rc = upload_vec(&a->d_term_slots, tslots)) != TE_OK) return rc;
-  TE_CUDA(cudaMalloc(&a->d_theta, sizeof(double) * a->K));
-  TE_CUDA(cudaMalloc(&a->d_max, sizeof(unsigned long long)));
-  TE_CUDA(cudaMalloc(&a->contrib, sizeof(double) * std::max<int64_t>(S.slots, 1)));
+  TE_CUDA(te_malloc(&a->d_theta, sizeof(double) * a->K));
+  TE_CUDA(te_malloc(&a->d_max, sizeof(unsigned long long)));
+  TE_CUDA(te_malloc(&a->contrib, sizeof(double) * std::max<int64_t>(S.slots, 1)));
   return TE_OK;
 }
 
@@ -517,15 +517,15 @@ extern "C" int te_adjoint_create(int n_terms, const te_matrix* terms, te_matrix 
   a->tau[0] = 0.0;
   for (int64_t i = 1; i < nt; ++i) a->tau[i] = std::min(T, std::max(a->tau[i], a->tau[i - 1]));
   // device buffers
-  if ((rc = te_cuda_check(cudaMalloc(&a->store_psi, sizeof(double2) * n * nt), "psi store")) != TE_OK) return fail(rc);
-  if ((rc = te_cuda_check(cudaMalloc(&a->store_lam, sizeof(double2) * n * nt), "lambda store")) != TE_OK)
+  if ((rc = te_cuda_check(te_malloc(&a->store_psi, sizeof(double2) * n * nt), "psi store")) != TE_OK) return fail(rc);
+  if ((rc = te_cuda_check(te_malloc(&a->store_lam, sizeof(double2) * n * nt), "lambda store")) != TE_OK)
     return fail(rc);
-  if ((rc = te_cuda_check(cudaMalloc(&a->lam0, sizeof(double2) * n * 2), "lambda")) != TE_OK) return fail(rc);
-  if ((rc = te_cuda_check(cudaMalloc(&a->red, sizeof(double) * 4096), "red")) != TE_OK) return fail(rc);
-  if ((rc = te_cuda_check(cudaMalloc(&a->counter, sizeof(unsigned int)), "counter")) != TE_OK) return fail(rc);
+  if ((rc = te_cuda_check(te_malloc(&a->lam0, sizeof(double2) * n * 2), "lambda")) != TE_OK) return fail(rc);
+  if ((rc = te_cuda_check(te_malloc(&a->red, sizeof(double) * 4096), "red")) != TE_OK) return fail(rc);
+  if ((rc = te_cuda_check(te_malloc(&a->counter, sizeof(unsigned int)), "counter")) != TE_OK) return fail(rc);
   if ((rc = te_cuda_check(cudaMemset(a->counter, 0, sizeof(unsigned int)), "counter")) != TE_OK) return fail(rc);
-  if ((rc = te_cuda_check(cudaMalloc(&a->d_scalar, sizeof(double)), "scalar")) != TE_OK) return fail(rc);
-  if ((rc = te_cuda_check(cudaMalloc(&a->d_grad, sizeof(double) * n_terms), "grad")) != TE_OK) return fail(rc);
+  if ((rc = te_cuda_check(te_malloc(&a->d_scalar, sizeof(double)), "scalar")) != TE_OK) return fail(rc);
+  if ((rc = te_cuda_check(te_malloc(&a->d_grad, sizeof(double) * n_terms), "grad")) != TE_OK) return fail(rc);
   std::vector<int> fi(nt), bi(nt);
   for (int64_t i = 0; i < nt; ++i) {
     fi[i] = (int)i;

@@ -219,39 +219,39 @@ void free_batch(te_batch b) {
   if (!b) return;
   if (b->g_step) cudaGraphExecDestroy(b->g_step);
   if (b->g_batch) cudaGraphExecDestroy(b->g_batch);
-  cudaFree(b->d_chunk_inst);
-  cudaFree(b->d_chunk_off);
-  cudaFree(b->d_col);
-  cudaFree(b->d_val);
-  cudaFree(b->d_inst_row);
-  cudaFree(b->d_inst_n);
-  cudaFree(b->d_inst_chunk);
-  cudaFree(b->ds);
-  cudaFree(b->V);
-  cudaFree(b->spare);
-  cudaFree(b->w);
-  cudaFree(b->sampled);
-  cudaFree(b->v0);
-  cudaFree(b->diag);
-  cudaFree(b->d_nobs);
-  cudaFree(b->d_result_off);
-  cudaFree(b->results);
-  cudaFree(b->d_flags);
-  cudaFreeHost(b->h_flags);
-  cudaFree(b->d_active);
-  cudaFree(b->d_active_count);
-  cudaFree(b->d_warp_begin);
-  cudaFree(b->d_inst_w0);
-  cudaFree(b->d_inst_nseg);
-  cudaFree(b->d_seg_base);
-  cudaFree(b->d_bar);
-  cudaFree(b->d_err);
-  cudaFree(b->d_steps);
-  cudaFree(b->d_next_run);
-  cudaFree(b->d_inst_nwrite);
-  cudaFree(b->d_arrivals);
-  cudaFree(b->d_inst_cost);
-  cudaFree(b->seg_partials);
+  te_free(b->d_chunk_inst);
+  te_free(b->d_chunk_off);
+  te_free(b->d_col);
+  te_free(b->d_val);
+  te_free(b->d_inst_row);
+  te_free(b->d_inst_n);
+  te_free(b->d_inst_chunk);
+  te_free(b->ds);
+  te_free(b->V);
+  te_free(b->spare);
+  te_free(b->w);
+  te_free(b->sampled);
+  te_free(b->v0);
+  te_free(b->diag);
+  te_free(b->d_nobs);
+  te_free(b->d_result_off);
+  te_free(b->results);
+  te_free(b->d_flags);
+  te_free_host(b->h_flags);
+  te_free(b->d_active);
+  te_free(b->d_active_count);
+  te_free(b->d_warp_begin);
+  te_free(b->d_inst_w0);
+  te_free(b->d_inst_nseg);
+  te_free(b->d_seg_base);
+  te_free(b->d_bar);
+  te_free(b->d_err);
+  te_free(b->d_steps);
+  te_free(b->d_next_run);
+  te_free(b->d_inst_nwrite);
+  te_free(b->d_arrivals);
+  te_free(b->d_inst_cost);
+  te_free(b->seg_partials);
   if (b->st) cudaStreamDestroy(b->st);
   delete b;
 }
@@ -541,7 +541,7 @@ extern "C" int te_batch_create(int n_instances, const te_matrix* H, const double
     }
   }
   off[chunks] = slots;
-  auto alloc = [&](void** p, size_t bytes) { return te_cuda_check(cudaMalloc(p, std::max<size_t>(bytes, 16)), "alloc"); };
+  auto alloc = [&](void** p, size_t bytes) { return te_cuda_check(te_malloc(p, std::max<size_t>(bytes, 16)), "alloc"); };
   const int vw = b->is_real ? 1 : 2;
   if ((rc = alloc((void**)&b->d_chunk_off, sizeof(int64_t) * (chunks + 1))) != TE_OK) return fail(rc);
   if ((rc = alloc((void**)&b->d_chunk_inst, sizeof(int32_t) * chunks)) != TE_OK) return fail(rc);
@@ -597,7 +597,7 @@ extern "C" int te_batch_create(int n_instances, const te_matrix* H, const double
   // segments: every warp has at most one per instance it touches
   if ((rc = alloc((void**)&b->seg_partials, sizeof(double) * 2 * ((int64_t)b->n_warps + n_instances + 1))) != TE_OK)
     return fail(rc);
-  TE_CUDA(cudaMallocHost(&b->h_flags, sizeof(int) * n_instances));
+  TE_CUDA(te_malloc_host(&b->h_flags, sizeof(int) * n_instances));
   TE_CUDA(cudaMemsetAsync(b->V, 0, sizeof(double2) * ld * b->m_max, st));
   TE_CUDA(cudaMemsetAsync(b->spare, 0, sizeof(double2) * ld, st));
   TE_CUDA(cudaMemsetAsync(b->w, 0, sizeof(double2) * ld, st));
@@ -614,7 +614,7 @@ extern "C" int te_batch_create(int n_instances, const te_matrix* H, const double
                                                                               b->v0 + b->inst_row[i]);
     TE_CUDA(cudaStreamSynchronize(st));
   }
-  cudaFree(tmp);
+  te_free(tmp);
   b->nobs.assign(n_instances, 0);
   TE_CUDA(cudaMemcpy(b->d_nobs, b->nobs.data(), sizeof(int) * n_instances, cudaMemcpyHostToDevice));
   *out = b;
@@ -657,7 +657,7 @@ extern "C" int te_batch_run(te_batch b, te_result* results) {
       b->result_off[i] = tot;
       tot += (int64_t)std::max(1, b->nobs[i]) * b->n_samples[i];
     }
-    TE_CUDA(cudaMalloc(&b->results, sizeof(double) * std::max<int64_t>(tot, 1)));
+    TE_CUDA(te_malloc(&b->results, sizeof(double) * std::max<int64_t>(tot, 1)));
     TE_CUDA(cudaMemset(b->results, 0, sizeof(double) * std::max<int64_t>(tot, 1)));
     TE_CUDA(cudaMemcpy(b->d_result_off, b->result_off.data(), sizeof(int64_t) * b->B, cudaMemcpyHostToDevice));
   }
@@ -778,11 +778,11 @@ extern "C" int te_batch_state(te_batch b, int instance, double* out_host) {
   }
   const int64_t n = b->inst_n[instance];
   double2* tmp = nullptr;
-  TE_CUDA(cudaMalloc(&tmp, sizeof(double2) * n));
+  TE_CUDA(te_malloc(&tmp, sizeof(double2) * n));
   te_launch_permute(n, b->H[instance]->sell.iperm, b->sampled + b->inst_row[instance], tmp, b->st);
   int rc = te_cuda_check(cudaMemcpyAsync(out_host, tmp, sizeof(double2) * n, cudaMemcpyDeviceToHost, b->st), "D2H");
   if (rc == TE_OK) rc = te_cuda_check(cudaStreamSynchronize(b->st), "sync");
-  cudaFree(tmp);
+  te_free(tmp);
   return rc;
 }
 

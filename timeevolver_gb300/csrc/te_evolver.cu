@@ -229,22 +229,22 @@ int process_batch(te_evolver ev, int* stop_at, bool synced) {
 
 void free_evolver(te_evolver ev) {
   if (!ev) return;
-  cudaFree(ev->ds);
-  cudaFreeHost(ev->sum);
-  cudaFreeHost(ev->host_state);
-  cudaFree(ev->slab);
-  cudaFree(ev->X);
+  te_free(ev->ds);
+  te_free_host(ev->sum);
+  te_free_host(ev->host_state);
+  te_free(ev->slab);
+  te_free(ev->X);
   te_seg_carry_free(&ev->seg);
-  cudaFree(ev->fx_acc);
-  cudaFree(ev->batch);
-  cudaFree(ev->orig_tmp);
-  cudaFree(ev->partials);
-  cudaFree(ev->results);
-  cudaFree(ev->sample_times);
+  te_free(ev->fx_acc);
+  te_free(ev->batch);
+  te_free(ev->orig_tmp);
+  te_free(ev->partials);
+  te_free(ev->results);
+  te_free(ev->sample_times);
   for (auto& o : ev->obs) {
-    cudaFree(o.diag_perm);
-    cudaFree(o.vec_perm);
-    cudaFree(o.dense);
+    te_free(o.diag_perm);
+    te_free(o.vec_perm);
+    te_free(o.dense);
   }
   for (auto e : ev->ev_pool) cudaEventDestroy(e);
   if (ev->st) cudaStreamDestroy(ev->st);
@@ -255,10 +255,10 @@ void free_evolver(te_evolver ev) {
 int alloc_results(te_evolver ev) {
   size_t count = std::max<size_t>(1, ev->obs.size()) * (size_t)ev->n_samples;
   if (count > ev->results_cap) {
-    cudaFree(ev->results);
+    te_free(ev->results);
     ev->results = nullptr;
     ev->results_cap = 0;
-    TE_CUDA(cudaMalloc(&ev->results, sizeof(double) * count));
+    TE_CUDA(te_malloc(&ev->results, sizeof(double) * count));
     ev->results_cap = count;
   }
   TE_CUDA(cudaMemsetAsync(ev->results, 0, sizeof(double) * count, ev->st));
@@ -274,10 +274,10 @@ int run(te_evolver ev, te_result* out) {
   for (auto& o : ev->obs) need_host |= (o.kind == 2 || o.kind == 3 || o.kind == 4);
   ev->max_batch = need_host ? 1 : (int)std::max<int64_t>(1, std::min<int64_t>(TE_SCAP, ((int64_t)256 << 20) / (16 * n)));
   if (ev->max_batch > ev->batch_cap) {  // kept across runs while large enough
-    cudaFree(ev->batch);
+    te_free(ev->batch);
     ev->batch = nullptr;
     ev->batch_cap = 0;
-    TE_CUDA(cudaMalloc(&ev->batch, sizeof(double2) * n * ev->max_batch));
+    TE_CUDA(te_malloc(&ev->batch, sizeof(double2) * n * ev->max_batch));
     ev->batch_cap = ev->max_batch;
   }
   int rc = alloc_results(ev);
@@ -358,9 +358,9 @@ int run(te_evolver ev, te_result* out) {
     // the fixed-point form and its vectors; without memory for them the
     // evolution runs the FP64 passes instead
     rc = te_sell_build_fixed(ev->H);
-    if (rc == TE_OK && !ev->X) rc = te_cuda_check(cudaMalloc(&ev->X, sizeof(int4) * n * ev->m), "fixed-point basis");
+    if (rc == TE_OK && !ev->X) rc = te_cuda_check(te_malloc(&ev->X, sizeof(int4) * n * ev->m), "fixed-point basis");
     if (rc == TE_OK && ev->H->sell.fix_nblk > 0 && !ev->fx_acc)
-      rc = te_cuda_check(cudaMalloc(&ev->fx_acc, sizeof(longlong2) * n), "fixed-point sums");
+      rc = te_cuda_check(te_malloc(&ev->fx_acc, sizeof(longlong2) * n), "fixed-point sums");
     if (rc == TE_ERR_OUT_OF_MEMORY) {
       cudaGetLastError();
       fix = false;
@@ -602,20 +602,20 @@ extern "C" int te_evolver_create(te_matrix H, const double* v_host, const te_par
   };
   if ((rc = te_cuda_check(cudaStreamCreateWithFlags(&ev->st, cudaStreamNonBlocking), "stream")) != TE_OK)
     return fail(rc);
-  if ((rc = te_cuda_check(cudaMalloc(&ev->ds, sizeof(TeDevState)), "state")) != TE_OK) return fail(rc);
+  if ((rc = te_cuda_check(te_malloc(&ev->ds, sizeof(TeDevState)), "state")) != TE_OK) return fail(rc);
   if ((rc = te_cuda_check(cudaMemset(ev->ds, 0, sizeof(TeDevState)), "state")) != TE_OK) return fail(rc);
-  if ((rc = te_cuda_check(cudaMallocHost(&ev->sum, sizeof(Summary)), "pinned")) != TE_OK) return fail(rc);
+  if ((rc = te_cuda_check(te_malloc_host(&ev->sum, sizeof(Summary)), "pinned")) != TE_OK) return fail(rc);
   if ((rc = te_seg_carry_alloc(H->sell, &ev->seg)) != TE_OK) return fail(rc);
   // basis columns, spare start vector, w, sampled state
-  if ((rc = te_cuda_check(cudaMalloc(&ev->slab, sizeof(double2) * n * (m + 3)), "Krylov basis")) != TE_OK)
+  if ((rc = te_cuda_check(te_malloc(&ev->slab, sizeof(double2) * n * (m + 3)), "Krylov basis")) != TE_OK)
     return fail(rc);
   for (int j = 0; j < m; ++j) ev->cols[j] = ev->slab + (int64_t)j * n;
   ev->spare = ev->slab + (int64_t)m * n;
   ev->w = ev->slab + (int64_t)(m + 1) * n;
   ev->sampled = ev->slab + (int64_t)(m + 2) * n;
-  if ((rc = te_cuda_check(cudaMalloc(&ev->partials, sizeof(double) * kPartials), "partials")) != TE_OK)
+  if ((rc = te_cuda_check(te_malloc(&ev->partials, sizeof(double) * kPartials), "partials")) != TE_OK)
     return fail(rc);
-  if ((rc = te_cuda_check(cudaMalloc(&ev->orig_tmp, sizeof(double2) * n), "tmp")) != TE_OK) return fail(rc);
+  if ((rc = te_cuda_check(te_malloc(&ev->orig_tmp, sizeof(double2) * n), "tmp")) != TE_OK) return fail(rc);
   // v (original order) -> permuted start vector
   if ((rc = te_cuda_check(cudaMemcpy(ev->orig_tmp, v_host, sizeof(double2) * n, cudaMemcpyHostToDevice), "H2D")) !=
       TE_OK)
@@ -643,11 +643,11 @@ extern "C" int te_evolver_add_sparse_observable(te_evolver ev, te_matrix O) {
   HostObs o;
   if (O->is_diag) {
     o.kind = 0;
-    TE_CUDA(cudaMalloc(&o.diag_perm, sizeof(double) * ev->n));
+    TE_CUDA(te_malloc(&o.diag_perm, sizeof(double) * ev->n));
     // permuted Re(diagonal): gather through the permutation of H
     te_launch_permute_real(ev->n, ev->H->sell.perm, O->diag_re, o.diag_perm, ev->st);
     if (int rc = te_cuda_check(cudaStreamSynchronize(ev->st), "diagonal observable")) {
-      cudaFree(o.diag_perm);
+      te_free(o.diag_perm);
       return rc;
     }
   } else {
@@ -669,10 +669,10 @@ extern "C" int te_evolver_add_dense_observable(te_evolver ev, const double* valu
   }
   HostObs o;
   o.kind = 4;
-  TE_CUDA(cudaMalloc(&o.dense, sizeof(double2) * n * n));
+  TE_CUDA(te_malloc(&o.dense, sizeof(double2) * n * n));
   const cudaError_t e = cudaMemcpy(o.dense, values_host, sizeof(double2) * n * n, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
-    cudaFree(o.dense);
+    te_free(o.dense);
     return te_cuda_check(e, "dense observable upload");
   }
   ev->obs.push_back(o);
@@ -703,7 +703,7 @@ extern "C" int te_evolver_add_vector_observable(te_evolver ev, const double* o_h
   }
   HostObs o;
   o.kind = 1;
-  TE_CUDA(cudaMalloc(&o.vec_perm, sizeof(double2) * ev->n));
+  TE_CUDA(te_malloc(&o.vec_perm, sizeof(double2) * ev->n));
   TE_CUDA(cudaMemcpy(ev->orig_tmp, o_host, sizeof(double2) * ev->n, cudaMemcpyHostToDevice));
   te_launch_permute(ev->n, ev->H->sell.perm, ev->orig_tmp, o.vec_perm, ev->st);
   TE_CUDA(cudaStreamSynchronize(ev->st));
@@ -716,7 +716,7 @@ extern "C" int te_evolver_add_callback_observable(te_evolver ev, te_observable_f
     te_set_error("te_evolver_add_callback_observable: invalid arguments");
     return TE_ERR_INVALID_ARG;
   }
-  if (!ev->host_state) TE_CUDA(cudaMallocHost(&ev->host_state, sizeof(double2) * ev->n));
+  if (!ev->host_state) TE_CUDA(te_malloc_host(&ev->host_state, sizeof(double2) * ev->n));
   HostObs o;
   o.kind = 3;
   o.fn = fn;
@@ -831,9 +831,9 @@ int te_evolver_set_schedule(te_evolver ev, const double* times_host, int64_t cou
       te_set_error("te_evolver_set_schedule: sample times must ascend within [0, t]");
       return TE_ERR_INVALID_ARG;
     }
-  cudaFree(ev->sample_times);
+  te_free(ev->sample_times);
   ev->sample_times = nullptr;
-  TE_CUDA(cudaMalloc(&ev->sample_times, sizeof(double) * count));
+  TE_CUDA(te_malloc(&ev->sample_times, sizeof(double) * count));
   TE_CUDA(cudaMemcpy(ev->sample_times, times_host, sizeof(double) * count, cudaMemcpyHostToDevice));
   ev->n_samples = count;
   ev->state_store = store_dev;

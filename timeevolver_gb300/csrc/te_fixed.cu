@@ -191,7 +191,7 @@ __global__ void fill_i32_kernel(int64_t count, int32_t* __restrict__ out, int32_
 
 template <typename T>
 void free_ptr(T*& p) {
-  cudaFree(p);
+  te_free(p);
   p = nullptr;
 }
 
@@ -223,7 +223,7 @@ void free_fixed(TeSell& S) {
 // sh: the largest chunk-row 1-norm maps below 2^61.
 int fixed_scale(TeSell& S, bool real) {
   unsigned long long* d_max = nullptr;
-  TE_CUDA(cudaMalloc(&d_max, sizeof(unsigned long long)));
+  TE_CUDA(te_malloc(&d_max, sizeof(unsigned long long)));
   int rc = te_cuda_check(cudaMemset(d_max, 0, sizeof(unsigned long long)), "fixed values");
   const int64_t threads = S.n_chunks * 32;
   const unsigned blocks = (unsigned)((threads + TE_THREADS - 1) / TE_THREADS);
@@ -231,7 +231,7 @@ int fixed_scale(TeSell& S, bool real) {
   if (rc == TE_OK && !real) fix_rownorm_kernel<false><<<blocks, TE_THREADS>>>(S.n_chunks, S.chunk_off, S.val, d_max);
   unsigned long long bits = 0;
   if (rc == TE_OK) rc = te_cuda_check(cudaMemcpy(&bits, d_max, sizeof(bits), cudaMemcpyDeviceToHost), "fixed values");
-  cudaFree(d_max);
+  te_free(d_max);
   if (rc != TE_OK) return rc;
   double rmax;
   std::memcpy(&rmax, &bits, sizeof(rmax));
@@ -259,14 +259,14 @@ int try_dictionary(TeSell& S, bool* packed) {
   int* d_index = nullptr;
   double* d_vals = nullptr;
   auto cleanup = [&]() {
-    cudaFree(d_table);
-    cudaFree(d_flags);
-    cudaFree(d_index);
-    cudaFree(d_vals);
+    te_free(d_table);
+    te_free(d_flags);
+    te_free(d_index);
+    te_free(d_vals);
   };
   int rc;
-  if ((rc = te_cuda_check(cudaMalloc(&d_table, sizeof(unsigned long long) * kDictSlots), "dictionary")) != TE_OK ||
-      (rc = te_cuda_check(cudaMalloc(&d_flags, 2 * sizeof(int)), "dictionary")) != TE_OK ||
+  if ((rc = te_cuda_check(te_malloc(&d_table, sizeof(unsigned long long) * kDictSlots), "dictionary")) != TE_OK ||
+      (rc = te_cuda_check(te_malloc(&d_flags, 2 * sizeof(int)), "dictionary")) != TE_OK ||
       (rc = te_cuda_check(cudaMemset(d_table, 0xff, sizeof(unsigned long long) * kDictSlots), "dictionary")) !=
           TE_OK ||
       (rc = te_cuda_check(cudaMemset(d_flags, 0, 2 * sizeof(int)), "dictionary")) != TE_OK) {
@@ -307,10 +307,10 @@ int try_dictionary(TeSell& S, bool* packed) {
     sorted[i] = vals[i].first;
   }
   const int nv = (int)vals.size();
-  if ((rc = te_cuda_check(cudaMalloc(&d_index, sizeof(int) * kDictSlots), "dictionary")) != TE_OK ||
-      (rc = te_cuda_check(cudaMalloc(&d_vals, sizeof(double) * std::max(nv, 1)), "dictionary")) != TE_OK ||
-      (rc = te_cuda_check(cudaMalloc(&S.fix_table, sizeof(int2) * std::max(nv, 1)), "dictionary")) != TE_OK ||
-      (rc = te_cuda_check(cudaMalloc(&S.fix_pk, sizeof(uint32_t) * std::max<int64_t>(S.slots, 1)), "dictionary")) !=
+  if ((rc = te_cuda_check(te_malloc(&d_index, sizeof(int) * kDictSlots), "dictionary")) != TE_OK ||
+      (rc = te_cuda_check(te_malloc(&d_vals, sizeof(double) * std::max(nv, 1)), "dictionary")) != TE_OK ||
+      (rc = te_cuda_check(te_malloc(&S.fix_table, sizeof(int2) * std::max(nv, 1)), "dictionary")) != TE_OK ||
+      (rc = te_cuda_check(te_malloc(&S.fix_pk, sizeof(uint32_t) * std::max<int64_t>(S.slots, 1)), "dictionary")) !=
           TE_OK ||
       (rc = te_cuda_check(cudaMemcpy(d_index, index.data(), sizeof(int) * kDictSlots, cudaMemcpyHostToDevice),
                           "dictionary")) != TE_OK ||
@@ -340,7 +340,7 @@ int fixed_values(TeSell& S, bool real) {
   S.fix_nvals = 0;
   if (!real) {  // complex: limbs of both parts per slot (no dictionary)
     if (!S.fix_val4 &&
-        (rc = te_cuda_check(cudaMalloc(&S.fix_val4, sizeof(int4) * std::max<int64_t>(S.slots, 1)),
+        (rc = te_cuda_check(te_malloc(&S.fix_val4, sizeof(int4) * std::max<int64_t>(S.slots, 1)),
                             "fixed values")) != TE_OK)
       return rc;
     fix_encode_complex_kernel<<<te_grid_fit((const void*)fix_encode_complex_kernel, S.slots, TE_THREADS),
@@ -354,7 +354,7 @@ int fixed_values(TeSell& S, bool real) {
     return TE_OK;
   }
   if (!S.fix_val &&
-      (rc = te_cuda_check(cudaMalloc(&S.fix_val, sizeof(int2) * std::max<int64_t>(S.slots, 1)), "fixed values")) !=
+      (rc = te_cuda_check(te_malloc(&S.fix_val, sizeof(int2) * std::max<int64_t>(S.slots, 1)), "fixed values")) !=
           TE_OK)
     return rc;
   fix_encode_values_kernel<<<te_grid_fit((const void*)fix_encode_values_kernel, S.slots, TE_THREADS), TE_THREADS>>>(
@@ -372,14 +372,14 @@ int fixed_schedule(TeSell& S, bool real) {
   std::vector<int32_t> wc;
   te_sell_schedule(off, S.n_chunks, bps, real, S.fix_grid, S.fix_saturated, wc);
   int32_t* d_wc = nullptr;
-  if ((rc = te_cuda_check(cudaMalloc(&d_wc, sizeof(int32_t) * wc.size()), "fixed schedule")) != TE_OK) return rc;
+  if ((rc = te_cuda_check(te_malloc(&d_wc, sizeof(int32_t) * wc.size()), "fixed schedule")) != TE_OK) return rc;
   rc = te_cuda_check(cudaMemcpy(d_wc, wc.data(), sizeof(int32_t) * wc.size(), cudaMemcpyHostToDevice),
                      "fixed schedule");
   if (rc != TE_OK) {
-    cudaFree(d_wc);
+    te_free(d_wc);
     return rc;
   }
-  cudaFree(S.fix_warp_chunk);
+  te_free(S.fix_warp_chunk);
   S.fix_warp_chunk = d_wc;  // marks the fixed-point data complete
   return TE_OK;
 }
@@ -402,11 +402,11 @@ int build_blocks(TeSell& S, bool real) {
   for (int b = 0; b <= nb; ++b) d.lo[b] = n * b / nb;
   int32_t *d_cnt = nullptr, *d_pos = nullptr;
   auto cleanup = [&]() {
-    cudaFree(d_cnt);
-    cudaFree(d_pos);
+    te_free(d_cnt);
+    te_free(d_pos);
   };
   int rc;
-  if ((rc = te_cuda_check(cudaMalloc(&d_cnt, sizeof(int32_t) * nb * n), "column blocks")) != TE_OK) return rc;
+  if ((rc = te_cuda_check(te_malloc(&d_cnt, sizeof(int32_t) * nb * n), "column blocks")) != TE_OK) return rc;
   if (real)
     block_count_kernel<true><<<te_grid_fit((const void*)block_count_kernel<true>, n, TE_THREADS), TE_THREADS>>>(
         n, S.chunk_off, S.col, S.fix_val, S.fix_val4, d, d_cnt);
@@ -449,15 +449,15 @@ int build_blocks(TeSell& S, bool real) {
     std::vector<int32_t> wc;
     te_sell_schedule(off, B.n_chunks, bps, real, B.grid, B.saturated, wc);
     const int64_t slots = std::max<int64_t>(B.slots, 1);
-    if ((rc = te_cuda_check(cudaMalloc(&B.chunk_off, sizeof(int64_t) * off.size()), "column blocks")) != TE_OK ||
-        (rc = te_cuda_check(cudaMalloc(&B.row, sizeof(int32_t) * row.size()), "column blocks")) != TE_OK ||
-        (rc = te_cuda_check(cudaMalloc(&B.col, sizeof(int32_t) * slots), "column blocks")) != TE_OK ||
-        (rc = te_cuda_check(cudaMalloc(&B.warp_chunk, sizeof(int32_t) * wc.size()), "column blocks")) != TE_OK)
+    if ((rc = te_cuda_check(te_malloc(&B.chunk_off, sizeof(int64_t) * off.size()), "column blocks")) != TE_OK ||
+        (rc = te_cuda_check(te_malloc(&B.row, sizeof(int32_t) * row.size()), "column blocks")) != TE_OK ||
+        (rc = te_cuda_check(te_malloc(&B.col, sizeof(int32_t) * slots), "column blocks")) != TE_OK ||
+        (rc = te_cuda_check(te_malloc(&B.warp_chunk, sizeof(int32_t) * wc.size()), "column blocks")) != TE_OK)
       break;
     if (real)
-      rc = te_cuda_check(cudaMalloc(&B.hv, sizeof(int2) * slots), "column blocks");
+      rc = te_cuda_check(te_malloc(&B.hv, sizeof(int2) * slots), "column blocks");
     else
-      rc = te_cuda_check(cudaMalloc(&B.hv4, sizeof(int4) * slots), "column blocks");
+      rc = te_cuda_check(te_malloc(&B.hv4, sizeof(int4) * slots), "column blocks");
     if (rc != TE_OK) break;
     cudaMemcpy(B.chunk_off, off.data(), sizeof(int64_t) * off.size(), cudaMemcpyHostToDevice);
     cudaMemcpy(B.row, row.data(), sizeof(int32_t) * row.size(), cudaMemcpyHostToDevice);
@@ -474,7 +474,7 @@ int build_blocks(TeSell& S, bool real) {
     fill.hv[b] = B.hv;
     fill.hv4[b] = B.hv4;
   }
-  if (rc == TE_OK) rc = te_cuda_check(cudaMalloc(&d_pos, sizeof(int32_t) * nb * n), "column blocks");
+  if (rc == TE_OK) rc = te_cuda_check(te_malloc(&d_pos, sizeof(int32_t) * nb * n), "column blocks");
   if (rc == TE_OK)
     rc = te_cuda_check(cudaMemcpy(d_pos, pos.data(), sizeof(int32_t) * nb * n, cudaMemcpyHostToDevice),
                        "column blocks");

@@ -297,6 +297,22 @@ cudaError_t te_launch_pdl(bool enable, void (*kernel)(KArgs...), int grid, int b
 // error reporting
 void te_set_error(const char* fmt, ...);
 int te_cuda_check(cudaError_t e, const char* what);
+
+// Allocation through the buffer cache (te_common.cu): te_malloc / te_free
+// replace cudaMalloc / cudaFree for every device buffer of the library,
+// te_malloc_host / te_free_host cudaMallocHost / cudaFreeHost.
+cudaError_t te_malloc_bytes(void** p, size_t bytes);
+cudaError_t te_free(void* p);
+cudaError_t te_malloc_host_bytes(void** p, size_t bytes);
+cudaError_t te_free_host(void* p);
+template <class T>
+inline cudaError_t te_malloc(T** p, size_t bytes) {
+  return te_malloc_bytes(reinterpret_cast<void**>(p), bytes);
+}
+template <class T>
+inline cudaError_t te_malloc_host(T** p, size_t bytes) {
+  return te_malloc_host_bytes(reinterpret_cast<void**>(p), bytes);
+}
 #define TE_CUDA(call)                                      \
   do {                                                     \
     int _rc = te_cuda_check((call), #call);                \

@@ -1029,20 +1029,20 @@ int te_tune_sell_lanes(te_matrix_s* A) {
   TeDevState* ds = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   auto cleanup = [&]() {
-    cudaFree(x);
-    cudaFree(xp);
-    cudaFree(w);
-    cudaFree(partials);
-    cudaFree(ds);
+    te_free(x);
+    te_free(xp);
+    te_free(w);
+    te_free(partials);
+    te_free(ds);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
   };
   int rc = TE_OK;
-  if ((rc = te_cuda_check(cudaMalloc(&x, sizeof(double2) * n), "tune")) == TE_OK &&
-      (rc = te_cuda_check(cudaMalloc(&xp, sizeof(double2) * n), "tune")) == TE_OK &&
-      (rc = te_cuda_check(cudaMalloc(&w, sizeof(double2) * n), "tune")) == TE_OK &&
-      (rc = te_cuda_check(cudaMalloc(&partials, sizeof(double) * 2 * 8 * 4096), "tune")) == TE_OK &&
-      (rc = te_cuda_check(cudaMalloc(&ds, sizeof(TeDevState)), "tune")) == TE_OK &&
+  if ((rc = te_cuda_check(te_malloc(&x, sizeof(double2) * n), "tune")) == TE_OK &&
+      (rc = te_cuda_check(te_malloc(&xp, sizeof(double2) * n), "tune")) == TE_OK &&
+      (rc = te_cuda_check(te_malloc(&w, sizeof(double2) * n), "tune")) == TE_OK &&
+      (rc = te_cuda_check(te_malloc(&partials, sizeof(double) * 2 * 8 * 4096), "tune")) == TE_OK &&
+      (rc = te_cuda_check(te_malloc(&ds, sizeof(TeDevState)), "tune")) == TE_OK &&
       (rc = te_cuda_check(cudaEventCreate(&e0), "tune")) == TE_OK &&
       (rc = te_cuda_check(cudaEventCreate(&e1), "tune")) == TE_OK) {
     TeDevState* hs = new TeDevState();

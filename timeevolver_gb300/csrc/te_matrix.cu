@@ -318,7 +318,7 @@ int scan_exclusive(const T* in, T* out, int64_t count) {
   if (count <= 0) return TE_OK;
   const int64_t tiles = (count + kScanTile - 1) / kScanTile;
   T* sums = nullptr;
-  int rc = te_cuda_check(cudaMalloc(&sums, sizeof(T) * tiles), "prefix sums");
+  int rc = te_cuda_check(te_malloc(&sums, sizeof(T) * tiles), "prefix sums");
   if (rc != TE_OK) return rc;
   scan_tiles_kernel<T><<<(unsigned)tiles, 256>>>(count, in, out, sums);
   if (tiles > 1) {
@@ -327,7 +327,7 @@ int scan_exclusive(const T* in, T* out, int64_t count) {
                                                                                                        sums);
   }
   rc = te_cuda_check(cudaGetLastError(), "prefix sums");
-  cudaFree(sums);
+  te_free(sums);
   return rc;
 }
 
@@ -559,16 +559,16 @@ __global__ void __launch_bounds__(TE_THREADS) mirror_norm1_kernel(int64_t n, con
 int te_seg_carry_alloc(const TeSell& S, TeSegCarry* c) {
   *c = TeSegCarry{};
   if (S.n_split == 0) return TE_OK;
-  TE_CUDA(cudaMalloc(&c->part, sizeof(double2) * S.n_seg));
-  int rc = te_cuda_check(cudaMalloc(&c->cnt, sizeof(unsigned int) * S.n_long), "segment carries");
+  TE_CUDA(te_malloc(&c->part, sizeof(double2) * S.n_seg));
+  int rc = te_cuda_check(te_malloc(&c->cnt, sizeof(unsigned int) * S.n_long), "segment carries");
   if (rc == TE_OK) rc = te_cuda_check(cudaMemset(c->cnt, 0, sizeof(unsigned int) * S.n_long), "segment carries");
   if (rc != TE_OK) te_seg_carry_free(c);
   return rc;
 }
 
 void te_seg_carry_free(TeSegCarry* c) {
-  cudaFree(c->part);
-  cudaFree(c->cnt);
+  te_free(c->part);
+  te_free(c->cnt);
   *c = TeSegCarry{};
 }
 
@@ -595,32 +595,32 @@ void te_sell_schedule(const std::vector<int64_t>& off, int64_t n_chunks, int blo
 namespace {
 
 void free_matrix(te_matrix_s* M) {
-  cudaFree(M->row_ptr);
-  cudaFree(M->col);
-  cudaFree(M->val);
-  cudaFree(M->diag_re);
-  cudaFree(M->diag_c);
-  cudaFree(M->sell.chunk_off);
-  cudaFree(M->sell.col);
-  cudaFree(M->sell.val);
-  cudaFree(M->sell.perm);
-  cudaFree(M->sell.iperm);
-  cudaFree(M->sell.warp_chunk);
-  cudaFree(M->sell.long_ptr);
-  cudaFree(M->sell.long_col);
-  cudaFree(M->sell.long_val);
-  cudaFree(M->sell.seg_row);
-  cudaFree(M->sell.seg_begin);
-  cudaFree(M->sell.row_seg);
-  cudaFree(M->sell.seg_part);
-  cudaFree(M->sell.seg_cnt);
+  te_free(M->row_ptr);
+  te_free(M->col);
+  te_free(M->val);
+  te_free(M->diag_re);
+  te_free(M->diag_c);
+  te_free(M->sell.chunk_off);
+  te_free(M->sell.col);
+  te_free(M->sell.val);
+  te_free(M->sell.perm);
+  te_free(M->sell.iperm);
+  te_free(M->sell.warp_chunk);
+  te_free(M->sell.long_ptr);
+  te_free(M->sell.long_col);
+  te_free(M->sell.long_val);
+  te_free(M->sell.seg_row);
+  te_free(M->sell.seg_begin);
+  te_free(M->sell.row_seg);
+  te_free(M->sell.seg_part);
+  te_free(M->sell.seg_cnt);
   te_sell_free_fixed(M->sell);
   delete M;
 }
 
 template <class T>
 int upload(T** dst, const T* src, size_t count) {
-  TE_CUDA(cudaMalloc(dst, sizeof(T) * std::max<size_t>(count, 1)));
+  TE_CUDA(te_malloc(dst, sizeof(T) * std::max<size_t>(count, 1)));
   if (count) TE_CUDA(cudaMemcpy(*dst, src, sizeof(T) * count, cudaMemcpyHostToDevice));
   return TE_OK;
 }
@@ -700,14 +700,14 @@ int sell_layout_device(te_matrix_s* M, const int32_t* d_rp, bool real) {
   S.n_chunks = (n + 31) / 32;
   int32_t *cnt = nullptr, *d_len = nullptr;
   auto done = [&](int rc) {
-    cudaFree(cnt);
-    cudaFree(d_len);
+    te_free(cnt);
+    te_free(d_len);
     return rc;
   };
-  int rc = te_cuda_check(cudaMalloc(&cnt, sizeof(int32_t) * n_keys * n_tiles), "layout");
-  if (rc == TE_OK) rc = te_cuda_check(cudaMalloc(&S.perm, sizeof(int32_t) * n), "layout");
-  if (rc == TE_OK) rc = te_cuda_check(cudaMalloc(&S.iperm, sizeof(int32_t) * n), "layout");
-  if (rc == TE_OK) rc = te_cuda_check(cudaMalloc(&S.chunk_off, sizeof(int64_t) * (S.n_chunks + 1)), "layout");
+  int rc = te_cuda_check(te_malloc(&cnt, sizeof(int32_t) * n_keys * n_tiles), "layout");
+  if (rc == TE_OK) rc = te_cuda_check(te_malloc(&S.perm, sizeof(int32_t) * n), "layout");
+  if (rc == TE_OK) rc = te_cuda_check(te_malloc(&S.iperm, sizeof(int32_t) * n), "layout");
+  if (rc == TE_OK) rc = te_cuda_check(te_malloc(&S.chunk_off, sizeof(int64_t) * (S.n_chunks + 1)), "layout");
   if (rc != TE_OK) return done(rc);
   layout_hist_kernel<<<(unsigned)n_tiles, 256, sizeof(int) * n_keys>>>(n, d_rp, (int)long_min, n_keys, n_tiles, cnt);
   if ((rc = scan_exclusive<int32_t>(cnt, cnt, n_keys * n_tiles)) != TE_OK) return done(rc);
@@ -720,7 +720,7 @@ int sell_layout_device(te_matrix_s* M, const int32_t* d_rp, bool real) {
   S.n_long = n_long;
   if (n_long > 0) {  // long rows: by length, longest first, ties in row order
     std::vector<int32_t> rows(n_long), len(n_long), sorted(n_long);
-    if ((rc = te_cuda_check(cudaMalloc(&d_len, sizeof(int32_t) * n_long), "layout")) != TE_OK) return done(rc);
+    if ((rc = te_cuda_check(te_malloc(&d_len, sizeof(int32_t) * n_long), "layout")) != TE_OK) return done(rc);
     long_len_kernel<<<te_grid_fit((const void*)long_len_kernel, n_long, TE_THREADS), TE_THREADS>>>(n_long, S.perm,
                                                                                                    d_rp, d_len);
     if ((rc = te_cuda_check(cudaMemcpy(rows.data(), S.perm, sizeof(int32_t) * n_long, cudaMemcpyDeviceToHost),
@@ -797,19 +797,19 @@ int long_rows_device(te_matrix_s* M, const int32_t* d_rp, const int32_t* d_ci, c
   if (nl == 0) return TE_OK;
   int32_t* d_len = nullptr;
   std::vector<int32_t> len(nl);
-  int rc = te_cuda_check(cudaMalloc(&d_len, sizeof(int32_t) * nl), "long rows");
+  int rc = te_cuda_check(te_malloc(&d_len, sizeof(int32_t) * nl), "long rows");
   if (rc != TE_OK) return rc;
   long_len_kernel<<<te_grid_fit((const void*)long_len_kernel, nl, TE_THREADS), TE_THREADS>>>(nl, S.perm, d_rp, d_len);
   rc = te_cuda_check(cudaMemcpy(len.data(), d_len, sizeof(int32_t) * nl, cudaMemcpyDeviceToHost), "long rows");
-  cudaFree(d_len);
+  te_free(d_len);
   if (rc != TE_OK) return rc;
   std::vector<int64_t> lp(nl + 1, 0);
   for (int64_t i = 0; i < nl; ++i) lp[i + 1] = lp[i] + len[i];
   if ((rc = upload(&S.long_ptr, lp.data(), lp.size())) != TE_OK) return rc;
   if ((rc = long_row_segments(S, lp)) != TE_OK) return rc;
   const int64_t ne = std::max<int64_t>(lp[nl], 1);
-  if ((rc = te_cuda_check(cudaMalloc(&S.long_col, sizeof(int32_t) * ne), "long rows")) != TE_OK ||
-      (rc = te_cuda_check(cudaMalloc(&S.long_val, sizeof(double) * (real ? 1 : 2) * ne), "long rows")) != TE_OK)
+  if ((rc = te_cuda_check(te_malloc(&S.long_col, sizeof(int32_t) * ne), "long rows")) != TE_OK ||
+      (rc = te_cuda_check(te_malloc(&S.long_val, sizeof(double) * (real ? 1 : 2) * ne), "long rows")) != TE_OK)
     return rc;
   const unsigned grid = (unsigned)std::min<int64_t>(nl, 4096);
   if (real)
@@ -965,17 +965,17 @@ int build_matrix_device(te_matrix_s* M, int32_t* d_rp, int32_t* d_ci, double2* d
   unsigned int* d_flags = nullptr;
   unsigned long long *d_u64 = nullptr, *d_colsum = nullptr;
   auto cleanup = [&]() {
-    cudaFree(d_flags);
-    cudaFree(d_u64);
-    cudaFree(d_colsum);
+    te_free(d_flags);
+    te_free(d_u64);
+    te_free(d_colsum);
   };
   auto fail = [&](int rc) {
-    cudaFree(d_v);
+    te_free(d_v);
     cleanup();
     return rc;
   };
-  if (te_cuda_check(cudaMalloc(&d_flags, sizeof(unsigned int)), "flags") != TE_OK) return fail(TE_ERR_CUDA);
-  if (te_cuda_check(cudaMalloc(&d_u64, 2 * sizeof(unsigned long long)), "flags") != TE_OK) return fail(TE_ERR_CUDA);
+  if (te_cuda_check(te_malloc(&d_flags, sizeof(unsigned int)), "flags") != TE_OK) return fail(TE_ERR_CUDA);
+  if (te_cuda_check(te_malloc(&d_u64, 2 * sizeof(unsigned long long)), "flags") != TE_OK) return fail(TE_ERR_CUDA);
   cudaMemset(d_flags, 0, sizeof(unsigned int));
   cudaMemset(d_u64, 0, 2 * sizeof(unsigned long long));
   const int gr = te_grid_fit((const void*)csr_scan_kernel, n, TE_THREADS);
@@ -1004,7 +1004,7 @@ int build_matrix_device(te_matrix_s* M, int32_t* d_rp, int32_t* d_ci, double2* d
   if (std::isnan(norm1_given) && vmax > 0.0 && nnz > 0) {
     const int e = 62 - (int)std::ceil(std::log2(vmax * (double)std::max<int64_t>(n, 1)));
     const double scale = std::ldexp(1.0, e);
-    if (te_cuda_check(cudaMalloc(&d_colsum, sizeof(unsigned long long) * M->n_cols), "colsum") != TE_OK)
+    if (te_cuda_check(te_malloc(&d_colsum, sizeof(unsigned long long) * M->n_cols), "colsum") != TE_OK)
       return fail(TE_ERR_CUDA);
     cudaMemset(d_colsum, 0, sizeof(unsigned long long) * M->n_cols);
     colsum_fixed_kernel<<<gr, TE_THREADS>>>(n, d_rp, d_ci, d_v, scale, d_colsum);
@@ -1018,7 +1018,7 @@ int build_matrix_device(te_matrix_s* M, int32_t* d_rp, int32_t* d_ci, double2* d
   // values: real matrices keep the real parts
   if (real) {
     double* vr = nullptr;
-    if (te_cuda_check(cudaMalloc(&vr, sizeof(double) * std::max<int64_t>(nnz, 1)), "values") != TE_OK)
+    if (te_cuda_check(te_malloc(&vr, sizeof(double) * std::max<int64_t>(nnz, 1)), "values") != TE_OK)
       return fail(TE_ERR_CUDA);
     real_part_kernel<<<te_grid_fit((const void*)real_part_kernel, nnz, TE_THREADS), TE_THREADS>>>(nnz, d_v, vr);
     M->val = vr;
@@ -1026,9 +1026,9 @@ int build_matrix_device(te_matrix_s* M, int32_t* d_rp, int32_t* d_ci, double2* d
     M->val = reinterpret_cast<double*>(d_v);
   }
   if (diag) {
-    if (te_cuda_check(cudaMalloc(&M->diag_re, sizeof(double) * n), "diag") != TE_OK ||
-        te_cuda_check(cudaMalloc(&M->diag_c, sizeof(double2) * n), "diag") != TE_OK) {
-      if (real) cudaFree(d_v);
+    if (te_cuda_check(te_malloc(&M->diag_re, sizeof(double) * n), "diag") != TE_OK ||
+        te_cuda_check(te_malloc(&M->diag_c, sizeof(double2) * n), "diag") != TE_OK) {
+      if (real) te_free(d_v);
       cleanup();
       return TE_ERR_CUDA;
     }
@@ -1047,9 +1047,9 @@ int build_matrix_device(te_matrix_s* M, int32_t* d_rp, int32_t* d_ci, double2* d
       if (rc == TE_OK) rc = sell_layout(M, rp_host, real, perm, iperm, off);
     }
     if (rc == TE_OK) rc = long_rows_device(M, d_rp, d_ci, d_v, real);
-    if (rc == TE_OK) rc = te_cuda_check(cudaMalloc(&S.col, sizeof(int32_t) * std::max<int64_t>(S.slots, 1)), "sell");
+    if (rc == TE_OK) rc = te_cuda_check(te_malloc(&S.col, sizeof(int32_t) * std::max<int64_t>(S.slots, 1)), "sell");
     if (rc == TE_OK)
-      rc = te_cuda_check(cudaMalloc(&S.val, sizeof(double) * (real ? 1 : 2) * std::max<int64_t>(S.slots, 1)), "sell");
+      rc = te_cuda_check(te_malloc(&S.val, sizeof(double) * (real ? 1 : 2) * std::max<int64_t>(S.slots, 1)), "sell");
     if (rc == TE_OK) {
       const int gf = te_grid_fit(real ? (const void*)fill_sell_kernel<true> : (const void*)fill_sell_kernel<false>,
                                  S.n_chunks * 32, TE_THREADS);
@@ -1062,7 +1062,7 @@ int build_matrix_device(te_matrix_s* M, int32_t* d_rp, int32_t* d_ci, double2* d
     }
   }
   if (rc == TE_OK) rc = te_cuda_check(cudaDeviceSynchronize(), "device build");
-  if (real) cudaFree(d_v);
+  if (real) te_free(d_v);
   cleanup();
   return rc;
 }
@@ -1182,17 +1182,17 @@ int create_coo_device(int64_t n_rows, int64_t n_cols, int64_t nnz, const uint64_
   unsigned int* d_flags = nullptr;
   unsigned long long* d_bad = nullptr;
   auto release = [&]() {
-    cudaFree(d_row);
-    cudaFree(d_col);
-    cudaFree(d_cnt);
-    cudaFree(d_flags);
-    cudaFree(d_bad);
+    te_free(d_row);
+    te_free(d_col);
+    te_free(d_cnt);
+    te_free(d_flags);
+    te_free(d_bad);
   };
   auto fail = [&](int rc) {
     release();
-    cudaFree(d_v);
-    cudaFree(d_rp);
-    cudaFree(d_ci);
+    te_free(d_v);
+    te_free(d_rp);
+    te_free(d_ci);
     return rc;
   };
   int dev = 0, pageable = 0;
@@ -1200,11 +1200,11 @@ int create_coo_device(int64_t n_rows, int64_t n_cols, int64_t nnz, const uint64_
   if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) pageable = 0;
   const char* copy_env = std::getenv("TE_COO_COPY");  // 1: the staging-copy path everywhere
   if (copy_env && copy_env[0] == '1') pageable = 0;
-  if (te_cuda_check(cudaMalloc(&d_v, sizeof(double2) * nnz), "coo") != TE_OK ||
-      te_cuda_check(cudaMalloc(&d_rp, sizeof(int32_t) * (n_rows + 1)), "coo") != TE_OK ||
-      te_cuda_check(cudaMalloc(&d_ci, sizeof(int32_t) * nnz), "coo") != TE_OK ||
-      te_cuda_check(cudaMalloc(&d_flags, sizeof(unsigned int)), "coo") != TE_OK ||
-      te_cuda_check(cudaMalloc(&d_bad, sizeof(unsigned long long)), "coo") != TE_OK)
+  if (te_cuda_check(te_malloc(&d_v, sizeof(double2) * nnz), "coo") != TE_OK ||
+      te_cuda_check(te_malloc(&d_rp, sizeof(int32_t) * (n_rows + 1)), "coo") != TE_OK ||
+      te_cuda_check(te_malloc(&d_ci, sizeof(int32_t) * nnz), "coo") != TE_OK ||
+      te_cuda_check(te_malloc(&d_flags, sizeof(unsigned int)), "coo") != TE_OK ||
+      te_cuda_check(te_malloc(&d_bad, sizeof(unsigned long long)), "coo") != TE_OK)
     return fail(TE_ERR_CUDA);
   const unsigned long long none = ~0ull;
   if (te_cuda_check(cudaMemset(d_flags, 0, sizeof(unsigned int)), "coo") != TE_OK ||
@@ -1218,8 +1218,8 @@ int create_coo_device(int64_t n_rows, int64_t n_cols, int64_t nnz, const uint64_
     coo_ingest_kernel<<<te_grid_fit((const void*)coo_ingest_kernel, nnz, TE_THREADS), TE_THREADS>>>(
         nnz, (uint64_t)n_rows, (uint64_t)n_cols, row_index, columns, values, d_rp, d_ci, d_v, d_flags, d_bad);
   } else {
-    if (te_cuda_check(cudaMalloc(&d_row, sizeof(uint64_t) * nnz), "coo") != TE_OK ||
-        te_cuda_check(cudaMalloc(&d_col, sizeof(uint64_t) * nnz), "coo") != TE_OK)
+    if (te_cuda_check(te_malloc(&d_row, sizeof(uint64_t) * nnz), "coo") != TE_OK ||
+        te_cuda_check(te_malloc(&d_col, sizeof(uint64_t) * nnz), "coo") != TE_OK)
       return fail(TE_ERR_CUDA);
     if (te_cuda_check(cudaMemcpy(d_row, row_index, sizeof(uint64_t) * nnz, cudaMemcpyHostToDevice), "coo") != TE_OK ||
         te_cuda_check(cudaMemcpy(d_col, columns, sizeof(uint64_t) * nnz, cudaMemcpyHostToDevice), "coo") != TE_OK ||
@@ -1242,7 +1242,7 @@ int create_coo_device(int64_t n_rows, int64_t n_cols, int64_t nnz, const uint64_
   if (pageable != 1) {
     // row pointers from the per-row counts (rows are sorted, so CSR order = input order)
     const int32_t nnz32 = (int32_t)nnz;
-    if (te_cuda_check(cudaMalloc(&d_cnt, sizeof(int32_t) * n_rows), "coo") != TE_OK ||
+    if (te_cuda_check(te_malloc(&d_cnt, sizeof(int32_t) * n_rows), "coo") != TE_OK ||
         te_cuda_check(cudaMemset(d_cnt, 0, sizeof(int32_t) * n_rows), "coo") != TE_OK)
       return fail(TE_ERR_CUDA);
     row_count_kernel<<<te_grid_fit((const void*)row_count_kernel, nnz, TE_THREADS), TE_THREADS>>>(nnz, d_row, d_cnt);
@@ -1376,14 +1376,14 @@ extern "C" int te_matrix_create_csr_device(int64_t n_rows, int64_t n_cols, int64
   int32_t *d_rp = nullptr, *d_ci = nullptr;
   double2* d_v = nullptr;
   auto fail = [&](int rc) {
-    cudaFree(d_rp);
-    cudaFree(d_ci);
-    cudaFree(d_v);
+    te_free(d_rp);
+    te_free(d_ci);
+    te_free(d_v);
     return rc;
   };
-  if (te_cuda_check(cudaMalloc(&d_rp, sizeof(int32_t) * (n_rows + 1)), "csr") != TE_OK ||
-      te_cuda_check(cudaMalloc(&d_ci, sizeof(int32_t) * std::max<int64_t>(nnz, 1)), "csr") != TE_OK ||
-      te_cuda_check(cudaMalloc(&d_v, sizeof(double2) * std::max<int64_t>(nnz, 1)), "csr") != TE_OK)
+  if (te_cuda_check(te_malloc(&d_rp, sizeof(int32_t) * (n_rows + 1)), "csr") != TE_OK ||
+      te_cuda_check(te_malloc(&d_ci, sizeof(int32_t) * std::max<int64_t>(nnz, 1)), "csr") != TE_OK ||
+      te_cuda_check(te_malloc(&d_v, sizeof(double2) * std::max<int64_t>(nnz, 1)), "csr") != TE_OK)
     return fail(TE_ERR_CUDA);
   if (te_cuda_check(cudaMemcpy(d_rp, row_ptr_dev, sizeof(int32_t) * (n_rows + 1), cudaMemcpyDeviceToDevice), "csr") !=
       TE_OK)
@@ -1547,14 +1547,14 @@ extern "C" int te_matrix_spmv_host(te_matrix A, double alpha_re, double alpha_im
   }
   const int64_t n = A->n_rows;
   double2 *x = nullptr, *y = nullptr;
-  TE_CUDA(cudaMalloc(&x, sizeof(double2) * n));
-  int rc = te_cuda_check(cudaMalloc(&y, sizeof(double2) * n), "cudaMalloc");
+  TE_CUDA(te_malloc(&x, sizeof(double2) * n));
+  int rc = te_cuda_check(te_malloc(&y, sizeof(double2) * n), "cudaMalloc");
   if (rc == TE_OK) rc = te_cuda_check(cudaMemcpy(x, in_host, sizeof(double2) * n, cudaMemcpyHostToDevice), "H2D");
   if (rc == TE_OK) rc = te_matrix_spmv(A, alpha_re, alpha_im, (const double*)x, (double*)y, nullptr);
   if (rc == TE_OK) rc = te_cuda_check(cudaDeviceSynchronize(), "spmv");
   if (rc == TE_OK) rc = te_cuda_check(cudaMemcpy(out_host, y, sizeof(double2) * n, cudaMemcpyDeviceToHost), "D2H");
-  cudaFree(x);
-  cudaFree(y);
+  te_free(x);
+  te_free(y);
   return rc;
 }
 

@@ -293,11 +293,11 @@ struct DeviceBasis {
   int64_t* d_n_s = nullptr;
   int64_t** d_ps = nullptr;
   ~DeviceBasis() {
-    cudaFree(occ);
-    cudaFree(keep);
-    for (int64_t* p : ps) cudaFree(p);
-    cudaFree(d_n_s);
-    cudaFree(d_ps);
+    te_free(occ);
+    te_free(keep);
+    for (int64_t* p : ps) te_free(p);
+    te_free(d_n_s);
+    te_free(d_ps);
   }
   Stages stages() const { return Stages{K, N, quant, nq, cap, d_n_s, d_ps, keep, occ, dim}; }
 };
@@ -335,18 +335,18 @@ int build_basis(int N, int K, int nq, int cap, int quant, DeviceBasis& B) {
   }
   const int64_t n_full = (int64_t)total;
   uint8_t* occ = nullptr;
-  TE_CUDA(cudaMalloc(&occ, (size_t)std::max<int64_t>(n_full, 1) * K));
+  TE_CUDA(te_malloc(&occ, (size_t)std::max<int64_t>(n_full, 1) * K));
   TE_CUDA(cudaMemset(occ, 0, (size_t)std::max<int64_t>(n_full, 1) * K));
   B.occ = occ;
   int64_t n = 1;
   int64_t* cnt = nullptr;
-  TE_CUDA(cudaMalloc(&cnt, sizeof(int64_t) * std::max<int64_t>(n_full, 1)));
+  TE_CUDA(te_malloc(&cnt, sizeof(int64_t) * std::max<int64_t>(n_full, 1)));
   int rc = TE_OK;
   for (int s = 0; s < K - 1 && rc == TE_OK; ++s) {
     const int m = K - 1 - s;
     B.n_s.push_back(n);
     int64_t* ps = nullptr;
-    if ((rc = te_cuda_check(cudaMalloc(&ps, sizeof(int64_t) * (n + 1)), "basis")) != TE_OK) break;
+    if ((rc = te_cuda_check(te_malloc(&ps, sizeof(int64_t) * (n + 1)), "basis")) != TE_OK) break;
     B.ps.push_back(ps);
     const int g = te_grid_for(n, 256, 4);
     stage_count_kernel<<<g, 256>>>(n, occ, K, N, quant, m >= K - nq ? cap : -1, cnt);
@@ -360,7 +360,7 @@ int build_basis(int N, int K, int nq, int cap, int quant, DeviceBasis& B) {
     stage_expand_kernel<<<g, 256>>>(n, occ, K, m, quant, ps);
     n += added;
   }
-  cudaFree(cnt);
+  te_free(cnt);
   if (rc != TE_OK) return rc;
   if (n != n_full) {
     te_set_error("te_model: basis enumeration inconsistent");
@@ -368,35 +368,35 @@ int build_basis(int N, int K, int nq, int cap, int quant, DeviceBasis& B) {
   }
   B.n_s.push_back(n);
   const bool filter = K == nq;
-  if (filter) TE_CUDA(cudaMalloc(&B.keep, sizeof(int64_t) * (n + 1)));
+  if (filter) TE_CUDA(te_malloc(&B.keep, sizeof(int64_t) * (n + 1)));
   finish_basis_kernel<<<te_grid_for(n, 256, 4), 256>>>(n, occ, K, N, cap, B.keep);
   B.dim = n;
   if (filter) {
     uint8_t* flags = nullptr;
     uint8_t* out = nullptr;
     int64_t count = 0;
-    TE_CUDA(cudaMalloc(&flags, n));
+    TE_CUDA(te_malloc(&flags, n));
     keep_flags_kernel<<<te_grid_for(n, 256, 4), 256>>>(n, B.keep, flags);
     rc = exclusive_scan(B.keep, n, B.keep, &count);
     if (rc == TE_OK && count != (int64_t)kept) {
       te_set_error("te_model: basis filter inconsistent");
       rc = TE_ERR_INVALID_ARG;
     }
-    if (rc == TE_OK) rc = te_cuda_check(cudaMalloc(&out, (size_t)std::max<int64_t>(count, 1) * K), "basis");
+    if (rc == TE_OK) rc = te_cuda_check(te_malloc(&out, (size_t)std::max<int64_t>(count, 1) * K), "basis");
     if (rc == TE_OK) compact_basis_kernel<<<te_grid_for(n, 256, 4), 256>>>(n, occ, K, flags, B.keep, out);
-    cudaFree(flags);
+    te_free(flags);
     if (rc != TE_OK) {
-      cudaFree(out);
+      te_free(out);
       return rc;
     }
     TE_CUDA(cudaDeviceSynchronize());
-    cudaFree(occ);
+    te_free(occ);
     B.occ = out;
     B.dim = count;
   }
-  TE_CUDA(cudaMalloc(&B.d_n_s, sizeof(int64_t) * B.n_s.size()));
+  TE_CUDA(te_malloc(&B.d_n_s, sizeof(int64_t) * B.n_s.size()));
   TE_CUDA(cudaMemcpy(B.d_n_s, B.n_s.data(), sizeof(int64_t) * B.n_s.size(), cudaMemcpyHostToDevice));
-  TE_CUDA(cudaMalloc(&B.d_ps, sizeof(int64_t*) * std::max<size_t>(B.ps.size(), 1)));
+  TE_CUDA(te_malloc(&B.d_ps, sizeof(int64_t*) * std::max<size_t>(B.ps.size(), 1)));
   if (!B.ps.empty())
     TE_CUDA(cudaMemcpy(B.d_ps, B.ps.data(), sizeof(int64_t*) * B.ps.size(), cudaMemcpyHostToDevice));
   return te_cuda_check(cudaDeviceSynchronize(), "basis");
@@ -496,17 +496,17 @@ extern "C" int te_model_create_device_basis(const te_basis_desc* basis, const te
   double2* d_val = nullptr;
   unsigned long long* d_norm = nullptr;
   auto fail = [&](int code) {
-    cudaFree(d_terms);
-    cudaFree(d_cnt);
-    cudaFree(d_rp);
-    cudaFree(d_col);
-    cudaFree(d_val);
-    cudaFree(d_norm);
+    te_free(d_terms);
+    te_free(d_cnt);
+    te_free(d_rp);
+    te_free(d_col);
+    te_free(d_val);
+    te_free(d_norm);
     return code;
   };
-  if (te_cuda_check(cudaMalloc(&d_terms, sizeof(DevTerm) * n_terms), "model") != TE_OK ||
-      te_cuda_check(cudaMalloc(&d_cnt, sizeof(int32_t) * n), "model") != TE_OK ||
-      te_cuda_check(cudaMalloc(&d_norm, sizeof(unsigned long long)), "model") != TE_OK)
+  if (te_cuda_check(te_malloc(&d_terms, sizeof(DevTerm) * n_terms), "model") != TE_OK ||
+      te_cuda_check(te_malloc(&d_cnt, sizeof(int32_t) * n), "model") != TE_OK ||
+      te_cuda_check(te_malloc(&d_norm, sizeof(unsigned long long)), "model") != TE_OK)
     return fail(TE_ERR_CUDA);
   cudaMemcpy(d_terms, dt.data(), sizeof(DevTerm) * n_terms, cudaMemcpyHostToDevice);
   cudaMemset(d_norm, 0, sizeof(unsigned long long));
@@ -517,7 +517,7 @@ extern "C" int te_model_create_device_basis(const te_basis_desc* basis, const te
   // stay below 2^31), narrowed to int32
   int64_t* d_rp64 = nullptr;
   int64_t nnz = 0;
-  if (te_cuda_check(cudaMalloc(&d_rp64, sizeof(int64_t) * (n + 1)), "model") != TE_OK) return fail(TE_ERR_CUDA);
+  if (te_cuda_check(te_malloc(&d_rp64, sizeof(int64_t) * (n + 1)), "model") != TE_OK) return fail(TE_ERR_CUDA);
   widen_counts_kernel<<<te_grid_fit((const void*)widen_counts_kernel, n + 1, TE_THREADS), TE_THREADS>>>(n, d_cnt,
                                                                                                       d_rp64);
   rc = te_scan_exclusive_i64(d_rp64, d_rp64, n + 1);
@@ -528,14 +528,14 @@ extern "C" int te_model_create_device_basis(const te_basis_desc* basis, const te
     rc = TE_ERR_UNSUPPORTED;
   }
   if (rc == TE_OK)
-    rc = te_cuda_check(cudaMalloc(&d_rp, sizeof(int32_t) * (n + 1)), "model");
+    rc = te_cuda_check(te_malloc(&d_rp, sizeof(int32_t) * (n + 1)), "model");
   if (rc == TE_OK)
     narrow_rp_kernel<<<te_grid_fit((const void*)narrow_rp_kernel, n + 1, TE_THREADS), TE_THREADS>>>(n + 1, d_rp64,
                                                                                                    d_rp);
-  cudaFree(d_rp64);
+  te_free(d_rp64);
   if (rc != TE_OK) return fail(rc);
-  if (te_cuda_check(cudaMalloc(&d_col, sizeof(int32_t) * std::max<int64_t>(nnz, 1)), "model") != TE_OK ||
-      te_cuda_check(cudaMalloc(&d_val, sizeof(double2) * std::max<int64_t>(nnz, 1)), "model") != TE_OK)
+  if (te_cuda_check(te_malloc(&d_col, sizeof(int32_t) * std::max<int64_t>(nnz, 1)), "model") != TE_OK ||
+      te_cuda_check(te_malloc(&d_val, sizeof(double2) * std::max<int64_t>(nnz, 1)), "model") != TE_OK)
     return fail(TE_ERR_CUDA);
   row_write_model_kernel<<<te_grid_fit((const void*)row_write_model_kernel, n, 128), 128>>>(
       st, n, d_terms, n_terms, d_rp, d_col, d_val, d_norm);
@@ -544,9 +544,9 @@ extern "C" int te_model_create_device_basis(const te_basis_desc* basis, const te
     return fail(TE_ERR_CUDA);
   double norm1;
   std::memcpy(&norm1, &bits, sizeof(norm1));
-  cudaFree(d_terms);
-  cudaFree(d_cnt);
-  cudaFree(d_norm);
+  te_free(d_terms);
+  te_free(d_cnt);
+  te_free(d_norm);
   d_terms = nullptr;
   d_cnt = nullptr;
   d_norm = nullptr;
@@ -586,17 +586,17 @@ extern "C" int te_model_basis_index(const te_basis_desc* basis, const int32_t* o
   if ((rc = build_model_basis(basis, MB)) != TE_OK) return rc;
   int* d_e = nullptr;
   int64_t* d_r = nullptr;
-  if (te_cuda_check(cudaMalloc(&d_e, sizeof(int) * n_modes), "index") != TE_OK ||
-      te_cuda_check(cudaMalloc(&d_r, sizeof(int64_t)), "index") != TE_OK) {
-    cudaFree(d_e);
-    cudaFree(d_r);
+  if (te_cuda_check(te_malloc(&d_e, sizeof(int) * n_modes), "index") != TE_OK ||
+      te_cuda_check(te_malloc(&d_r, sizeof(int64_t)), "index") != TE_OK) {
+    te_free(d_e);
+    te_free(d_r);
     return TE_ERR_CUDA;
   }
   cudaMemcpy(d_e, occupation, sizeof(int) * n_modes, cudaMemcpyHostToDevice);
   state_index_kernel<<<1, 32>>>(MB.view, d_e, d_r);
   rc = te_cuda_check(cudaMemcpy(index, d_r, sizeof(int64_t), cudaMemcpyDeviceToHost), "index");
-  cudaFree(d_e);
-  cudaFree(d_r);
+  te_free(d_e);
+  te_free(d_r);
   return rc;
 }
 

@@ -26,7 +26,7 @@ extern "C" int te_probe_fp64_tflops(double* tflops) {
   if (!tflops) return TE_ERR_INVALID_ARG;
   const int blocks = te_num_sms() * 4, threads = 256, iters = 1024;
   double* out = nullptr;
-  TE_CUDA(cudaMalloc(&out, sizeof(double) * blocks * threads));
+  TE_CUDA(te_malloc(&out, sizeof(double) * blocks * threads));
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -44,7 +44,7 @@ extern "C" int te_probe_fp64_tflops(double* tflops) {
   int rc = te_cuda_check(cudaGetLastError(), "fp64 probe");
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  cudaFree(out);
+  te_free(out);
   if (rc != TE_OK) return rc;
   *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
   return TE_OK;
@@ -65,7 +65,7 @@ extern "C" int te_probe_fp64_issue(int warps, int blocks, double* cycles_indep, 
   cudaGetDevice(&dev);
   TE_CUDA(cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, dev));
   double* out = nullptr;
-  TE_CUDA(cudaMalloc(&out, sizeof(double) * blocks * threads));
+  TE_CUDA(te_malloc(&out, sizeof(double) * blocks * threads));
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -85,7 +85,7 @@ extern "C" int te_probe_fp64_issue(int warps, int blocks, double* cycles_indep, 
   int rc = te_cuda_check(cudaGetLastError(), "fp64 issue probe");
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  cudaFree(out);
+  te_free(out);
   if (rc != TE_OK) return rc;
   const double cycles_per_ms = (double)khz;  // clock rate in kHz = cycles per ms
   *cycles_indep = ms[0] * cycles_per_ms / (8.0 * iters * warps);
@@ -271,26 +271,26 @@ extern "C" int te_probe_gather(te_matrix M, int64_t n_rows, int64_t n_gathers, i
   unsigned long long* sum = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   auto done = [&](int rc) {
-    cudaFree(X);
-    cudaFree(out);
-    cudaFree(own_idx);
-    cudaFree(err);
-    cudaFree(sum);
+    te_free(X);
+    te_free(out);
+    te_free(own_idx);
+    te_free(err);
+    te_free(sum);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     return rc;
   };
-  if (te_cuda_check(cudaMalloc(&X, sizeof(int4) * table), "gather probe") != TE_OK ||
-      te_cuda_check(cudaMalloc(&out, sizeof(int4) * warps * 32), "gather probe") != TE_OK ||
-      te_cuda_check(cudaMalloc(&err, sizeof(unsigned int)), "gather probe") != TE_OK ||
-      te_cuda_check(cudaMalloc(&sum, sizeof(unsigned long long)), "gather probe") != TE_OK ||
+  if (te_cuda_check(te_malloc(&X, sizeof(int4) * table), "gather probe") != TE_OK ||
+      te_cuda_check(te_malloc(&out, sizeof(int4) * warps * 32), "gather probe") != TE_OK ||
+      te_cuda_check(te_malloc(&err, sizeof(unsigned int)), "gather probe") != TE_OK ||
+      te_cuda_check(te_malloc(&sum, sizeof(unsigned long long)), "gather probe") != TE_OK ||
       te_cuda_check(cudaMemset(err, 0, sizeof(unsigned int)), "gather probe") != TE_OK ||
       te_cuda_check(cudaMemset(sum, 0, sizeof(unsigned long long)), "gather probe") != TE_OK)
     return done(TE_ERR_CUDA);
   gather_fill_table<<<te_grid_for(table, 256, 4), 256>>>(X, table);
   const int32_t* idx = M ? M->sell.col : nullptr;
   if (!M) {
-    if (te_cuda_check(cudaMalloc(&own_idx, sizeof(int32_t) * count), "gather probe") != TE_OK) return done(TE_ERR_CUDA);
+    if (te_cuda_check(te_malloc(&own_idx, sizeof(int32_t) * count), "gather probe") != TE_OK) return done(TE_ERR_CUDA);
     gather_random_indices<<<te_grid_for(count, 256, 4), 256>>>(own_idx, count, table, 0x5eedull);
     idx = own_idx;
   }

@@ -208,8 +208,8 @@ __global__ void scale_real_kernel(int64_t n, double* __restrict__ x, double s) {
 template <class T>
 struct DevBuf {
   T* p = nullptr;
-  ~DevBuf() { cudaFree(p); }
-  int alloc(int64_t count) { return te_cuda_check(cudaMalloc(&p, sizeof(T) * std::max<int64_t>(count, 1)), "zipf"); }
+  ~DevBuf() { te_free(p); }
+  int alloc(int64_t count) { return te_cuda_check(te_malloc(&p, sizeof(T) * std::max<int64_t>(count, 1)), "zipf"); }
   T* release() {
     T* q = p;
     p = nullptr;
@@ -310,16 +310,16 @@ extern "C" int te_matrix_create_zipf(int64_t n, double exponent, int32_t min_len
   TE_CUDA(cudaMemset(d_fill.p, 0, sizeof(int32_t) * n));
   scatter_kernel<<<g, TE_THREADS>>>(n, d_rpa.p, d_len.p, d_cola.p, d_vala.p, d_rps.p, d_fill.p, d_tcol.p, d_tval.p,
                                     d_ttag.p);
-  cudaFree(d_cola.release());
-  cudaFree(d_vala.release());
+  te_free(d_cola.release());
+  te_free(d_vala.release());
   // sort each row by (column, tag), then merge the pairs
   if ((rc = d_scol.alloc(nnz_s)) != TE_OK || (rc = d_sval.alloc(nnz_s)) != TE_OK || (rc = d_stag.alloc(nnz_s)) != TE_OK)
     return rc;
   sort_rows_kernel<<<te_grid_fit((const void*)sort_rows_kernel, n * 32, TE_THREADS), TE_THREADS>>>(
       n, d_rps.p, d_tcol.p, d_tval.p, d_ttag.p, d_scol.p, d_sval.p, d_stag.p);
-  cudaFree(d_tcol.release());
-  cudaFree(d_tval.release());
-  cudaFree(d_ttag.release());
+  te_free(d_tcol.release());
+  te_free(d_tval.release());
+  te_free(d_ttag.release());
   if ((rc = d_mlen.alloc(n)) != TE_OK) return rc;
   merged_length_kernel<<<g, TE_THREADS>>>(n, d_rps.p, d_scol.p, d_mlen.p);
   std::vector<int32_t> mlen(n);
@@ -331,26 +331,26 @@ extern "C" int te_matrix_create_zipf(int64_t n, double exponent, int32_t min_len
   const int64_t nnz_h = rph64[n];
   int32_t *d_rph = nullptr, *d_hcol = nullptr;
   double2* d_hval = nullptr;
-  if (te_cuda_check(cudaMalloc(&d_rph, sizeof(int32_t) * (n + 1)), "zipf") != TE_OK ||
-      te_cuda_check(cudaMalloc(&d_hcol, sizeof(int32_t) * std::max<int64_t>(nnz_h, 1)), "zipf") != TE_OK ||
-      te_cuda_check(cudaMalloc(&d_hval, sizeof(double2) * std::max<int64_t>(nnz_h, 1)), "zipf") != TE_OK) {
-    cudaFree(d_rph);
-    cudaFree(d_hcol);
-    cudaFree(d_hval);
+  if (te_cuda_check(te_malloc(&d_rph, sizeof(int32_t) * (n + 1)), "zipf") != TE_OK ||
+      te_cuda_check(te_malloc(&d_hcol, sizeof(int32_t) * std::max<int64_t>(nnz_h, 1)), "zipf") != TE_OK ||
+      te_cuda_check(te_malloc(&d_hval, sizeof(double2) * std::max<int64_t>(nnz_h, 1)), "zipf") != TE_OK) {
+    te_free(d_rph);
+    te_free(d_hcol);
+    te_free(d_hval);
     return TE_ERR_CUDA;
   }
   cudaMemcpy(d_rph, rph.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice);
   merge_rows_kernel<<<g, TE_THREADS>>>(n, d_rps.p, d_scol.p, d_sval.p, d_rph, d_hcol, d_hval);
   rc = te_cuda_check(cudaDeviceSynchronize(), "zipf build");
   if (rc != TE_OK) {
-    cudaFree(d_rph);
-    cudaFree(d_hcol);
-    cudaFree(d_hval);
+    te_free(d_rph);
+    te_free(d_hcol);
+    te_free(d_hval);
     return rc;
   }
-  cudaFree(d_scol.release());
-  cudaFree(d_sval.release());
-  cudaFree(d_stag.release());
+  te_free(d_scol.release());
+  te_free(d_sval.release());
+  te_free(d_stag.release());
   te_matrix H = nullptr;
   if ((rc = te_matrix_adopt_device_csr(n, n, rph[n], d_rph, d_hcol, d_hval, &H, NAN)) != TE_OK) return rc;
 

@@ -152,10 +152,14 @@ int te_matrix_long_segments(te_matrix A, int64_t* segments, int64_t* split_rows,
  * reference).  1: one lane per row (the layout's native form); 2 or 4: each
  * row's entries are split over 2 or 4 lanes of a warp, which multiplies the
  * warps in flight for matrices too small to fill the GPU.  0 (the default):
- * te_evolver_create tunes it by timing the Lanczos pass for 1, 2 and 4 on the
- * matrix and keeps 2 or 4 only when more than 10% faster; the choice changes
- * the summation order of a row (results differ by rounding), so it is made
- * once per matrix.  Setting 1, 2 or 4 pins it. */
+ * chosen from the matrix's shape on first use -- 2 when the matrix has at
+ * least 2048 chunks of 32 rows, fewer chunks than the GPU has resident warps
+ * and no long rows, else 1 -- so that the same matrix always gets the same
+ * choice (it changes the summation order of a row, so results differ by
+ * rounding between choices).  -1: the autotuner -- time the Lanczos pass for
+ * 1, 2 and 4 on the matrix on first use and keep 2 or 4 only when more than
+ * 10% faster (two copies of a matrix near that margin may be tuned
+ * differently).  Setting 1, 2 or 4 pins it. */
 int te_matrix_set_spmv_lanes(te_matrix A, int lanes);
 /* Fixed-point form of a matrix for TE_OPT_FIXED_SPMV (no counterpart in the
  * reference), built by the first evolver that uses it: *state 0 not built,
@@ -174,8 +178,8 @@ int te_matrix_fixed_layout(te_matrix A, int* state, int* n_values, int* scale_sh
  * dictionary or long rows are never blocked).  Drops an existing fixed-point
  * form; the next evolver run that uses it builds it again. */
 int te_matrix_set_fixed_blocks(te_matrix A, int n_blocks);
-/* Current lanes per row (1, 2, 4), tuning first if tune_now != 0 and the
- * choice is still open; a negative value is an error code. */
+/* Current lanes per row (1, 2, 4), making the shape-based choice first if
+ * tune_now != 0 and it is still open; a negative value is an error code. */
 int te_matrix_spmv_lanes(te_matrix A, int tune_now);
 
 /* ------------------------------------------------- models built on the GPU */

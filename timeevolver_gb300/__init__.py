@@ -406,7 +406,8 @@ class Matrix:
         return k
 
     def set_spmv_lanes(self, lanes):
-        """Pin the lanes per row (1, 2, 4) or reopen the choice (0)."""
+        """Pin the lanes per row (1, 2, 4), reopen the choice by shape (0) or
+        let the autotuner time the variants on first use (-1)."""
         _check(lib().te_matrix_set_spmv_lanes(self.handle, int(lanes)), "te_matrix_set_spmv_lanes")
 
     def to_coo(self):

@@ -138,6 +138,7 @@ struct TeSell {
   // or set through te_matrix_set_spmv_lanes; lanes_fixed once chosen
   int lanes = 1;
   bool lanes_fixed = false;
+  bool lanes_timed = false;  // chosen by timing the variants (te_matrix_set_spmv_lanes(A, -1))
   // Long rows: rows longer than max(1024, 32 x mean length) -- the first n_long
   // rows of the sorted order -- have no slots in the chunks (one of them would
   // pad its chunk to 32 x its length); their entries form a CSR in the sorted

@@ -1006,17 +1006,24 @@ void te_launch_lanczos_apply(const TeSell& A, bool is_real, const double2* u_j, 
                 A.col, A.val, te_long_rows(A, carry), u_j, u_jm1, w, ds, partials, j);
 }
 
-// Autotuning of the lanes per row of the FP64 passes (the fixed-point passes
-// always use one lane per row): time the three-term apply pass (the dominant
-// kernel) for K = 1, 2, 4 on the matrix itself, with scratch vectors
-// and a scratch state, and keep K > 1 only when it is clearly (> 10%) faster,
-// so that the choice -- which changes the rounding of the row sums -- is
-// stable from run to run.  Matrices that give every resident warp at least 8
-// chunks keep K = 1 without timing, and so do matrices of fewer than 2048
-// chunks, whose Lanczos iterations run in the persistent kernel (K = 1).
-int te_tune_sell_lanes(te_matrix_s* A) {
+// Lanes per row of the FP64 passes (the fixed-point passes always use one
+// lane per row), chosen from the matrix's shape so that the same matrix always
+// gets the same K -- K changes the rounding of the row sums.  Two lanes per
+// row when the chunks are fewer than the resident warps (with one lane some
+// warps would have no chunk), else one.  Timed on GB300 (apply pass per
+// launch, K = 1 / 2 / 4): L=10 (2 887 chunks, 7 296 resident warps) 24.1 /
+// 22.1 / 26.8 us; L=11 (11 011 chunks) 38 / 41 / 61 us; L=12 97 / 122 / 197
+// us; four lanes never won where this choice applies.  Matrices of fewer than
+// 2048 chunks run their Lanczos iterations in the persistent kernel (K = 1);
+// matrices with long rows keep K = 1.  te_matrix_set_spmv_lanes overrides.
+//
+// The autotuner proper (te_matrix_set_spmv_lanes(A, -1)): time the
+// three-term apply pass (the dominant kernel) for K = 1, 2, 4 on the matrix
+// itself, with scratch vectors and a scratch state, and keep K > 1 only when
+// it is more than 10% faster.  It follows the GPU it runs on, but two copies
+// of one matrix near that margin can be tuned differently.
+static int tune_lanes_timed(te_matrix_s* A) {
   TeSell& S = A->sell;
-  if (S.lanes_fixed) return TE_OK;
   const int64_t resident_warps = (int64_t)te_num_sms() * te_sell_blocks_per_sm(A->is_real) * (TE_THREADS / 32);
   S.lanes = 1;
   if (S.n_chunks >= 8 * resident_warps || S.n_chunks < 2048 || S.n_long > 0) {
@@ -1081,6 +1088,16 @@ int te_tune_sell_lanes(te_matrix_s* A) {
     if (best[v] < best[pick]) pick = v;
   if (pick != 0 && best[pick] > 0.9f * best[0]) pick = 0;
   S.lanes = cand[pick];
+  S.lanes_fixed = true;
+  return TE_OK;
+}
+
+int te_tune_sell_lanes(te_matrix_s* A) {
+  TeSell& S = A->sell;
+  if (S.lanes_fixed) return TE_OK;
+  if (S.lanes_timed) return tune_lanes_timed(A);
+  const int64_t resident_warps = (int64_t)te_num_sms() * te_sell_blocks_per_sm(A->is_real) * (TE_THREADS / 32);
+  S.lanes = (S.n_chunks >= 2048 && S.n_chunks < resident_warps && S.n_long == 0) ? 2 : 1;
   S.lanes_fixed = true;
   return TE_OK;
 }

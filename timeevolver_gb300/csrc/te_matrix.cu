@@ -1461,16 +1461,17 @@ extern "C" int te_matrix_fixed_layout(te_matrix A, int* state, int* n_values, in
 }
 
 extern "C" int te_matrix_set_spmv_lanes(te_matrix A, int lanes) {
-  if (!A || A->n_rows != A->n_cols || !(lanes == 0 || lanes == 1 || lanes == 2 || lanes == 4)) {
-    te_set_error("te_matrix_set_spmv_lanes: square matrix and lanes 0 (tune), 1, 2 or 4 required");
+  if (!A || A->n_rows != A->n_cols || !(lanes == -1 || lanes == 0 || lanes == 1 || lanes == 2 || lanes == 4)) {
+    te_set_error("te_matrix_set_spmv_lanes: square matrix and lanes -1 (timed), 0 (by shape), 1, 2 or 4 required");
     return TE_ERR_INVALID_ARG;
   }
   if (lanes > 1 && A->sell.n_long > 0) {
     te_set_error("te_matrix_set_spmv_lanes: a matrix with long rows uses one lane per row");
     return TE_ERR_UNSUPPORTED;
   }
-  A->sell.lanes = lanes == 0 ? 1 : lanes;
-  A->sell.lanes_fixed = lanes != 0;
+  A->sell.lanes = lanes <= 0 ? 1 : lanes;
+  A->sell.lanes_fixed = lanes > 0;
+  A->sell.lanes_timed = lanes == -1;
   return TE_OK;
 }
 

@@ -171,6 +171,10 @@ __device__ __forceinline__ int te_fix_scale(double bound) {
 #define TE_FIX_UNROLL 2
 #endif
 constexpr int kTeFixUnroll = TE_FIX_UNROLL;  // slots per lane in flight
+// Slots per lane in flight in the column-block passes: 3 measured 2.437 ms
+// per apply of the dim-1e7 Zipf matrix against 2.478 (2) and 2.451 (4), all
+// at 6 blocks of 256 per SM without spills.
+constexpr int kTeFixBlockUnroll = 3;
 
 // hi-part product of two limb-split values c = c1 2^31 + c0, x = x1 2^31 + x0
 // in units of 2^62: c1 x1 + 2 (hi32(c1 x0) + hi32(c0 x1)), below c x / 2^62 by
@@ -203,10 +207,11 @@ __device__ __forceinline__ void te_fix_mac(const int2 h, const int4 x, int64_t& 
 // is left out: at most 5 units of 2^62 per slot of a total below 2^122, so
 // the row error is below k 1.25 2^-56 R U + (k + 1) 2^-61 R U + 2^-53 |y|
 // for k slots, R the largest row 1-norm and U the bound on max|u|.
+template <int U = kTeFixUnroll>
 __device__ __forceinline__ longlong2 te_sell_row_fix_sum(int64_t s, int64_t e, const int32_t* __restrict__ col,
                                                          const int2* __restrict__ hv, const int4* __restrict__ X) {
   int64_t sr = 0, si = 0;
-#pragma unroll(kTeFixUnroll)
+#pragma unroll(U)
   for (; s < e; s += 32) te_fix_mac(__ldcs(hv + s), __ldg(X + __ldcs(col + s)), sr, si);  // {h0, h1}, {re0, re1, im0, im1}
   return make_longlong2(sr, si);
 }
@@ -239,10 +244,11 @@ __device__ __forceinline__ double2 te_sell_row_fix_packed(int64_t s, int64_t e, 
 // (Re = hr xr - hi xi, Im = hr xi + hi xr), so the per-slot term of the
 // error bound is four times the real one: below (5 k 2^-56 + (2 k + 1) 2^-61)
 // R U + 2^-53 |y|.
+template <int U = kTeFixUnroll>
 __device__ __forceinline__ longlong2 te_sell_row_fix_c_sum(int64_t s, int64_t e, const int32_t* __restrict__ col,
                                                            const int4* __restrict__ hv, const int4* __restrict__ X) {
   int64_t sr = 0, si = 0;
-#pragma unroll(kTeFixUnroll)
+#pragma unroll(U)
   for (; s < e; s += 32) {
     const int4 h = __ldcs(hv + s);
     const int4 x = __ldg(X + __ldcs(col + s));

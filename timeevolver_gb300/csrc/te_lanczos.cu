@@ -358,7 +358,8 @@ __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) fix_block_kerne
   const int64_t c_begin = warp_chunk[wid], c_end = warp_chunk[wid + 1];
   for (int64_t c = c_begin; c < c_end; ++c) {
     const int64_t s0 = __ldg(chunk_off + c), s1 = __ldg(chunk_off + c + 1);
-    longlong2 S = REAL ? te_sell_row_fix_sum(s0 + lane, s1, col, hv, X) : te_sell_row_fix_c_sum(s0 + lane, s1, col, hv4, X);
+    longlong2 S = REAL ? te_sell_row_fix_sum<kTeFixBlockUnroll>(s0 + lane, s1, col, hv, X)
+                       : te_sell_row_fix_c_sum<kTeFixBlockUnroll>(s0 + lane, s1, col, hv4, X);
     const int64_t i = c * 32 + lane;
     if (i < n_rows) {
       const int32_t r = __ldg(row + i);

@@ -1142,7 +1142,7 @@ int create_coo_host(int64_t n_rows, int64_t n_cols, int64_t nnz, const uint64_t*
   return finish_create(n_rows, n_cols, rp, ci, vv, out, norm1);
 }
 
-// A CPU read of one word in every 4 KiB of the host arrays, on a few threads,
+// A CPU read of one word in every 4 KiB of the host arrays, on up to 16 threads,
 // before the device reads them in place.  The GPU reaches pageable host memory
 // through the CPU's page tables; without this pass the same 405 MB read by the
 // ingest kernel alternated between 2.8 ms and 60-130 ms from call to call (with
@@ -1152,7 +1152,7 @@ void touch_host_pages(const void* const* ptrs, const size_t* bytes, int count) {
   const size_t kStride = 4096;
   size_t pages = 0;
   for (int a = 0; a < count; ++a) pages += (bytes[a] + kStride - 1) / kStride;
-  const int T = (int)std::max<size_t>(1, std::min<size_t>(4, pages >> 12));
+  const int T = (int)std::max<size_t>(1, std::min<size_t>(16, pages >> 14));  // 16 K pages per thread
   std::atomic<uint64_t> sink(0);
   auto work = [&](int t) {
     uint64_t acc = 0;

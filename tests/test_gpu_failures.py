@@ -112,6 +112,36 @@ def test_nan_start_vector_rejected(te_gpu):
     assert e.value.code == TE_ERR_NOT_NORMALIZED
 
 
+def test_normalisation_check_large_vector(te_gpu):
+    """The start vector's normalisation check (krylovTimeEvolver.cpp:45-48) on a
+    vector long enough for the multi-threaded sum (2^21 values and more): a
+    norm 2 tol away from 1 is rejected, one tol/2 away is accepted, as is a
+    NaN anywhere; the same for te_evolver_reset."""
+    n = 1 << 20  # 2^21 doubles
+    rows = np.arange(n, dtype=np.int64)
+    M = te_gpu.Matrix.from_coo(n, (rows, rows, np.ones(n, dtype=np.complex128)))
+    rng = np.random.default_rng(11)
+    v = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    v /= np.linalg.norm(v)
+    tol = 1e-8
+    ev = te_gpu.Evolver(M, v * (1.0 + 0.5 * tol), 0.1, 0.1, [], tol=tol, m=10)
+    try:
+        with pytest.raises(te_gpu.TeError) as e:
+            ev.reset(v * (1.0 + 2.0 * tol))
+        assert e.value.code == TE_ERR_NOT_NORMALIZED
+        bad = v.copy()
+        bad[n - 3] = np.nan
+        with pytest.raises(te_gpu.TeError) as e:
+            ev.reset(bad)
+        assert e.value.code == TE_ERR_NOT_NORMALIZED
+    finally:
+        ev.close()
+    with pytest.raises(te_gpu.TeError) as e:
+        te_gpu.Evolver(M, v * (1.0 + 2.0 * tol), 0.1, 0.1, [], tol=tol, m=10)
+    assert e.value.code == TE_ERR_NOT_NORMALIZED
+    M.close()
+
+
 def test_unreachable_tolerance_no_step(te_gpu, oracle_lib):
     """Krylov dimension 2 at tol 1e-12: each halving lowers the error per unit
     time by only 2, so 20 halvings cannot meet the tolerance rate."""

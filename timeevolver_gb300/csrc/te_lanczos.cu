@@ -75,7 +75,10 @@ __device__ __forceinline__ double2 apply_row_epilogue(int64_t r, double2 y, doub
 // K lanes per row: K = 1 walks the matrix's static chunk schedule; K = 2, 4
 // (small matrices, chosen by te_tune_sell_lanes) give each warp 32/K rows and
 // stride over (chunk, part) units.
-template <bool REAL, bool HAS_PREV, bool FOLD, int K>
+// LONG: the matrix has long rows (merge-path segments).  Matrices without
+// them take the instantiation without that loop, whose registers otherwise
+// spill from the slot loop.
+template <bool REAL, bool HAS_PREV, bool FOLD, int K, bool LONG = true>
 __global__ void __launch_bounds__(TE_THREADS, (REAL && K == 1) ? 6 : 5) lanczos_apply_kernel(
     int64_t n, int64_t n_chunks, const int32_t* __restrict__ warp_chunk, const int64_t* __restrict__ chunk_off,
     const int32_t* __restrict__ col, const double* __restrict__ val, TeLongRows L, const double2* __restrict__ u_j,
@@ -101,7 +104,7 @@ __global__ void __launch_bounds__(TE_THREADS, (REAL && K == 1) ? 6 : 5) lanczos_
   if (K == 1) {
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
     // long rows (sorted rows 0..L.n-1) by merge-path segments, one warp each
-    for (int64_t sg = wid; sg < L.n_seg; sg += warps) {
+    for (int64_t sg = wid; LONG && sg < L.n_seg; sg += warps) {
       int64_t lr;
       double2 y;
       const int done = te_long_segment<REAL>(L, sg, u_j, lane, &lr, &y);
@@ -112,11 +115,14 @@ __global__ void __launch_bounds__(TE_THREADS, (REAL && K == 1) ? 6 : 5) lanczos_
         te_split_row_publish(L, lr, a2);
       }
     }
-    const int64_t c_end = warp_chunk[wid + 1];
-    for (int64_t c = warp_chunk[wid]; c < c_end; ++c) {
+    // 32-bit chunk counter and an unsigned live-row test (rows < 2^31): fewer
+    // registers across the slot loop
+    const int c_end = warp_chunk[wid + 1];
+    const uint32_t live_lo = (uint32_t)L.n, live_cnt = (uint32_t)(n - L.n);
+    for (int c = warp_chunk[wid]; c < c_end; ++c) {
       const double2 y = te_sell_row<REAL>(chunk_off, col, val, u_j, c, lane);
-      const int64_t r = c * 32 + lane;
-      if (r < n && r >= L.n) apply_row_epilogue<HAS_PREV, FOLD>(r, y, g, cw, u_j, u_jm1, w, acc);
+      const int64_t r = (int64_t)c * 32 + lane;
+      if ((uint32_t)r - live_lo < live_cnt) apply_row_epilogue<HAS_PREV, FOLD>(r, y, g, cw, u_j, u_jm1, w, acc);
     }
   } else {
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -268,7 +274,7 @@ struct TeFixMatrix {
   int nvals, cbits, sh;
 };
 
-template <bool HAS_PREV, int FMT>
+template <bool HAS_PREV, int FMT, bool LONG = true>  // LONG: as for lanczos_apply_kernel
 __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_fix_kernel(
     int64_t n, const int32_t* __restrict__ warp_chunk, const int64_t* __restrict__ chunk_off, TeFixMatrix M,
     TeLongRows L, const int4* __restrict__ X, const double2* __restrict__ u_j, const double2* __restrict__ u_jm1,
@@ -297,7 +303,7 @@ __global__ void __launch_bounds__(TE_THREADS, TE_FIX_MIN_BLOCKS) lanczos_apply_f
   unsigned int wmax = 0;
   const int64_t wid = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t sg = wid; sg < L.n_seg; sg += warps) {  // long rows: merge-path segments, FP64
+  for (int64_t sg = wid; LONG && sg < L.n_seg; sg += warps) {  // long rows: merge-path segments, FP64
     int64_t lr;
     double2 y;
     const int done = te_long_segment<FMT != 2>(L, sg, u_j, lane, &lr, &y);
@@ -961,21 +967,24 @@ namespace {
 using ApplyKernel = void (*)(int64_t, int64_t, const int32_t*, const int64_t*, const int32_t*, const double*,
                              TeLongRows, const double2*, const double2*, double2*, TeDevState*, double*, int);
 
-template <int K>
+template <int K, bool LONG>
 ApplyKernel apply_kernel_for(bool is_real, bool has_prev, bool fold) {
   static const ApplyKernel table[2][2][2] = {
-      {{lanczos_apply_kernel<false, false, false, K>, lanczos_apply_kernel<false, false, true, K>},
-       {lanczos_apply_kernel<false, true, false, K>, lanczos_apply_kernel<false, true, true, K>}},
-      {{lanczos_apply_kernel<true, false, false, K>, lanczos_apply_kernel<true, false, true, K>},
-       {lanczos_apply_kernel<true, true, false, K>, lanczos_apply_kernel<true, true, true, K>}}};
+      {{lanczos_apply_kernel<false, false, false, K, LONG>, lanczos_apply_kernel<false, false, true, K, LONG>},
+       {lanczos_apply_kernel<false, true, false, K, LONG>, lanczos_apply_kernel<false, true, true, K, LONG>}},
+      {{lanczos_apply_kernel<true, false, false, K, LONG>, lanczos_apply_kernel<true, false, true, K, LONG>},
+       {lanczos_apply_kernel<true, true, false, K, LONG>, lanczos_apply_kernel<true, true, true, K, LONG>}}};
   return table[is_real ? 1 : 0][has_prev ? 1 : 0][fold ? 1 : 0];
 }
 
-ApplyKernel apply_kernel(int lanes, bool is_real, bool has_prev, bool fold) {
+// K > 1 never has long rows (te_matrix_set_spmv_lanes refuses them).
+ApplyKernel apply_kernel(int lanes, bool is_real, bool has_prev, bool fold, bool has_long = true) {
   switch (lanes) {
-    case 2: return apply_kernel_for<2>(is_real, has_prev, fold);
-    case 4: return apply_kernel_for<4>(is_real, has_prev, fold);
-    default: return apply_kernel_for<1>(is_real, has_prev, fold);
+    case 2: return apply_kernel_for<2, false>(is_real, has_prev, fold);
+    case 4: return apply_kernel_for<4, false>(is_real, has_prev, fold);
+    default:
+      return has_long ? apply_kernel_for<1, true>(is_real, has_prev, fold)
+                      : apply_kernel_for<1, false>(is_real, has_prev, fold);
   }
 }
 
@@ -1001,7 +1010,7 @@ void te_launch_lanczos_apply(const TeSell& A, bool is_real, const double2* u_j, 
                              TeDevState* ds, double* partials, int j, bool fold, cudaStream_t st,
                              const TeSegCarry* carry) {
   const int lanes = A.lanes;
-  const ApplyKernel k = apply_kernel(lanes, is_real, u_jm1 != nullptr, fold);
+  const ApplyKernel k = apply_kernel(lanes, is_real, u_jm1 != nullptr, fold, A.n_seg > 0);
   const int grid = lanes == 1 ? A.grid : apply_grid_k(A, lanes, k);
   te_launch_pdl(lanes == 1 && A.saturated, k, grid, TE_THREADS, st, A.n, A.n_chunks, A.warp_chunk, A.chunk_off,
                 A.col, A.val, te_long_rows(A, carry), u_j, u_jm1, w, ds, partials, j);
@@ -1129,12 +1138,15 @@ namespace {
 using ApplyFixKernel = void (*)(int64_t, const int32_t*, const int64_t*, TeFixMatrix, TeLongRows, const int4*,
                                 const double2*, const double2*, double2*, TeDevState*, double*, int);
 
-ApplyFixKernel apply_fix_kernel(int fmt, bool has_prev) {
-  static const ApplyFixKernel table[3][2] = {
-      {lanczos_apply_fix_kernel<false, 0>, lanczos_apply_fix_kernel<true, 0>},
-      {lanczos_apply_fix_kernel<false, 1>, lanczos_apply_fix_kernel<true, 1>},
-      {lanczos_apply_fix_kernel<false, 2>, lanczos_apply_fix_kernel<true, 2>}};
-  return table[fmt][has_prev ? 1 : 0];
+ApplyFixKernel apply_fix_kernel(int fmt, bool has_prev, bool has_long = true) {
+  static const ApplyFixKernel table[2][3][2] = {
+      {{lanczos_apply_fix_kernel<false, 0, false>, lanczos_apply_fix_kernel<true, 0, false>},
+       {lanczos_apply_fix_kernel<false, 1, false>, lanczos_apply_fix_kernel<true, 1, false>},
+       {lanczos_apply_fix_kernel<false, 2, false>, lanczos_apply_fix_kernel<true, 2, false>}},
+      {{lanczos_apply_fix_kernel<false, 0, true>, lanczos_apply_fix_kernel<true, 0, true>},
+       {lanczos_apply_fix_kernel<false, 1, true>, lanczos_apply_fix_kernel<true, 1, true>},
+       {lanczos_apply_fix_kernel<false, 2, true>, lanczos_apply_fix_kernel<true, 2, true>}}};
+  return table[has_long ? 1 : 0][fmt][has_prev ? 1 : 0];
 }
 
 }  // namespace
@@ -1171,7 +1183,8 @@ void te_launch_lanczos_apply_fix(const TeSell& A, const int4* X, const double2* 
   const int fmt = A.fix_val4 ? 2 : (A.fix_pk ? 1 : 0);
   const TeFixMatrix M{A.col, A.fix_val, A.fix_val4, A.fix_pk, A.fix_table, A.fix_nvals, A.fix_cbits, A.fix_sh};
   const size_t smem = fmt == 1 ? sizeof(int2) * A.fix_nvals : 0;
-  te_launch_pdl_smem(A.fix_saturated, apply_fix_kernel(fmt, u_jm1 != nullptr), A.fix_grid, TE_THREADS, smem, st, A.n,
+  te_launch_pdl_smem(A.fix_saturated, apply_fix_kernel(fmt, u_jm1 != nullptr, A.n_seg > 0), A.fix_grid, TE_THREADS,
+                     smem, st, A.n,
                      A.fix_warp_chunk, A.chunk_off, M, te_long_rows(A, carry), X, u_j, u_jm1, w, ds, partials, j);
 }
 

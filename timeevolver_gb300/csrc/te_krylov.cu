@@ -842,13 +842,16 @@ __device__ void krylov_step_body(TeDevState* ds, int mode, KSmem* S) {
   save_krylov_data(C);
 }
 
-__global__ void __launch_bounds__(TE_THREADS) krylov_kernel(TeDevState* ds, int mode) {
+// One block (one per SM at most: the shared memory of KSmem), so the whole
+// register file is available; at the default budget of 64 registers the
+// kernel spilled 260 bytes.
+__global__ void __launch_bounds__(TE_THREADS, 1) krylov_kernel(TeDevState* ds, int mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   krylov_step_body(ds, mode, reinterpret_cast<KSmem*>(smem_raw));
 }
 
 // Batched evolutions: block b runs the step of instance b.
-__global__ void __launch_bounds__(TE_THREADS) krylov_batch_kernel(TeDevState* states, int mode) {
+__global__ void __launch_bounds__(TE_THREADS, 1) krylov_batch_kernel(TeDevState* states, int mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   krylov_step_body(states + blockIdx.x, mode, reinterpret_cast<KSmem*>(smem_raw));
 }

@@ -31,7 +31,7 @@ MORE = re.compile(r":(\d+)(?:-(\d+))?")
 
 # files of this repository that share a name with a reference file: a citation
 # is a reference citation when it names the reference's directory
-OWN_PREFIXES = ("timeevolver_gb300/", "host/", "csrc/", "include/", "oracle/", "tests/", "_work/")
+OWN_PREFIXES = ("timeevolver_gb300/", "host/", "csrc/", "include/", "oracle/", "tests/")
 
 
 def _table():
